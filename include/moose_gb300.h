@@ -1,0 +1,327 @@
+/*
+ * moose_gb300.h -- C ABI of the GB300 (sm_103a) HSolve.
+ *
+ * A drop-in for MOOSE's Hines solver (`HSolve`, reference `hsolve/HSolve.h:20`)
+ * and for the per-step work of `HSolveActive::step`
+ * (`hsolve/HSolveActive.cpp:45-66`).  The MOOSE side (an `HSolve` C++ class
+ * registered under the same Cinfo name, fields and zombie classes) reads the
+ * model once at setup, exactly as `HSolveActive::setup` does
+ * (`hsolve/HSolveActiveSetup.cpp:17-41`), fills an `HsCellDesc`, and from then
+ * on calls only the functions below.  No C++ types, exceptions or torch types
+ * cross this boundary: plain pointers, sizes and `int` status codes.
+ *
+ * Conventions
+ *  - Every function returns an HS_* status; 0 is success.  On failure the
+ *    message is available from hs_last_error().
+ *  - Indices are "model indices": positions in the arrays of the HsCellDesc
+ *    the solver was created from (MOOSE's Id -> index map of
+ *    `HSolve::localIndex`, `hsolve/HSolveInterface.cpp:23-36`, becomes the
+ *    caller's own Id -> model-index map).
+ *  - All quantities are SI, as in MOOSE (V, ohm, F, S, A, s, mM).
+ */
+#ifndef MOOSE_GB300_H
+#define MOOSE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Status codes (reference: `cerr` + early return, `hsolve/HSolve.cpp:409-434`,
+ * and `assert` on unknown Ids, `hsolve/HSolveInterface.cpp:33`).        */
+#define HS_OK        0
+#define HS_EINVAL    1   /* bad argument, index or model                 */
+#define HS_EDEVICE   2   /* CUDA error                                   */
+#define HS_ENOMEM    3   /* host or device allocation failed             */
+#define HS_ETIMEOUT  4   /* a bounded device wait gave up                */
+#define HS_ESTATE    5   /* call not valid in the current state          */
+#define HS_ENOTSUP   6   /* feature not supported by this build          */
+#define HS_ECAPACITY 7   /* request larger than a fixed capacity         */
+
+/* Precision of the per-step arithmetic. */
+#define HS_PREC_FP64  0  /* every operation in FP64, reference order      */
+#define HS_PREC_MIXED 1  /* FP32 gates/tables/synapses, FP64 matrix+solve */
+
+/* ------------------------------------------------------------------ */
+/* Model description.  One HsCellDesc describes what `HSolveActive::setup`
+ * reads from the MOOSE object graph for one cell.                      */
+
+/* An HHGate rate table (`biophysics/HHGate.cpp:539-620`): A = alpha and
+ * B = alpha+beta sampled at min + i*(max-min)/divs, i = 0..divs.        */
+typedef struct HsGateTable {
+    double min;
+    double max;
+    uint32_t divs;
+    const double* A;          /* divs+1 entries */
+    const double* B;          /* divs+1 entries */
+} HsGateTable;
+
+/* An HHGate2D table pair (`builtins/Interpol2D.cpp`): entry [ix][iy] at
+ * A[ix*(ydivs+1)+iy], x = xmin + ix*(xmax-xmin)/xdivs, same for y.      */
+typedef struct HsGate2DTable {
+    double xmin, xmax;
+    double ymin, ymax;
+    uint32_t xdivs, ydivs;
+    const double* A;          /* (xdivs+1)*(ydivs+1) entries */
+    const double* B;
+} HsGate2DTable;
+
+/* HHChannel2D index codes (`biophysics/HHChannel2D.cpp` `dependency`). */
+#define HS_DEP_VOLT      0    /* "VOLT_INDEX"    */
+#define HS_DEP_C1        1    /* "C1_INDEX"      */
+#define HS_DEP_C2        2    /* "C2_INDEX"      */
+#define HS_DEP_VOLT_C1   3    /* "VOLT_C1_INDEX" */
+#define HS_DEP_VOLT_C2   4    /* "VOLT_C2_INDEX" */
+#define HS_DEP_C1_C2     5    /* "C1_C2_INDEX"   */
+
+typedef struct HsCellDesc {
+    /* Compartments.  `parent[i]` is the morphological parent (the source of
+     * the `axial` message into i) or -1.  Several children of one parent are
+     * connected in increasing child index: that is the message order that
+     * `HSolveUtils::adjacent`/`children` see (`hsolve/HSolveUtils.cpp:27-44`). */
+    uint32_t n_compt;
+    const int32_t* parent;
+    const double* Ra;
+    const double* Rm;
+    const double* Cm;
+    const double* Em;
+    const double* initVm;
+    const double* Vm;          /* value at setup (V_ before reinit) */
+    const double* inject;      /* basal inject at setup              */
+
+    /* Leakage channels (`HSolvePassive::initialize`, Thevenin sum). */
+    uint32_t n_leak;
+    const uint32_t* leak_compt;
+    const double* leak_Ek;
+    const double* leak_Gk;
+
+    /* Prototype HHGate tables, shared by channels (`HSolveUtils::gates`
+     * with getOriginals). */
+    uint32_t n_gate;
+    const HsGateTable* gate;
+
+    /* HHChannels taken over by the solver (`readHHChannels`).  Channels of
+     * one compartment are in message order = increasing channel index.   */
+    uint32_t n_chan;
+    const uint32_t* chan_compt;
+    const double* chan_Gbar;
+    const double* chan_Ek;
+    const double* chan_Xpower;
+    const double* chan_Ypower;
+    const double* chan_Zpower;
+    const int32_t* chan_xgate;       /* gate table index, or -1 */
+    const int32_t* chan_ygate;
+    const int32_t* chan_zgate;
+    const int32_t* chan_instant;     /* bit 1 X, 2 Y, 4 Z          */
+    const double* chan_modulation;
+    const int32_t* chan_use_conc;    /* Z gate tabulated on Ca     */
+    const double* chan_X;
+    const double* chan_Y;
+    const double* chan_Z;
+    const int32_t* chan_ca_target;   /* pool fed by IkOut, or -1   */
+    const int32_t* chan_ca_depend;   /* pool read by `concen`, or -1 */
+
+    /* CaConc pools (`readCalcium`; B from shell volume,
+     * `biophysics/CaConcBase.cpp:259-269`, is computed by the caller). */
+    uint32_t n_pool;
+    const uint32_t* pool_compt;
+    const double* pool_Ca;
+    const double* pool_CaBasal;
+    const double* pool_tau;
+    const double* pool_B;
+    const double* pool_ceiling;
+    const double* pool_floor;
+
+    /* External HHChannel2D objects (tick 4; `biophysics/HHChannel2D.cpp:327-369`).
+     * X gate only (Xpower > 0), looked up on (dep0, dep1) of `xindex`.  */
+    uint32_t n_gate2d;
+    const HsGate2DTable* gate2d;
+    uint32_t n_chan2d;
+    const uint32_t* c2d_compt;
+    const double* c2d_Gbar;
+    const double* c2d_Ek;
+    const double* c2d_Xpower;
+    const int32_t* c2d_xgate;        /* gate2d index */
+    const int32_t* c2d_xindex;       /* HS_DEP_* */
+    const int32_t* c2d_conc1_pool;   /* pool whose concOut feeds conc1, or -1 */
+    const int32_t* c2d_conc2_pool;
+    const int32_t* c2d_instant;
+    const double* c2d_modulation;
+    const double* c2d_X;             /* initial X (the `X` field set before reinit) */
+
+    /* External SynChans (tick 4; `biophysics/SynChan.cpp:171-251`) with one
+     * SimpleSynHandler each (tick 1; `synapse/SimpleSynHandler.cpp:86-119`). */
+    uint32_t n_syn;
+    const uint32_t* syn_compt;
+    const double* syn_Gbar;
+    const double* syn_Ek;
+    const double* syn_tau1;
+    const double* syn_tau2;
+    const double* syn_modulation;
+    /* Synaptic events already queued in each handler: event e arrives at
+     * SynChan `ev_syn[e]` with time ev_time[e] (spike time + synapse delay)
+     * and weight ev_weight[e].  Any order. */
+    uint32_t n_event;
+    const uint32_t* ev_syn;
+    const double* ev_time;
+    const double* ev_weight;
+
+    /* SpikeGens driven by the solver (`readSynapses`, `SpikeGen::process`). */
+    uint32_t n_spikegen;
+    const uint32_t* sg_compt;
+    const double* sg_threshold;
+    const double* sg_refractT;
+    const int32_t* sg_edge;
+
+    /* Basal-inject schedule: before step stim_step[k] (0-based, counted from
+     * reinit) the compartment's `inject` field is set to stim_value[k], as a
+     * script does between `moose.start()` calls.  Sorted by step.        */
+    uint32_t n_stim;
+    const uint32_t* stim_compt;
+    const uint32_t* stim_step;
+    const double* stim_value;
+} HsCellDesc;
+
+/* ------------------------------------------------------------------ */
+/* Library */
+
+/* Message for the last failing call on this thread. */
+const char* hs_last_error(void);
+/* Number of CUDA devices visible (0 when none); never fails. */
+int hs_device_count(void);
+/* Library build string (architecture and flags). */
+const char* hs_build_info(void);
+
+/* ------------------------------------------------------------------ */
+/* Drop-in solver: one HSolve instance per cell.
+ * Lifecycle mirrors `HSolve`: setPath/setup -> reinit -> process ...     */
+typedef struct HsSolver HsSolver;
+
+/* HSolve::setPath -> HSolve::setup (`hsolve/HSolve.cpp:286-334`):
+ * `seed` is the compartment found under `target`; `dt` is the HSolve `dt`
+ * field, used for the matrix, CmByDt and Ca factors.                    */
+int hs_create(const HsCellDesc* cell, uint32_t seed, double dt, int precision,
+              HsSolver** out);
+int hs_destroy(HsSolver* s);
+
+/* HSolve::reinit (`hsolve/HSolve.cpp:229-233`): `clock_dt` is the tick dt
+ * used by gates, external objects and spike detection.                  */
+int hs_reinit(HsSolver* s, double clock_dt);
+/* nsteps calls of HSolve::process, with tick-1/4 external objects. */
+int hs_process(HsSolver* s, uint32_t nsteps);
+/* Wait for queued device work of this solver. */
+int hs_sync(HsSolver* s);
+
+/* Solver fields (`hsolve/HSolve.cpp:87-156`). */
+int hs_set_ca_advance(HsSolver* s, int ca_advance);
+int hs_get_ca_advance(HsSolver* s, int* out);
+/* vMin,vMax,vDiv,caMin,caMax,caDiv after setup (recomputed from the gates,
+ * `hsolve/HSolveActiveSetup.cpp:367-414`). */
+int hs_get_table_grid(HsSolver* s, double* vmin, double* vmax, int* vdiv,
+                      double* camin, double* camax, int* cadiv);
+int hs_get_nsteps(HsSolver* s, uint64_t* out);
+
+/* Zombie fields by (kind, field, model index).  Kinds and fields below. */
+#define HS_KIND_COMPT   0
+#define HS_KIND_CHAN    1
+#define HS_KIND_POOL    2
+#define HS_KIND_CHAN2D  3
+#define HS_KIND_SYNCHAN 4
+
+/* compartment fields (`hsolve/HSolveInterface.cpp:66-244`) */
+#define HS_F_VM        0
+#define HS_F_CM        1
+#define HS_F_EM        2
+#define HS_F_RM        3
+#define HS_F_RA        4
+#define HS_F_INITVM    5
+#define HS_F_IM        6   /* read-only */
+#define HS_F_INJECT    7
+/* channel fields (`hsolve/HSolveInterface.cpp:262-451`) */
+#define HS_F_GBAR     10
+#define HS_F_EK       11
+#define HS_F_GK       12
+#define HS_F_IK       13   /* read-only */
+#define HS_F_X        14
+#define HS_F_Y        15
+#define HS_F_Z        16
+#define HS_F_INSTANT  17
+#define HS_F_MODULATION 18
+#define HS_F_XPOWER   19
+#define HS_F_YPOWER   20
+#define HS_F_ZPOWER   21
+/* pool fields (`hsolve/HSolveInterface.cpp:453-533`) */
+#define HS_F_CA       30
+#define HS_F_CABASAL  31
+#define HS_F_CEILING  32
+#define HS_F_FLOOR    33
+#define HS_F_TAU      34   /* write-only pair with B: set both via hs_set_tau_b */
+#define HS_F_B        35
+
+int hs_get_field(HsSolver* s, int kind, int field, uint32_t index, double* out);
+int hs_set_field(HsSolver* s, int kind, int field, uint32_t index, double value);
+int hs_set_tau_b(HsSolver* s, uint32_t pool, double tau, double B);
+
+/* Message destinations into the solver, applied at the next step only
+ * (`HSolve::addInject`, `addGkEk`, `addConc`, `iCa`). */
+int hs_add_inject(HsSolver* s, uint32_t compt, double value);
+int hs_add_gkek(HsSolver* s, uint32_t compt, double Gk, double Ek);
+int hs_add_conc(HsSolver* s, uint32_t chan, double conc);
+int hs_add_ica(HsSolver* s, uint32_t pool, double ica);
+
+/* Bulk reads in model order (n = n_compt / n_pool). */
+int hs_read_vm(HsSolver* s, double* out, uint32_t n);
+int hs_read_ca(HsSolver* s, double* out, uint32_t n);
+
+/* Trace recording: every `stride` steps, Vm of the listed compartments is
+ * appended to a device buffer (a Table on tick 8 reading `HSolve::getVm`). */
+int hs_record(HsSolver* s, const uint32_t* compts, uint32_t n, uint32_t stride,
+              uint32_t capacity_samples);
+int hs_read_trace(HsSolver* s, double* out, uint32_t capacity, uint32_t* n_samples);
+
+/* Spikes from the SpikeGens: (spikegen model index, time) pairs. */
+int hs_read_spikes(HsSolver* s, uint32_t* gen, double* time, uint32_t capacity,
+                   uint32_t* n);
+
+/* ------------------------------------------------------------------ */
+/* Batched solver: many cells packed by size into one persistent kernel.
+ * No counterpart in the reference (it runs one serial HSolve per cell).  */
+typedef struct HsBatch HsBatch;
+
+typedef struct HsBatchTuning {
+    uint32_t threads_per_cta;   /* 0 = autotuned */
+    uint32_t warps_per_cell_max;/* 0 = autotuned */
+    uint32_t steps_per_launch;  /* 0 = autotuned */
+    uint32_t use_graph;         /* capture the dt loop as a CUDA graph */
+} HsBatchTuning;
+
+int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds,
+                    uint32_t n_cells, double dt, int precision,
+                    const HsBatchTuning* tuning, HsBatch** out);
+int hs_batch_destroy(HsBatch* b);
+int hs_batch_reinit(HsBatch* b, double clock_dt);
+int hs_batch_process(HsBatch* b, uint32_t nsteps);
+int hs_batch_sync(HsBatch* b);
+/* Vm of every compartment of cell `cell` in model order. */
+int hs_batch_read_vm(HsBatch* b, uint32_t cell, double* out, uint32_t n);
+int hs_batch_read_ca(HsBatch* b, uint32_t cell, double* out, uint32_t n);
+int hs_batch_record(HsBatch* b, const uint32_t* cell, const uint32_t* compt,
+                    uint32_t n, uint32_t stride, uint32_t capacity_samples);
+int hs_batch_read_trace(HsBatch* b, double* out, uint32_t capacity,
+                        uint32_t* n_samples);
+int hs_batch_read_spikes(HsBatch* b, uint32_t* cell, uint32_t* gen,
+                         double* time, uint32_t capacity, uint32_t* n);
+/* Statistics of the packing: compartments, cells, CTAs, launches/step. */
+int hs_batch_info(HsBatch* b, uint64_t* n_compt, uint32_t* n_ctas,
+                  uint32_t* threads_per_cta, uint32_t* steps_per_launch);
+/* Average duration (ms) of the stepping kernel launches timed with CUDA
+ * events on the batch's stream since the last call, and their count. */
+int hs_batch_kernel_time(HsBatch* b, double* avg_ms, uint32_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MOOSE_GB300_H */

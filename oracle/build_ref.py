@@ -1,0 +1,148 @@
+#!/usr/bin/env python3
+"""Build recipe for the unmodified reference MOOSE (pymoose) from its own sources.
+
+Test infrastructure only.  This script compiles the reference C++ sources where
+they lie (``$MOOSE_REF_SRC``, default ``/root/reference``) with plain ``g++``
+and links them into a Python extension under ``oracle/_ref/moose/``.  It does
+not run the reference's own build system (meson): the per-directory source
+lists are read out of each ``<dir>/meson.build`` file and compiled directly.
+
+Differences from the reference's meson recipe, and why:
+  * no ``-DUSE_GSL`` / ``-DUSE_HDF5``: GSL and HDF5 are absent here.  Every
+    GSL use is ``#ifdef USE_GSL``-guarded, except ``ksolve/SteadyStateGsl.cpp``
+    which is left out (chemical steady-state solver, not on the HSolve path).
+  * ``-ffp-contract=off``: keep ``a*b+c`` as two rounded operations, so the
+    reference's FP64 arithmetic is the plain IEEE sequence the oracle and the
+    GPU drop-in restate.
+  * unit tests: a second object set compiled with ``-DDO_UNIT_TESTS`` is not
+    needed; the passive-solver known-answer harness (``ref_passive_harness.cpp``)
+    links the reference's own HinesMatrix/HSolvePassive objects directly.
+
+Outputs (git-ignored): ``oracle/_ref/obj/**.o``, ``oracle/_ref/libmooseref.a``,
+``oracle/_ref/moose/_moose*.so`` plus a copy of the reference's pure-Python
+``moose`` package next to it, and ``oracle/_ref/ref_passive_harness``.
+
+Usage:  python oracle/build_ref.py [-j N]
+"""
+import argparse
+import concurrent.futures as cf
+import os
+import re
+import shutil
+import subprocess
+import sys
+import sysconfig
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+SRC = os.environ.get("MOOSE_REF_SRC", "/root/reference")
+
+# Sub-libraries linked whole into _moose (reference meson.build, `sublibs`).
+SUBDIRS = [
+    "external/libsoda", "external/fmt", "basecode", "biophysics", "builtins",
+    "device", "diffusion", "examples", "hsolve", "intfire", "kinetics",
+    "ksolve", "mesh", "mpi", "msg", "pybind11", "randnum", "scheduling",
+    "shell", "signeur", "synapse", "utility",
+]
+EXCLUDE = {
+    "ksolve/SteadyStateGsl.cpp",      # GSL-only translation unit
+}
+
+CXXFLAGS = [
+    "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-fvisibility=hidden",
+    "-w", '-DMOOSE_VERSION="4.1.0"', '-DCOMPILER_STRING="gcc"',
+]
+
+
+def sources():
+    out = []
+    seen = set()
+    for d in SUBDIRS:
+        mb = os.path.join(SRC, d, "meson.build")
+        # drop meson comments: commented-out entries are not part of the build
+        text = "\n".join(l.split("#", 1)[0] for l in open(mb).read().splitlines())
+        for name in re.findall(r"'([^']+\.(?:cpp|cc))'", text):
+            rel = os.path.normpath(os.path.join(d, name))
+            if rel in EXCLUDE or rel in seen:
+                continue
+            seen.add(rel)
+            out.append(rel)
+    return out
+
+
+def includes():
+    import pybind11
+    return [
+        "-I" + os.path.join(SRC, "external/fmt/include"),
+        "-I" + os.path.join(SRC, "external/libsoda"),
+        "-I" + os.path.join(SRC, "external/exprtk"),
+        "-I" + os.path.join(SRC),
+        "-I" + pybind11.get_include(),
+        "-I" + sysconfig.get_paths()["include"],
+    ]
+
+
+def compile_one(rel, inc):
+    src = os.path.join(SRC, rel)
+    obj = os.path.join(OUT, "obj", rel + ".o")
+    os.makedirs(os.path.dirname(obj), exist_ok=True)
+    if os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(src):
+        return obj, None
+    cmd = ["g++"] + CXXFLAGS + inc + ["-I" + os.path.dirname(src), "-c", src, "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return obj, r.stderr[-4000:]
+    return obj, None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("-j", type=int, default=os.cpu_count() or 4)
+    args = ap.parse_args()
+    if not os.path.isdir(SRC):
+        print("reference sources not found at", SRC, file=sys.stderr)
+        return 2
+    os.makedirs(OUT, exist_ok=True)
+    inc = includes()
+    srcs = sources()
+    objs, errors = [], []
+    with cf.ThreadPoolExecutor(args.j) as ex:
+        for obj, err in ex.map(lambda s: compile_one(s, inc), srcs):
+            objs.append(obj)
+            if err:
+                errors.append((obj, err))
+    pym_obj, err = compile_one("pybind11/pymoose.cpp", inc)
+    if err:
+        errors.append((pym_obj, err))
+    if errors:
+        for obj, err in errors:
+            print("FAILED", obj, "\n", err, file=sys.stderr)
+        return 1
+    lib = os.path.join(OUT, "libmooseref.a")
+    if os.path.exists(lib):
+        os.remove(lib)
+    subprocess.check_call(["ar", "rcs", lib] + objs)
+    pkg = os.path.join(OUT, "moose")
+    if os.path.isdir(pkg):
+        shutil.rmtree(pkg)
+    shutil.copytree(os.path.join(SRC, "python", "moose"), pkg)
+    ext = os.path.join(pkg, "_moose" + sysconfig.get_config_var("EXT_SUFFIX"))
+    subprocess.check_call(
+        ["g++", "-shared", "-o", ext, pym_obj, "-Wl,--whole-archive", lib,
+         "-Wl,--no-whole-archive", "-lpthread"])
+    rd = os.path.join(OUT, "rdesigneur")
+    if os.path.isdir(rd):
+        shutil.rmtree(rd)
+    shutil.copytree(os.path.join(SRC, "python", "rdesigneur"), rd)
+    harness = os.path.join(HERE, "ref_passive_harness.cpp")
+    if os.path.exists(harness):
+        subprocess.check_call(
+            ["g++"] + CXXFLAGS[:3] + ["-fPIC", "-w"] + inc +
+            ["-I" + os.path.join(SRC, "hsolve"), harness, "-o",
+             os.path.join(OUT, "ref_passive_harness"), lib, "-lpthread"])
+    print("built", ext)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

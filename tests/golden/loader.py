@@ -1,0 +1,23 @@
+"""Rebuild the CellModel stored in a golden .npz (keys written by
+make_golden_active.save_model) so that any machine steps bit-identical input."""
+import numpy as np
+
+
+def load_model(z, prefix="model_"):
+    import sys, os
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(
+        os.path.abspath(__file__)))), "moose-core_gb300"))
+    from moose_gb300.abi import CellModel, _ARRAYS
+    kw = {k: z[prefix + k] for k in _ARRAYS}
+    gates = []
+    for i in range(int(z[prefix + "ngates"])):
+        AB = z[prefix + "gate%d" % i]
+        mn, mx = z[prefix + "gate%d_range" % i]
+        gates.append((float(mn), float(mx), AB[0], AB[1]))
+    gates2d = []
+    for i in range(int(z[prefix + "ngates2d"])):
+        AB = z[prefix + "gate2d%d" % i]
+        r = z[prefix + "gate2d%d_range" % i]
+        gates2d.append((float(r[0]), float(r[1]), float(r[2]), float(r[3]), AB[0], AB[1]))
+    meta = {k[5:]: z[k] for k in z.files if k.startswith("meta_")}
+    return CellModel(seed=int(z[prefix + "seed"]), gates=gates, gates2d=gates2d, meta=meta, **kw)
