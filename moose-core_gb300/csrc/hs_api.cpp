@@ -1,0 +1,566 @@
+// hs_api.cpp -- C ABI of the GB300 HSolve drop-in (include/moose_gb300.h).
+//
+// An HsSolver is one HSolve instance: its plan (host), one device arena with
+// all per-cell arrays, and one CUDA stream.  Field access mirrors
+// hsolve/HSolveInterface.cpp:66-533 including its quirks (setEm/setRm reset
+// EmByRm to Em/Rm; setCm refreshes CmByDt with the current dt_; setRa only
+// stores Ra; modulation ignores non-positive values).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/moose_gb300.h"
+#include "hs_cell.h"
+#include "hs_plan.h"
+
+using namespace hsg;
+
+namespace {
+thread_local std::string g_err;
+
+int setErr(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+int cudaErr(cudaError_t e, const char* where) {
+    return setErr(HS_EDEVICE, std::string(where) + ": " + cudaGetErrorString(e));
+}
+}  // namespace
+
+struct HsSolver {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    CellPlan P;
+    Arena arena;
+    DevCell dc;
+    double dt_ = 0;          // HSolve::dt_ (setup dt, clock dt after reinit)
+    double clockDt = 0;
+    bool reinited = false;
+    int precision = HS_PREC_FP64;
+    std::vector<double> initVm, injBasal;
+    std::vector<uint8_t> injPresent;
+    uint32_t* recCompt = nullptr;
+    double* recBuf = nullptr;
+    std::vector<uint32_t> recHost;
+};
+
+extern "C" {
+
+const char* hs_last_error(void) { return g_err.c_str(); }
+
+int hs_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+const char* hs_build_info(void) {
+    return "moose_gb300 HSolve: sm_103a; FP64 kernels built with --fmad=false";
+}
+
+int hs_create(const HsCellDesc* cell, uint32_t seed, double dt, int precision, HsSolver** out) {
+    if (!cell || !out) return setErr(HS_EINVAL, "null argument");
+    *out = nullptr;
+    if (precision != HS_PREC_FP64)
+        return setErr(HS_ENOTSUP, "the drop-in solver runs FP64; mixed precision is a batch option");
+    HsSolver* s = new (std::nothrow) HsSolver();
+    if (!s) return setErr(HS_ENOMEM, "host allocation failed");
+    std::string err;
+    try {
+        if (!buildPlan(*cell, seed, dt, s->P, err)) {
+            delete s;
+            return setErr(HS_EINVAL, err);
+        }
+    } catch (const std::bad_alloc&) {
+        delete s;
+        return setErr(HS_ENOMEM, "host allocation failed during setup");
+    } catch (...) {
+        delete s;
+        return setErr(HS_EINVAL, "setup failed");
+    }
+    if (hs_device_count() == 0) {
+        delete s;
+        return setErr(HS_EDEVICE, "no CUDA device");
+    }
+    cudaError_t e = cudaGetDevice(&s->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete s;
+        return cudaErr(e, "stream");
+    }
+    const uint32_t spikeCap = 1u << 16;
+    Arena dry;
+    layoutCell(s->P, dry, s->dc, spikeCap, 0, 0, s->st, nullptr);
+    s->arena.size = dry.used + 256;
+    e = cudaMalloc(&s->arena.base, s->arena.size);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->arena.base, 0, s->arena.size, s->st);
+    if (e == cudaSuccess) e = layoutCell(s->P, s->arena, s->dc, spikeCap, 0, 0, s->st, nullptr);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) {
+        int rc = cudaErr(e, "device setup");
+        hs_destroy(s);
+        return rc;
+    }
+    s->dt_ = dt;
+    s->dc.dt = dt;
+    s->precision = precision;
+    s->initVm = s->P.initVm;
+    s->injBasal = s->P.injBasal;
+    s->injPresent = s->P.injPresent;
+    *out = s;
+    return HS_OK;
+}
+
+int hs_destroy(HsSolver* s) {
+    if (!s) return HS_OK;
+    if (s->st) cudaStreamSynchronize(s->st);
+    if (s->arena.base) cudaFree(s->arena.base);
+    if (s->recCompt) cudaFree(s->recCompt);
+    if (s->recBuf) cudaFree(s->recBuf);
+    if (s->st) cudaStreamDestroy(s->st);
+    delete s;
+    return HS_OK;
+}
+
+int hs_reinit(HsSolver* s, double clock_dt) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    if (!(clock_dt > 0)) return setErr(HS_EINVAL, "clock dt must be positive");
+    s->dt_ = clock_dt;            // HSolve::reinit: dt_ = p->dt
+    s->clockDt = clock_dt;
+    s->dc.dt = clock_dt;
+    cudaError_t e = reinitCellState(s->P, s->dc, clock_dt, s->initVm, s->injBasal, s->injPresent, s->st);
+    if (e == cudaSuccess) e = launchReinitGatesFp64(s->dc, s->st);
+    if (e == cudaSuccess && s->dc.nRec) {
+        // sample 0: a Table reading Vm at reinit
+        std::vector<double> row(s->dc.nRec);
+        for (uint32_t r = 0; r < s->dc.nRec; ++r) row[r] = s->initVm[s->recHost[r]];
+        e = cudaMemcpyAsync(s->dc.recBuf, row.data(), row.size() * 8, cudaMemcpyHostToDevice, s->st);
+        DevCtl ctl{};
+        ctl.nSamples = 1;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(s->dc.ctl, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, s->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) return cudaErr(e, "reinit");
+    s->reinited = true;
+    return HS_OK;
+}
+
+int hs_process(HsSolver* s, uint32_t nsteps) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    if (!s->reinited) return setErr(HS_ESTATE, "reinit before process");
+    if (nsteps == 0) return HS_OK;
+    cudaError_t e = launchStepFp64(s->dc, nsteps, s->st);
+    if (e != cudaSuccess) return cudaErr(e, "process");
+    return HS_OK;
+}
+
+int hs_sync(HsSolver* s) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    cudaError_t e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) return cudaErr(e, "sync");
+    return HS_OK;
+}
+
+int hs_set_ca_advance(HsSolver* s, int v) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    if (v != 0 && v != 1) return setErr(HS_EINVAL, "HSolve: caAdvance should be either 0 or 1");
+    s->dc.caAdvance = v;
+    return HS_OK;
+}
+
+int hs_get_ca_advance(HsSolver* s, int* out) {
+    if (!s || !out) return setErr(HS_EINVAL, "null argument");
+    *out = s->dc.caAdvance;
+    return HS_OK;
+}
+
+int hs_get_table_grid(HsSolver* s, double* vmin, double* vmax, int* vdiv, double* camin,
+                      double* camax, int* cadiv) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    if (vmin) *vmin = s->P.vMin;
+    if (vmax) *vmax = s->P.vMax;
+    if (vdiv) *vdiv = s->P.vDiv;
+    if (camin) *camin = s->P.caMin;
+    if (camax) *camax = s->P.caMax;
+    if (cadiv) *cadiv = s->P.caDiv;
+    return HS_OK;
+}
+
+int hs_get_nsteps(HsSolver* s, uint64_t* out) {
+    if (!s || !out) return setErr(HS_EINVAL, "null argument");
+    DevCtl ctl;
+    cudaError_t e = cudaMemcpyAsync(&ctl, s->dc.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) return cudaErr(e, "get nsteps");
+    *out = ctl.nSteps;
+    return HS_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+template <class T>
+int readDev(HsSolver* s, const T* p, T* out) {
+    cudaError_t e = cudaMemcpyAsync(out, p, sizeof(T), cudaMemcpyDeviceToHost, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    return e == cudaSuccess ? HS_OK : cudaErr(e, "field read");
+}
+template <class T>
+int writeDev(HsSolver* s, T* p, T v) {
+    cudaError_t e = cudaMemcpyAsync(p, &v, sizeof(T), cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    return e == cudaSuccess ? HS_OK : cudaErr(e, "field write");
+}
+
+int comptIndex(HsSolver* s, uint32_t m, uint32_t* h) {
+    if (m >= s->P.hinesOf.size() || s->P.hinesOf[m] < 0)
+        return setErr(HS_EINVAL, "compartment is not handled by this solver");
+    *h = (uint32_t)s->P.hinesOf[m];
+    return HS_OK;
+}
+int chanIndex(HsSolver* s, uint32_t m, uint32_t* q) {
+    if (m >= s->P.chanSolverOf.size() || s->P.chanSolverOf[m] < 0)
+        return setErr(HS_EINVAL, "channel is not handled by this solver");
+    *q = (uint32_t)s->P.chanSolverOf[m];
+    return HS_OK;
+}
+int poolIndex(HsSolver* s, uint32_t m, uint32_t* p) {
+    if (m >= s->P.poolSolverOf.size() || s->P.poolSolverOf[m] < 0)
+        return setErr(HS_EINVAL, "pool is not handled by this solver");
+    *p = (uint32_t)s->P.poolSolverOf[m];
+    return HS_OK;
+}
+// state index of gate w (0 X, 1 Y, 2 Z) of solver channel q, or -1
+int64_t gateState(HsSolver* s, uint32_t q, int w) {
+    double pw[3] = {s->P.Xpow[q], s->P.Ypow[q], s->P.Zpow[q]};
+    if (pw[w] == 0.0) return -1;
+    int64_t k = s->P.stateOff[q];
+    for (int i = 0; i < w; ++i) if (pw[i] > 0.0) ++k;
+    return k;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hs_get_field(HsSolver* s, int kind, int field, uint32_t index, double* out) {
+    if (!s || !out) return setErr(HS_EINVAL, "null argument");
+    uint32_t i;
+    int rc;
+    const CellPlan& P = s->P;
+    switch (kind) {
+    case HS_KIND_COMPT:
+        if ((rc = comptIndex(s, index, &i))) return rc;
+        switch (field) {
+        case HS_F_VM: return readDev(s, s->dc.V + i, out);
+        case HS_F_CM: *out = P.Cm[i]; return HS_OK;
+        case HS_F_EM: *out = P.Em[i]; return HS_OK;
+        case HS_F_RM: *out = P.Rm[i]; return HS_OK;
+        case HS_F_RA: *out = P.Ra[i]; return HS_OK;
+        case HS_F_INITVM: *out = s->initVm[i]; return HS_OK;
+        case HS_F_INJECT: {
+            uint8_t present;
+            if ((rc = readDev(s, s->dc.injPresent + i, &present))) return rc;
+            if (!present) { *out = 0.0; return HS_OK; }
+            return readDev(s, s->dc.injBasal + i, out);
+        }
+        case HS_F_IM: {   // HSolve::getIm (hsolve/HSolveInterface.cpp:161-182)
+            double V, EmByRm, pg, pge;
+            if ((rc = readDev(s, s->dc.V + i, &V)) || (rc = readDev(s, s->dc.EmByRm + i, &EmByRm)) ||
+                (rc = readDev(s, s->dc.prevExt + 2 * i, &pg)) || (rc = readDev(s, s->dc.prevExt + 2 * i + 1, &pge)))
+                return rc;
+            double Im = EmByRm - V / P.Rm[i];
+            for (uint32_t q = P.chanPtr[i]; q < P.chanPtr[i + 1]; ++q) {
+                double gk, ek;
+                if ((rc = readDev(s, s->dc.Gk + q, &gk)) || (rc = readDev(s, s->dc.Ek + q, &ek))) return rc;
+                Im += (ek - V) * gk;
+            }
+            Im += pge - pg * V;
+            *out = Im;
+            return HS_OK;
+        }
+        }
+        return setErr(HS_EINVAL, "unknown compartment field");
+    case HS_KIND_CHAN: {
+        if ((rc = chanIndex(s, index, &i))) return rc;
+        int64_t k;
+        switch (field) {
+        case HS_F_GBAR: return readDev(s, s->dc.Gbar + i, out);
+        case HS_F_EK: return readDev(s, s->dc.Ek + i, out);
+        case HS_F_GK: return readDev(s, s->dc.Gk + i, out);
+        case HS_F_IK: {
+            double gk, ek, V;
+            if ((rc = readDev(s, s->dc.Gk + i, &gk)) || (rc = readDev(s, s->dc.Ek + i, &ek))) return rc;
+            uint32_t ic = 0;
+            while (P.chanPtr[ic + 1] <= i) ++ic;
+            if ((rc = readDev(s, s->dc.V + ic, &V))) return rc;
+            *out = (ek - V) * gk;
+            return HS_OK;
+        }
+        case HS_F_X: case HS_F_Y: case HS_F_Z:
+            k = gateState(s, i, field - HS_F_X);
+            if (k < 0) { *out = 0.0; return HS_OK; }
+            return readDev(s, s->dc.state + k, out);
+        case HS_F_INSTANT: {
+            int32_t v;
+            if ((rc = readDev(s, s->dc.instant + i, &v))) return rc;
+            *out = v;
+            return HS_OK;
+        }
+        case HS_F_MODULATION: return readDev(s, s->dc.mod + i, out);
+        case HS_F_XPOWER: return readDev(s, s->dc.Xpow + i, out);
+        case HS_F_YPOWER: return readDev(s, s->dc.Ypow + i, out);
+        case HS_F_ZPOWER: return readDev(s, s->dc.Zpow + i, out);
+        }
+        return setErr(HS_EINVAL, "unknown channel field");
+    }
+    case HS_KIND_POOL:
+        if ((rc = poolIndex(s, index, &i))) return rc;
+        switch (field) {
+        case HS_F_CA: return readDev(s, s->dc.ca + i, out);
+        case HS_F_CABASAL: return readDev(s, s->dc.CaBasal + i, out);
+        case HS_F_CEILING: return readDev(s, s->dc.ceil + i, out);
+        case HS_F_FLOOR: return readDev(s, s->dc.floor_ + i, out);
+        }
+        return setErr(HS_EINVAL, "unknown pool field");
+    case HS_KIND_CHAN2D:
+        if (index >= P.K2) return setErr(HS_EINVAL, "HHChannel2D index out of range");
+        if (field == HS_F_X) return readDev(s, s->dc.c2dX + index, out);
+        if (field == HS_F_GK) return readDev(s, s->dc.c2dGk + index, out);
+        if (field == HS_F_GBAR) return readDev(s, s->dc.c2dGbar + index, out);
+        if (field == HS_F_EK) return readDev(s, s->dc.c2dEk + index, out);
+        return setErr(HS_EINVAL, "unknown HHChannel2D field");
+    case HS_KIND_SYNCHAN:
+        if (index >= P.S) return setErr(HS_EINVAL, "SynChan index out of range");
+        if (field == HS_F_GK) return readDev(s, s->dc.synGk + index, out);
+        if (field == HS_F_X) return readDev(s, s->dc.synX + index, out);
+        if (field == HS_F_Y) return readDev(s, s->dc.synY + index, out);
+        if (field == HS_F_EK) return readDev(s, s->dc.synEk + index, out);
+        return setErr(HS_EINVAL, "unknown SynChan field");
+    }
+    return setErr(HS_EINVAL, "unknown object kind");
+}
+
+int hs_set_field(HsSolver* s, int kind, int field, uint32_t index, double value) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    uint32_t i;
+    int rc;
+    CellPlan& P = s->P;
+    switch (kind) {
+    case HS_KIND_COMPT:
+        if ((rc = comptIndex(s, index, &i))) return rc;
+        switch (field) {
+        case HS_F_VM: return writeDev(s, s->dc.V + i, value);
+        case HS_F_CM:
+            P.Cm[i] = value;
+            return writeDev(s, s->dc.CmByDt + i, 2.0 * value / s->dt_);
+        case HS_F_EM:
+            P.Em[i] = value;
+            return writeDev(s, s->dc.EmByRm + i, value / P.Rm[i]);
+        case HS_F_RM:
+            P.Rm[i] = value;
+            return writeDev(s, s->dc.EmByRm + i, P.Em[i] / value);
+        case HS_F_RA: P.Ra[i] = value; return HS_OK;
+        case HS_F_INITVM: s->initVm[i] = value; return HS_OK;
+        case HS_F_INJECT:
+            s->injBasal[i] = value;
+            s->injPresent[i] = 1;
+            if ((rc = writeDev<uint8_t>(s, s->dc.injPresent + i, 1))) return rc;
+            return writeDev(s, s->dc.injBasal + i, value);
+        }
+        return setErr(HS_EINVAL, "compartment field not writable");
+    case HS_KIND_CHAN: {
+        if ((rc = chanIndex(s, index, &i))) return rc;
+        int64_t k;
+        switch (field) {
+        case HS_F_GBAR: return writeDev(s, s->dc.Gbar + i, value);
+        case HS_F_EK: return writeDev(s, s->dc.Ek + i, value);
+        case HS_F_GK: return writeDev(s, s->dc.Gk + i, value);
+        case HS_F_X: case HS_F_Y: case HS_F_Z:
+            k = gateState(s, i, field - HS_F_X);
+            if (k < 0) return HS_OK;
+            return writeDev(s, s->dc.state + k, value);
+        case HS_F_INSTANT: return writeDev<int32_t>(s, s->dc.instant + i, (int32_t)value);
+        case HS_F_MODULATION:
+            if (value > 0.0) return writeDev(s, s->dc.mod + i, value);
+            return HS_OK;
+        }
+        return setErr(HS_EINVAL, "channel field not writable");
+    }
+    case HS_KIND_POOL: {
+        if ((rc = poolIndex(s, index, &i))) return rc;
+        double basal, cc;
+        switch (field) {
+        case HS_F_CA:   // HSolve::setCa: ca_ = Ca, c_ = Ca - CaBasal_
+            if ((rc = readDev(s, s->dc.CaBasal + i, &basal))) return rc;
+            if ((rc = writeDev(s, s->dc.ca + i, value))) return rc;
+            return writeDev(s, s->dc.c + i, value - basal);
+        case HS_F_CABASAL:   // CaConcStruct::setCaBasal keeps Ca
+            if ((rc = readDev(s, s->dc.CaBasal + i, &basal)) || (rc = readDev(s, s->dc.c + i, &cc))) return rc;
+            if ((rc = writeDev(s, s->dc.c + i, cc + (basal - value)))) return rc;
+            return writeDev(s, s->dc.CaBasal + i, value);
+        case HS_F_CEILING: return writeDev(s, s->dc.ceil + i, value);
+        case HS_F_FLOOR: return writeDev(s, s->dc.floor_ + i, value);
+        }
+        return setErr(HS_EINVAL, "pool field not writable");
+    }
+    case HS_KIND_CHAN2D:
+        if (index >= P.K2) return setErr(HS_EINVAL, "HHChannel2D index out of range");
+        if (field == HS_F_GBAR) return writeDev(s, s->dc.c2dGbar + index, value);
+        if (field == HS_F_EK) return writeDev(s, s->dc.c2dEk + index, value);
+        if (field == HS_F_MODULATION) return writeDev(s, s->dc.c2dMod + index, value);
+        return setErr(HS_EINVAL, "HHChannel2D field not writable");
+    case HS_KIND_SYNCHAN:
+        if (index >= P.S) return setErr(HS_EINVAL, "SynChan index out of range");
+        if (field == HS_F_EK) return writeDev(s, s->dc.synEk + index, value);
+        if (field == HS_F_MODULATION) return writeDev(s, s->dc.synMod + index, value);
+        return setErr(HS_EINVAL, "SynChan field not writable");
+    }
+    return setErr(HS_EINVAL, "unknown object kind");
+}
+
+int hs_set_tau_b(HsSolver* s, uint32_t pool, double tau, double B) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    uint32_t i;
+    int rc;
+    if ((rc = poolIndex(s, pool, &i))) return rc;
+    if (!(tau != 0.0)) return setErr(HS_EINVAL, "tau must be non-zero");
+    double dt = s->dt_;   // CaConcStruct::setTauB with HSolve::dt_
+    if ((rc = writeDev(s, s->dc.f1 + i, 4.0 / (2.0 + dt / tau) - 1.0))) return rc;
+    return writeDev(s, s->dc.f2 + i, 2.0 * B * dt / (2.0 + dt / tau));
+}
+
+int hs_add_inject(HsSolver* s, uint32_t compt, double value) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    uint32_t i;
+    int rc;
+    if ((rc = comptIndex(s, compt, &i))) return rc;
+    double cur;
+    if ((rc = readDev(s, s->dc.injVarying + i, &cur))) return rc;
+    s->injPresent[i] = 1;
+    if ((rc = writeDev<uint8_t>(s, s->dc.injPresent + i, 1))) return rc;
+    return writeDev(s, s->dc.injVarying + i, cur + value);
+}
+
+int hs_add_gkek(HsSolver* s, uint32_t compt, double Gk, double Ek) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    uint32_t i;
+    int rc;
+    if ((rc = comptIndex(s, compt, &i))) return rc;
+    double g, ge;
+    if ((rc = readDev(s, s->dc.ext + 2 * i, &g)) || (rc = readDev(s, s->dc.ext + 2 * i + 1, &ge))) return rc;
+    if ((rc = writeDev(s, s->dc.ext + 2 * i, g + Gk))) return rc;
+    return writeDev(s, s->dc.ext + 2 * i + 1, ge + Gk * Ek);
+}
+
+int hs_add_conc(HsSolver* s, uint32_t chan, double conc) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    uint32_t q;
+    int rc;
+    if ((rc = chanIndex(s, chan, &q))) return rc;
+    return writeDev(s, s->dc.extCa + q, conc);
+}
+
+int hs_add_ica(HsSolver* s, uint32_t pool, double ica) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    uint32_t p;
+    int rc;
+    if ((rc = poolIndex(s, pool, &p))) return rc;
+    double cur;
+    if ((rc = readDev(s, s->dc.iCa + p, &cur))) return rc;
+    return writeDev(s, s->dc.iCa + p, cur + ica);
+}
+
+int hs_read_vm(HsSolver* s, double* out, uint32_t n) {
+    if (!s || !out) return setErr(HS_EINVAL, "null argument");
+    if (n != s->P.hinesOf.size()) return setErr(HS_EINVAL, "n must equal the model's compartment count");
+    std::vector<double> v(s->P.N);
+    cudaError_t e = cudaMemcpyAsync(v.data(), s->dc.V, v.size() * 8, cudaMemcpyDeviceToHost, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) return cudaErr(e, "read vm");
+    for (uint32_t m = 0; m < n; ++m) out[m] = s->P.hinesOf[m] < 0 ? NAN : v[s->P.hinesOf[m]];
+    return HS_OK;
+}
+
+int hs_read_ca(HsSolver* s, double* out, uint32_t n) {
+    if (!s || !out) return setErr(HS_EINVAL, "null argument");
+    if (n != s->P.poolSolverOf.size()) return setErr(HS_EINVAL, "n must equal the model's pool count");
+    std::vector<double> v(s->P.P + 1);
+    cudaError_t e = cudaMemcpyAsync(v.data(), s->dc.ca, s->P.P * 8, cudaMemcpyDeviceToHost, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) return cudaErr(e, "read ca");
+    for (uint32_t m = 0; m < n; ++m) out[m] = s->P.poolSolverOf[m] < 0 ? NAN : v[s->P.poolSolverOf[m]];
+    return HS_OK;
+}
+
+int hs_record(HsSolver* s, const uint32_t* compts, uint32_t n, uint32_t stride, uint32_t capacity) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    if (n && (!compts || stride == 0 || capacity == 0)) return setErr(HS_EINVAL, "bad recording request");
+    cudaStreamSynchronize(s->st);
+    if (s->recCompt) cudaFree(s->recCompt);
+    if (s->recBuf) cudaFree(s->recBuf);
+    s->recCompt = nullptr;
+    s->recBuf = nullptr;
+    s->recHost.clear();
+    for (uint32_t r = 0; r < n; ++r) {
+        uint32_t h;
+        int rc = comptIndex(s, compts[r], &h);
+        if (rc) return rc;
+        s->recHost.push_back(h);
+    }
+    s->dc.nRec = 0;
+    if (!n) return HS_OK;
+    cudaError_t e = cudaMalloc(&s->recCompt, n * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&s->recBuf, (size_t)n * capacity * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(s->recCompt, s->recHost.data(), n * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cudaErr(e, "record");
+    s->dc.nRec = n;
+    s->dc.recStride = stride;
+    s->dc.recCap = capacity;
+    s->dc.recCompt = s->recCompt;
+    s->dc.recBuf = s->recBuf;
+    return HS_OK;
+}
+
+int hs_read_trace(HsSolver* s, double* out, uint32_t capacity, uint32_t* n_samples) {
+    if (!s || !n_samples) return setErr(HS_EINVAL, "null argument");
+    DevCtl ctl;
+    cudaError_t e = cudaMemcpyAsync(&ctl, s->dc.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) return cudaErr(e, "read trace");
+    uint32_t stored = ctl.nSamples < s->dc.recCap ? ctl.nSamples : s->dc.recCap;
+    *n_samples = ctl.nSamples;
+    if (out && s->dc.nRec) {
+        uint32_t k = stored < capacity ? stored : capacity;
+        e = cudaMemcpy(out, s->dc.recBuf, (size_t)k * s->dc.nRec * 8, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cudaErr(e, "read trace");
+    }
+    return HS_OK;
+}
+
+int hs_read_spikes(HsSolver* s, uint32_t* gen, double* time, uint32_t capacity, uint32_t* n) {
+    if (!s || !n) return setErr(HS_EINVAL, "null argument");
+    DevCtl ctl;
+    cudaError_t e = cudaMemcpyAsync(&ctl, s->dc.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) return cudaErr(e, "read spikes");
+    *n = ctl.nSpikes;
+    uint32_t stored = ctl.nSpikes < s->dc.spikeCap ? ctl.nSpikes : s->dc.spikeCap;
+    uint32_t k = stored < capacity ? stored : capacity;
+    if (k && gen) e = cudaMemcpy(gen, s->dc.spikeGen, k * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && k && time) e = cudaMemcpy(time, s->dc.spikeTime, k * 8, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cudaErr(e, "read spikes");
+    if (ctl.nSpikes > s->dc.spikeCap) return setErr(HS_ECAPACITY, "spike buffer overflowed");
+    return HS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,325 @@
+// hs_fp64.cu -- the FP64 drop-in HSolve step on GB300 (sm_103a).
+//
+// One CTA steps one cell for `nsteps` clock steps without returning to the
+// host.  Per step, in the reference's tick order (scheduling/Clock.cpp:872-921):
+//   tick 0   basal-inject schedule
+//   tick 1/4 SimpleSynHandler -> SynChan, HHChannel2D  (one thread per object)
+//   tick 6   HSolveActive::step (hsolve/HSolveActive.cpp:45-66):
+//            advanceChannels + calculateChannelCurrents + updateMatrix
+//            (one thread per compartment), forward elimination and back
+//            substitution (warp 0, level by level over the pull programs),
+//            advanceCalcium (one thread per pool), SpikeGens, trace record.
+// Compiled with --fmad=false: every operation is the reference's IEEE
+// operation in the reference's order, so Vm/Ca are bit-identical to the CPU
+// HSolve wherever no libm call is involved (exp/log only in HHChannel2D and
+// non-integer gate powers).
+#include <cuda_runtime.h>
+
+#include "hs_device.cuh"
+
+namespace hsg {
+
+// ---- tick 1/4: external objects -------------------------------------------
+__device__ __forceinline__ void synchanStep(const DevCell& c, uint32_t k, double currTime) {
+    // SimpleSynHandler::vProcess: deliver events with time <= currTime
+    double activation = 0.0;
+    uint32_t e = c.evCur[k], end = c.evPtr[k + 1];
+    while (e < end && c.evTime[e] <= currTime) {
+        activation += c.evW[e] / c.dt;
+        ++e;
+    }
+    c.evCur[k] = e;
+    double act = c.synAct[k];
+    if (activation != 0.0) act += activation;
+    // SynChan::calcGk
+    double X = act * c.synXc1[k] + c.synX[k] * c.synXc2[k];
+    double Y = X * c.synYc1[k] + c.synY[k] * c.synYc2[k];
+    c.synX[k] = X;
+    c.synY[k] = Y;
+    c.synAct[k] = 0.0;
+    c.synGk[k] = Y * c.synNorm[k] * c.synMod[k];
+}
+
+__device__ __forceinline__ double depValue(int dep, double vm, double c1, double c2) {
+    return dep == 0 ? vm : dep == 1 ? c1 : dep == 2 ? c2 : 0.0;
+}
+
+__device__ __forceinline__ void chan2dStep(const DevCell& c, uint32_t k) {
+    double g = c.c2dGbar[k];
+    double xp = c.c2dXpow[k];
+    if (xp > 0) {
+        int gi = c.c2dGate[k];
+        double vm = c.c2dVm[k], c1 = c.c2dC1[k], c2 = c.c2dC2[k];
+        double x = depValue(c.c2dDep0[k], vm, c1, c2);
+        double y = depValue(c.c2dDep1[k], vm, c1, c2);
+        double A, B;
+        interp2dBoth(c.g2dAB + c.g2dOff[gi], c.g2dGeom + 6 * gi, c.g2dN[2 * gi],
+                     c.g2dN[2 * gi + 1], x, y, A, B);
+        double X = c.c2dX[k];
+        if (c.c2dInstant[k] & 1) {
+            X = A / B;
+        } else if (B > 1.0e-10) {   // HHChannelBase::integrate (exponential Euler)
+            double e = exp(-B * c.dt);
+            X = X * e + (A / B) * (1 - e);
+        } else {
+            X = X + A * c.dt;
+        }
+        c.c2dX[k] = X;
+        g *= takePower(X, xp);
+    }
+    c.c2dGk[k] = g * c.c2dMod[k];
+}
+
+// ---- tick 6, per compartment: channels + matrix row -----------------------
+__device__ __forceinline__ void comptStep(const DevCell& c, uint32_t ic) {
+    double V = c.V[ic];
+    Row vRow = tableRow(V, c.vMin, c.vMax, c.vDx, c.vCol);
+    double GkSum = 0.0, GkEkSum = 0.0;
+    for (uint32_t q = c.chanPtr[ic]; q < c.chanPtr[ic + 1]; ++q) {
+        int32_t s = c.stateOff[q];
+        int inst = c.instant[q];
+        double fraction = c.mod[q];
+        double C1, C2;
+        double xp = c.Xpow[q], yp = c.Ypow[q], zp = c.Zpow[q];
+        double xs = 0, ys = 0, zs = 0;
+        if (xp > 0.0) {
+            tableLookup(c.vTab, c.vCol, c.colX[q], vRow, C1, C2);
+            xs = gateStep(c.state[s], C1, C2, c.dt, inst & 1);
+            c.state[s++] = xs;
+        }
+        if (yp > 0.0) {
+            tableLookup(c.vTab, c.vCol, c.colY[q], vRow, C1, C2);
+            ys = gateStep(c.state[s], C1, C2, c.dt, inst & 2);
+            c.state[s++] = ys;
+        }
+        if (zp > 0.0) {
+            int32_t src = c.zSrc[q];
+            if (src >= 0) {
+                Row r = tableRow(c.ca[src], c.caMin, c.caMax, c.caDx, c.caCol);
+                tableLookup(c.caTab, c.caCol, c.colZ[q], r, C1, C2);
+            } else if (c.extCa[q] > 0) {
+                Row r = tableRow(c.extCa[q], c.caMin, c.caMax, c.caDx, c.caCol);
+                tableLookup(c.caTab, c.caCol, c.colZ[q], r, C1, C2);
+            } else {
+                tableLookup(c.vTab, c.vCol, c.colZ[q], vRow, C1, C2);
+            }
+            zs = gateStep(c.state[s], C1, C2, c.dt, inst & 4);
+            c.state[s] = zs;
+        }
+        // ChannelStruct::process
+        if (xp > 0.0) fraction *= takePower(xs, xp);
+        if (yp > 0.0) fraction *= takePower(ys, yp);
+        if (zp > 0.0) fraction *= takePower(zs, zp);
+        double gk = c.Gbar[q] * fraction;
+        c.Gk[q] = gk;
+        GkSum += gk;
+        GkEkSum += gk * c.Ek[q];
+    }
+    // external conductances in tick-4 send order (HSolve::addGkEk)
+    double eg = c.ext[2 * ic], ege = c.ext[2 * ic + 1];
+    for (uint32_t k = c.extPtr[ic]; k < c.extPtr[ic + 1]; ++k) {
+        int32_t code = c.extList[k];
+        double gk = code >= 0 ? c.c2dGk[code] : c.synGk[-code - 1];
+        double ek = code >= 0 ? c.c2dEk[code] : c.synEk[-code - 1];
+        eg += gk;
+        ege += gk * ek;
+    }
+    c.prevExt[2 * ic] = eg;
+    c.prevExt[2 * ic + 1] = ege;
+    // HSolveActive::updateMatrix
+    const uint32_t N = c.N;
+    double diag = c.HS2[ic] + GkSum;
+    double rhs = V * c.CmByDt[ic] + c.EmByRm[ic] + GkEkSum;
+    if (c.injPresent[ic]) rhs += c.injVarying[ic] + c.injBasal[ic];
+    diag += eg;
+    rhs += ege;
+    c.M[ic] = diag;
+    c.M[N + ic] = rhs;
+}
+
+// ---- elimination (one warp) -------------------------------------------------
+__device__ __forceinline__ void eliminateWarp(const DevCell& c, uint32_t lane) {
+    double* M = c.M;
+    for (uint32_t l = 0; l < c.fLevels; ++l) {
+        for (uint32_t k = c.fLevelPtr[l] + lane; k < c.fLevelPtr[l + 1]; k += 32) {
+            for (uint32_t o = c.fOpPtr[k]; o < c.fOpPtr[k + 1]; ++o) {
+                int4 op = c.fOps[o];
+                M[op.x] -= M[op.y] / M[op.w] * M[op.z];
+            }
+        }
+        __syncwarp();
+    }
+    const uint32_t N = c.N;
+    for (uint32_t l = 0; l < c.bLevels; ++l) {
+        for (uint32_t k = c.bLevelPtr[l] + lane; k < c.bLevelPtr[l + 1]; k += 32) {
+            uint32_t i = c.bRows[k];
+            double v = M[N + i];
+            for (uint32_t t = c.bTermPtr[k]; t < c.bTermPtr[k + 1]; ++t) {
+                int2 term = c.bTerms[t];
+                v -= M[term.x] * c.VMid[term.y];
+            }
+            v /= M[i];
+            c.VMid[i] = v;
+            c.V[i] = 2 * v - c.V[i];
+        }
+        __syncwarp();
+    }
+}
+
+// ---- advanceCalcium, per pool ----------------------------------------------
+__device__ __forceinline__ void poolStep(const DevCell& c, uint32_t p) {
+    double act = c.iCa[p];
+    for (uint32_t f = c.feedPtr[p]; f < c.feedPtr[p + 1]; ++f) {
+        uint32_t q = c.feedChan[f];
+        uint32_t ic = c.chanCompt[q];
+        double v = c.caAdvance == 1 ? c.VMid[ic] : (2 * c.VMid[ic] - c.V[ic]);
+        act += c.Gk[q] * (c.Ek[q] - v);
+    }
+    double cc = c.f1[p] * c.c[p] + c.f2[p] * act;
+    double ca = c.CaBasal[p] + cc;
+    if (c.ceil[p] > 0 && ca > c.ceil[p]) {
+        ca = c.ceil[p];
+        cc = ca - c.CaBasal[p];
+    }
+    if (ca < c.floor_[p]) {
+        ca = c.floor_[p];
+        cc = ca - c.CaBasal[p];
+    }
+    c.c[p] = cc;
+    c.ca[p] = ca;
+    c.iCa[p] = 0.0;
+}
+
+__global__ void __launch_bounds__(256) hsStepFp64(DevCell c, uint32_t nsteps) {
+    const uint32_t tid = threadIdx.x, nth = blockDim.x;
+    __shared__ unsigned long long s_step;
+    __shared__ uint32_t s_stim, s_spk, s_smp;
+    if (tid == 0) {
+        s_step = c.ctl->nSteps;
+        s_stim = c.ctl->stimPtr;
+        s_spk = c.ctl->nSpikes;
+        s_smp = c.ctl->nSamples;
+    }
+    __syncthreads();
+    for (uint32_t s = 0; s < nsteps; ++s) {
+        const unsigned long long step = s_step;
+        const double currTime = c.dt * (double)(step + 1);   // Clock: dt_ * endStep
+        if (tid == 0) {
+            uint32_t sp = s_stim;
+            while (sp < c.nStim && c.stimStep[sp] <= step) {
+                uint32_t h = c.stimCompt[sp];
+                c.injPresent[h] = 1;
+                c.injBasal[h] = c.stimValue[sp];
+                ++sp;
+            }
+            s_stim = sp;
+        }
+        for (uint32_t k = tid; k < c.S; k += nth) synchanStep(c, k, currTime);
+        for (uint32_t k = tid; k < c.K2; k += nth) chan2dStep(c, k);
+        __syncthreads();
+        for (uint32_t h = tid; h < c.H; h += nth) c.M[2 * c.N + h] = c.HJ0[h];
+        for (uint32_t ic = tid; ic < c.N; ic += nth) comptStep(c, ic);
+        __syncthreads();
+        if (tid < 32) eliminateWarp(c, tid);
+        __syncthreads();
+        for (uint32_t p = tid; p < c.P; p += nth) poolStep(c, p);
+        __syncthreads();
+        // sendValues for the next step's tick-4 objects; SpikeGens; traces
+        for (uint32_t k = tid; k < c.K2; k += nth) {
+            c.c2dVm[k] = c.V[c.c2dCompt[k]];
+            if (c.c2dConc1[k] >= 0) c.c2dC1[k] = c.ca[c.c2dConc1[k]];
+            if (c.c2dConc2[k] >= 0) c.c2dC2[k] = c.ca[c.c2dConc2[k]];
+        }
+        if (tid == 0) {
+            for (uint32_t k = 0; k < c.SG; ++k) {
+                double V = c.V[c.sgCompt[k]];
+                if (V > c.sgThreshold[k]) {
+                    if ((currTime + c.dt / 2.0) >= (c.sgLast[k] + c.sgRefract[k])) {
+                        if (!(c.sgEdge[k] && c.sgFired[k])) {
+                            uint32_t n = s_spk;
+                            if (n < c.spikeCap) {
+                                c.spikeGen[n] = k;
+                                c.spikeTime[n] = currTime;
+                            }
+                            s_spk = n + 1;
+                            c.sgLast[k] = currTime;
+                            c.sgFired[k] = 1;
+                        }
+                    }
+                } else {
+                    c.sgFired[k] = 0;
+                }
+            }
+        }
+        if (c.nRec && ((step + 1) % c.recStride) == 0) {
+            uint32_t smp = s_smp;
+            if (smp < c.recCap)
+                for (uint32_t r = tid; r < c.nRec; r += nth)
+                    c.recBuf[(size_t)smp * c.nRec + r] = c.V[c.recCompt[r]];
+        }
+        for (uint32_t ic = tid; ic < c.N; ic += nth) {
+            c.injVarying[ic] = 0.0;
+            c.ext[2 * ic] = 0.0;
+            c.ext[2 * ic + 1] = 0.0;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            if (c.nRec && ((step + 1) % c.recStride) == 0) s_smp = s_smp + 1;
+            s_step = step + 1;
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        c.ctl->nSteps = s_step;
+        c.ctl->stimPtr = s_stim;
+        c.ctl->nSpikes = s_spk;
+        c.ctl->nSamples = s_smp;
+    }
+}
+
+// Reinit of gate states (HSolveActive::reinitChannels), one thread per
+// compartment, after V and ca were set on the host side.
+__global__ void hsReinitGatesFp64(DevCell c) {
+    for (uint32_t ic = blockIdx.x * blockDim.x + threadIdx.x; ic < c.N; ic += gridDim.x * blockDim.x) {
+        Row vRow = tableRow(c.V[ic], c.vMin, c.vMax, c.vDx, c.vCol);
+        for (uint32_t q = c.chanPtr[ic]; q < c.chanPtr[ic + 1]; ++q) {
+            int32_t s = c.stateOff[q];
+            double C1, C2;
+            if (c.Xpow[q] > 0.0) {
+                tableLookup(c.vTab, c.vCol, c.colX[q], vRow, C1, C2);
+                c.state[s++] = C1 / C2;
+            }
+            if (c.Ypow[q] > 0.0) {
+                tableLookup(c.vTab, c.vCol, c.colY[q], vRow, C1, C2);
+                c.state[s++] = C1 / C2;
+            }
+            if (c.Zpow[q] > 0.0) {
+                int32_t src = c.zSrc[q];
+                if (src >= 0) {
+                    Row r = tableRow(c.ca[src], c.caMin, c.caMax, c.caDx, c.caCol);
+                    tableLookup(c.caTab, c.caCol, c.colZ[q], r, C1, C2);
+                } else if (c.extCa[q] > 0) {
+                    Row r = tableRow(c.extCa[q], c.caMin, c.caMax, c.caDx, c.caCol);
+                    tableLookup(c.caTab, c.caCol, c.colZ[q], r, C1, C2);
+                } else {
+                    tableLookup(c.vTab, c.vCol, c.colZ[q], vRow, C1, C2);
+                }
+                c.state[s] = C1 / C2;
+            }
+        }
+    }
+}
+
+cudaError_t launchStepFp64(const DevCell& c, uint32_t nsteps, cudaStream_t st) {
+    hsStepFp64<<<1, 256, 0, st>>>(c, nsteps);
+    return cudaGetLastError();
+}
+
+cudaError_t launchReinitGatesFp64(const DevCell& c, cudaStream_t st) {
+    uint32_t blocks = (c.N + 255) / 256;
+    if (blocks == 0) blocks = 1;
+    hsReinitGatesFp64<<<blocks, 256, 0, st>>>(c);
+    return cudaGetLastError();
+}
+
+}  // namespace hsg

@@ -1,0 +1,114 @@
+// hs_plan.h -- host-side HSolve setup for the GB300 solver.
+//
+// Builds, from an HsCellDesc, everything `HSolveActive::setup` builds
+// (hsolve/HSolveActiveSetup.cpp:17-41): the Hines ordering of
+// `HSolvePassive::walkTree` (hsolve/HSolvePassive.cpp:45-98), the matrix and
+// junction groups of `HinesMatrix::setup` (hsolve/HinesMatrix.cpp:25-223),
+// channel/gate/Ca-pool arrays and the merged rate tables of
+// `createLookupTables` (hsolve/HSolveActiveSetup.cpp:339-526).
+//
+// The reference walks its elimination as one serial sweep over an operand
+// "pointer program" (`makeOperands`, hsolve/HinesMatrix.cpp:226-365).  Here
+// that program is recompiled into a *pull* form: every matrix entry belongs
+// to one row, each row applies the updates aimed at its entries in the
+// reference's order, and rows are grouped into dependency levels.  All rows
+// of a level can run in parallel and the result is bit-identical to the
+// serial sweep, because each entry still sees the same operations in the
+// same order.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/moose_gb300.h"
+
+namespace hsg {
+
+// One forward-elimination update `t -= (l / diag[p]) * a` (entries index the
+// cell's M array: [0,N) diag, [N,2N) rhs, [2N,2N+H) HJ, [2N+H,3N+H) off).
+struct FwdOp {
+    int32_t t, l, a, p;
+};
+// One back-substitution term `v -= coef * VMid[src]`.
+struct BwdTerm {
+    int32_t coef, src;
+};
+
+struct Table {
+    double min = 0, max = 0, dx = 0;
+    uint32_t nPts = 0, nCol = 0;
+    std::vector<double> data;  // nPts x nCol, row-major, [A,B] per species
+};
+
+struct Gate2D {
+    double xmin, xmax, ymin, ymax, invDx, invDy;
+    uint32_t nx, ny;           // xdivs+1, ydivs+1
+    std::vector<double> AB;    // interleaved A,B: [(ix*ny+iy)*2 + {0,1}]
+};
+
+struct CellPlan {
+    uint32_t N = 0, H = 0;
+    double dtSetup = 0;
+    std::vector<uint32_t> modelOf;      // hines -> model compartment
+    std::vector<int64_t> hinesOf;       // model -> hines (-1 if not in tree)
+    // compartments (Hines order)
+    std::vector<double> V0, initVm, CmByDt, EmByRm, HS2, off, injBasal;
+    std::vector<uint8_t> injPresent;
+    std::vector<double> Ra, Rm, Cm, Em;
+    std::vector<std::vector<uint32_t>> children;
+    std::vector<double> HJ0;            // HJCopy
+    // elimination programs
+    std::vector<uint32_t> fLevelPtr, fRows, fOpPtr;   // fOpPtr indexed by position in fRows
+    std::vector<FwdOp> fOps;
+    std::vector<uint32_t> bLevelPtr, bRows, bTermPtr;
+    std::vector<BwdTerm> bTerms;
+    uint32_t maxLevelWidthF = 0, maxLevelWidthB = 0;
+    // channels (solver order)
+    uint32_t C = 0, G = 0;
+    std::vector<uint32_t> chanPtr;      // N+1
+    std::vector<double> Gbar, Ek, Xpow, Ypow, Zpow, modulation;
+    std::vector<int32_t> instant, stateOff, colX, colY, colZ, zSrc;  // zSrc: pool, -1 V row, -2 extCa row
+    std::vector<uint32_t> chanModel;
+    std::vector<int64_t> chanSolverOf;  // model -> solver
+    std::vector<double> state0;
+    // pools (solver order)
+    uint32_t P = 0;
+    std::vector<uint32_t> poolPtr;      // N+1 pools of each compartment
+    std::vector<double> CaBasal, f1, f2, ceiling, floor_, c0;
+    std::vector<int32_t> caTarget;      // per channel: pool or -1
+    std::vector<uint32_t> feedPtr, feedChan;  // per pool: channels feeding it, channel order
+    std::vector<uint32_t> poolModel;
+    std::vector<int64_t> poolSolverOf;
+    Table vTable, caTable;
+    double vMin = 0, vMax = 0, caMin = 0, caMax = 0;
+    int vDiv = 0, caDiv = 0;
+    // external tick-4 objects
+    uint32_t K2 = 0, S = 0, SG = 0;
+    std::vector<Gate2D> gates2d;
+    std::vector<uint32_t> c2dCompt;     // hines
+    std::vector<double> c2dGbar, c2dEk, c2dXpow, c2dMod, c2dX0;
+    std::vector<int32_t> c2dGate, c2dDep0, c2dDep1, c2dConc1, c2dConc2, c2dInstant;
+    std::vector<uint32_t> synCompt;     // hines
+    std::vector<double> synGbar, synEk, synTau1, synTau2, synMod;
+    std::vector<uint32_t> evPtr;        // S+1
+    std::vector<double> evTime, evW;
+    // per compartment, external channels in tick-4 send order:
+    // code >= 0: HHChannel2D k; code < 0: SynChan (-code - 1)
+    std::vector<uint32_t> extPtr;
+    std::vector<int32_t> extList;
+    std::vector<uint32_t> sgCompt;
+    std::vector<double> sgThreshold, sgRefract;
+    std::vector<int32_t> sgEdge;
+    std::vector<uint32_t> stimStep, stimCompt;
+    std::vector<double> stimValue;
+};
+
+// Build the plan; returns false and sets err on invalid input.
+bool buildPlan(const HsCellDesc& d, uint32_t seed, double dt, CellPlan& plan, std::string& err);
+
+// SynChan reinit constants (biophysics/SynChan.cpp:171-251), host libm.
+void synchanConstants(double tau1, double tau2, double gbar, double dt, double* xc1,
+                      double* xc2, double* yc1, double* yc2, double* norm);
+
+}  // namespace hsg

@@ -98,6 +98,7 @@ def compile_one(rel, inc):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("-j", type=int, default=os.cpu_count() or 4)
+    ap.add_argument("--keep-objects", action="store_true")
     args = ap.parse_args()
     if not os.path.isdir(SRC):
         print("reference sources not found at", SRC, file=sys.stderr)
@@ -140,6 +141,11 @@ def main():
             ["g++"] + CXXFLAGS[:3] + ["-fPIC", "-w"] + inc +
             ["-I" + os.path.join(SRC, "hsolve"), harness, "-o",
              os.path.join(OUT, "ref_passive_harness"), lib, "-lpthread"])
+    if not args.keep_objects:
+        # objects and the archive are only needed to relink; the extension and
+        # the harness are what the tests use
+        shutil.rmtree(os.path.join(OUT, "obj"), ignore_errors=True)
+        os.remove(lib)
     print("built", ext)
     return 0
 

@@ -1,0 +1,61 @@
+"""The C-ABI library: it builds, loads, exports every function that
+include/moose_gb300.h declares, and rejects bad models with status codes
+(validation runs before any device work, so this needs no GPU)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from moose_gb300 import _native, models
+from moose_gb300.abi import HS_EDEVICE, HS_EINVAL, HS_ENOTSUP, HS_PREC_FP64, HS_PREC_MIXED, CellModel
+
+
+def test_library_exports_every_declared_symbol():
+    L = _native.load()
+    names = _native.declared_symbols()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_build_info():
+    assert b"sm_103a" in _native.load().hs_build_info()
+
+
+def _create(model, seed=0, dt=25e-6, prec=HS_PREC_FP64):
+    L = _native.load()
+    d = model.desc()
+    h = C.c_void_p()
+    rc = L.hs_create(C.byref(d), seed, dt, prec, C.byref(h))
+    if rc == 0:
+        L.hs_destroy(h)
+    return rc, L.hs_last_error().decode()
+
+
+def test_rejects_bad_models():
+    m = models.config1_cell(n_cable=5)
+    rc, msg = _create(m, seed=99)
+    assert rc == HS_EINVAL and "seed" in msg
+    rc, msg = _create(m, dt=-1.0)
+    assert rc == HS_EINVAL and "dt" in msg
+    bad = models.config1_cell(n_cable=5)
+    bad.parent[3] = 3
+    rc, msg = _create(bad)
+    assert rc == HS_EINVAL
+    cyc = models.config1_cell(n_cable=5)
+    cyc.parent[0] = 5          # soma's parent is the last segment: a loop
+    rc, msg = _create(cyc)
+    assert rc == HS_EINVAL and "tree" in msg
+    g = models.config1_cell(n_cable=5)
+    g.chan_xgate[0] = 17
+    rc, msg = _create(g)
+    assert rc == HS_EINVAL and "gate" in msg
+    rc, msg = _create(m, prec=HS_PREC_MIXED)
+    assert rc == HS_ENOTSUP
+
+
+def test_valid_model_without_gpu_reports_device_error():
+    if _native.load().hs_device_count() > 0:
+        pytest.skip("a GPU is present")
+    rc, msg = _create(models.config1_cell(n_cable=5))
+    assert rc == HS_EDEVICE

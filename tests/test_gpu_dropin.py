@@ -1,0 +1,146 @@
+"""The FP64 drop-in HSolve on the GPU against the oracle and the reference's
+golden traces.
+
+Bars: bit-for-bit equality where no libm call is on the path (HH channels,
+junctions, CaConc, SynChan, SpikeGen); for cells with an HHChannel2D (device
+exp vs glibc exp) |dV| <= 1e-9 * max(|V_ref|, 1 mV) and
+|dCa| <= 1e-9 * max(|Ca_ref|, CaBasal), with identical spike counts.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from loader import load_model
+from moose_gb300 import models
+from moose_gb300.abi import HS_KIND_CHAN, HS_KIND_COMPT, HS_KIND_POOL, FIELDS, CellModel
+from moose_gb300.hsolve import HSolve
+from oracle import OracleCell
+
+pytestmark = pytest.mark.gpu
+
+
+def run_golden(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    m = load_model(z)
+    dt = float(z["dt"])
+    h = HSolve(m, dt=float(z["dt_setup"]) if "dt_setup" in z.files else dt)
+    if "ca_advance" in z.files:
+        h.caAdvance = int(z["ca_advance"])
+    h.target = m.seed
+    rec = z["rec"]
+    n, stride = int(z["nsteps"]), int(z["stride"])
+    h.record(rec, stride, n // stride + 1)
+    h.reinit(dt)
+    cas = [h.ca()[rec]] if len(m.pool_compt) else []
+    if cas:
+        for _ in range(n // stride):
+            h.process(stride)
+            cas.append(h.ca()[rec])
+    else:
+        h.process(n)
+    h.sync()
+    return z, h, h.trace(), (np.array(cas).T if cas else None)
+
+
+def test_hh_cable_golden_bit_exact():
+    z, h, vm, _ = run_golden("active_hh_cable")
+    assert vm.shape == z["vm"].shape
+    assert np.array_equal(vm, z["vm"])
+    assert np.array_equal(h.vm(), z["final_vm"])
+    g, t = h.spikes()
+    assert np.array_equal(t, z["spikes"])
+
+
+@pytest.mark.parametrize("name", ["active_branched_kca", "active_branched_caadv0"])
+def test_branched_golden_within_1e9(name):
+    z, h, vm, ca = run_golden(name)
+    ref = z["vm"]
+    assert np.all(np.abs(vm - ref) <= 1e-9 * np.maximum(np.abs(ref), 1e-3))
+    basal = 5e-5
+    assert np.all(np.abs(ca - z["ca"]) <= 1e-9 * np.maximum(np.abs(z["ca"]), basal))
+    assert len(h.spikes()[1]) == len(z["spikes"])
+
+
+def _compare_with_oracle(m, dt, nsteps, chunk, exact=True, dt_setup=None, ca_adv=1):
+    h = HSolve(m, dt=dt_setup or dt)
+    h.caAdvance = ca_adv
+    h.target = m.seed
+    h.reinit(dt)
+    oc = OracleCell(m, dt_setup or dt)
+    oc.set_ca_advance(ca_adv)
+    oc.reinit(dt)
+    for _ in range(nsteps // chunk):
+        h.process(chunk)
+        oc.step(chunk)
+        gv, ov = h.vm(), oc.vm()
+        if exact:
+            assert np.array_equal(gv, ov)
+        else:
+            assert np.all(np.abs(gv - ov) <= 1e-9 * np.maximum(np.abs(ov), 1e-3))
+    return h, oc
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_trees_bit_exact(seed):
+    """HH cells on random trees with junctions of rank up to 5."""
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.integers(2, 400))
+    parent, d, L = models.branched_morphology(rng, n, 0.6, 6)
+    m = models.active_cell(parent, d, L, inject=0.6e-9, gca=15.0, gkca=0.0)
+    # drop the 2-D channel so the whole path is libm-free
+    for k in list(vars(m)):
+        if k.startswith("c2d_"):
+            setattr(m, k, getattr(m, k)[:0])
+    m.gates2d = []
+    m.seed = int(rng.integers(0, n))
+    _compare_with_oracle(m, 25e-6, 600, 150)
+
+
+def test_reference_unit_cells_bit_exact():
+    """The nine unit-test cells of hsolve/HinesMatrix.cpp as passive models."""
+    import json
+    cells = json.load(open(os.path.join(GOLDEN, "passive_kat.json")))["cells"][:9]
+    for c in cells:
+        ch = c["children"]
+        n = len(ch)
+        parent = np.full(n, -1, np.int32)
+        for p, kids in enumerate(ch):
+            for k in kids:
+                parent[k] = p
+        i = np.arange(n, dtype=float)
+        m = CellModel(parent=parent, Ra=15.0 + 3.0 * i, Rm=45.0 + 15.0 * i, Cm=500.0 + 200.0 * i * i,
+                      Em=np.full(n, -0.06), initVm=-0.06 + 0.01 * i, Vm=-0.06 + 0.01 * i,
+                      inject=np.zeros(n), seed=int(np.argmax(parent < 0)))
+        _compare_with_oracle(m, 1.0, 20, 1)
+
+
+def test_field_writes_match_oracle():
+    m = models.config1_cell(n_cable=30)
+    dt = 25e-6
+    h, oc = _compare_with_oracle(m, dt, 200, 100)
+    for obj in ((HS_KIND_COMPT, "Cm", 3, 2e-12), (HS_KIND_COMPT, "Em", 5, -0.07),
+                (HS_KIND_COMPT, "Rm", 7, 3e9), (HS_KIND_COMPT, "inject", 0, 0.3e-9),
+                (HS_KIND_COMPT, "Vm", 11, -0.02), (HS_KIND_CHAN, "Gbar", 4, 1e-8),
+                (HS_KIND_CHAN, "X", 9, 0.5), (HS_KIND_CHAN, "modulation", 1, 1.5)):
+        kind, f, i, v = obj
+        h._set(kind, FIELDS[f], i, v)
+        oc.set(kind, FIELDS[f], i, v)
+    for _ in range(4):
+        h.process(50)
+        oc.step(50)
+        assert np.array_equal(h.vm(), oc.vm())
+    for kind, f, i in ((HS_KIND_COMPT, "Im", 4), (HS_KIND_CHAN, "Gk", 6), (HS_KIND_CHAN, "Ik", 6),
+                       (HS_KIND_CHAN, "Y", 0), (HS_KIND_COMPT, "Cm", 3)):
+        assert h._get(kind, FIELDS[f], i) == oc.get(kind, FIELDS[f], i)
+
+
+def test_process_in_chunks_equals_one_call():
+    m = models.config1_cell(n_cable=50)
+    a = HSolve(m, dt=25e-6); a.target = 0; a.reinit(25e-6)
+    b = HSolve(m, dt=25e-6); b.target = 0; b.reinit(25e-6)
+    a.process(3000)
+    for _ in range(30):
+        b.process(100)
+    assert np.array_equal(a.vm(), b.vm())
