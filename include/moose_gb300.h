@@ -291,17 +291,21 @@ int hs_read_spikes(HsSolver* s, uint32_t* gen, double* time, uint32_t capacity,
  * No counterpart in the reference (it runs one serial HSolve per cell).  */
 typedef struct HsBatch HsBatch;
 
+/* Launch shape of the batched kernel (0 keeps the current value).  One
+ * warp steps one cell; cells are packed over ctas_per_sm x SM-count CTAs. */
 typedef struct HsBatchTuning {
-    uint32_t threads_per_cta;   /* 0 = autotuned */
-    uint32_t warps_per_cell_max;/* 0 = autotuned */
-    uint32_t steps_per_launch;  /* 0 = autotuned */
-    uint32_t use_graph;         /* capture the dt loop as a CUDA graph */
+    uint32_t threads_per_cta;   /* multiple of 32, at most 1024 (default 256) */
+    uint32_t ctas_per_sm;       /* CTAs per SM in the single wave (default 4) */
+    uint32_t steps_per_launch;  /* dt steps per kernel launch (default 100) */
+    uint32_t use_graph;         /* capture a process() call as a CUDA graph */
 } HsBatchTuning;
 
 int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds,
                     uint32_t n_cells, double dt, int precision,
                     const HsBatchTuning* tuning, HsBatch** out);
 int hs_batch_destroy(HsBatch* b);
+/* Re-pack the cells for a new launch shape (the autotuner's knob). */
+int hs_batch_tune(HsBatch* b, const HsBatchTuning* tuning);
 int hs_batch_reinit(HsBatch* b, double clock_dt);
 int hs_batch_process(HsBatch* b, uint32_t nsteps);
 int hs_batch_sync(HsBatch* b);

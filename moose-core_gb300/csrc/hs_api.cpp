@@ -31,12 +31,17 @@ int cudaErr(cudaError_t e, const char* where) {
 }
 }  // namespace
 
+namespace hsg {
+int setLastError(int code, const std::string& msg) { return setErr(code, msg); }
+}  // namespace hsg
+
 struct HsSolver {
     int device = 0;
     cudaStream_t st = nullptr;
     CellPlan P;
     Arena arena;
     DevCell dc;
+    DevCell* dcDev = nullptr;    // device copy of dc (for the reinit kernel)
     double dt_ = 0;          // HSolve::dt_ (setup dt, clock dt after reinit)
     double clockDt = 0;
     bool reinited = false;
@@ -97,11 +102,13 @@ int hs_create(const HsCellDesc* cell, uint32_t seed, double dt, int precision, H
     }
     const uint32_t spikeCap = 1u << 16;
     Arena dry;
-    layoutCell(s->P, dry, s->dc, spikeCap, 0, 0, s->st, nullptr);
+    layoutCell(s->P, dry, s->dc, spikeCap, s->st);
+    dry.take<DevCell>(1);
     s->arena.size = dry.used + 256;
     e = cudaMalloc(&s->arena.base, s->arena.size);
     if (e == cudaSuccess) e = cudaMemsetAsync(s->arena.base, 0, s->arena.size, s->st);
-    if (e == cudaSuccess) e = layoutCell(s->P, s->arena, s->dc, spikeCap, 0, 0, s->st, nullptr);
+    if (e == cudaSuccess) e = layoutCell(s->P, s->arena, s->dc, spikeCap, s->st);
+    s->dcDev = s->arena.take<DevCell>(1);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
     if (e != cudaSuccess) {
         int rc = cudaErr(e, "device setup");
@@ -135,18 +142,14 @@ int hs_reinit(HsSolver* s, double clock_dt) {
     s->dt_ = clock_dt;            // HSolve::reinit: dt_ = p->dt
     s->clockDt = clock_dt;
     s->dc.dt = clock_dt;
-    cudaError_t e = reinitCellState(s->P, s->dc, clock_dt, s->initVm, s->injBasal, s->injPresent, s->st);
-    if (e == cudaSuccess) e = launchReinitGatesFp64(s->dc, s->st);
-    if (e == cudaSuccess && s->dc.nRec) {
-        // sample 0: a Table reading Vm at reinit
-        std::vector<double> row(s->dc.nRec);
-        for (uint32_t r = 0; r < s->dc.nRec; ++r) row[r] = s->initVm[s->recHost[r]];
-        e = cudaMemcpyAsync(s->dc.recBuf, row.data(), row.size() * 8, cudaMemcpyHostToDevice, s->st);
-        DevCtl ctl{};
-        ctl.nSamples = 1;
-        if (e == cudaSuccess) e = cudaMemcpyAsync(s->dc.ctl, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, s->st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
-    }
+    std::vector<double> sc(5 * (size_t)s->P.S + 1);
+    synConsts(s->P, clock_dt, sc.data());
+    cudaError_t e = cudaMemcpyAsync((void*)s->dc.synConst, sc.data(), 5 * (size_t)s->P.S * 8,
+                                    cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->dc.initVm, s->initVm.data(), s->P.N * 8, cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->dcDev, &s->dc, sizeof(DevCell), cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess) e = launchReinitFp64(s->dcDev, 1, s->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
     if (e != cudaSuccess) return cudaErr(e, "reinit");
     s->reinited = true;
@@ -370,7 +373,7 @@ int hs_set_field(HsSolver* s, int kind, int field, uint32_t index, double value)
             P.Rm[i] = value;
             return writeDev(s, s->dc.EmByRm + i, P.Em[i] / value);
         case HS_F_RA: P.Ra[i] = value; return HS_OK;
-        case HS_F_INITVM: s->initVm[i] = value; return HS_OK;
+        case HS_F_INITVM: s->initVm[i] = value; return HS_OK;   // used at the next reinit
         case HS_F_INJECT:
             s->injBasal[i] = value;
             s->injPresent[i] = 1;
@@ -524,6 +527,7 @@ int hs_record(HsSolver* s, const uint32_t* compts, uint32_t n, uint32_t stride, 
     if (e == cudaSuccess) e = cudaMemcpy(s->recCompt, s->recHost.data(), n * 4, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cudaErr(e, "record");
     s->dc.nRec = n;
+    s->dc.recLd = n;
     s->dc.recStride = stride;
     s->dc.recCap = capacity;
     s->dc.recCompt = s->recCompt;

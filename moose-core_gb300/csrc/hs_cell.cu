@@ -28,8 +28,7 @@ struct Uploader {
 }  // namespace
 
 cudaError_t layoutCell(const CellPlan& P, Arena& a, DevCell& c, uint32_t spikeCap,
-                       uint32_t recCap, uint32_t nRec, cudaStream_t st,
-                       std::vector<void*>* /*pinnedKeep*/) {
+                       cudaStream_t st, const CellShared* sh) {
     Uploader u{a, st};
     const uint32_t N = P.N, H = P.H;
     std::memset(&c, 0, sizeof(c));
@@ -40,6 +39,9 @@ cudaError_t layoutCell(const CellPlan& P, Arena& a, DevCell& c, uint32_t spikeCa
     c.caAdvance = 1;
     c.dt = P.dtSetup;
     c.V = u.put(P.V0);
+    c.initVm = sh ? sh->initVm : u.put(P.initVm);
+    c.synConst = sh ? sh->synConst : u.zeros<double>(5 * (size_t)P.S);
+    c.c2dX0 = u.put(P.c2dX0);
     c.VMid = u.zeros<double>(N);
     {
         std::vector<double> M(3 * (size_t)N + H, 0.0);
@@ -98,23 +100,30 @@ cudaError_t layoutCell(const CellPlan& P, Arena& a, DevCell& c, uint32_t spikeCa
     c.iCa = u.zeros<double>(P.P);
     c.feedPtr = u.put(P.feedPtr);
     c.feedChan = u.put(P.feedChan);
-    c.vTab = u.put(P.vTable.data);
+    c.vTab = sh ? sh->vTab : u.put(P.vTable.data);
     c.vCol = P.vTable.nCol; c.vMin = P.vTable.min; c.vMax = P.vTable.max; c.vDx = P.vTable.dx;
-    c.caTab = u.put(P.caTable.data);
+    c.caTab = sh ? sh->caTab : u.put(P.caTable.data);
     c.caCol = P.caTable.nCol; c.caMin = P.caTable.min; c.caMax = P.caTable.max; c.caDx = P.caTable.dx;
     {
         std::vector<double> AB, geom;
         std::vector<uint64_t> off;
         std::vector<uint32_t> nn;
         for (const Gate2D& g : P.gates2d) {
-            off.push_back(AB.size());
-            AB.insert(AB.end(), g.AB.begin(), g.AB.end());
+            if (!sh) {
+                off.push_back(AB.size());
+                AB.insert(AB.end(), g.AB.begin(), g.AB.end());
+            }
             geom.insert(geom.end(), {g.xmin, g.xmax, g.ymin, g.ymax, g.invDx, g.invDy});
             nn.push_back(g.nx);
             nn.push_back(g.ny);
         }
-        c.g2dAB = u.put(AB);
-        c.g2dOff = u.put(off);
+        if (sh) {
+            c.g2dAB = sh->g2dBase;
+            c.g2dOff = u.put(sh->g2dOff);
+        } else {
+            c.g2dAB = u.put(AB);
+            c.g2dOff = u.put(off);
+        }
         c.g2dGeom = u.put(geom);
         c.g2dN = u.put(nn);
     }
@@ -163,66 +172,18 @@ cudaError_t layoutCell(const CellPlan& P, Arena& a, DevCell& c, uint32_t spikeCa
     c.stimCompt = u.put(P.stimCompt);
     c.stimValue = u.put(P.stimValue);
     c.injPresent = u.put(P.injPresent);
-    c.nRec = nRec;
+    c.nRec = 0;
     c.recStride = 1;
-    c.recCap = recCap;
-    c.recCompt = u.zeros<uint32_t>(nRec);
-    c.recBuf = u.zeros<double>((size_t)recCap * nRec);
+    c.recCap = 0;
+    c.recLd = 0;
     c.ctl = u.zeros<DevCtl>(1);
     return u.err;
 }
 
-cudaError_t reinitCellState(const CellPlan& P, const DevCell& c, double dt,
-                            const std::vector<double>& initVm, const std::vector<double>& injBasal,
-                            const std::vector<uint8_t>& injPresent, cudaStream_t st) {
-    cudaError_t e = cudaSuccess;
-    auto up = [&](void* dst, const void* src, size_t bytes) {
-        if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
-    };
-    auto zero = [&](void* dst, size_t bytes) {
-        if (e == cudaSuccess && bytes) e = cudaMemsetAsync(dst, 0, bytes, st);
-    };
-    // staged host copies must live until the copies ran: keep them static per call
-    // by synchronising at the end.
-    std::vector<double> xc1(P.S), xc2(P.S), yc1(P.S), yc2(P.S), norm(P.S);
+void synConsts(const CellPlan& P, double dt, double* out) {
     for (uint32_t k = 0; k < P.S; ++k)
-        synchanConstants(P.synTau1[k], P.synTau2[k], P.synGbar[k], dt, &xc1[k], &xc2[k], &yc1[k],
-                         &yc2[k], &norm[k]);
-    up(c.synXc1, xc1.data(), P.S * 8);
-    up(c.synXc2, xc2.data(), P.S * 8);
-    up(c.synYc1, yc1.data(), P.S * 8);
-    up(c.synYc2, yc2.data(), P.S * 8);
-    up(c.synNorm, norm.data(), P.S * 8);
-    zero(c.synX, P.S * 8);
-    zero(c.synY, P.S * 8);
-    zero(c.synAct, P.S * 8);
-    zero(c.synGk, P.S * 8);
-    up(c.evCur, P.evPtr.data(), P.S * 4);
-    up(c.c2dX, P.c2dX0.data(), P.K2 * 8);
-    zero(c.c2dGk, P.K2 * 8);
-    std::vector<double> vm(P.K2), c1(P.K2, 0.0), c2(P.K2, 0.0);
-    for (uint32_t k = 0; k < P.K2; ++k) {
-        vm[k] = initVm[P.c2dCompt[k]];
-        if (P.c2dConc1[k] >= 0) c1[k] = P.CaBasal[P.c2dConc1[k]];
-        if (P.c2dConc2[k] >= 0) c2[k] = P.CaBasal[P.c2dConc2[k]];
-    }
-    up(c.c2dVm, vm.data(), P.K2 * 8);
-    up(c.c2dC1, c1.data(), P.K2 * 8);
-    up(c.c2dC2, c2.data(), P.K2 * 8);
-    zero(c.ext, 2 * (size_t)P.N * 8);
-    std::vector<double> last(P.SG);
-    for (uint32_t k = 0; k < P.SG; ++k) last[k] = -P.sgRefract[k];
-    up(c.sgLast, last.data(), P.SG * 8);
-    up(c.V, initVm.data(), P.N * 8);
-    zero(c.iCa, P.P * 8);
-    zero(c.c, P.P * 8);
-    up(c.ca, P.CaBasal.data(), P.P * 8);
-    up(c.injBasal, injBasal.data(), P.N * 8);
-    up(c.injPresent, injPresent.data(), P.N);
-    zero(c.injVarying, P.N * 8);
-    zero(c.ctl, sizeof(DevCtl));
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    return e;
+        synchanConstants(P.synTau1[k], P.synTau2[k], P.synGbar[k], dt, out + 5 * k, out + 5 * k + 1,
+                         out + 5 * k + 2, out + 5 * k + 3, out + 5 * k + 4);
 }
 
 }  // namespace hsg

@@ -26,17 +26,29 @@ struct Arena {
 
 // Lays out (dry run with base == nullptr to size the arena) and uploads one
 // cell; fills `dc`.  Static arrays are copied with cudaMemcpyAsync on `st`.
+// A batch passes `shared`: device arrays it owns (initVm and SynChan
+// constants of all cells contiguous, for one-copy reinit) and rate tables
+// shared by the cells that have identical ones.
+struct CellShared {
+    double* initVm = nullptr;
+    double* synConst = nullptr;
+    const double* vTab = nullptr;
+    const double* caTab = nullptr;
+    const double* g2dBase = nullptr;
+    std::vector<uint64_t> g2dOff;    // per gate2d of the cell, offset from g2dBase
+};
 cudaError_t layoutCell(const CellPlan& P, Arena& a, DevCell& dc, uint32_t spikeCap,
-                       uint32_t recCap, uint32_t nRec, cudaStream_t st,
-                       std::vector<void*>* pinnedKeep);
+                       cudaStream_t st, const CellShared* shared = nullptr);
 
-// Host-side reinit of one cell's device state (HSolveActive::reinit plus the
-// tick-1/4 objects' reinit); gates are set by the reinit kernel afterwards.
-cudaError_t reinitCellState(const CellPlan& P, const DevCell& dc, double clockDt,
-                            const std::vector<double>& initVm, const std::vector<double>& injBasal,
-                            const std::vector<uint8_t>& injPresent, cudaStream_t st);
+// SynChan reinit constants of one cell at the clock dt, 5 per SynChan
+// (xc1, xc2, yc1, yc2, norm), computed with the host libm as the reference does.
+void synConsts(const CellPlan& P, double dt, double* out);
 
 cudaError_t launchStepFp64(const DevCell& c, uint32_t nsteps, cudaStream_t st);
-cudaError_t launchReinitGatesFp64(const DevCell& c, cudaStream_t st);
+// HSolveActive::reinit + tick-1/4 object reinit of `nCells` cells, on device.
+cudaError_t launchReinitFp64(const DevCell* cells, uint32_t nCells, cudaStream_t st);
+cudaError_t launchBatchStepFp64(const DevCell* cells, const uint32_t* warpCellPtr,
+                                const uint32_t* warpCells, uint32_t nWarps, uint32_t nsteps,
+                                uint32_t threadsPerCta, cudaStream_t st);
 
 }  // namespace hsg

@@ -33,6 +33,7 @@ struct DevCell {
     double dt;                   // clock dt
     // compartments
     double *V, *VMid, *M, *HJ0, *HS2, *CmByDt, *EmByRm, *injBasal, *injVarying, *ext, *prevExt;
+    double* initVm;              // reinit values (HSolveActive::reinitCompartments)
     const uint32_t *chanPtr, *poolPtr, *extPtr;
     const int32_t* extList;
     // elimination programs
@@ -63,9 +64,11 @@ struct DevCell {
     const uint32_t* c2dCompt;
     const int32_t *c2dGate, *c2dDep0, *c2dDep1, *c2dConc1, *c2dConc2, *c2dInstant;
     double *c2dGbar, *c2dEk, *c2dXpow, *c2dMod, *c2dX, *c2dGk, *c2dVm, *c2dC1, *c2dC2;
+    const double* c2dX0;         // X at reinit
     // SynChans
     const uint32_t* synCompt;
     double *synEk, *synMod, *synX, *synY, *synAct, *synGk, *synXc1, *synXc2, *synYc1, *synYc2, *synNorm;
+    const double* synConst;      // per SynChan: xc1, xc2, yc1, yc2, norm at the clock dt
     const uint32_t* evPtr;
     uint32_t* evCur;
     const double *evTime, *evW;
@@ -81,7 +84,7 @@ struct DevCell {
     const double* stimValue;
     uint8_t* injPresent;
     // trace recording
-    uint32_t nRec, recStride, recCap;
+    uint32_t nRec, recStride, recCap, recLd;
     const uint32_t* recCompt;
     double* recBuf;
     DevCtl* ctl;

@@ -190,40 +190,39 @@ __device__ __forceinline__ void poolStep(const DevCell& c, uint32_t p) {
     c.iCa[p] = 0.0;
 }
 
-__global__ void __launch_bounds__(256) hsStepFp64(DevCell c, uint32_t nsteps) {
-    const uint32_t tid = threadIdx.x, nth = blockDim.x;
-    __shared__ unsigned long long s_step;
-    __shared__ uint32_t s_stim, s_spk, s_smp;
-    if (tid == 0) {
-        s_step = c.ctl->nSteps;
-        s_stim = c.ctl->stimPtr;
-        s_spk = c.ctl->nSpikes;
-        s_smp = c.ctl->nSamples;
-    }
-    __syncthreads();
-    for (uint32_t s = 0; s < nsteps; ++s) {
-        const unsigned long long step = s_step;
+// One cell, `nsteps` steps, executed by a group of `nth` threads (a whole
+// CTA for the drop-in, one warp for the batch).  `barrier` orders the phases.
+template <bool WARP>
+__device__ __forceinline__ void groupSync() {
+    if (WARP) __syncwarp();
+    else __syncthreads();
+}
+
+template <bool WARP>
+__device__ void stepCell(const DevCell& c, uint32_t nsteps, uint32_t tid, uint32_t nth) {
+    unsigned long long step = c.ctl->nSteps;
+    uint32_t stimPtr = c.ctl->stimPtr, nSpikes = c.ctl->nSpikes, nSamples = c.ctl->nSamples;
+    groupSync<WARP>();
+    for (uint32_t s = 0; s < nsteps; ++s, ++step) {
         const double currTime = c.dt * (double)(step + 1);   // Clock: dt_ * endStep
         if (tid == 0) {
-            uint32_t sp = s_stim;
-            while (sp < c.nStim && c.stimStep[sp] <= step) {
-                uint32_t h = c.stimCompt[sp];
+            while (stimPtr < c.nStim && c.stimStep[stimPtr] <= step) {
+                uint32_t h = c.stimCompt[stimPtr];
                 c.injPresent[h] = 1;
-                c.injBasal[h] = c.stimValue[sp];
-                ++sp;
+                c.injBasal[h] = c.stimValue[stimPtr];
+                ++stimPtr;
             }
-            s_stim = sp;
         }
         for (uint32_t k = tid; k < c.S; k += nth) synchanStep(c, k, currTime);
         for (uint32_t k = tid; k < c.K2; k += nth) chan2dStep(c, k);
-        __syncthreads();
+        groupSync<WARP>();
         for (uint32_t h = tid; h < c.H; h += nth) c.M[2 * c.N + h] = c.HJ0[h];
         for (uint32_t ic = tid; ic < c.N; ic += nth) comptStep(c, ic);
-        __syncthreads();
-        if (tid < 32) eliminateWarp(c, tid);
-        __syncthreads();
+        groupSync<WARP>();
+        if (WARP || tid < 32) eliminateWarp(c, tid & 31);
+        groupSync<WARP>();
         for (uint32_t p = tid; p < c.P; p += nth) poolStep(c, p);
-        __syncthreads();
+        groupSync<WARP>();
         // sendValues for the next step's tick-4 objects; SpikeGens; traces
         for (uint32_t k = tid; k < c.K2; k += nth) {
             c.c2dVm[k] = c.V[c.c2dCompt[k]];
@@ -236,12 +235,11 @@ __global__ void __launch_bounds__(256) hsStepFp64(DevCell c, uint32_t nsteps) {
                 if (V > c.sgThreshold[k]) {
                     if ((currTime + c.dt / 2.0) >= (c.sgLast[k] + c.sgRefract[k])) {
                         if (!(c.sgEdge[k] && c.sgFired[k])) {
-                            uint32_t n = s_spk;
-                            if (n < c.spikeCap) {
-                                c.spikeGen[n] = k;
-                                c.spikeTime[n] = currTime;
+                            if (nSpikes < c.spikeCap) {
+                                c.spikeGen[nSpikes] = k;
+                                c.spikeTime[nSpikes] = currTime;
                             }
-                            s_spk = n + 1;
+                            ++nSpikes;
                             c.sgLast[k] = currTime;
                             c.sgFired[k] = 1;
                         }
@@ -252,61 +250,127 @@ __global__ void __launch_bounds__(256) hsStepFp64(DevCell c, uint32_t nsteps) {
             }
         }
         if (c.nRec && ((step + 1) % c.recStride) == 0) {
-            uint32_t smp = s_smp;
-            if (smp < c.recCap)
+            if (nSamples < c.recCap)
                 for (uint32_t r = tid; r < c.nRec; r += nth)
-                    c.recBuf[(size_t)smp * c.nRec + r] = c.V[c.recCompt[r]];
+                    c.recBuf[(size_t)nSamples * c.recLd + r] = c.V[c.recCompt[r]];
+            ++nSamples;
         }
         for (uint32_t ic = tid; ic < c.N; ic += nth) {
             c.injVarying[ic] = 0.0;
             c.ext[2 * ic] = 0.0;
             c.ext[2 * ic + 1] = 0.0;
         }
-        __syncthreads();
-        if (tid == 0) {
-            if (c.nRec && ((step + 1) % c.recStride) == 0) s_smp = s_smp + 1;
-            s_step = step + 1;
-        }
-        __syncthreads();
+        groupSync<WARP>();
     }
     if (tid == 0) {
-        c.ctl->nSteps = s_step;
-        c.ctl->stimPtr = s_stim;
-        c.ctl->nSpikes = s_spk;
-        c.ctl->nSamples = s_smp;
+        c.ctl->nSteps = step;
+        c.ctl->stimPtr = stimPtr;
+        c.ctl->nSpikes = nSpikes;
+        c.ctl->nSamples = nSamples;
     }
 }
 
-// Reinit of gate states (HSolveActive::reinitChannels), one thread per
-// compartment, after V and ca were set on the host side.
-__global__ void hsReinitGatesFp64(DevCell c) {
-    for (uint32_t ic = blockIdx.x * blockDim.x + threadIdx.x; ic < c.N; ic += gridDim.x * blockDim.x) {
-        Row vRow = tableRow(c.V[ic], c.vMin, c.vMax, c.vDx, c.vCol);
-        for (uint32_t q = c.chanPtr[ic]; q < c.chanPtr[ic + 1]; ++q) {
-            int32_t s = c.stateOff[q];
-            double C1, C2;
-            if (c.Xpow[q] > 0.0) {
-                tableLookup(c.vTab, c.vCol, c.colX[q], vRow, C1, C2);
-                c.state[s++] = C1 / C2;
-            }
-            if (c.Ypow[q] > 0.0) {
-                tableLookup(c.vTab, c.vCol, c.colY[q], vRow, C1, C2);
-                c.state[s++] = C1 / C2;
-            }
-            if (c.Zpow[q] > 0.0) {
-                int32_t src = c.zSrc[q];
-                if (src >= 0) {
-                    Row r = tableRow(c.ca[src], c.caMin, c.caMax, c.caDx, c.caCol);
-                    tableLookup(c.caTab, c.caCol, c.colZ[q], r, C1, C2);
-                } else if (c.extCa[q] > 0) {
-                    Row r = tableRow(c.extCa[q], c.caMin, c.caMax, c.caDx, c.caCol);
-                    tableLookup(c.caTab, c.caCol, c.colZ[q], r, C1, C2);
-                } else {
-                    tableLookup(c.vTab, c.vCol, c.colZ[q], vRow, C1, C2);
-                }
-                c.state[s] = C1 / C2;
-            }
+__global__ void __launch_bounds__(256) hsStepFp64(DevCell c, uint32_t nsteps) {
+    stepCell<false>(c, nsteps, threadIdx.x, blockDim.x);
+}
+
+// Batched FP64: one warp per cell, cells listed per warp (packed by size).
+__global__ void __launch_bounds__(256) hsBatchStepFp64(const DevCell* __restrict__ cells,
+                                                       const uint32_t* __restrict__ warpCellPtr,
+                                                       const uint32_t* __restrict__ warpCells,
+                                                       uint32_t nWarps, uint32_t nsteps) {
+    uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t lane = threadIdx.x & 31;
+    if (w >= nWarps) return;
+    for (uint32_t k = warpCellPtr[w]; k < warpCellPtr[w + 1]; ++k) {
+        const DevCell& c = cells[warpCells[k]];
+        stepCell<true>(c, nsteps, lane, 32);
+    }
+}
+
+__device__ void reinitGatesCompt(const DevCell& c, uint32_t ic) {
+    Row vRow = tableRow(c.V[ic], c.vMin, c.vMax, c.vDx, c.vCol);
+    for (uint32_t q = c.chanPtr[ic]; q < c.chanPtr[ic + 1]; ++q) {
+        int32_t s = c.stateOff[q];
+        double C1, C2;
+        if (c.Xpow[q] > 0.0) {
+            tableLookup(c.vTab, c.vCol, c.colX[q], vRow, C1, C2);
+            c.state[s++] = C1 / C2;
         }
+        if (c.Ypow[q] > 0.0) {
+            tableLookup(c.vTab, c.vCol, c.colY[q], vRow, C1, C2);
+            c.state[s++] = C1 / C2;
+        }
+        if (c.Zpow[q] > 0.0) {
+            int32_t src = c.zSrc[q];
+            if (src >= 0) {
+                Row r = tableRow(c.ca[src], c.caMin, c.caMax, c.caDx, c.caCol);
+                tableLookup(c.caTab, c.caCol, c.colZ[q], r, C1, C2);
+            } else if (c.extCa[q] > 0) {
+                Row r = tableRow(c.extCa[q], c.caMin, c.caMax, c.caDx, c.caCol);
+                tableLookup(c.caTab, c.caCol, c.colZ[q], r, C1, C2);
+            } else {
+                tableLookup(c.vTab, c.vCol, c.colZ[q], vRow, C1, C2);
+            }
+            c.state[s] = C1 / C2;
+        }
+    }
+}
+
+// HSolveActive::reinit (hsolve/HSolveActiveSetup.cpp:43-160) and the reinit
+// of the tick-1/4 objects (SynChan::vReinit, SimpleSynHandler::vReinit with
+// the description's events queued again, HHChannel2D X), one warp per cell.
+__global__ void hsReinitFp64(const DevCell* __restrict__ cells, uint32_t nCells) {
+    uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t lane = threadIdx.x & 31;
+    if (w >= nCells) return;
+    const DevCell& c = cells[w];
+    for (uint32_t k = lane; k < c.S; k += 32) {
+        c.synXc1[k] = c.synConst[5 * k];
+        c.synXc2[k] = c.synConst[5 * k + 1];
+        c.synYc1[k] = c.synConst[5 * k + 2];
+        c.synYc2[k] = c.synConst[5 * k + 3];
+        c.synNorm[k] = c.synConst[5 * k + 4];
+        c.synX[k] = 0.0;
+        c.synY[k] = 0.0;
+        c.synAct[k] = 0.0;
+        c.synGk[k] = 0.0;
+        c.evCur[k] = c.evPtr[k];
+    }
+    for (uint32_t i = lane; i < c.N; i += 32) {
+        c.V[i] = c.initVm[i];
+        c.ext[2 * i] = 0.0;
+        c.ext[2 * i + 1] = 0.0;
+        c.injVarying[i] = 0.0;
+    }
+    for (uint32_t k = lane; k < c.SG; k += 32) c.sgLast[k] = -c.sgRefract[k];
+    for (uint32_t p = lane; p < c.P; p += 32) {
+        c.iCa[p] = 0.0;
+        c.c[p] = 0.0;
+        c.ca[p] = c.CaBasal[p];
+    }
+    if (lane == 0) {
+        c.ctl->nSteps = 0;
+        c.ctl->stimPtr = 0;
+        c.ctl->nSpikes = 0;
+        c.ctl->nSamples = 0;
+        c.ctl->err = 0;
+    }
+    __syncwarp();
+    // sendValues: the tick-4 objects see initVm and CaBasal
+    for (uint32_t k = lane; k < c.K2; k += 32) {
+        c.c2dX[k] = c.c2dX0[k];
+        c.c2dGk[k] = 0.0;
+        c.c2dVm[k] = c.V[c.c2dCompt[k]];
+        c.c2dC1[k] = c.c2dConc1[k] >= 0 ? c.ca[c.c2dConc1[k]] : 0.0;
+        c.c2dC2[k] = c.c2dConc2[k] >= 0 ? c.ca[c.c2dConc2[k]] : 0.0;
+    }
+    for (uint32_t ic = lane; ic < c.N; ic += 32) reinitGatesCompt(c, ic);
+    // a Table reading Vm at reinit records sample 0
+    if (c.nRec && c.recCap) {
+        for (uint32_t r = lane; r < c.nRec; r += 32) c.recBuf[r] = c.V[c.recCompt[r]];
+        __syncwarp();
+        if (lane == 0) c.ctl->nSamples = 1;
     }
 }
 
@@ -315,10 +379,17 @@ cudaError_t launchStepFp64(const DevCell& c, uint32_t nsteps, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launchReinitGatesFp64(const DevCell& c, cudaStream_t st) {
-    uint32_t blocks = (c.N + 255) / 256;
-    if (blocks == 0) blocks = 1;
-    hsReinitGatesFp64<<<blocks, 256, 0, st>>>(c);
+cudaError_t launchBatchStepFp64(const DevCell* cells, const uint32_t* warpCellPtr,
+                                const uint32_t* warpCells, uint32_t nWarps, uint32_t nsteps,
+                                uint32_t threadsPerCta, cudaStream_t st) {
+    uint32_t blocks = (nWarps * 32 + threadsPerCta - 1) / threadsPerCta;
+    hsBatchStepFp64<<<blocks, threadsPerCta, 0, st>>>(cells, warpCellPtr, warpCells, nWarps, nsteps);
+    return cudaGetLastError();
+}
+
+cudaError_t launchReinitFp64(const DevCell* cells, uint32_t nCells, cudaStream_t st) {
+    uint32_t blocks = (nCells * 32 + 255) / 256;
+    hsReinitFp64<<<blocks ? blocks : 1, 256, 0, st>>>(cells, nCells);
     return cudaGetLastError();
 }
 

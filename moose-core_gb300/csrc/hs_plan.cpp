@@ -49,7 +49,9 @@ bool walkTree(const HsCellDesc& d, const Adj& ch, uint32_t seed, std::vector<uin
     std::vector<int64_t> adj;
     adjacent(d, ch, seed, -1, adj);
     if (adj.size() > 1) {
+        uint32_t guard = 0;
         while (!adj.empty()) {
+            if (++guard > d.n_compt) return false;   // a cycle: not a tree
             int64_t previous = seed;
             seed = (uint32_t)adj[0];
             adj.clear();
@@ -142,7 +144,8 @@ void synchanConstants(double tau1, double tau2, double gbar, double dt, double* 
     }
 }
 
-bool buildPlan(const HsCellDesc& d, uint32_t seed, double dt, CellPlan& P, std::string& err) {
+bool buildPlan(const HsCellDesc& d, uint32_t seed, double dt, CellPlan& P, std::string& err,
+               const PlanOptions& opt) {
     auto fail = [&](const std::string& m) { err = m; return false; };
     if (d.n_compt == 0) return fail("cell has no compartments");
     if (seed >= d.n_compt) return fail("seed compartment index out of range");
@@ -599,10 +602,14 @@ bool buildPlan(const HsCellDesc& d, uint32_t seed, double dt, CellPlan& P, std::
         G2.nx = t.xdivs + 1; G2.ny = t.ydivs + 1;
         G2.invDx = (double)t.xdivs / (t.xmax - t.xmin);
         G2.invDy = (double)t.ydivs / (t.ymax - t.ymin);
-        G2.AB.resize((size_t)G2.nx * G2.ny * 2);
-        for (size_t i = 0; i < (size_t)G2.nx * G2.ny; ++i) {
-            G2.AB[2 * i] = t.A[i];
-            G2.AB[2 * i + 1] = t.B[i];
+        G2.srcA = t.A;
+        G2.srcB = t.B;
+        if (opt.copyTables2d) {
+            G2.AB.resize((size_t)G2.nx * G2.ny * 2);
+            for (size_t i = 0; i < (size_t)G2.nx * G2.ny; ++i) {
+                G2.AB[2 * i] = t.A[i];
+                G2.AB[2 * i + 1] = t.B[i];
+            }
         }
         P.gates2d.push_back(std::move(G2));
     }

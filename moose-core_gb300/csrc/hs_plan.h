@@ -44,7 +44,12 @@ struct Table {
 struct Gate2D {
     double xmin, xmax, ymin, ymax, invDx, invDy;
     uint32_t nx, ny;           // xdivs+1, ydivs+1
-    std::vector<double> AB;    // interleaved A,B: [(ix*ny+iy)*2 + {0,1}]
+    const double *srcA, *srcB; // the description's tables (identity for sharing)
+    std::vector<double> AB;    // interleaved A,B: [(ix*ny+iy)*2 + {0,1}] (if copied)
+};
+
+struct PlanOptions {
+    bool copyTables2d = true;  // batches share 2-D tables and skip the copy
 };
 
 struct CellPlan {
@@ -105,7 +110,8 @@ struct CellPlan {
 };
 
 // Build the plan; returns false and sets err on invalid input.
-bool buildPlan(const HsCellDesc& d, uint32_t seed, double dt, CellPlan& plan, std::string& err);
+bool buildPlan(const HsCellDesc& d, uint32_t seed, double dt, CellPlan& plan, std::string& err,
+               const PlanOptions& opt = PlanOptions());
 
 // SynChan reinit constants (biophysics/SynChan.cpp:171-251), host libm.
 void synchanConstants(double tau1, double tau2, double gbar, double dt, double* xc1,

@@ -56,6 +56,7 @@ def load(build_if_missing=True):
         "hs_batch_create": (i32, [C.POINTER(HsCellDesc), pu, u32, d, i32, C.POINTER(HsBatchTuning),
                                   C.POINTER(vp)]),
         "hs_batch_destroy": (i32, [vp]),
+        "hs_batch_tune": (i32, [vp, C.POINTER(HsBatchTuning)]),
         "hs_batch_reinit": (i32, [vp, d]),
         "hs_batch_process": (i32, [vp, u32]),
         "hs_batch_sync": (i32, [vp]),

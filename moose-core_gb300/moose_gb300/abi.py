@@ -70,7 +70,7 @@ class HsCellDesc(C.Structure):
 
 
 class HsBatchTuning(C.Structure):
-    _fields_ = [("threads_per_cta", C.c_uint32), ("warps_per_cell_max", C.c_uint32),
+    _fields_ = [("threads_per_cta", C.c_uint32), ("ctas_per_sm", C.c_uint32),
                 ("steps_per_launch", C.c_uint32), ("use_graph", C.c_uint32)]
 
 

@@ -1,0 +1,112 @@
+"""Batched HSolve: many cells stepped by one persistent kernel.
+
+Each cell is set up exactly like the drop-in ``HSolve`` (same Hines setup,
+same reinit semantics).  ``precision=HS_PREC_FP64`` keeps the drop-in's exact
+arithmetic (bit-identical results); ``HS_PREC_MIXED`` runs gates, tables,
+synapses and Ca pools in FP32 with an FP64 matrix and solve.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _native
+from .abi import HS_PREC_FP64, HsBatchTuning, HsCellDesc
+
+
+class Batch:
+    def __init__(self, cells, dt, precision=HS_PREC_FP64, seeds=None, threads_per_cta=0,
+                 ctas_per_sm=0, steps_per_launch=0, use_graph=True):
+        self.cells = list(cells)
+        self.n = len(self.cells)
+        descs = (HsCellDesc * self.n)()
+        for i, m in enumerate(self.cells):
+            descs[i] = m.desc()
+        self._descs = descs
+        seeds = np.ascontiguousarray([m.seed for m in self.cells] if seeds is None else seeds, np.uint32)
+        self._seeds = seeds
+        tun = HsBatchTuning(threads_per_cta, ctas_per_sm, steps_per_launch, 1 if use_graph else 0)
+        h = C.c_void_p()
+        _native.check(_native.load().hs_batch_create(descs, seeds.ctypes.data_as(C.POINTER(C.c_uint32)), self.n,
+                                                     float(dt), int(precision), C.byref(tun), C.byref(h)))
+        self._h = h
+        self.precision = precision
+        self._rec = None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _native.load().hs_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def tune(self, threads_per_cta=0, ctas_per_sm=0, steps_per_launch=0, use_graph=True):
+        t = HsBatchTuning(threads_per_cta, ctas_per_sm, steps_per_launch, 1 if use_graph else 0)
+        _native.check(_native.load().hs_batch_tune(self._h, C.byref(t)))
+
+    def reinit(self, dt):
+        _native.check(_native.load().hs_batch_reinit(self._h, float(dt)))
+
+    def process(self, nsteps):
+        _native.check(_native.load().hs_batch_process(self._h, int(nsteps)))
+
+    def sync(self):
+        _native.check(_native.load().hs_batch_sync(self._h))
+
+    def vm(self, cell):
+        out = np.empty(self.cells[cell].n_compt)
+        _native.check(_native.load().hs_batch_read_vm(self._h, cell, out.ctypes.data_as(C.POINTER(C.c_double)),
+                                                      len(out)))
+        return out
+
+    def ca(self, cell):
+        out = np.empty(len(self.cells[cell].pool_compt))
+        if len(out):
+            _native.check(_native.load().hs_batch_read_ca(self._h, cell,
+                                                          out.ctypes.data_as(C.POINTER(C.c_double)), len(out)))
+        return out
+
+    def record(self, cells, compts, stride, capacity):
+        c = np.ascontiguousarray(cells, np.uint32)
+        m = np.ascontiguousarray(compts, np.uint32)
+        self._rec = (c, m, int(capacity))
+        pu = C.POINTER(C.c_uint32)
+        _native.check(_native.load().hs_batch_record(self._h, c.ctypes.data_as(pu), m.ctypes.data_as(pu), len(c),
+                                                     int(stride), int(capacity)))
+
+    def trace(self):
+        """Samples x recorded columns, columns grouped by cell in cell order."""
+        c, m, cap = self._rec
+        out = np.empty((cap, len(c)))
+        n = C.c_uint32()
+        _native.check(_native.load().hs_batch_read_trace(self._h, out.ctypes.data_as(C.POINTER(C.c_double)), cap,
+                                                         C.byref(n)))
+        order = sorted(range(len(c)), key=lambda k: (int(c[k]), k))
+        return out[:min(n.value, cap)], [(int(c[k]), int(m[k])) for k in order]
+
+    def spikes(self):
+        L = _native.load()
+        n = C.c_uint32()
+        L.hs_batch_read_spikes(self._h, None, None, None, 0, C.byref(n))
+        cells = np.empty(n.value, np.uint32)
+        gens = np.empty(n.value, np.uint32)
+        t = np.empty(n.value)
+        pu = C.POINTER(C.c_uint32)
+        _native.check(L.hs_batch_read_spikes(self._h, cells.ctypes.data_as(pu), gens.ctypes.data_as(pu),
+                                             t.ctypes.data_as(C.POINTER(C.c_double)), n.value, C.byref(n)))
+        return cells, gens, t
+
+    def info(self):
+        nc = C.c_uint64()
+        ctas, tpc, spl = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        _native.check(_native.load().hs_batch_info(self._h, C.byref(nc), C.byref(ctas), C.byref(tpc), C.byref(spl)))
+        return dict(n_compt=nc.value, n_ctas=ctas.value, threads_per_cta=tpc.value, steps_per_launch=spl.value)
+
+    def kernel_time(self):
+        """(average ms per stepping launch, launches) since the last call."""
+        ms, n = C.c_double(), C.c_uint32()
+        _native.check(_native.load().hs_batch_kernel_time(self._h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value

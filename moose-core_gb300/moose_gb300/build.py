@@ -3,7 +3,7 @@
 Translation units:
   * ``hs_fp64.cu``  -- FP64 kernels, ``--fmad=false`` so every a*b+c stays two
     IEEE roundings, exactly as the reference CPU code computes it;
-  * ``hs_batch.cu`` -- batched kernels (FP64 and mixed precision);
+  * ``hs_mixed.cu`` -- the mixed-precision batched kernel (FMA contraction on);
   * ``hs_cell.cu``  -- device-arena upload;
   * ``hs_plan.cpp``, ``hs_api.cpp``, ``hs_batch_api.cpp`` -- host setup and
     the C ABI, ``-ffp-contract=off`` for the same reason.
@@ -33,7 +33,7 @@ def _cuda_include():
 
 UNITS = {
     "hs_fp64.cu": ["--fmad=false"],
-    "hs_batch.cu": [],
+    "hs_mixed.cu": [],
     "hs_cell.cu": ["--fmad=false"],
     "hs_plan.cpp": None,
     "hs_api.cpp": None,

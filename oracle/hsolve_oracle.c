@@ -229,7 +229,9 @@ static int walkTree(OrcCell* c, const Adj* ch, uint32_t seed) {
     ivec adj = {0};
     adjacent(d, ch, seed, -1, &adj);
     if (adj.n > 1) {
+        uint32_t guard = 0;
         while (adj.n) {
+            if (++guard > d->n_compt) { free(adj.v); return -1; }   /* a cycle */
             int64_t previous = seed;
             seed = (uint32_t)adj.v[0];
             adj.n = 0;

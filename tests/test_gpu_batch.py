@@ -1,0 +1,102 @@
+"""Batched HSolve on the GPU.
+
+FP64 batch: every cell bit-identical to its own drop-in HSolve (same
+arithmetic, one warp per cell instead of one CTA).
+Mixed batch: |dVm| <= 0.1 mV against the FP64 oracle over the whole run and
+spike times within 0.05 ms, the tolerances of the mixed-precision workload.
+"""
+import numpy as np
+import pytest
+
+from moose_gb300 import models
+from moose_gb300.abi import HS_PREC_FP64, HS_PREC_MIXED
+from moose_gb300.batch import Batch
+from moose_gb300.hsolve import HSolve
+from oracle import OracleCell
+
+pytestmark = pytest.mark.gpu
+
+DT = 25e-6
+
+
+def small_population(n_cells, seed, n_syn=0, t_end=0.05, max_children=4, lo=20, hi=300):
+    rng = np.random.default_rng(seed)
+    kA, kB = models.kca_2d_tables(vdivs=300, cadivs=300)
+    cells = []
+    for i in range(n_cells):
+        crng = np.random.default_rng([seed, i])
+        n = int(crng.integers(lo, hi))
+        parent, d, L = models.branched_morphology(crng, n, 0.5, max_children)
+        cells.append(models.active_cell(parent, d, L, inject=float(crng.uniform(0.2e-9, 1e-9)),
+                                        n_syn=n_syn, rng=crng, t_end=t_end, kca_tables=(kA, kB),
+                                        syn_rate=40.0))
+    return cells
+
+
+def test_fp64_batch_matches_dropin_bit_exact():
+    cells = small_population(12, 3, n_syn=6)
+    b = Batch(cells, DT, HS_PREC_FP64, threads_per_cta=64, ctas_per_sm=1, steps_per_launch=37)
+    b.reinit(DT)
+    b.process(400)
+    for i, m in enumerate(cells):
+        h = HSolve(m, dt=DT)
+        h.target = m.seed
+        h.reinit(DT)
+        h.process(400)
+        assert np.array_equal(b.vm(i), h.vm()), "cell %d" % i
+        assert np.array_equal(b.ca(i), h.ca()), "cell %d" % i
+
+
+def test_fp64_batch_graph_and_chunks_agree():
+    cells = small_population(5, 4)
+    a = Batch(cells, DT, HS_PREC_FP64, steps_per_launch=50, use_graph=True)
+    c = Batch(cells, DT, HS_PREC_FP64, steps_per_launch=7, use_graph=False)
+    a.reinit(DT)
+    c.reinit(DT)
+    a.process(300)
+    for _ in range(6):
+        c.process(50)
+    for i in range(len(cells)):
+        assert np.array_equal(a.vm(i), c.vm(i))
+
+
+def test_mixed_batch_within_tolerance_of_fp64_oracle():
+    cells = small_population(16, 5, n_syn=8, t_end=0.1)
+    b = Batch(cells, DT, HS_PREC_MIXED, steps_per_launch=100)
+    b.reinit(DT)
+    nsteps, chunk = 4000, 100
+    oracles = []
+    for m in cells:
+        oc = OracleCell(m, DT)
+        oc.reinit(DT)
+        oracles.append(oc)
+    worst = 0.0
+    for _ in range(nsteps // chunk):
+        b.process(chunk)
+        for i, oc in enumerate(oracles):
+            oc.step(chunk)
+            worst = max(worst, float(np.abs(b.vm(i) - oc.vm()).max()))
+    assert worst <= 1e-4, "max |dVm| = %g V" % worst
+    cell_ids, gens, t = b.spikes()
+    for i, oc in enumerate(oracles):
+        ref = oc.spikes()[1]
+        got = np.sort(t[cell_ids == i])
+        assert len(got) == len(ref), "cell %d spike count %d vs %d" % (i, len(got), len(ref))
+        if len(ref):
+            assert np.abs(got - ref).max() <= 5e-5
+
+
+def test_mixed_recording_and_tuning():
+    cells = small_population(6, 6)
+    b = Batch(cells, DT, HS_PREC_MIXED)
+    b.record([0, 0, 3, 5], [0, 4, 0, 2], 10, 51)
+    b.reinit(DT)
+    b.process(200)
+    b.tune(threads_per_cta=128, ctas_per_sm=2, steps_per_launch=25)
+    b.process(300)
+    tr, cols = b.trace()
+    assert tr.shape == (51, 4)
+    assert cols == [(0, 0), (0, 4), (3, 0), (5, 2)]
+    assert np.array_equal(tr[-1], [b.vm(c)[m] for c, m in cols])
+    ms, n = b.kernel_time()
+    assert n >= 1 and ms > 0
