@@ -1,0 +1,435 @@
+#!/usr/bin/env python3
+"""bench.py -- HSolve compartment-steps/s on GB300.
+
+Workload (one GPU): the 4,096-cell mixed-precision batch -- seeded synthetic
+cells with log-uniform 50..5,000 compartments, junctions of up to 4 children,
+HH Na/K + Ca(HVA) + K(Ca) (HHChannel2D on Vm x Ca) + CaConc on every
+compartment, 200 dual-exponential SynChans per cell driven by 5 Hz Poisson
+trains, a somatic step current, dt = 25 us.  One bench step is one chunk of
+--chunk (default 200) dt steps of all cells.  Data are synthetic (seeded);
+the working set (~1 GB of state) is larger than L2, so no L2 flush is needed.
+
+The JSON line carries:
+  value      mixed-precision batch, device-timed (CUDA events on the batch's
+             stream), inputs resident on the GPU;
+  e2e        the same through the C ABI with host buffers: every step copies
+             the somatic inject of every cell from pinned host memory and
+             reads back the somatic Vm trace of the chunk;
+  fp64_dropin the plain FP64 drop-in (one HSolve instance per cell, one CTA
+             each) on a sample of the same cells, and the ratio to `value`;
+  accuracy   max |dVm| and spike-time shift of the mixed batch against the
+             FP64 path (bit-identical to the reference HSolve) on a subset;
+  roofline   the stepping kernel against the measured HBM copy bandwidth;
+  cpu_baseline the CPU restatement of HSolve (the oracle) on the host cores.
+With --impl reference the line is the CPU HSolve on all host cores instead.
+With --gpus N (torchrun) every rank runs its own replica ("replicas only").
+"""
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "moose-core_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+DT = 25e-6
+CONFIG = 4
+SEED = 1
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the oracle (CPU restatement of HSolve), one process per core
+
+def _cpu_worker(conn, cell_ids, n_cells, t_end):
+    import numpy as np  # noqa: F401
+    from moose_gb300 import models
+    from oracle import OracleCell
+    sizes, _, _ = models.population_sizes(CONFIG, SEED, n_cells)
+    kca = models.kca_2d_tables()
+    cells = [models.make_cell(CONFIG, SEED, i, t_end=t_end, kca_tables=kca, sizes=sizes) for i in cell_ids]
+    oc = []
+    for m in cells:
+        o = OracleCell(m, DT)
+        o.reinit(DT)
+        oc.append(o)
+    ncomp = sum(m.n_compt for m in cells)
+    conn.send(("ready", ncomp))
+    while True:
+        msg = conn.recv()
+        if msg is None:
+            break
+        t0 = time.perf_counter()
+        for o in oc:
+            o.step(msg)
+        conn.send(("done", time.perf_counter() - t0))
+
+
+class CpuPool:
+    """Cells of the workload split over `workers` processes (LPT on size)."""
+
+    def __init__(self, cell_ids, n_cells, workers, t_end):
+        from moose_gb300 import models
+        sizes, _, _ = models.population_sizes(CONFIG, SEED, n_cells)
+        groups = [[] for _ in range(workers)]
+        load = [0] * workers
+        for i in sorted(cell_ids, key=lambda k: -sizes[k]):
+            w = load.index(min(load))
+            groups[w].append(i)
+            load[w] += int(sizes[i])
+        ctx = mp.get_context("spawn")
+        self.conns, self.procs = [], []
+        for g in groups:
+            if not g:
+                continue
+            a, b = ctx.Pipe()
+            p = ctx.Process(target=_cpu_worker, args=(b, g, n_cells, t_end), daemon=True)
+            p.start()
+            self.conns.append(a)
+            self.procs.append(p)
+        self.ncomp = sum(c.recv()[1] for c in self.conns)
+        self.workers = len(self.conns)
+
+    def step(self, n):
+        for c in self.conns:
+            c.send(n)
+        return max(c.recv()[1] for c in self.conns)
+
+    def close(self):
+        for c in self.conns:
+            c.send(None)
+        for p in self.procs:
+            p.join(timeout=10)
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), "--query-gpu=" + self.FIELDS,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait(timeout=10)
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.count(",") >= 6]
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[0]))
+                mx = float(r[1])
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if r[3 + k].strip().lower() == "active":
+                    reasons.add(name)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def _traffic_from_profiles():
+    """DRAM bytes per stepping launch per compartment-step from the committed
+    ncu summary, if there is one."""
+    path = os.path.join(ROOT, "profiles", "hsBatchStepMixed_4096cells.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_compartment_step:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+
+def run_reference(args, rank, world):
+    """The CPU HSolve (oracle port) on every host core, on bounded samples of
+    the workload: each step advances a fixed subset of cells by --ref-chunk dt."""
+    if rank != 0:
+        return None
+    workers = os.cpu_count() or 1
+    ids = list(range(0, args.cells, max(1, args.cells // args.ref_cells)))[: args.ref_cells]
+    t_end = (args.warmup + args.steps + 2) * args.ref_chunk * DT
+    pool = CpuPool(ids, args.cells, workers, t_end)
+    for _ in range(args.warmup):
+        pool.step(args.ref_chunk)
+    total = 0.0
+    for _ in range(args.steps):
+        total += pool.step(args.ref_chunk)
+    pool.close()
+    value = pool.ncomp * args.ref_chunk * args.steps / total
+    sample = "%d of %d cells (%d compartments) x %d dt steps per step, %d processes" % (
+        len(ids), args.cells, pool.ncomp, args.ref_chunk, pool.workers)
+    return {"metric": "compartment-steps/s", "impl": "reference", "value": value,
+            "unit": "compartment-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": "hsolve_4096cells_mixed_syn200", "cells": args.cells, "dt_s": DT,
+                       "chunk_dt_steps": args.ref_chunk},
+            "cpu_baseline": {"value": value, "unit": "compartment-steps/s", "cores": pool.workers,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "compartment-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def run_ours(args, rank, world, cpu_pool):
+    import numpy as np
+    import torch
+    from moose_gb300 import models
+    from moose_gb300.abi import HS_PREC_FP64, HS_PREC_MIXED
+    from moose_gb300.batch import Batch
+    from moose_gb300.hsolve import HSolve
+    from moose_gb300.perf import algorithmic_bytes
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    total_steps = (args.warmup + 2 * args.steps + 4) * args.chunk
+    t_end = total_steps * DT
+    kca = models.kca_2d_tables()
+    sizes, _, _ = models.population_sizes(CONFIG, SEED, args.cells)
+    cells = [models.make_cell(CONFIG, SEED, i, t_end=t_end, kca_tables=kca, sizes=sizes)
+             for i in range(args.cells)]
+    ncomp = sum(m.n_compt for m in cells)
+    b = Batch(cells, DT, HS_PREC_MIXED, steps_per_launch=args.steps_per_launch)
+    spl = b.info()["steps_per_launch"]
+    stride = 10
+    cap = total_steps // stride + 2
+    somas = np.zeros(args.cells, np.uint32)
+    b.record(np.arange(args.cells), somas, stride, cap)
+    b.inject_targets(np.arange(args.cells), somas)
+    b.reinit(DT)
+    stream = torch.cuda.ExternalStream(b.stream())
+    inj_host = torch.empty(args.cells, dtype=torch.float64).pin_memory()
+    inj_values = np.array([m.inject[0] for m in cells])
+    trace_host = torch.empty((args.chunk // stride, args.cells), dtype=torch.float64).pin_memory()
+
+    # warm-up
+    for _ in range(args.warmup):
+        b.process(args.chunk)
+    b.sync()
+    b.kernel_time()
+    # device-timed throughput, inputs resident
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        b.process(args.chunk)
+    ev1.record(stream)
+    b.sync()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    dev_ms = ev0.elapsed_time(ev1)
+    k_ms, k_n = b.kernel_time()
+    # end to end through the C ABI: inject in from pinned memory, trace out
+    if world > 1:
+        torch.distributed.barrier()
+    done = b.info()
+    first = (args.warmup + args.steps) * args.chunk // stride + 1
+    t0 = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(args.steps):
+        inj_host.copy_(torch.from_numpy(inj_values * (1.0 + 0.01 * (k % 3))))
+        b.set_inject(inj_host)
+        b.process(args.chunk)
+        b.trace_window(first, args.chunk // stride, trace_host)
+        first += args.chunk // stride
+    e1.record(stream)
+    b.sync()
+    e2e_ms = e0.elapsed_time(e1)
+    e2e_wall = time.perf_counter() - t0
+    e2e_ms = max(e2e_ms, e2e_wall * 1e3)
+    del done
+
+    def reduce_max(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    dev_ms = reduce_max(dev_ms)
+    e2e_ms = reduce_max(e2e_ms)
+    value = world * ncomp * args.chunk * args.steps / (dev_ms / 1e3)
+    e2e_value = world * ncomp * args.chunk * args.steps / (e2e_ms / 1e3)
+
+    out = None
+    if rank == 0:
+        peak, peak_kind = _peaks()
+        bytes_step, bpc = algorithmic_bytes(cells, HS_PREC_MIXED)
+        achieved = bytes_step * spl / (k_ms / 1e3) / 1e9 if k_ms > 0 else None
+        tpc = _traffic_from_profiles()
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if achieved else None,
+                "traffic": tpc * ncomp * spl if tpc else None,
+                "kernel": "hsBatchStepMixed", "algorithmic_bytes_per_compartment_step": round(bpc, 1),
+                "launch_ms": k_ms, "launches_timed": k_n, "peak_source": peak_kind}
+        # plain FP64 drop-in on a sample of the same cells: one HSolve per cell
+        dropin = None
+        if not args.skip_dropin:
+            ids = list(range(0, args.cells, max(1, args.cells // args.dropin_cells)))[: args.dropin_cells]
+            hs = []
+            for i in ids:
+                h = HSolve(cells[i], dt=DT)
+                h.target = cells[i].seed
+                h.reinit(DT)
+                hs.append(h)
+            for h in hs:
+                h.process(20)
+            for h in hs:
+                h.sync()
+            t0 = time.perf_counter()
+            for h in hs:
+                h.process(args.dropin_steps)
+            for h in hs:
+                h.sync()
+            wall = time.perf_counter() - t0
+            nc = sum(cells[i].n_compt for i in ids)
+            dv = nc * args.dropin_steps / wall
+            dropin = {"value": dv, "unit": "compartment-steps/s",
+                      "sample": "%d of %d cells as separate FP64 HSolve instances (one stream each), %d dt steps"
+                                % (len(ids), args.cells, args.dropin_steps),
+                      "mixed_batch_over_fp64_dropin": value / world / dv}
+            for h in hs:
+                h.close()
+        acc = None
+        if not args.skip_accuracy:
+            ids = list(range(0, args.cells, max(1, args.cells // args.acc_cells)))[: args.acc_cells]
+            sub = [cells[i] for i in ids]
+            f = Batch(sub, DT, HS_PREC_FP64)
+            mx = Batch(sub, DT, HS_PREC_MIXED)
+            ssub = np.zeros(len(sub), np.uint32)
+            for bb in (f, mx):
+                bb.record(np.arange(len(sub)), ssub, 1, args.acc_steps + 1)
+                bb.reinit(DT)
+                bb.process(args.acc_steps)
+                bb.sync()
+            tf, tm = f.trace()[0], mx.trace()[0]
+            dv = float(np.abs(tf - tm).max())
+            dall = max(float(np.abs(f.vm(i) - mx.vm(i)).max()) for i in range(len(sub)))
+            cf, _, sf = f.spikes()
+            cm, _, sm = mx.spikes()
+            shift, counts_equal = 0.0, True
+            for i in range(len(sub)):
+                a, bsp = np.sort(sf[cf == i]), np.sort(sm[cm == i])
+                if len(a) != len(bsp):
+                    counts_equal = False
+                elif len(a):
+                    shift = max(shift, float(np.abs(a - bsp).max()))
+            acc = {"max_abs_dVm_V": max(dv, dall), "max_spike_shift_s": shift,
+                   "spike_counts_equal": counts_equal, "spikes": int(len(sf)),
+                   "sample": "%d cells, %d dt steps, soma every step + all compartments at the end, "
+                             "mixed batch vs FP64 batch (bit-identical to the reference HSolve)"
+                             % (len(sub), args.acc_steps)}
+            f.close()
+            mx.close()
+        cpu = None
+        if cpu_pool is not None:
+            tcpu = cpu_pool.step(args.cpu_chunk)
+            tcpu += cpu_pool.step(args.cpu_chunk)
+            cv = cpu_pool.ncomp * 2 * args.cpu_chunk / tcpu
+            cpu = {"value": cv, "unit": "compartment-steps/s", "cores": cpu_pool.workers, "kind": "port",
+                   "sample": "%d compartments of the workload's cells x %d dt steps in %d processes"
+                             % (cpu_pool.ncomp, 2 * args.cpu_chunk, cpu_pool.workers)}
+        launches = args.steps * math.ceil(args.chunk / spl)
+        out = {"metric": "compartment-steps/s", "value": value, "unit": "compartment-steps/s",
+               "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+               "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "mixed (f32 channels, f64 solve)",
+               "data": "synthetic (seeded cells; working set larger than L2, no flush)",
+               "config": {"workload": "hsolve_4096cells_mixed_syn200", "cells": args.cells,
+                          "compartments": ncomp, "dt_s": DT, "chunk_dt_steps": args.chunk,
+                          "steps_per_launch": spl, "synchans_per_cell": 200, "parallelism": "replicas"},
+               "e2e": {"value": e2e_value, "unit": "compartment-steps/s",
+                       "h2d_bytes_per_step": args.cells * 8,
+                       "d2h_bytes_per_step": (args.chunk // stride) * args.cells * 8},
+               "roofline": roof, "cpu_baseline": cpu, "fp64_dropin": dropin, "accuracy": acc,
+               "clocks": clk, "gpu_launches": launches}
+    b.close()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cells", type=int, default=4096)
+    ap.add_argument("--chunk", type=int, default=200, help="dt steps per bench step")
+    ap.add_argument("--steps-per-launch", type=int, default=0)
+    ap.add_argument("--dropin-cells", type=int, default=128)
+    ap.add_argument("--dropin-steps", type=int, default=200)
+    ap.add_argument("--acc-cells", type=int, default=32)
+    ap.add_argument("--acc-steps", type=int, default=4000)
+    ap.add_argument("--cpu-cells", type=int, default=128)
+    ap.add_argument("--cpu-chunk", type=int, default=400)
+    ap.add_argument("--ref-cells", type=int, default=128)
+    ap.add_argument("--ref-chunk", type=int, default=100)
+    ap.add_argument("--skip-dropin", action="store_true")
+    ap.add_argument("--skip-accuracy", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+        if out is not None:
+            print(json.dumps(out))
+        return 0
+    # the CPU pool is spawned before the first GPU call
+    cpu_pool = None
+    if rank == 0 and not args.skip_cpu:
+        ids = list(range(0, args.cells, max(1, args.cells // args.cpu_cells)))[: args.cpu_cells]
+        cpu_pool = CpuPool(ids, args.cells, os.cpu_count() or 1, (2 * args.cpu_chunk + 2) * DT)
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    out = run_ours(args, rank, world, cpu_pool)
+    if cpu_pool is not None:
+        cpu_pool.close()
+    if out is not None:
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -316,8 +316,21 @@ int hs_batch_record(HsBatch* b, const uint32_t* cell, const uint32_t* compt,
                     uint32_t n, uint32_t stride, uint32_t capacity_samples);
 int hs_batch_read_trace(HsBatch* b, double* out, uint32_t capacity,
                         uint32_t* n_samples);
+/* Samples [first, first+count) of the recording (rows of all recorded
+ * columns), e.g. the samples of the last process() call. */
+int hs_batch_read_trace_window(HsBatch* b, uint32_t first, uint32_t count,
+                               double* out);
+/* Writing the `inject` field of many compartments between process() calls
+ * (ZombieCompartment inject -> HSolve::setInject): register the targets
+ * once, then copy one value per target from host memory (pinned memory makes
+ * the copy asynchronous); the values apply from the next step. */
+int hs_batch_inject_targets(HsBatch* b, const uint32_t* cell, const uint32_t* compt,
+                            uint32_t n);
+int hs_batch_set_inject(HsBatch* b, const double* values, uint32_t n);
 int hs_batch_read_spikes(HsBatch* b, uint32_t* cell, uint32_t* gen,
                          double* time, uint32_t capacity, uint32_t* n);
+/* The CUDA stream (a cudaStream_t) the batch runs on, for event timing. */
+int hs_batch_stream(HsBatch* b, void** stream);
 /* Statistics of the packing: compartments, cells, CTAs, launches/step. */
 int hs_batch_info(HsBatch* b, uint64_t* n_compt, uint32_t* n_ctas,
                   uint32_t* threads_per_cta, uint32_t* steps_per_launch);

@@ -38,6 +38,8 @@ cudaError_t launchBatchStepMixed(const MixBatch& b, const uint32_t* warpCellPtr,
                                  uint32_t nWarps, uint32_t nsteps, uint32_t threadsPerCta, cudaStream_t st);
 cudaError_t launchBatchReinitMixed(const MixBatch& b, const double* initVm, const float* c2dX0,
                                    const uint32_t* evStart, cudaStream_t st);
+cudaError_t launchScatterInject(double* const* addr, uint8_t* const* flag, const double* val, uint32_t n,
+                                cudaStream_t st);
 }  // namespace hsg
 
 using namespace hsg;
@@ -144,6 +146,13 @@ struct HsBatch {
     uint32_t recCap = 0, recStride = 1;
     // spikes
     uint32_t spikeCap = 1024;
+    // inject targets
+    DevBuf injBuf;
+    double** dInjAddr = nullptr;
+    uint8_t** dInjFlag = nullptr;
+    double* dInjVal = nullptr;
+    uint32_t nInjTargets = 0;
+    std::vector<std::vector<int32_t>> injEntryOf;   // mixed: per cell, compartment -> entry
     // timing: event pairs around each stepping launch
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> evs;
     size_t evUsed = 0;
@@ -447,6 +456,8 @@ int buildMixed(HsBatch* b) {
                 injVal.push_back(0.0);
             }
         R.nInj = (uint32_t)injNode.size() - R.inj0;
+        b->injEntryOf.emplace_back(P.hinesOf.size(), -1);
+        for (auto& kv : injEntry) b->injEntryOf.back()[P.modelOf[kv.first]] = (int32_t)(R.inj0 + kv.second);
         R.stim0 = (uint32_t)stimStep.size();
         for (uint32_t k = 0; k < P.stimCompt.size(); ++k) {
             stimStep.push_back(P.stimStep[k]);
@@ -493,7 +504,7 @@ int buildMixed(HsBatch* b) {
             for (uint32_t p = pb; p < pe; ++p) {
                 H.poolOf[ci][P.poolModel[p]] = (int64_t)poolC.size();
                 poolC.push_back(0.f);
-                poolF1.push_back((float)P.f1[p]);
+                poolF1.push_back((float)(1.0 - P.f1[p]));     // decay per step, in FP64
                 poolF2.push_back((float)P.f2[p]);
                 poolBasal.push_back((float)P.CaBasal[p]);
                 poolCeil.push_back((float)P.ceiling[p]);
@@ -693,11 +704,13 @@ int buildMixed(HsBatch* b) {
     m.spikeTime = D.zeros<float>((size_t)nC * b->spikeCap, st);
     m.vTab = D.up(vtab, st);
     m.vCol = V0.nCol;
+    m.vRows = V0.nPts;
     m.vMin = (float)V0.min;
     m.vMax = (float)V0.max;
     m.vInvDx = (float)(1.0 / V0.dx);
     m.caTab = D.up(catab, st);
     m.caCol = C0.nCol;
+    m.caRows = C0.nPts;
     m.caMin = (float)C0.min;
     m.caMax = (float)C0.max;
     m.caInvDx = C0.dx != 0.0 ? (float)(1.0 / C0.dx) : 0.f;
@@ -775,9 +788,10 @@ int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds, uint32_t n_c
         if (tuning->steps_per_launch) b->stepsPerLaunch = tuning->steps_per_launch;
         b->useGraph = tuning->use_graph != 0;
     }
-    if (b->threadsPerCta % 32 || b->threadsPerCta > 1024) {
+    if (b->threadsPerCta % 32 || b->threadsPerCta > 512 ||
+        (precision == HS_PREC_FP64 && b->threadsPerCta > 256)) {
         hs_batch_destroy(b);
-        return berr(HS_EINVAL, "threads_per_cta must be a multiple of 32, at most 1024");
+        return berr(HS_EINVAL, "threads_per_cta must be a multiple of 32, at most 512 (256 for FP64)");
     }
     int rc = precision == HS_PREC_FP64 ? buildFp64(b, cells) : buildMixed(b);
     if (rc == HS_OK && precision == HS_PREC_FP64) rc = uploadDcs(b);
@@ -802,6 +816,7 @@ int hs_batch_destroy(HsBatch* b) {
     b->buf.freeAll();
     b->packBuf.freeAll();
     b->recBuf.freeAll();
+    b->injBuf.freeAll();
     if (b->arena.base) cudaFree(b->arena.base);
     if (b->st) cudaStreamDestroy(b->st);
     delete b;
@@ -811,8 +826,8 @@ int hs_batch_destroy(HsBatch* b) {
 int hs_batch_tune(HsBatch* b, const HsBatchTuning* t) {
     if (!b || !t) return berr(HS_EINVAL, "null argument");
     if (t->threads_per_cta) {
-        if (t->threads_per_cta % 32 || t->threads_per_cta > 1024)
-            return berr(HS_EINVAL, "threads_per_cta must be a multiple of 32, at most 1024");
+        if (t->threads_per_cta % 32 || t->threads_per_cta > 512)
+            return berr(HS_EINVAL, "threads_per_cta must be a multiple of 32, at most 512");
         b->threadsPerCta = t->threads_per_cta;
     }
     if (t->ctas_per_sm) b->ctasPerSm = t->ctas_per_sm;
@@ -966,6 +981,12 @@ int hs_batch_kernel_time(HsBatch* b, double* avg_ms, uint32_t* launches) {
     return HS_OK;
 }
 
+int hs_batch_stream(HsBatch* b, void** stream) {
+    if (!b || !stream) return berr(HS_EINVAL, "null argument");
+    *stream = (void*)b->st;
+    return HS_OK;
+}
+
 int hs_batch_info(HsBatch* b, uint64_t* n_compt, uint32_t* n_ctas, uint32_t* threads_per_cta,
                   uint32_t* steps_per_launch) {
     if (!b) return berr(HS_EINVAL, "null batch");
@@ -1110,6 +1131,57 @@ int hs_batch_read_trace(HsBatch* b, double* out, uint32_t capacity, uint32_t* n_
         if (e != cudaSuccess) return cerr(e, "batch trace");
     }
     return HS_OK;
+}
+
+int hs_batch_read_trace_window(HsBatch* b, uint32_t first, uint32_t count, double* out) {
+    if (!b || (!out && count)) return berr(HS_EINVAL, "null argument");
+    if (b->rec.empty()) return berr(HS_ESTATE, "nothing is recorded");
+    if ((uint64_t)first + count > b->recCap) return berr(HS_ECAPACITY, "window beyond the recording capacity");
+    if (!count) return HS_OK;
+    cudaError_t e = cudaMemcpyAsync(out, b->recBase + (size_t)first * b->rec.size(),
+                                    (size_t)count * b->rec.size() * 8, cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    return e == cudaSuccess ? HS_OK : cerr(e, "trace window");
+}
+
+int hs_batch_inject_targets(HsBatch* b, const uint32_t* cell, const uint32_t* compt, uint32_t n) {
+    if (!b || (n && (!cell || !compt))) return berr(HS_EINVAL, "null argument");
+    std::vector<double*> addr(n);
+    std::vector<uint8_t*> flag(n, nullptr);
+    for (uint32_t k = 0; k < n; ++k) {
+        if (cell[k] >= b->nCells) return berr(HS_EINVAL, "inject target cell out of range");
+        const CellPlan& P = b->plans[cell[k]];
+        if (compt[k] >= P.hinesOf.size() || P.hinesOf[compt[k]] < 0)
+            return berr(HS_EINVAL, "inject target compartment not in the cell");
+        if (b->precision == HS_PREC_FP64) {
+            uint32_t h = (uint32_t)P.hinesOf[compt[k]];
+            addr[k] = b->dcs[cell[k]].injBasal + h;
+            flag[k] = b->dcs[cell[k]].injPresent + h;
+        } else {
+            int32_t e = b->injEntryOf[cell[k]][compt[k]];
+            if (e < 0)
+                return berr(HS_ENOTSUP, "mixed batch: compartment had no inject or stimulus at setup");
+            addr[k] = b->mb.injVal + e;
+        }
+    }
+    cudaStreamSynchronize(b->st);
+    b->injBuf.freeAll();
+    b->injBuf.err = cudaSuccess;
+    b->dInjAddr = b->injBuf.up(addr, b->st);
+    b->dInjFlag = b->injBuf.up(flag, b->st);
+    b->dInjVal = b->injBuf.alloc<double>(n);
+    if (b->injBuf.err == cudaSuccess) b->injBuf.err = cudaStreamSynchronize(b->st);
+    if (b->injBuf.err != cudaSuccess) return cerr(b->injBuf.err, "inject targets");
+    b->nInjTargets = n;
+    return HS_OK;
+}
+
+int hs_batch_set_inject(HsBatch* b, const double* values, uint32_t n) {
+    if (!b || (n && !values)) return berr(HS_EINVAL, "null argument");
+    if (n != b->nInjTargets) return berr(HS_EINVAL, "n must equal the registered target count");
+    cudaError_t e = cudaMemcpyAsync(b->dInjVal, values, (size_t)n * 8, cudaMemcpyHostToDevice, b->st);
+    if (e == cudaSuccess) e = launchScatterInject(b->dInjAddr, b->dInjFlag, b->dInjVal, n, b->st);
+    return e == cudaSuccess ? HS_OK : cerr(e, "set inject");
 }
 
 int hs_batch_read_spikes(HsBatch* b, uint32_t* cell, uint32_t* gen, double* time, uint32_t capacity,

@@ -54,10 +54,11 @@ struct RowF {
     float frac;
 };
 
-__device__ __forceinline__ RowF rowF(const float* T, uint32_t nCol, float x, float mn, float mx, float invDx) {
+__device__ __forceinline__ RowF rowF(const float* T, uint32_t nCol, uint32_t nRows, float x, float mn,
+                                     float mx, float invDx) {
     x = fminf(fmaxf(x, mn), mx);
     float div = (x - mn) * invDx;
-    unsigned int i = (unsigned int)div;
+    unsigned int i = min((unsigned int)div, nRows - 2);   // rows i and i+1 exist
     RowF r;
     r.frac = div - (float)i;
     r.p = T + (size_t)i * nCol;
@@ -72,8 +73,12 @@ __device__ __forceinline__ float gateF(const RowF& r, uint32_t nCol, int col, fl
     float C1 = fmaf(b.x - a.x, r.frac, a.x);
     float C2 = fmaf(b.y - a.y, r.frac, a.y);
     if (inst) return __fdividef(C1, C2);
-    float temp = fmaf(hdt, C2, 1.0f);
-    return __fdividef(fmaf(x, 2.0f - temp, dt * C1), temp);
+    // The reference's trapezoidal step (x(2-T) + dt C1)/T with T = 1 + h,
+    // h = dt/2 C2 (hsolve/HSolveActive.cpp:272-273), written as the
+    // increment x + (dt C1 - 2 h x)/(1 + h): the same number in exact
+    // arithmetic, but FP32 keeps the small h instead of rounding it into 1 + h.
+    float h = hdt * C2;
+    return x + __fdividef(fmaf(-2.0f * h, x, dt * C1), 1.0f + h);
 }
 
 __device__ __forceinline__ void interp2dF(const float* T, const float* geom, uint32_t nx, uint32_t ny,
@@ -103,7 +108,7 @@ __device__ __forceinline__ void nodeRow(const MixBatch& b, uint32_t n, unsigned 
     const double V = b.V[n];
     const float v = (float)V;
     const float dt = b.dtf, hdt = 0.5f * b.dtf;
-    RowF vr = rowF(b.vTab, b.vCol, v, b.vMin, b.vMax, b.vInvDx);
+    RowF vr = rowF(b.vTab, b.vCol, b.vRows, v, b.vMin, b.vMax, b.vInvDx);
     float G = 0.f, GE = 0.f;
     const uint32_t p0 = b.pool0[n], p1 = b.pool0[n + 1];
     float cg[4] = {0.f, 0.f, 0.f, 0.f}, cge[4] = {0.f, 0.f, 0.f, 0.f};
@@ -124,7 +129,7 @@ __device__ __forceinline__ void nodeRow(const MixBatch& b, uint32_t n, unsigned 
         if (t.zp) {
             float z;
             if (t.zSrc >= 0) {
-                RowF cr = rowF(b.caTab, b.caCol, b.poolCa[p0 + t.zSrc], b.caMin, b.caMax, b.caInvDx);
+                RowF cr = rowF(b.caTab, b.caCol, b.caRows, b.poolCa[p0 + t.zSrc], b.caMin, b.caMax, b.caInvDx);
                 z = gateF(cr, b.caCol, t.colZ, b.state[s], dt, hdt, t.instant & 4);
             } else {
                 z = gateF(vr, b.vCol, t.colZ, b.state[s], dt, hdt, t.instant & 4);
@@ -158,8 +163,10 @@ __device__ __forceinline__ void nodeRow(const MixBatch& b, uint32_t n, unsigned 
         float X = b.c2dX[k];
         if (t.instant & 1) X = __fdividef(A, B);
         else if (B > 1.0e-10f) {
-            float e = __expf(-B * dt);
-            X = fmaf(X, e, __fdividef(A, B) * (1.f - e));
+            // HHChannelBase::integrate, X e + (A/B)(1 - e) with e = exp(-B dt),
+            // as X + (A/B - X)(1 - e) with 1 - e = -expm1(-B dt) (no cancellation)
+            float em = -expm1f(-B * dt);
+            X = fmaf(__fdividef(A, B) - X, em, X);
         } else X = fmaf(A, dt, X);
         b.c2dX[k] = X;
         float gk = b.c2dGbar[k] * powi(X, t.xp, t.xpf);
@@ -201,21 +208,29 @@ __device__ void stepCellMixed(const MixBatch& b, uint32_t cell, uint32_t nsteps,
             }
         }
         __syncwarp();
-        // forward: assembly + elimination, deepest level first
+        // assembly: every compartment's channels and FP64 row, in parallel;
+        // the row is staged in inv (pivot) and rhsF (right-hand side)
+        for (uint32_t i = lane; i < cr.nNodes; i += 32) {
+            const uint32_t n = base + i;
+            const uint32_t info = b.nodeInfo[n];
+            if (info & kNodeCenter) continue;
+            double d, r;
+            nodeRow(b, n, step, d, r);
+            if (info & kNodeInject)
+                for (uint32_t k = 0; k < cr.nInj; ++k)
+                    if (b.injNode[cr.inj0 + k] == i) r += b.injVal[cr.inj0 + k];
+            b.inv[n] = d;
+            b.rhsF[n] = r;
+        }
+        __syncwarp();
+        // forward elimination, deepest level first: pull the children's
+        // eliminated rows, keep 1/pivot and the eliminated rhs
         for (int L = (int)cr.nLevels - 1; L >= 0; --L) {
             for (uint32_t i = lp[L] + lane; i < lp[L + 1]; i += 32) {
                 const uint32_t n = base + i;
-                const uint32_t info = b.nodeInfo[n];
-                double d, r;
-                if (info & kNodeCenter) {
-                    d = b.HS2[n];
-                    r = 0.0;
-                } else {
-                    nodeRow(b, n, step, d, r);
-                    if (info & kNodeInject)
-                        for (uint32_t k = 0; k < cr.nInj; ++k)
-                            if (b.injNode[cr.inj0 + k] == i) r += b.injVal[cr.inj0 + k];
-                }
+                const bool center = b.nodeInfo[n] & kNodeCenter;
+                double d = center ? b.HS2[n] : b.inv[n];
+                double r = center ? 0.0 : b.rhsF[n];
                 for (uint32_t c = b.child0[n]; c < b.child0[n + 1]; ++c) {
                     const double oc = b.off[c];
                     const double f = oc * b.inv[c];
@@ -242,7 +257,9 @@ __device__ void stepCellMixed(const MixBatch& b, uint32_t cell, uint32_t nsteps,
                     const float vca = (float)(b.caAdvance == 1 ? vm : fma(2.0, vm, -Vnew));
                     for (uint32_t p = b.pool0[n]; p < b.pool0[n + 1]; ++p) {
                         float act = fmaf(-b.caG[p], vca, b.caGE[p]);
-                        float c = fmaf(b.poolF1[p], b.poolC[p], b.poolF2[p] * act);
+                        // c f1 + f2 act with f1 = 1 - g1 (g1 = 1 - f1 from FP64)
+                        float c0 = b.poolC[p];
+                        float c = fmaf(-b.poolF1[p], c0, c0) + b.poolF2[p] * act;
                         float ca = b.poolBasal[p] + c;
                         if (b.poolCeil[p] > 0.f && ca > b.poolCeil[p]) { ca = b.poolCeil[p]; c = ca - b.poolBasal[p]; }
                         if (ca < b.poolFloor[p]) { ca = b.poolFloor[p]; c = ca - b.poolBasal[p]; }
@@ -290,7 +307,7 @@ __device__ void stepCellMixed(const MixBatch& b, uint32_t cell, uint32_t nsteps,
     }
 }
 
-__global__ void __launch_bounds__(256) hsBatchStepMixed(MixBatch b, const uint32_t* __restrict__ warpCellPtr,
+__global__ void __launch_bounds__(512) hsBatchStepMixed(MixBatch b, const uint32_t* __restrict__ warpCellPtr,
                                                         const uint32_t* __restrict__ warpCells,
                                                         uint32_t nWarps, uint32_t nsteps) {
     uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -320,7 +337,7 @@ __global__ void hsBatchReinitMixed(MixBatch b, const double* __restrict__ initVm
         uint32_t n = cr.node0 + i;
         if (b.nodeInfo[n] & kNodeCenter) continue;
         float v = (float)b.V[n];
-        RowF vr = rowF(b.vTab, b.vCol, v, b.vMin, b.vMax, b.vInvDx);
+        RowF vr = rowF(b.vTab, b.vCol, b.vRows, v, b.vMin, b.vMax, b.vInvDx);
         uint32_t s = b.state0[n];
         uint32_t p0 = b.pool0[n];
         for (uint32_t q = b.chan0[n]; q < b.chan0[n + 1]; ++q) {
@@ -329,7 +346,7 @@ __global__ void hsBatchReinitMixed(MixBatch b, const double* __restrict__ initVm
             if (t.yp) b.state[s++] = gateF(vr, b.vCol, t.colY, 0.f, 0.f, 0.f, true);
             if (t.zp) {
                 if (t.zSrc >= 0) {
-                    RowF cr2 = rowF(b.caTab, b.caCol, b.poolCa[p0 + t.zSrc], b.caMin, b.caMax, b.caInvDx);
+                    RowF cr2 = rowF(b.caTab, b.caCol, b.caRows, b.poolCa[p0 + t.zSrc], b.caMin, b.caMax, b.caInvDx);
                     b.state[s++] = gateF(cr2, b.caCol, t.colZ, 0.f, 0.f, 0.f, true);
                 } else {
                     b.state[s++] = gateF(vr, b.vCol, t.colZ, 0.f, 0.f, 0.f, true);
@@ -352,6 +369,22 @@ __global__ void hsBatchReinitMixed(MixBatch b, const double* __restrict__ initVm
     if (cr.nRec)
         for (uint32_t r = lane; r < cr.nRec; r += 32)
             b.recBuf[cr.rec0 + r] = b.V[cr.node0 + b.recNode[cr.rec0 + r]];
+}
+
+// Scatter of host-supplied inject values to their solver slots.
+__global__ void hsScatterInject(double* const* __restrict__ addr, uint8_t* const* __restrict__ flag,
+                                const double* __restrict__ val, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    *addr[i] = val[i];
+    if (flag[i]) *flag[i] = 1;
+}
+
+cudaError_t launchScatterInject(double* const* addr, uint8_t* const* flag, const double* val, uint32_t n,
+                                cudaStream_t st) {
+    if (!n) return cudaSuccess;
+    hsScatterInject<<<(n + 255) / 256, 256, 0, st>>>(addr, flag, val, n);
+    return cudaGetLastError();
 }
 
 cudaError_t uploadMixedTypes(const ChanType* ct, int nct, const C2dType* kt, int nkt, const SynType* st,

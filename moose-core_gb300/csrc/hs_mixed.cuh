@@ -80,7 +80,7 @@ struct MixBatch {
     float* chanGk;               // last conductance (field read-back)
     // pools
     float *poolC, *poolCa, *caG, *caGE;
-    const float *poolF1, *poolF2, *poolBasal, *poolCeil, *poolFloor;
+    const float *poolF1, *poolF2, *poolBasal, *poolCeil, *poolFloor;   // poolF1 holds 1 - factor1
     // HHChannel2D
     const uint8_t* c2dType;
     const float* c2dGbar;        // Gbar * modulation
@@ -115,10 +115,10 @@ struct MixBatch {
     float* spikeTime;
     // rate tables (FP32): V table A/B interleaved per species
     const float* vTab;
-    uint32_t vCol;
+    uint32_t vCol, vRows;        // rows = divisions + 2 (last row repeated)
     float vMin, vMax, vInvDx;
     const float* caTab;
-    uint32_t caCol;
+    uint32_t caCol, caRows;
     float caMin, caMax, caInvDx;
     // recording
     const uint32_t* recNode;

@@ -87,6 +87,29 @@ class Batch:
         order = sorted(range(len(c)), key=lambda k: (int(c[k]), k))
         return out[:min(n.value, cap)], [(int(c[k]), int(m[k])) for k in order]
 
+    def trace_window(self, first, count, out=None):
+        """Samples [first, first+count) into `out` (a host buffer, e.g. pinned)."""
+        ncol = len(self._rec[0])
+        if out is None:
+            out = np.empty((count, ncol))
+        ptr = out.data_ptr() if hasattr(out, "data_ptr") else out.ctypes.data
+        _native.check(_native.load().hs_batch_read_trace_window(self._h, int(first), int(count), C.c_void_p(ptr)))
+        return out
+
+    def inject_targets(self, cells, compts):
+        c = np.ascontiguousarray(cells, np.uint32)
+        m = np.ascontiguousarray(compts, np.uint32)
+        self._inj = (c, m)
+        pu = C.POINTER(C.c_uint32)
+        _native.check(_native.load().hs_batch_inject_targets(self._h, c.ctypes.data_as(pu), m.ctypes.data_as(pu),
+                                                             len(c)))
+
+    def set_inject(self, values):
+        """One value per registered target; `values` may be a numpy array or a
+        pinned torch tensor (float64)."""
+        ptr = values.data_ptr() if hasattr(values, "data_ptr") else values.ctypes.data
+        _native.check(_native.load().hs_batch_set_inject(self._h, C.c_void_p(ptr), len(self._inj[0])))
+
     def spikes(self):
         L = _native.load()
         n = C.c_uint32()
@@ -98,6 +121,12 @@ class Batch:
         _native.check(L.hs_batch_read_spikes(self._h, cells.ctypes.data_as(pu), gens.ctypes.data_as(pu),
                                              t.ctypes.data_as(C.POINTER(C.c_double)), n.value, C.byref(n)))
         return cells, gens, t
+
+    def stream(self):
+        """The cudaStream_t handle (int) the batch's kernels run on."""
+        s = C.c_void_p()
+        _native.check(_native.load().hs_batch_stream(self._h, C.byref(s)))
+        return s.value or 0
 
     def info(self):
         nc = C.c_uint64()

@@ -309,6 +309,30 @@ def loguniform_int(rng, lo, hi, size):
     return np.exp(rng.uniform(math.log(lo), math.log(hi), size)).round().astype(int)
 
 
+def population_sizes(config, seed=1, n_cells=None):
+    """Compartment counts of a workload's cells (drawn before the cells)."""
+    rng = np.random.default_rng(seed)
+    if config == 2:
+        return rng.integers(100, 1001, n_cells or 256), 2, 0
+    if config in (3, 4):
+        return loguniform_int(rng, 50, 5000, n_cells or 4096), 4, (200 if config == 4 else 0)
+    raise ValueError("unknown config %r" % config)
+
+
+def make_cell(config, seed, i, n_cells=None, t_end=1.0, kca_tables=None, sizes=None):
+    """Cell i of a workload, built alone (identical to population()[i])."""
+    if sizes is None:
+        sizes, maxc, nsyn = population_sizes(config, seed, n_cells)
+    else:
+        _, maxc, nsyn = population_sizes(config, seed, 1)
+    if kca_tables is None:
+        kca_tables = kca_2d_tables()
+    crng = np.random.default_rng([seed, i])
+    parent, d, L = branched_morphology(crng, int(sizes[i]), 0.5, maxc)
+    inj = float(crng.uniform(0.1e-9, 1e-9))
+    return active_cell(parent, d, L, inject=inj, n_syn=nsyn, rng=crng, t_end=t_end, kca_tables=kca_tables)
+
+
 def population(config, seed=1, n_cells=None, t_end=1.0, kca_tables=None):
     """Cells of a named workload.
 
@@ -317,24 +341,8 @@ def population(config, seed=1, n_cells=None, t_end=1.0, kca_tables=None):
     config 4: config 3 cells + 200 SynChans each (5 Hz Poisson, tau1 1 ms,
               tau2 3 ms, weights lognormal median 0.5 nS).
     """
-    rng = np.random.default_rng(seed)
     if kca_tables is None:
         kca_tables = kca_2d_tables()
-    if config == 2:
-        n_cells = n_cells or 256
-        sizes = rng.integers(100, 1001, n_cells)
-        maxc, nsyn = 2, 0
-    elif config in (3, 4):
-        n_cells = n_cells or 4096
-        sizes = loguniform_int(rng, 50, 5000, n_cells)
-        maxc, nsyn = 4, (200 if config == 4 else 0)
-    else:
-        raise ValueError("unknown config %r" % config)
-    cells = []
-    for i in range(n_cells):
-        crng = np.random.default_rng([seed, i])
-        parent, d, L = branched_morphology(crng, int(sizes[i]), 0.5, maxc)
-        inj = float(crng.uniform(0.1e-9, 1e-9))
-        cells.append(active_cell(parent, d, L, inject=inj, n_syn=nsyn, rng=crng,
-                                 t_end=t_end, kca_tables=kca_tables))
-    return cells
+    sizes, _, _ = population_sizes(config, seed, n_cells)
+    return [make_cell(config, seed, i, t_end=t_end, kca_tables=kca_tables, sizes=sizes)
+            for i in range(len(sizes))]
