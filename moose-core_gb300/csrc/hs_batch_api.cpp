@@ -34,8 +34,9 @@ namespace hsg {
 int setLastError(int code, const std::string& msg);
 cudaError_t uploadMixedTypes(const ChanType* ct, int nct, const C2dType* kt, int nkt, const SynType* st,
                              int nst, cudaStream_t s);
-cudaError_t launchBatchStepMixed(const MixBatch& b, const uint32_t* warpCellPtr, const uint32_t* warpCells,
-                                 uint32_t nWarps, uint32_t nsteps, uint32_t threadsPerCta, cudaStream_t st);
+cudaError_t launchBatchStepMixed(const MixBatch& b, const uint32_t* teamCellPtr, const uint32_t* teamCells,
+                                 uint32_t nTeams, uint32_t warpsPerTeam, uint32_t threadsPerCta, uint32_t nsteps,
+                                 cudaStream_t st);
 cudaError_t launchBatchReinitMixed(const MixBatch& b, const double* initVm, const float* c2dX0,
                                    const uint32_t* evStart, cudaStream_t st);
 cudaError_t launchScatterInject(double* const* addr, uint8_t* const* flag, const double* val, uint32_t n,
@@ -101,6 +102,7 @@ struct MixHost {
     std::vector<std::tuple<double, double, double>> synTypeKey;
     std::vector<uint8_t> synTypeOf;
     uint64_t nNodes = 0;
+    std::vector<double> elimCost;                 // per cell: estimated elimination time
 };
 
 }  // namespace
@@ -117,7 +119,8 @@ struct HsBatch {
     std::vector<CellPlan> plans;
     uint64_t nCompt = 0;
     // packing / tuning
-    uint32_t threadsPerCta = 256, ctasPerSm = 4, stepsPerLaunch = 100;
+    uint32_t threadsPerCta = 256, ctasPerSm = 4, stepsPerLaunch = 100, warpsPerTeam = 2;
+    uint32_t levelCost = 8;  // mixed: cost of a schedule level in serial node steps
     bool useGraph = true;
     uint32_t nWarps = 0, nCtas = 0;
     uint32_t *dWarpPtr = nullptr, *dWarpCells = nullptr;
@@ -169,9 +172,12 @@ namespace {
 cudaError_t launchStep(HsBatch* b, uint32_t k) {
     if (b->precision == HS_PREC_FP64)
         return launchBatchStepFp64(b->dDcs, b->dWarpPtr, b->dWarpCells, b->nWarps, k, b->threadsPerCta, b->st);
-    return launchBatchStepMixed(b->mb, b->dWarpPtr, b->dWarpCells, b->nWarps, k, b->threadsPerCta, b->st);
+    return launchBatchStepMixed(b->mb, b->dWarpPtr, b->dWarpCells, b->nWarps, b->warpsPerTeam, b->threadsPerCta, k,
+                                b->st);
 }
 
+// Longest-processing-time packing: cells to the CTAs of one wave, then to
+// the teams (of warpsPerTeam warps) inside each CTA.
 int repack(HsBatch* b) {
     b->packBuf.freeAll();
     b->packBuf.err = cudaSuccess;
@@ -179,13 +185,21 @@ int repack(HsBatch* b) {
         cudaGraphExecDestroy(b->gexec);
         b->gexec = nullptr;
     }
-    uint32_t warpsPerCta = b->threadsPerCta / 32;
+    const uint32_t W = b->precision == HS_PREC_FP64 ? 1 : b->warpsPerTeam;
+    const uint32_t teamsPerCta = b->threadsPerCta / (32 * W);
+    if (teamsPerCta == 0 || teamsPerCta > 15 || b->threadsPerCta % (32 * W))
+        return berr(HS_EINVAL, "threads_per_cta must hold 1..15 teams of warps_per_team warps");
     b->nCtas = std::max<uint32_t>(1, b->nSm * b->ctasPerSm);
-    b->nWarps = b->nCtas * warpsPerCta;
+    b->nWarps = b->nCtas * teamsPerCta;     // teams (a team is one warp for FP64)
     std::vector<double> cost(b->nCells);
     for (uint32_t c = 0; c < b->nCells; ++c) {
-        const CellPlan& P = b->plans[c];
-        cost[c] = P.N + 0.3 * P.C + 0.5 * P.S + 2.0 * (P.fLevelPtr.size() + P.bLevelPtr.size());
+        if (b->precision == HS_PREC_FP64) {
+            const CellPlan& P = b->plans[c];
+            cost[c] = P.N + 0.3 * P.C + 0.5 * P.S + 2.0 * (P.fLevelPtr.size() + P.bLevelPtr.size());
+        } else {
+            const MixCellRange& R = b->mh.cells[c];
+            cost[c] = std::ceil(R.nNodes / (32.0 * W)) * 8.0 + b->mh.elimCost[c];
+        }
     }
     std::vector<uint32_t> order(b->nCells);
     for (uint32_t c = 0; c < b->nCells; ++c) order[c] = c;
@@ -198,23 +212,24 @@ int repack(HsBatch* b) {
         Item it = cta.top();
         cta.pop();
         ctaCells[it.second].push_back(c);
-        cta.push({it.first + cost[c], it.second});
+        // a CTA runs its teams concurrently: its load is spread over them
+        cta.push({it.first + cost[c] / teamsPerCta, it.second});
     }
-    std::vector<std::vector<uint32_t>> warpCells(b->nWarps);
+    std::vector<std::vector<uint32_t>> teamCells(b->nWarps);
     for (uint32_t k = 0; k < b->nCtas; ++k) {
         std::priority_queue<Item, std::vector<Item>, std::greater<Item>> wq;
-        for (uint32_t w = 0; w < warpsPerCta; ++w) wq.push({0.0, k * warpsPerCta + w});
+        for (uint32_t w = 0; w < teamsPerCta; ++w) wq.push({0.0, k * teamsPerCta + w});
         for (uint32_t c : ctaCells[k]) {
             Item it = wq.top();
             wq.pop();
-            warpCells[it.second].push_back(c);
+            teamCells[it.second].push_back(c);
             wq.push({it.first + cost[c], it.second});
         }
     }
     std::vector<uint32_t> ptr(b->nWarps + 1, 0), cells;
     for (uint32_t w = 0; w < b->nWarps; ++w) {
-        ptr[w + 1] = ptr[w] + (uint32_t)warpCells[w].size();
-        cells.insert(cells.end(), warpCells[w].begin(), warpCells[w].end());
+        ptr[w + 1] = ptr[w] + (uint32_t)teamCells[w].size();
+        cells.insert(cells.end(), teamCells[w].begin(), teamCells[w].end());
     }
     b->dWarpPtr = b->packBuf.up(ptr, b->st);
     b->dWarpCells = b->packBuf.up(cells, b->st);
@@ -335,6 +350,106 @@ int8_t powCode(double p, float& pf) {
     return -1;
 }
 
+// Elimination schedule of one tree (see MixCellRange).  Maximal subtrees of
+// at most S nodes become level-0 units in post-order; the nodes above them are
+// cut into unbranched chains, bottom to top, a chain one level above the
+// highest chain hanging below it.  S = 0 gives chains only; S >= T one serial
+// unit.  The estimated time of a level is the serial node count of its
+// busiest thread (units dealt round-robin, longest first, over `nth` threads)
+// plus `levelCost` for the barrier and memory round trip that ends it.
+struct UnitPlan {
+    std::vector<uint32_t> order;                       // tree node of each new index
+    std::vector<uint32_t> levelPtr;                    // unit offsets per level
+    std::vector<std::pair<uint32_t, uint32_t>> units;  // new-index ranges
+    double cost = 0;
+};
+
+UnitPlan planUnits(const std::vector<std::vector<uint32_t>>& tk, const std::vector<uint32_t>& bfs, uint32_t S,
+                   uint32_t nth, double levelCost) {
+    const uint32_t T = (uint32_t)tk.size();
+    std::vector<uint32_t> sz(T, 1), par(T, ~0u);
+    for (uint32_t t = 0; t < T; ++t)
+        for (uint32_t c : tk[t]) par[c] = t;
+    for (uint32_t k = T; k-- > 0;) {
+        const uint32_t t = bfs[k];
+        if (par[t] != ~0u) sz[par[t]] += sz[t];
+    }
+    auto small = [&](uint32_t t) { return sz[t] <= S; };
+    std::vector<std::vector<uint32_t>> unitNodes;
+    std::vector<uint32_t> unitLevel;
+    std::vector<uint32_t> stack;
+    for (uint32_t t : bfs) {
+        if (!small(t) || (par[t] != ~0u && small(par[t]))) continue;
+        // post-order of the subtree at t: children before their parent
+        std::vector<uint32_t> post;
+        stack.assign(1, t);
+        while (!stack.empty()) {
+            uint32_t u = stack.back();
+            stack.pop_back();
+            post.push_back(u);
+            for (uint32_t c : tk[u]) stack.push_back(c);
+        }
+        std::reverse(post.begin(), post.end());
+        unitNodes.push_back(std::move(post));
+        unitLevel.push_back(0);
+    }
+    std::vector<uint32_t> chainOf(T, ~0u);
+    for (uint32_t k = T; k-- > 0;) {
+        const uint32_t t = bfs[k];
+        if (small(t)) continue;
+        uint32_t nTop = 0, top = 0, lvl = 1;
+        for (uint32_t c : tk[t])
+            if (!small(c)) {
+                ++nTop;
+                top = c;
+                lvl = std::max(lvl, unitLevel[chainOf[c]] + 1);
+            }
+        if (nTop == 1) {
+            chainOf[t] = chainOf[top];
+            unitNodes[chainOf[t]].push_back(t);
+        } else {
+            chainOf[t] = (uint32_t)unitNodes.size();
+            unitNodes.push_back({t});
+            unitLevel.push_back(lvl);
+        }
+    }
+    uint32_t maxL = 0;
+    for (uint32_t l : unitLevel) maxL = std::max(maxL, l);
+    std::vector<std::vector<uint32_t>> byLevel(maxL + 1);
+    for (uint32_t u = 0; u < unitNodes.size(); ++u) byLevel[unitLevel[u]].push_back(u);
+    UnitPlan P;
+    P.levelPtr.push_back(0);
+    for (auto& L : byLevel) {
+        if (L.empty()) continue;
+        std::stable_sort(L.begin(), L.end(),
+                         [&](uint32_t x, uint32_t y) { return unitNodes[x].size() > unitNodes[y].size(); });
+        double busiest = 0;
+        for (size_t i = 0; i < L.size(); i += nth) busiest += (double)unitNodes[L[i]].size();
+        P.cost += busiest + levelCost;
+        for (uint32_t u : L) {
+            const uint32_t a = (uint32_t)P.order.size();
+            P.order.insert(P.order.end(), unitNodes[u].begin(), unitNodes[u].end());
+            P.units.push_back({a, (uint32_t)P.order.size()});
+        }
+        P.levelPtr.push_back((uint32_t)P.units.size());
+    }
+    return P;
+}
+
+// The cheapest schedule over subtree bounds 0, 1, 2, 3, 4, 6, 8, 12, ...
+UnitPlan bestUnits(const std::vector<std::vector<uint32_t>>& tk, const std::vector<uint32_t>& bfs, uint32_t nth,
+                   double levelCost) {
+    const uint32_t T = (uint32_t)tk.size();
+    UnitPlan best = planUnits(tk, bfs, 0, nth, levelCost);
+    for (uint32_t p = 1; p < 2 * T; p *= 2)
+        for (uint32_t S : {p, p + p / 2}) {
+            if (S == 0 || S > T) continue;
+            UnitPlan u = planUnits(tk, bfs, S, nth, levelCost);
+            if (u.cost < best.cost) best = std::move(u);
+        }
+    return best;
+}
+
 int buildMixed(HsBatch* b) {
     const uint32_t nC = b->nCells;
     MixHost& H = b->mh;
@@ -348,18 +463,21 @@ int buildMixed(HsBatch* b) {
             return berr(HS_ENOTSUP, "mixed batch: all cells must share one rate-table set");
     }
     std::vector<float> vtab(V0.data.begin(), V0.data.end()), catab(C0.data.begin(), C0.data.end());
-    // 2-D tables by source identity, FP32 (A,B) interleaved
     std::map<std::tuple<const double*, const double*, uint32_t, uint32_t>, int> g2dIndex;
     std::vector<float> g2d, g2dGeom;
     std::vector<uint64_t> g2dOff;
     std::vector<uint32_t> g2dN;
     std::vector<ChanType> ctypes;
     std::vector<C2dType> ktypes;
-    // node arrays
-    std::vector<uint32_t> levelPtr, nodeInfo, child0, parent, chan0, state0, pool0, c2d0, syn0;
-    std::vector<double> off, HS2, CmByDt, EmByRm, Vinit;
-    std::vector<uint8_t> chanType, c2dType, synTypeV;
-    std::vector<float> chanGbar, state, poolC, poolF1, poolF2, poolBasal, poolCeil, poolFloor, c2dGbar, c2dX;
+    // node-major staging
+    std::vector<uint32_t> unitPtr, childList, nodeInfo, ctype4, childStart, parent, syn0;
+    std::vector<uint2> units;
+    const uint32_t nth = 32 * std::max<uint32_t>(1, b->warpsPerTeam);
+    H.elimCost.assign(nC, 0.0);
+    std::vector<double> off, offsq, HS2, CmByDt, EmByRm, Vinit;
+    std::vector<float> gbar4, state12;    // 4 and 12 values per node
+    std::vector<float> poolBasal, poolG1, poolF2, poolCeil, poolFloor, k2gbar, k2x0;
+    std::vector<uint8_t> synTypeV;
     std::vector<uint32_t> injNode, stimStep, stimEntry, sgNode;
     std::vector<double> injVal, stimValue;
     std::vector<float> sgThresh, sgRefract;
@@ -367,10 +485,11 @@ int buildMixed(HsBatch* b) {
     H.cells.resize(nC);
     H.nodeOf.resize(nC);
     H.poolOf.resize(nC);
+    b->injEntryOf.clear();
     for (uint32_t ci = 0; ci < nC; ++ci) {
         const CellPlan& P = b->plans[ci];
         const uint32_t N = P.N;
-        // star-form tree
+        // star-form tree: junctions of >= 3 compartments get a node
         std::vector<int64_t> mparent(N, -1);
         for (uint32_t i = 0; i < N; ++i)
             for (uint32_t c : P.children[i]) mparent[c] = i;
@@ -409,39 +528,33 @@ int buildMixed(HsBatch* b) {
             }
         }
         const uint32_t T = (uint32_t)diag.size();
-        // breadth-first order from the root
         std::vector<uint32_t> bfs;
-        std::vector<uint32_t> level;
         bfs.reserve(T);
         bfs.push_back((uint32_t)root);
-        std::vector<uint32_t> lvl(T, 0);
         for (size_t k = 0; k < bfs.size(); ++k)
-            for (uint32_t c : tk[bfs[k]]) {
-                lvl[c] = lvl[bfs[k]] + 1;
-                bfs.push_back(c);
-            }
+            for (uint32_t c : tk[bfs[k]]) bfs.push_back(c);
         if (bfs.size() != T) return berr(HS_EINVAL, "mixed batch: tree construction failed");
+        UnitPlan U = bestUnits(tk, bfs, nth, (double)b->levelCost);
+        H.elimCost[ci] = 2.0 * U.cost;
+        const std::vector<uint32_t>& order = U.order;
         std::vector<uint32_t> pos(T);
-        for (uint32_t k = 0; k < T; ++k) pos[bfs[k]] = k;
+        for (uint32_t k = 0; k < T; ++k) pos[order[k]] = k;
         MixCellRange& R = H.cells[ci];
         const uint32_t node0 = (uint32_t)nodeInfo.size();
         R.node0 = node0;
         R.nNodes = T;
-        R.level0 = (uint32_t)levelPtr.size();
-        uint32_t nL = lvl[bfs.back()] + 1;
-        R.nLevels = nL;
-        {
-            std::vector<uint32_t> lp(nL + 1, 0);
-            for (uint32_t k = 0; k < T; ++k) lp[lvl[bfs[k]] + 1]++;
-            for (uint32_t l = 0; l < nL; ++l) lp[l + 1] += lp[l];
-            levelPtr.insert(levelPtr.end(), lp.begin(), lp.end());
-        }
+        R.level0 = (uint32_t)unitPtr.size();
+        R.nLevels = (uint32_t)U.levelPtr.size() - 1;
+        R.unit0 = (uint32_t)units.size();
+        R.child0 = (uint32_t)childList.size();
+        unitPtr.insert(unitPtr.end(), U.levelPtr.begin(), U.levelPtr.end());
+        for (auto& u : U.units) units.push_back(make_uint2(u.first, u.second));
         H.nodeOf[ci].assign(P.hinesOf.size(), -1);
         for (size_t m = 0; m < P.hinesOf.size(); ++m)
             if (P.hinesOf[m] >= 0) H.nodeOf[ci][m] = node0 + pos[P.hinesOf[m]];
         H.poolOf[ci].assign(P.poolSolverOf.size(), -1);
         // inject entries: basal injects and stimulus targets
-        std::map<uint32_t, uint32_t> injEntry;   // compartment -> entry
+        std::map<uint32_t, uint32_t> injEntry;
         R.inj0 = (uint32_t)injNode.size();
         for (uint32_t i = 0; i < N; ++i)
             if (P.injPresent[i]) {
@@ -475,206 +588,212 @@ int buildMixed(HsBatch* b) {
         R.nSg = P.SG;
         R.rec0 = 0;
         R.nRec = 0;
-        // per compartment lists of external objects
         std::vector<std::vector<uint32_t>> c2dOf(N), synOf(N);
         for (uint32_t k = 0; k < P.K2; ++k) c2dOf[P.c2dCompt[k]].push_back(k);
         for (uint32_t k = 0; k < P.S; ++k) synOf[P.synCompt[k]].push_back(k);
         for (uint32_t k = 0; k < T; ++k) {
-            const uint32_t t = bfs[k];
+            const uint32_t t = order[k];
             const bool center = t >= N;
-            uint32_t info = center ? kNodeCenter : 0;
-            if (!center && injEntry.count(t)) info |= kNodeInject;
-            nodeInfo.push_back(info);
-            child0.push_back(0);    // filled below
-            parent.push_back(0);
+            const uint32_t nch = (uint32_t)tk[t].size();
+            if (nch > 255) return berr(HS_ENOTSUP, "mixed batch: more than 255 children at a node");
+            uint32_t info = (center ? kNodeCenter : 0) | (nch << 16) | ((uint32_t)kNoType << 8);
+            uint32_t types = 0xFFFFFFFFu;
+            childStart.push_back((uint32_t)childList.size() - R.child0);
+            for (uint32_t c : tk[t]) childList.push_back(pos[c]);
+            parent.push_back(k == 0 ? ~0u : 0);      // filled below
             off.push_back(toff[t]);
+            offsq.push_back(toff[t] * toff[t]);
             HS2.push_back(diag[t]);
             CmByDt.push_back(center ? 0.0 : P.CmByDt[t]);
             EmByRm.push_back(center ? 0.0 : P.EmByRm[t]);
             Vinit.push_back(center ? 0.0 : P.initVm[t]);
             H.initVm.push_back(center ? 0.0 : P.initVm[t]);
-            chan0.push_back((uint32_t)chanGbar.size());
-            state0.push_back((uint32_t)state.size());
-            pool0.push_back((uint32_t)poolC.size());
-            c2d0.push_back((uint32_t)c2dGbar.size());
+            size_t g0 = gbar4.size(), s0 = state12.size();
+            gbar4.resize(g0 + kMaxChan, 0.f);
+            state12.resize(s0 + 3 * kMaxChan, 0.f);
+            float pb = 0.f, pg1 = 0.f, pf2 = 0.f, pce = 0.f, pfl = 0.f, kg = 0.f, kx = 0.f;
             syn0.push_back((uint32_t)synTypeV.size());
-            if (center) continue;
-            const uint32_t pb = P.poolPtr[t], pe = P.poolPtr[t + 1];
-            if (pe - pb > 4) return berr(HS_ENOTSUP, "mixed batch: more than 4 Ca pools in a compartment");
-            for (uint32_t p = pb; p < pe; ++p) {
-                H.poolOf[ci][P.poolModel[p]] = (int64_t)poolC.size();
-                poolC.push_back(0.f);
-                poolF1.push_back((float)(1.0 - P.f1[p]));     // decay per step, in FP64
-                poolF2.push_back((float)P.f2[p]);
-                poolBasal.push_back((float)P.CaBasal[p]);
-                poolCeil.push_back((float)P.ceiling[p]);
-                poolFloor.push_back((float)P.floor_[p]);
-            }
-            for (uint32_t q = P.chanPtr[t]; q < P.chanPtr[t + 1]; ++q) {
-                ChanType ty;
-                std::memset(&ty, 0, sizeof(ty));
-                ty.ek = (float)P.Ek[q];
-                ty.xp = powCode(P.Xpow[q], ty.xpf);
-                ty.yp = powCode(P.Ypow[q], ty.ypf);
-                ty.zp = powCode(P.Zpow[q], ty.zpf);
-                ty.instant = (int8_t)P.instant[q];
-                ty.colX = (int16_t)(P.colX[q] < 0 ? 0 : P.colX[q]);
-                ty.colY = (int16_t)(P.colY[q] < 0 ? 0 : P.colY[q]);
-                ty.colZ = (int16_t)(P.colZ[q] < 0 ? 0 : P.colZ[q]);
-                ty.zSrc = -1;
-                if (P.Zpow[q] > 0.0 && P.zSrc[q] >= 0) {
-                    if (P.zSrc[q] < (int32_t)pb || P.zSrc[q] >= (int32_t)pe)
-                        return berr(HS_ENOTSUP, "mixed batch: Ca-dependent gate reads another compartment's pool");
-                    ty.zSrc = (int8_t)(P.zSrc[q] - pb);
+            if (!center) {
+                if (injEntry.count(t)) info |= kNodeInject;
+                const uint32_t pb0 = P.poolPtr[t], pe0 = P.poolPtr[t + 1];
+                if (pe0 - pb0 > 1) return berr(HS_ENOTSUP, "mixed batch: more than one Ca pool in a compartment");
+                if (pe0 > pb0) {
+                    info |= kNodePool;
+                    H.poolOf[ci][P.poolModel[pb0]] = node0 + k;
+                    pb = (float)P.CaBasal[pb0];
+                    pg1 = (float)(1.0 - P.f1[pb0]);     // decay per step, from FP64
+                    pf2 = (float)P.f2[pb0];
+                    pce = (float)P.ceiling[pb0];
+                    pfl = (float)P.floor_[pb0];
                 }
-                ty.caTarget = -1;
-                if (P.caTarget[q] >= 0) {
-                    if (P.caTarget[q] < (int32_t)pb || P.caTarget[q] >= (int32_t)pe)
-                        return berr(HS_ENOTSUP, "mixed batch: channel feeds another compartment's pool");
-                    ty.caTarget = (int8_t)(P.caTarget[q] - pb);
-                }
-                int ti = typeIndex(ctypes, ty, kMaxChanTypes);
-                if (ti < 0) return berr(HS_ENOTSUP, "mixed batch: too many channel types");
-                chanType.push_back((uint8_t)ti);
-                chanGbar.push_back((float)(P.Gbar[q] * P.modulation[q]));
-                int s = P.stateOff[q];
-                if (P.Xpow[q] > 0.0) state.push_back((float)P.state0[s++]);
-                if (P.Ypow[q] > 0.0) state.push_back((float)P.state0[s++]);
-                if (P.Zpow[q] > 0.0) state.push_back((float)P.state0[s++]);
-            }
-            for (uint32_t k : c2dOf[t]) {
-                const Gate2D& G = P.gates2d[P.c2dGate[k]];
-                auto key = std::make_tuple(G.srcA, G.srcB, G.nx, G.ny);
-                auto it = g2dIndex.find(key);
-                if (it == g2dIndex.end()) {
-                    if (g2dIndex.size() >= 127) return berr(HS_ENOTSUP, "mixed batch: too many 2-D tables");
-                    int gi = (int)g2dN.size() / 2;
-                    size_t n = (size_t)G.nx * G.ny;
-                    g2dOff.push_back(g2d.size());
-                    size_t o = g2d.size();
-                    g2d.resize(o + 2 * n);
-                    for (size_t i = 0; i < n; ++i) {
-                        g2d[o + 2 * i] = (float)G.srcA[i];
-                        g2d[o + 2 * i + 1] = (float)G.srcB[i];
+                const uint32_t q0 = P.chanPtr[t], q1 = P.chanPtr[t + 1];
+                if (q1 - q0 > (uint32_t)kMaxChan)
+                    return berr(HS_ENOTSUP, "mixed batch: more than 4 HHChannels in a compartment");
+                for (uint32_t q = q0; q < q1; ++q) {
+                    ChanType ty;
+                    std::memset(&ty, 0, sizeof(ty));
+                    ty.ek = (float)P.Ek[q];
+                    ty.xp = powCode(P.Xpow[q], ty.xpf);
+                    ty.yp = powCode(P.Ypow[q], ty.ypf);
+                    ty.zp = powCode(P.Zpow[q], ty.zpf);
+                    ty.instant = (int8_t)P.instant[q];
+                    ty.colX = (int16_t)(P.colX[q] < 0 ? 0 : P.colX[q]);
+                    ty.colY = (int16_t)(P.colY[q] < 0 ? 0 : P.colY[q]);
+                    ty.colZ = (int16_t)(P.colZ[q] < 0 ? 0 : P.colZ[q]);
+                    if (P.Zpow[q] > 0.0 && P.zSrc[q] >= 0) {
+                        if (P.zSrc[q] != (int32_t)pb0 || pe0 == pb0)
+                            return berr(HS_ENOTSUP, "mixed batch: Ca-dependent gate reads another compartment's pool");
+                        ty.zCa = 1;
                     }
-                    g2dGeom.insert(g2dGeom.end(), {(float)G.xmin, (float)G.ymin, (float)G.invDx, (float)G.invDy,
-                                                   (float)G.xmax, (float)G.ymax});
-                    g2dN.push_back(G.nx);
-                    g2dN.push_back(G.ny);
-                    it = g2dIndex.emplace(key, gi).first;
+                    if (P.caTarget[q] >= 0) {
+                        if (P.caTarget[q] != (int32_t)pb0 || pe0 == pb0)
+                            return berr(HS_ENOTSUP, "mixed batch: channel feeds another compartment's pool");
+                        ty.caTarget = 1;
+                    }
+                    int ti = typeIndex(ctypes, ty, kMaxChanTypes - 1);
+                    if (ti < 0) return berr(HS_ENOTSUP, "mixed batch: too many channel types");
+                    const uint32_t j = q - q0;
+                    types = (types & ~(0xFFu << (8 * j))) | ((uint32_t)ti << (8 * j));
+                    gbar4[g0 + j] = (float)(P.Gbar[q] * P.modulation[q]);
+                    int s = P.stateOff[q];
+                    if (P.Xpow[q] > 0.0) state12[s0 + 3 * j] = (float)P.state0[s++];
+                    if (P.Ypow[q] > 0.0) state12[s0 + 3 * j + 1] = (float)P.state0[s++];
+                    if (P.Zpow[q] > 0.0) state12[s0 + 3 * j + 2] = (float)P.state0[s++];
                 }
-                C2dType ky;
-                std::memset(&ky, 0, sizeof(ky));
-                ky.ek = (float)P.c2dEk[k];
-                ky.xp = powCode(P.c2dXpow[k], ky.xpf);
-                ky.dep0 = (int8_t)P.c2dDep0[k];
-                ky.dep1 = (int8_t)P.c2dDep1[k];
-                ky.conc1 = -1;
-                ky.conc2 = -1;
-                if (P.c2dConc1[k] >= 0) {
-                    if (P.c2dConc1[k] < (int32_t)pb || P.c2dConc1[k] >= (int32_t)pe)
+                if (c2dOf[t].size() > 1) return berr(HS_ENOTSUP, "mixed batch: more than one HHChannel2D in a compartment");
+                for (uint32_t kk : c2dOf[t]) {
+                    const Gate2D& G = P.gates2d[P.c2dGate[kk]];
+                    auto key = std::make_tuple(G.srcA, G.srcB, G.nx, G.ny);
+                    auto it = g2dIndex.find(key);
+                    if (it == g2dIndex.end()) {
+                        if (g2dIndex.size() >= 127) return berr(HS_ENOTSUP, "mixed batch: too many 2-D tables");
+                        int gi = (int)g2dN.size() / 2;
+                        size_t nn = (size_t)G.nx * G.ny;
+                        g2dOff.push_back(g2d.size());
+                        size_t o = g2d.size();
+                        g2d.resize(o + 2 * nn);
+                        for (size_t i = 0; i < nn; ++i) {
+                            g2d[o + 2 * i] = (float)G.srcA[i];
+                            g2d[o + 2 * i + 1] = (float)G.srcB[i];
+                        }
+                        g2dGeom.insert(g2dGeom.end(), {(float)G.xmin, (float)G.ymin, (float)G.invDx, (float)G.invDy,
+                                                       (float)G.xmax, (float)G.ymax});
+                        g2dN.push_back(G.nx);
+                        g2dN.push_back(G.ny);
+                        it = g2dIndex.emplace(key, gi).first;
+                    }
+                    C2dType ky;
+                    std::memset(&ky, 0, sizeof(ky));
+                    ky.ek = (float)P.c2dEk[kk];
+                    ky.xp = powCode(P.c2dXpow[kk], ky.xpf);
+                    auto dep = [&](int d) -> int8_t {
+                        if (d == 0) return 0;
+                        if (d == 1) return 1;
+                        return -2;
+                    };
+                    if (P.c2dConc2[kk] >= 0 || P.c2dDep0[kk] == 2 || P.c2dDep1[kk] == 2)
+                        return berr(HS_ENOTSUP, "mixed batch: HHChannel2D on a second concentration");
+                    if (P.c2dConc1[kk] >= 0 && (P.c2dConc1[kk] != (int32_t)pb0 || pe0 == pb0))
                         return berr(HS_ENOTSUP, "mixed batch: HHChannel2D reads another compartment's pool");
-                    ky.conc1 = (int8_t)(P.c2dConc1[k] - pb);
+                    ky.dep0 = P.c2dDep0[kk] < 0 ? -1 : dep(P.c2dDep0[kk]);
+                    ky.dep1 = P.c2dDep1[kk] < 0 ? -1 : dep(P.c2dDep1[kk]);
+                    ky.instant = (int8_t)P.c2dInstant[kk];
+                    ky.gate = (int8_t)it->second;
+                    int ti = typeIndex(ktypes, ky, kMaxC2dTypes - 1);
+                    if (ti < 0) return berr(HS_ENOTSUP, "mixed batch: too many HHChannel2D types");
+                    info = (info & ~(0xFFu << 8)) | ((uint32_t)ti << 8);
+                    kg = (float)(P.c2dGbar[kk] * P.c2dMod[kk]);
+                    kx = (float)P.c2dX0[kk];
                 }
-                if (P.c2dConc2[k] >= 0) {
-                    if (P.c2dConc2[k] < (int32_t)pb || P.c2dConc2[k] >= (int32_t)pe)
-                        return berr(HS_ENOTSUP, "mixed batch: HHChannel2D reads another compartment's pool");
-                    ky.conc2 = (int8_t)(P.c2dConc2[k] - pb);
+                if (!synOf[t].empty()) info |= kNodeSyn;
+                for (uint32_t kk : synOf[t]) {
+                    auto key = std::make_tuple(P.synTau1[kk], P.synTau2[kk], P.synEk[kk]);
+                    size_t ti = 0;
+                    while (ti < H.synTypeKey.size() && H.synTypeKey[ti] != key) ++ti;
+                    if (ti == H.synTypeKey.size()) {
+                        if (ti >= (size_t)kMaxSynTypes) return berr(HS_ENOTSUP, "mixed batch: too many SynChan types");
+                        H.synTypeKey.push_back(key);
+                    }
+                    synTypeV.push_back((uint8_t)ti);
+                    H.synGbar.push_back(P.synGbar[kk]);
+                    H.synTau1.push_back(P.synTau1[kk]);
+                    H.synTau2.push_back(P.synTau2[kk]);
+                    H.synMod.push_back(P.synMod[kk]);
+                    H.evStart.push_back((uint32_t)H.evTime.size());
+                    for (uint32_t e = P.evPtr[kk]; e < P.evPtr[kk + 1]; ++e) {
+                        H.evTime.push_back(P.evTime[e]);
+                        H.evW.push_back(P.evW[e]);
+                    }
+                    H.evEnd.push_back((uint32_t)H.evTime.size());
                 }
-                ky.instant = (int8_t)P.c2dInstant[k];
-                ky.gate = (int8_t)it->second;
-                int ti = typeIndex(ktypes, ky, kMaxC2dTypes);
-                if (ti < 0) return berr(HS_ENOTSUP, "mixed batch: too many HHChannel2D types");
-                c2dType.push_back((uint8_t)ti);
-                c2dGbar.push_back((float)(P.c2dGbar[k] * P.c2dMod[k]));
-                c2dX.push_back((float)P.c2dX0[k]);
-                H.c2dX0.push_back((float)P.c2dX0[k]);
             }
-            for (uint32_t k : synOf[t]) {
-                auto key = std::make_tuple(P.synTau1[k], P.synTau2[k], P.synEk[k]);
-                size_t ti = 0;
-                while (ti < H.synTypeKey.size() && H.synTypeKey[ti] != key) ++ti;
-                if (ti == H.synTypeKey.size()) {
-                    if (ti >= (size_t)kMaxSynTypes) return berr(HS_ENOTSUP, "mixed batch: too many SynChan types");
-                    H.synTypeKey.push_back(key);
-                }
-                synTypeV.push_back((uint8_t)ti);
-                H.synGbar.push_back(P.synGbar[k]);
-                H.synTau1.push_back(P.synTau1[k]);
-                H.synTau2.push_back(P.synTau2[k]);
-                H.synMod.push_back(P.synMod[k]);
-                H.evStart.push_back((uint32_t)H.evTime.size());
-                for (uint32_t e = P.evPtr[k]; e < P.evPtr[k + 1]; ++e) {
-                    H.evTime.push_back(P.evTime[e]);
-                    H.evW.push_back(P.evW[e]);
-                }
-                H.evEnd.push_back((uint32_t)H.evTime.size());
-            }
+            nodeInfo.push_back(info);
+            ctype4.push_back(types);
+            poolBasal.push_back(pb);
+            poolG1.push_back(pg1);
+            poolF2.push_back(pf2);
+            poolCeil.push_back(pce);
+            poolFloor.push_back(pfl);
+            k2gbar.push_back(kg);
+            k2x0.push_back(kx);
         }
-        // children CSR and parents in global node indices
-        {
-            uint32_t next = node0 + 1;
-            for (uint32_t k = 0; k < T; ++k) {
-                child0[node0 + k] = next;
-                for (uint32_t c : tk[bfs[k]]) parent[node0 + pos[c]] = node0 + k;
-                next += (uint32_t)tk[bfs[k]].size();
-            }
-            parent[node0] = ~0u;
-        }
+        for (uint32_t k = 0; k < T; ++k)
+            for (uint32_t c : tk[order[k]]) parent[node0 + pos[c]] = k;
     }
-    // closing CSR entries
     const uint32_t nN = (uint32_t)nodeInfo.size();
-    child0.push_back(nN);
-    chan0.push_back((uint32_t)chanGbar.size());
-    state0.push_back((uint32_t)state.size());
-    pool0.push_back((uint32_t)poolC.size());
-    c2d0.push_back((uint32_t)c2dGbar.size());
     syn0.push_back((uint32_t)synTypeV.size());
+    const uint64_t ld = (nN + 31) / 32 * 32;
     H.nNodes = nN;
-    // upload
+    // slot-major arrays [slot][ld]
+    std::vector<float> gbarS((size_t)kMaxChan * ld, 0.f), stateS((size_t)3 * kMaxChan * ld, 0.f);
+    for (uint32_t n = 0; n < nN; ++n) {
+        for (int j = 0; j < kMaxChan; ++j) gbarS[(size_t)j * ld + n] = gbar4[(size_t)n * kMaxChan + j];
+        for (int j = 0; j < 3 * kMaxChan; ++j) stateS[(size_t)j * ld + n] = state12[(size_t)n * 3 * kMaxChan + j];
+    }
+    gbar4.clear();
+    state12.clear();
+    H.c2dX0 = k2x0;
     DevBuf& D = b->buf;
     cudaStream_t st = b->st;
     MixBatch& m = b->mb;
     std::memset(&m, 0, sizeof(m));
     m.nCells = nC;
+    m.ld = ld;
     m.cells = D.up(H.cells, st);
-    m.levelPtr = D.up(levelPtr, st);
+    m.unitPtr = D.up(unitPtr, st);
+    m.units = D.up(units, st);
+    m.childList = D.up(childList, st);
     m.nodeInfo = D.up(nodeInfo, st);
-    m.child0 = D.up(child0, st);
+    m.ctype4 = D.up(ctype4, st);
+    m.childStart = D.up(childStart, st);
     m.parent = D.up(parent, st);
     m.off = D.up(off, st);
+    m.offsq = D.up(offsq, st);
     m.HS2 = D.up(HS2, st);
     m.CmByDt = D.up(CmByDt, st);
     m.EmByRm = D.up(EmByRm, st);
     m.V = D.up(Vinit, st);
-    m.VMid = D.zeros<double>(nN, st);
-    m.rhsF = D.zeros<double>(nN, st);
     m.inv = D.zeros<double>(nN, st);
-    m.chan0 = D.up(chan0, st);
-    m.state0 = D.up(state0, st);
-    m.pool0 = D.up(pool0, st);
-    m.c2d0 = D.up(c2d0, st);
-    m.syn0 = D.up(syn0, st);
-    m.chanType = D.up(chanType, st);
-    m.chanGbar = D.up(chanGbar, st);
-    m.state = D.up(state, st);
-    m.chanGk = D.zeros<float>(chanGbar.size(), st);
-    m.poolC = D.up(poolC, st);
+    m.gEl = D.zeros<double>(nN, st);
+    m.VMid = D.zeros<double>(nN, st);
+    m.caG = D.zeros<float>(nN, st);
+    m.caGE = D.zeros<float>(nN, st);
+    m.gbar = D.up(gbarS, st);
+    m.state = D.up(stateS, st);
+    m.poolC = D.zeros<float>(nN, st);
     m.poolCa = D.up(poolBasal, st);
-    m.caG = D.zeros<float>(poolC.size(), st);
-    m.caGE = D.zeros<float>(poolC.size(), st);
-    m.poolF1 = D.up(poolF1, st);
+    m.poolG1 = D.up(poolG1, st);
     m.poolF2 = D.up(poolF2, st);
     m.poolBasal = D.up(poolBasal, st);
     m.poolCeil = D.up(poolCeil, st);
     m.poolFloor = D.up(poolFloor, st);
-    m.c2dType = D.up(c2dType, st);
-    m.c2dGbar = D.up(c2dGbar, st);
-    m.c2dX = D.up(c2dX, st);
+    m.k2gbar = D.up(k2gbar, st);
+    m.k2x = D.up(k2x0, st);
     m.g2d = D.up(g2d, st);
     m.g2dOff = D.up(g2dOff, st);
     m.g2dGeom = D.up(g2dGeom, st);
     m.g2dN = D.up(g2dN, st);
+    m.syn0 = D.up(syn0, st);
     m.synType = D.up(synTypeV, st);
     m.synX = D.zeros<float>(synTypeV.size(), st);
     m.synY = D.zeros<float>(synTypeV.size(), st);
@@ -785,7 +904,9 @@ int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds, uint32_t n_c
     if (tuning) {
         if (tuning->threads_per_cta) b->threadsPerCta = tuning->threads_per_cta;
         if (tuning->ctas_per_sm) b->ctasPerSm = tuning->ctas_per_sm;
+        if (tuning->warps_per_team) b->warpsPerTeam = tuning->warps_per_team;
         if (tuning->steps_per_launch) b->stepsPerLaunch = tuning->steps_per_launch;
+        if (tuning->level_cost) b->levelCost = tuning->level_cost;
         b->useGraph = tuning->use_graph != 0;
     }
     if (b->threadsPerCta % 32 || b->threadsPerCta > 512 ||
@@ -831,6 +952,7 @@ int hs_batch_tune(HsBatch* b, const HsBatchTuning* t) {
         b->threadsPerCta = t->threads_per_cta;
     }
     if (t->ctas_per_sm) b->ctasPerSm = t->ctas_per_sm;
+    if (t->warps_per_team) b->warpsPerTeam = t->warps_per_team;
     if (t->steps_per_launch) b->stepsPerLaunch = t->steps_per_launch;
     b->useGraph = t->use_graph != 0;
     cudaStreamSynchronize(b->st);

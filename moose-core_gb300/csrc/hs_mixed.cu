@@ -1,20 +1,24 @@
 // hs_mixed.cu -- mixed-precision batched HSolve step (sm_103a).
 //
-// One warp steps one cell; a warp owns a list of cells (packed by size on
-// the host) and runs each for `nsteps` steps before moving on.  Per step:
-//   tick 0   stimulus schedule (lane 0)
-//   forward  levels deepest -> root.  A node at level L computes its own
-//            channels (FP32 tables, gates, conductances; the K(Ca) 2-D gate;
-//            its SynChans), assembles its FP64 matrix row, pulls the
-//            eliminated rows of its children (FP64), and stores its
-//            eliminated rhs and the reciprocal of its pivot.
-//   backward levels root -> deepest: VMid = (rhs - off*VMid[parent])/pivot,
-//            V = 2*VMid - V, then the node's Ca pools (HSolveActive::
-//            advanceCalcium with VMid), FP32.
-//   SpikeGens (lane 0), trace record.
+// A team of W warps steps one cell at a time; every team owns a list of
+// cells (packed by cost on the host) and runs each for `nsteps` steps before
+// moving on.  A team synchronises with a named barrier (bar.sync id, 32*W),
+// or __syncwarp when W = 1.  Per step:
+//   tick 0    stimulus schedule
+//   assembly  every compartment node, in parallel over the team: FP32 rate
+//             lookup and gate update for each channel slot, conductances,
+//             the K(Ca) 2-D gate, SynChans; FP64 matrix row.
+//   forward   work units level by level (hs_mixed.cuh), each unit serially
+//             by one thread: pull the children's eliminated rows
+//             (diag -= off^2/pivot_c, rhs -= off*g_c), keep 1/pivot and
+//             g = rhs/pivot (FP64).
+//   backward  the same units in reverse: VMid = g - (off/pivot)*VMid[parent],
+//             V = 2*VMid - V, then the node's Ca pool (FP32).
+//   SpikeGens, trace record.
 // Reference routines: hsolve/HSolveActive.cpp:45-332, hsolve/HSolvePassive.cpp:
-// 246-401 (same tree sweep, star form), biophysics/HHChannel2D.cpp:327-369,
-// biophysics/SynChan.cpp:200-224, biophysics/SpikeGen.cpp:202-216.
+// 246-401 (the same elimination, tree form), biophysics/HHChannel2D.cpp:327-369,
+// biophysics/SynChan.cpp:200-224, synapse/SimpleSynHandler.cpp:98-113,
+// biophysics/SpikeGen.cpp:202-216.
 #include <cuda_runtime.h>
 
 #include "hs_mixed.cuh"
@@ -25,17 +29,15 @@ __constant__ ChanType c_chanTypes[kMaxChanTypes];
 __constant__ C2dType c_c2dTypes[kMaxC2dTypes];
 __constant__ SynType c_synTypes[kMaxSynTypes];
 
-// Reciprocal of a positive FP64 pivot: FP32 hardware approximation as the
-// seed, then two Newton-Raphson steps x <- x + x(1 - d x) in FP64 (each
-// doubles the correct bits: ~2^-22 -> 2^-44 -> full precision).
+// Reciprocal of a positive FP64 pivot: the FP32 hardware approximation
+// (relative error below 2^-22) refined by one Newton-Raphson step
+// x <- x + x(1 - d x) in FP64, which squares the error (below 2^-44).
 __device__ __forceinline__ double rcpNewton(double d) {
     float f = __double2float_rn(d);
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(f));
     double x = (double)r;
     double e = fma(-d, x, 1.0);
-    x = fma(x, e, x);
-    e = fma(-d, x, 1.0);
     return fma(x, e, x);
 }
 
@@ -102,176 +104,215 @@ __device__ __forceinline__ void interp2dF(const float* T, const float* geom, uin
     B = z00.y * w00 + z10.y * w10 + z01.y * w01 + z11.y * xFyF;
 }
 
-// Channels, K(Ca), SynChans and matrix row of one compartment node.
-__device__ __forceinline__ void nodeRow(const MixBatch& b, uint32_t n, unsigned long long step,
-                                        double& diag, double& rhs) {
+// Channels, K(Ca), SynChans and FP64 matrix row of one compartment node.
+__device__ __forceinline__ void nodeRow(const MixBatch& b, uint32_t n, uint32_t info,
+                                        unsigned long long step, double& diag, double& rhs) {
+    const uint64_t ld = b.ld;
     const double V = b.V[n];
+    const uint32_t types = b.ctype4[n];
     const float v = (float)V;
     const float dt = b.dtf, hdt = 0.5f * b.dtf;
+    const float ca = (info & kNodePool) ? b.poolCa[n] : 0.f;
     RowF vr = rowF(b.vTab, b.vCol, b.vRows, v, b.vMin, b.vMax, b.vInvDx);
-    float G = 0.f, GE = 0.f;
-    const uint32_t p0 = b.pool0[n], p1 = b.pool0[n + 1];
-    float cg[4] = {0.f, 0.f, 0.f, 0.f}, cge[4] = {0.f, 0.f, 0.f, 0.f};
-    uint32_t s = b.state0[n];
-    for (uint32_t q = b.chan0[n]; q < b.chan0[n + 1]; ++q) {
-        const ChanType& t = c_chanTypes[b.chanType[q]];
+    float G = 0.f, GE = 0.f, cg = 0.f, cge = 0.f;
+#pragma unroll
+    for (int j = 0; j < kMaxChan; ++j) {
+        const uint32_t tj = (types >> (8 * j)) & 0xFF;
+        if (tj == kNoType) break;
+        const ChanType& t = c_chanTypes[tj];
         float frac = 1.f;
+        float* st = b.state + (uint64_t)(3 * j) * ld + n;
         if (t.xp) {
-            float x = gateF(vr, b.vCol, t.colX, b.state[s], dt, hdt, t.instant & 1);
-            b.state[s++] = x;
+            float x = gateF(vr, b.vCol, t.colX, st[0], dt, hdt, t.instant & 1);
+            st[0] = x;
             frac *= powi(x, t.xp, t.xpf);
         }
         if (t.yp) {
-            float y = gateF(vr, b.vCol, t.colY, b.state[s], dt, hdt, t.instant & 2);
-            b.state[s++] = y;
+            float y = gateF(vr, b.vCol, t.colY, st[ld], dt, hdt, t.instant & 2);
+            st[ld] = y;
             frac *= powi(y, t.yp, t.ypf);
         }
         if (t.zp) {
             float z;
-            if (t.zSrc >= 0) {
-                RowF cr = rowF(b.caTab, b.caCol, b.caRows, b.poolCa[p0 + t.zSrc], b.caMin, b.caMax, b.caInvDx);
-                z = gateF(cr, b.caCol, t.colZ, b.state[s], dt, hdt, t.instant & 4);
+            if (t.zCa) {
+                RowF cr = rowF(b.caTab, b.caCol, b.caRows, ca, b.caMin, b.caMax, b.caInvDx);
+                z = gateF(cr, b.caCol, t.colZ, st[2 * ld], dt, hdt, t.instant & 4);
             } else {
-                z = gateF(vr, b.vCol, t.colZ, b.state[s], dt, hdt, t.instant & 4);
+                z = gateF(vr, b.vCol, t.colZ, st[2 * ld], dt, hdt, t.instant & 4);
             }
-            b.state[s++] = z;
+            st[2 * ld] = z;
             frac *= powi(z, t.zp, t.zpf);
         }
-        float gk = b.chanGbar[q] * frac;
-        b.chanGk[q] = gk;
+        const float gk = b.gbar[(uint64_t)j * ld + n] * frac;
         G += gk;
         GE = fmaf(gk, t.ek, GE);
-        if (t.caTarget >= 0 && t.caTarget < 4) {
-            cg[t.caTarget] += gk;
-            cge[t.caTarget] = fmaf(gk, t.ek, cge[t.caTarget]);
+        if (t.caTarget) {
+            cg += gk;
+            cge = fmaf(gk, t.ek, cge);
         }
     }
-    for (uint32_t p = p0; p < p1 && p - p0 < 4; ++p) {
-        b.caG[p] = cg[p - p0];
-        b.caGE[p] = cge[p - p0];
+    if (info & kNodePool) {
+        b.caG[n] = cg;
+        b.caGE[n] = cge;
     }
-    // K(Ca) and other HHChannel2D: inputs are Vm and Ca of the previous step
-    for (uint32_t k = b.c2d0[n]; k < b.c2d0[n + 1]; ++k) {
-        const C2dType& t = c_c2dTypes[b.c2dType[k]];
-        float c1 = t.conc1 >= 0 ? b.poolCa[p0 + t.conc1] : 0.f;
-        float c2 = t.conc2 >= 0 ? b.poolCa[p0 + t.conc2] : 0.f;
-        float x = t.dep0 == 0 ? v : t.dep0 == 1 ? c1 : t.dep0 == 2 ? c2 : 0.f;
-        float y = t.dep1 == 0 ? v : t.dep1 == 1 ? c1 : t.dep1 == 2 ? c2 : 0.f;
+    // HHChannel2D (K(Ca)): inputs are Vm and Ca of the previous step
+    const uint32_t k2 = (info >> 8) & 0xFF;
+    if (k2 != kNoType) {
+        const C2dType& t = c_c2dTypes[k2];
+        float x = t.dep0 == 0 ? v : t.dep0 == 1 ? ca : 0.f;
+        float y = t.dep1 == 0 ? v : t.dep1 == 1 ? ca : 0.f;
         float A, B;
         interp2dF(b.g2d + b.g2dOff[t.gate], b.g2dGeom + 6 * t.gate, b.g2dN[2 * t.gate],
                   b.g2dN[2 * t.gate + 1], x, y, A, B);
-        float X = b.c2dX[k];
+        float X = b.k2x[n];
         if (t.instant & 1) X = __fdividef(A, B);
         else if (B > 1.0e-10f) {
             // HHChannelBase::integrate, X e + (A/B)(1 - e) with e = exp(-B dt),
-            // as X + (A/B - X)(1 - e) with 1 - e = -expm1(-B dt) (no cancellation)
+            // as X + (A/B - X)(1 - e), 1 - e = -expm1(-B dt) (no cancellation)
             float em = -expm1f(-B * dt);
             X = fmaf(__fdividef(A, B) - X, em, X);
         } else X = fmaf(A, dt, X);
-        b.c2dX[k] = X;
-        float gk = b.c2dGbar[k] * powi(X, t.xp, t.xpf);
+        b.k2x[n] = X;
+        float gk = b.k2gbar[n] * powi(X, t.xp, t.xpf);
         G += gk;
         GE = fmaf(gk, t.ek, GE);
     }
     // SynChans: events delivered this step (SimpleSynHandler), dual exponential
-    for (uint32_t k = b.syn0[n]; k < b.syn0[n + 1]; ++k) {
-        const SynType& t = c_synTypes[b.synType[k]];
-        uint32_t e = b.evCur[k];
-        const uint32_t end = b.evEnd[k];
-        float act = 0.f;
-        while (e < end && b.evStep[e] <= step) act += b.evAct[e++];
-        b.evCur[k] = e;
-        float X = fmaf(act, t.xc1, b.synX[k] * t.xc2);
-        float Y = fmaf(X, t.yc1, b.synY[k] * t.yc2);
-        b.synX[k] = X;
-        b.synY[k] = Y;
-        float gk = Y * b.synNorm[k];
-        G += gk;
-        GE = fmaf(gk, t.ek, GE);
+    if (info & kNodeSyn) {
+        for (uint32_t k = b.syn0[n]; k < b.syn0[n + 1]; ++k) {
+            const SynType& t = c_synTypes[b.synType[k]];
+            uint32_t e = b.evCur[k];
+            const uint32_t end = b.evEnd[k];
+            float act = 0.f;
+            while (e < end && b.evStep[e] <= step) act += b.evAct[e++];
+            b.evCur[k] = e;
+            float X = fmaf(act, t.xc1, b.synX[k] * t.xc2);
+            float Y = fmaf(X, t.yc1, b.synY[k] * t.yc2);
+            b.synX[k] = X;
+            b.synY[k] = Y;
+            float gk = Y * b.synNorm[k];
+            G += gk;
+            GE = fmaf(gk, t.ek, GE);
+        }
     }
     diag = b.HS2[n] + (double)G;
     rhs = fma(V, b.CmByDt[n], b.EmByRm[n]) + (double)GE;
 }
 
-__device__ void stepCellMixed(const MixBatch& b, uint32_t cell, uint32_t nsteps, uint32_t lane) {
+struct Team {
+    uint32_t tid, nth, bar;
+};
+
+__device__ __forceinline__ void teamSync(const Team& t) {
+    if (t.nth == 32) __syncwarp();
+    else asm volatile("bar.sync %0, %1;" ::"r"(t.bar), "r"(t.nth) : "memory");
+}
+
+__device__ void stepCell(const MixBatch& b, uint32_t cell, uint32_t nsteps, const Team& tm) {
     const MixCellRange cr = b.cells[cell];
-    const uint32_t* lp = b.levelPtr + cr.level0;
     const uint32_t base = cr.node0;
     unsigned long long step = b.stepCount[cell];
     uint32_t stimCur = b.stimCur[cell];
     uint32_t spk = b.spikeCount[cell];
     for (uint32_t s = 0; s < nsteps; ++s, ++step) {
-        if (lane == 0) {
+        if (tm.tid == 0) {
             while (stimCur < cr.nStim && b.stimStep[cr.stim0 + stimCur] <= step) {
                 b.injVal[cr.inj0 + b.stimEntry[cr.stim0 + stimCur]] = b.stimValue[cr.stim0 + stimCur];
                 ++stimCur;
             }
         }
-        __syncwarp();
-        // assembly: every compartment's channels and FP64 row, in parallel;
-        // the row is staged in inv (pivot) and rhsF (right-hand side)
-        for (uint32_t i = lane; i < cr.nNodes; i += 32) {
+        teamSync(tm);
+        // assembly, all compartment nodes in parallel; rows staged in inv/gEl
+        for (uint32_t i = tm.tid; i < cr.nNodes; i += tm.nth) {
             const uint32_t n = base + i;
             const uint32_t info = b.nodeInfo[n];
-            if (info & kNodeCenter) continue;
+            if (info & kNodeCenter) {
+                b.inv[n] = b.HS2[n];
+                b.gEl[n] = 0.0;
+                continue;
+            }
             double d, r;
-            nodeRow(b, n, step, d, r);
+            nodeRow(b, n, info, step, d, r);
             if (info & kNodeInject)
                 for (uint32_t k = 0; k < cr.nInj; ++k)
                     if (b.injNode[cr.inj0 + k] == i) r += b.injVal[cr.inj0 + k];
             b.inv[n] = d;
-            b.rhsF[n] = r;
+            b.gEl[n] = r;
         }
-        __syncwarp();
-        // forward elimination, deepest level first: pull the children's
-        // eliminated rows, keep 1/pivot and the eliminated rhs
-        for (int L = (int)cr.nLevels - 1; L >= 0; --L) {
-            for (uint32_t i = lp[L] + lane; i < lp[L + 1]; i += 32) {
-                const uint32_t n = base + i;
-                const bool center = b.nodeInfo[n] & kNodeCenter;
-                double d = center ? b.HS2[n] : b.inv[n];
-                double r = center ? 0.0 : b.rhsF[n];
-                for (uint32_t c = b.child0[n]; c < b.child0[n + 1]; ++c) {
-                    const double oc = b.off[c];
-                    const double f = oc * b.inv[c];
-                    d = fma(-f, oc, d);
-                    r = fma(-f, b.rhsF[c], r);
-                }
-                b.inv[n] = rcpNewton(d);
-                b.rhsF[n] = r;
-            }
-            __syncwarp();
-        }
-        // backward substitution, root first; then V and the Ca pools
+        teamSync(tm);
+        // forward elimination: units level by level, each unit serially;
+        // every node pulls its children (diag -= off^2/pivot_c, rhs -= off*g_c)
+        const uint32_t* up = b.unitPtr + cr.level0;
+        const uint2* un = b.units + cr.unit0;
+        const uint32_t* cl = b.childList + cr.child0;
         for (uint32_t L = 0; L < cr.nLevels; ++L) {
-            for (uint32_t i = lp[L] + lane; i < lp[L + 1]; i += 32) {
-                const uint32_t n = base + i;
-                double r = b.rhsF[n];
-                if (L > 0) r = fma(-b.off[n], b.VMid[b.parent[n]], r);
-                const double vm = r * b.inv[n];
-                b.VMid[n] = vm;
-                if (!(b.nodeInfo[n] & kNodeCenter)) {
-                    const double Vold = b.V[n];
-                    const double Vnew = fma(2.0, vm, -Vold);
-                    b.V[n] = Vnew;
-                    const float vca = (float)(b.caAdvance == 1 ? vm : fma(2.0, vm, -Vnew));
-                    for (uint32_t p = b.pool0[n]; p < b.pool0[n + 1]; ++p) {
-                        float act = fmaf(-b.caG[p], vca, b.caGE[p]);
-                        // c f1 + f2 act with f1 = 1 - g1 (g1 = 1 - f1 from FP64)
-                        float c0 = b.poolC[p];
-                        float c = fmaf(-b.poolF1[p], c0, c0) + b.poolF2[p] * act;
-                        float ca = b.poolBasal[p] + c;
-                        if (b.poolCeil[p] > 0.f && ca > b.poolCeil[p]) { ca = b.poolCeil[p]; c = ca - b.poolBasal[p]; }
-                        if (ca < b.poolFloor[p]) { ca = b.poolFloor[p]; c = ca - b.poolBasal[p]; }
-                        b.poolC[p] = c;
-                        b.poolCa[p] = ca;
+            for (uint32_t u = up[L] + tm.tid; u < up[L + 1]; u += tm.nth) {
+                const uint2 rg = un[u];
+                // the node eliminated just before is the last child in
+                // post-order and the lower neighbour in a chain: its pivot
+                // and g stay in registers
+                double pIv = 0.0, pG = 0.0;
+                for (uint32_t v = rg.x; v < rg.y; ++v) {
+                    const uint32_t n = base + v;
+                    double d = b.inv[n], r = b.gEl[n];
+                    const uint32_t cs = b.childStart[n], nc = (b.nodeInfo[n] >> 16) & 0xFF;
+                    for (uint32_t k = cs; k < cs + nc; ++k) {
+                        const uint32_t cv = cl[k];
+                        const uint32_t c = base + cv;
+                        const bool prev = cv + 1 == v && v > rg.x;
+                        const double ivc = prev ? pIv : b.inv[c];
+                        const double gc = prev ? pG : b.gEl[c];
+                        d = fma(-b.offsq[c], ivc, d);
+                        r = fma(-b.off[c], gc, r);
+                    }
+                    pIv = rcpNewton(d);
+                    pG = r * pIv;
+                    b.inv[n] = pIv;
+                    b.gEl[n] = pG;
+                }
+            }
+            teamSync(tm);
+        }
+        // back substitution in the reverse order: VMid = g - (off/pivot) VMid[parent],
+        // V = 2 VMid - V, then the node's Ca pool
+        for (int L = (int)cr.nLevels - 1; L >= 0; --L) {
+            for (uint32_t u = up[L] + tm.tid; u < up[L + 1]; u += tm.nth) {
+                const uint2 rg = un[u];
+                double pVm = 0.0;   // VMid of the node substituted just before
+                for (uint32_t v = rg.y; v-- > rg.x;) {
+                    const uint32_t n = base + v;
+                    double vm = b.gEl[n];
+                    const uint32_t pa = b.parent[n];
+                    if (pa != ~0u) {
+                        const double vp = (pa == v + 1 && v + 1 < rg.y) ? pVm : b.VMid[base + pa];
+                        vm = fma(-(b.off[n] * b.inv[n]), vp, vm);
+                    }
+                    pVm = vm;
+                    b.VMid[n] = vm;
+                    const uint32_t info = b.nodeInfo[n];
+                    if (!(info & kNodeCenter)) {
+                        const double Vold = b.V[n];
+                        const double Vnew = fma(2.0, vm, -Vold);
+                        b.V[n] = Vnew;
+                        if (info & kNodePool) {
+                            const float vca = (float)(b.caAdvance == 1 ? vm : fma(2.0, vm, -Vnew));
+                            float act = fmaf(-b.caG[n], vca, b.caGE[n]);
+                            // c f1 + f2 act with f1 = 1 - g1 (g1 = 1 - f1 from FP64)
+                            float c0v = b.poolC[n];
+                            float c = fmaf(-b.poolG1[n], c0v, c0v) + b.poolF2[n] * act;
+                            float cav = b.poolBasal[n] + c;
+                            if (b.poolCeil[n] > 0.f && cav > b.poolCeil[n]) { cav = b.poolCeil[n]; c = cav - b.poolBasal[n]; }
+                            if (cav < b.poolFloor[n]) { cav = b.poolFloor[n]; c = cav - b.poolBasal[n]; }
+                            b.poolC[n] = c;
+                            b.poolCa[n] = cav;
+                        }
                     }
                 }
             }
-            __syncwarp();
+            teamSync(tm);
         }
-        // SpikeGens (SpikeGen::process with the HSolve's V and currTime)
-        if (lane == 0) {
+        // SpikeGens (SpikeGen::process with the solver's V and currTime)
+        if (tm.tid == 0) {
             const double currTime = b.dt * (double)(step + 1);
             for (uint32_t k = cr.sg0; k < cr.sg0 + cr.nSg; ++k) {
                 double Vs = b.V[base + b.sgNode[k]];
@@ -295,77 +336,87 @@ __device__ void stepCellMixed(const MixBatch& b, uint32_t cell, uint32_t nsteps,
         if (cr.nRec && ((step + 1) % b.recStride) == 0) {
             uint32_t smp = (uint32_t)((step + 1) / b.recStride);
             if (smp < b.recCap)
-                for (uint32_t r = lane; r < cr.nRec; r += 32)
+                for (uint32_t r = tm.tid; r < cr.nRec; r += tm.nth)
                     b.recBuf[(size_t)smp * b.recLd + cr.rec0 + r] = b.V[base + b.recNode[cr.rec0 + r]];
         }
-        __syncwarp();
+        teamSync(tm);
     }
-    if (lane == 0) {
+    if (tm.tid == 0) {
         b.stepCount[cell] = step;
         b.stimCur[cell] = stimCur;
         b.spikeCount[cell] = spk;
     }
 }
 
-__global__ void __launch_bounds__(512) hsBatchStepMixed(MixBatch b, const uint32_t* __restrict__ warpCellPtr,
-                                                        const uint32_t* __restrict__ warpCells,
-                                                        uint32_t nWarps, uint32_t nsteps) {
-    uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t lane = threadIdx.x & 31;
-    if (w >= nWarps) return;
-    for (uint32_t k = warpCellPtr[w]; k < warpCellPtr[w + 1]; ++k) stepCellMixed(b, warpCells[k], nsteps, lane);
+__global__ void __launch_bounds__(512) hsBatchStepMixed(MixBatch b, const uint32_t* __restrict__ teamCellPtr,
+                                                        const uint32_t* __restrict__ teamCells, uint32_t nTeams,
+                                                        uint32_t warpsPerTeam, uint32_t nsteps) {
+    const uint32_t teamsPerCta = blockDim.x / (32 * warpsPerTeam);
+    const uint32_t teamInCta = threadIdx.x / (32 * warpsPerTeam);
+    const uint32_t team = blockIdx.x * teamsPerCta + teamInCta;
+    if (team >= nTeams) return;     // whole teams leave together
+    Team tm;
+    tm.nth = 32 * warpsPerTeam;
+    tm.tid = threadIdx.x - teamInCta * tm.nth;
+    tm.bar = teamInCta + 1;
+    for (uint32_t k = teamCellPtr[team]; k < teamCellPtr[team + 1]; ++k) stepCell(b, teamCells[k], nsteps, tm);
 }
 
 // Reinit: V = initVm, gates at their steady state, Ca = CaBasal, synapses,
 // K(Ca) X, spike and stimulus state.  One warp per cell.
 __global__ void hsBatchReinitMixed(MixBatch b, const double* __restrict__ initVm,
-                                   const float* __restrict__ c2dX0, const uint32_t* __restrict__ evStart) {
+                                   const float* __restrict__ k2x0, const uint32_t* __restrict__ evStart) {
     uint32_t cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     uint32_t lane = threadIdx.x & 31;
     if (cell >= b.nCells) return;
     const MixCellRange cr = b.cells[cell];
+    const uint64_t ld = b.ld;
     for (uint32_t i = lane; i < cr.nNodes; i += 32) {
-        uint32_t n = cr.node0 + i;
+        const uint32_t n = cr.node0 + i;
+        const uint32_t info = b.nodeInfo[n];
         b.V[n] = initVm[n];
-        for (uint32_t p = b.pool0[n]; p < b.pool0[n + 1]; ++p) {
-            b.poolC[p] = 0.f;
-            b.poolCa[p] = b.poolBasal[p];
+        if (info & kNodeCenter) continue;
+        if (info & kNodePool) {
+            b.poolC[n] = 0.f;
+            b.poolCa[n] = b.poolBasal[n];
         }
-    }
-    __syncwarp();
-    for (uint32_t i = lane; i < cr.nNodes; i += 32) {
-        uint32_t n = cr.node0 + i;
-        if (b.nodeInfo[n] & kNodeCenter) continue;
-        float v = (float)b.V[n];
-        RowF vr = rowF(b.vTab, b.vCol, b.vRows, v, b.vMin, b.vMax, b.vInvDx);
-        uint32_t s = b.state0[n];
-        uint32_t p0 = b.pool0[n];
-        for (uint32_t q = b.chan0[n]; q < b.chan0[n + 1]; ++q) {
-            const ChanType& t = c_chanTypes[b.chanType[q]];
-            if (t.xp) b.state[s++] = gateF(vr, b.vCol, t.colX, 0.f, 0.f, 0.f, true);
-            if (t.yp) b.state[s++] = gateF(vr, b.vCol, t.colY, 0.f, 0.f, 0.f, true);
+        const float ca = (info & kNodePool) ? b.poolCa[n] : 0.f;
+        RowF vr = rowF(b.vTab, b.vCol, b.vRows, (float)b.V[n], b.vMin, b.vMax, b.vInvDx);
+        const uint32_t types = b.ctype4[n];
+        for (int j = 0; j < kMaxChan; ++j) {
+            const uint32_t tj = (types >> (8 * j)) & 0xFF;
+            if (tj == kNoType) break;
+            const ChanType& t = c_chanTypes[tj];
+            float* st = b.state + (uint64_t)(3 * j) * ld + n;
+            if (t.xp) st[0] = gateF(vr, b.vCol, t.colX, 0.f, 0.f, 0.f, true);
+            if (t.yp) st[ld] = gateF(vr, b.vCol, t.colY, 0.f, 0.f, 0.f, true);
             if (t.zp) {
-                if (t.zSrc >= 0) {
-                    RowF cr2 = rowF(b.caTab, b.caCol, b.caRows, b.poolCa[p0 + t.zSrc], b.caMin, b.caMax, b.caInvDx);
-                    b.state[s++] = gateF(cr2, b.caCol, t.colZ, 0.f, 0.f, 0.f, true);
+                if (t.zCa) {
+                    RowF cr2 = rowF(b.caTab, b.caCol, b.caRows, ca, b.caMin, b.caMax, b.caInvDx);
+                    st[2 * ld] = gateF(cr2, b.caCol, t.colZ, 0.f, 0.f, 0.f, true);
                 } else {
-                    b.state[s++] = gateF(vr, b.vCol, t.colZ, 0.f, 0.f, 0.f, true);
+                    st[2 * ld] = gateF(vr, b.vCol, t.colZ, 0.f, 0.f, 0.f, true);
                 }
             }
         }
-        for (uint32_t k = b.c2d0[n]; k < b.c2d0[n + 1]; ++k) b.c2dX[k] = c2dX0[k];
-        for (uint32_t k = b.syn0[n]; k < b.syn0[n + 1]; ++k) {
-            b.synX[k] = 0.f;
-            b.synY[k] = 0.f;
-            b.evCur[k] = evStart[k];
-        }
+        if (((info >> 8) & 0xFF) != kNoType) b.k2x[n] = k2x0[n];
+        if (info & kNodeSyn)
+            for (uint32_t k = b.syn0[n]; k < b.syn0[n + 1]; ++k) {
+                b.synX[k] = 0.f;
+                b.synY[k] = 0.f;
+                b.evCur[k] = evStart[k];
+            }
     }
-    for (uint32_t k = cr.sg0 + lane; k < cr.sg0 + cr.nSg; k += 32) b.sgLast[k] = -b.sgRefract[k];
+    for (uint32_t k = cr.sg0 + lane; k < cr.sg0 + cr.nSg; k += 32) {
+        b.sgLast[k] = -b.sgRefract[k];
+        b.sgFired[k] = 0;
+    }
     if (lane == 0) {
         b.stepCount[cell] = 0;
         b.stimCur[cell] = 0;
         b.spikeCount[cell] = 0;
     }
+    __syncwarp();
     if (cr.nRec)
         for (uint32_t r = lane; r < cr.nRec; r += 32)
             b.recBuf[cr.rec0 + r] = b.V[cr.node0 + b.recNode[cr.rec0 + r]];
@@ -398,17 +449,19 @@ cudaError_t uploadMixedTypes(const ChanType* ct, int nct, const C2dType* kt, int
     return e;
 }
 
-cudaError_t launchBatchStepMixed(const MixBatch& b, const uint32_t* warpCellPtr, const uint32_t* warpCells,
-                                 uint32_t nWarps, uint32_t nsteps, uint32_t threadsPerCta, cudaStream_t st) {
-    uint32_t blocks = (nWarps * 32 + threadsPerCta - 1) / threadsPerCta;
-    hsBatchStepMixed<<<blocks, threadsPerCta, 0, st>>>(b, warpCellPtr, warpCells, nWarps, nsteps);
+cudaError_t launchBatchStepMixed(const MixBatch& b, const uint32_t* teamCellPtr, const uint32_t* teamCells,
+                                 uint32_t nTeams, uint32_t warpsPerTeam, uint32_t threadsPerCta, uint32_t nsteps,
+                                 cudaStream_t st) {
+    uint32_t teamsPerCta = threadsPerCta / (32 * warpsPerTeam);
+    uint32_t blocks = (nTeams + teamsPerCta - 1) / teamsPerCta;
+    hsBatchStepMixed<<<blocks, threadsPerCta, 0, st>>>(b, teamCellPtr, teamCells, nTeams, warpsPerTeam, nsteps);
     return cudaGetLastError();
 }
 
-cudaError_t launchBatchReinitMixed(const MixBatch& b, const double* initVm, const float* c2dX0,
+cudaError_t launchBatchReinitMixed(const MixBatch& b, const double* initVm, const float* k2x0,
                                    const uint32_t* evStart, cudaStream_t st) {
     uint32_t blocks = (b.nCells * 32 + 255) / 256;
-    hsBatchReinitMixed<<<blocks ? blocks : 1, 256, 0, st>>>(b, initVm, c2dX0, evStart);
+    hsBatchReinitMixed<<<blocks ? blocks : 1, 256, 0, st>>>(b, initVm, k2x0, evStart);
     return cudaGetLastError();
 }
 
