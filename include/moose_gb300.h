@@ -291,19 +291,21 @@ int hs_read_spikes(HsSolver* s, uint32_t* gen, double* time, uint32_t capacity,
  * No counterpart in the reference (it runs one serial HSolve per cell).  */
 typedef struct HsBatch HsBatch;
 
-/* Launch shape of the batched kernel (0 keeps the current value).  A team of
- * warps steps one cell (one warp in FP64); cells are packed over
- * ctas_per_sm x SM-count CTAs. */
+/* Launch shape of the batched kernel (0 keeps the current value).
+ * FP64: one warp steps one cell; cells are packed over ctas_per_sm x
+ * SM-count CTAs.  Mixed: one CTA steps a forest of cells at a time; a forest
+ * holds its elimination arrays in the CTA's shared memory (30 B per node),
+ * so ctas_per_sm and forest_nodes set the forest size.  Changing either on
+ * a mixed batch renumbers its nodes: its state, recording and inject
+ * targets start over and hs_batch_reinit must follow. */
 typedef struct HsBatchTuning {
-    uint32_t threads_per_cta;   /* multiple of 32, at most 1024 (default 256) */
-    uint32_t ctas_per_sm;       /* CTAs per SM in the single wave (default 4) */
+    uint32_t threads_per_cta;   /* multiple of 32; FP64 <= 256 (default 256),
+                                   mixed <= 1024 (default 512) */
+    uint32_t ctas_per_sm;       /* CTAs per SM (default 4 FP64, 1 mixed) */
     uint32_t steps_per_launch;  /* dt steps per kernel launch (default 100) */
     uint32_t use_graph;         /* capture a process() call as a CUDA graph */
-    uint32_t warps_per_team;    /* mixed: warps stepping one cell (default 2) */
-    uint32_t level_cost;        /* mixed, creation only: cost of one level of
-                                   the elimination schedule in serial node
-                                   steps, which sets how much of each tree is
-                                   eliminated serially per thread (default 8) */
+    uint32_t forest_nodes;      /* mixed: most nodes per shared-memory forest
+                                   (0: as many as shared memory holds) */
 } HsBatchTuning;
 
 int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds,

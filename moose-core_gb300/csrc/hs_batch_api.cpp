@@ -34,10 +34,10 @@ namespace hsg {
 int setLastError(int code, const std::string& msg);
 cudaError_t uploadMixedTypes(const ChanType* ct, int nct, const C2dType* kt, int nkt, const SynType* st,
                              int nst, cudaStream_t s);
-cudaError_t launchBatchStepMixed(const MixBatch& b, const uint32_t* teamCellPtr, const uint32_t* teamCells,
-                                 uint32_t nTeams, uint32_t warpsPerTeam, uint32_t threadsPerCta, uint32_t nsteps,
-                                 cudaStream_t st);
-cudaError_t launchBatchReinitMixed(const MixBatch& b, const double* initVm, const float* c2dX0,
+cudaError_t launchForestStepMixed(const MixBatch& b, const uint32_t* ctaPtr, const uint32_t* ctaForests,
+                                  uint32_t nCtas, uint32_t threadsPerCta, uint32_t smemBytes, uint32_t cap,
+                                  uint32_t nsteps, cudaStream_t st);
+cudaError_t launchBatchReinitMixed(const MixBatch& b, uint32_t nNodes, const double* initVm, const float* c2dX0,
                                    const uint32_t* evStart, cudaStream_t st);
 cudaError_t launchScatterInject(double* const* addr, uint8_t* const* flag, const double* val, uint32_t n,
                                 cudaStream_t st);
@@ -102,7 +102,7 @@ struct MixHost {
     std::vector<std::tuple<double, double, double>> synTypeKey;
     std::vector<uint8_t> synTypeOf;
     uint64_t nNodes = 0;
-    std::vector<double> elimCost;                 // per cell: estimated elimination time
+    uint32_t nForests = 0, nShared = 0;           // forests, of them in shared memory
 };
 
 }  // namespace
@@ -119,11 +119,14 @@ struct HsBatch {
     std::vector<CellPlan> plans;
     uint64_t nCompt = 0;
     // packing / tuning
-    uint32_t threadsPerCta = 256, ctasPerSm = 4, stepsPerLaunch = 100, warpsPerTeam = 2;
-    uint32_t levelCost = 8;  // mixed: cost of a schedule level in serial node steps
+    uint32_t threadsPerCta = 256, ctasPerSm = 4, stepsPerLaunch = 100;
+    uint32_t forestNodes = 0;    // mixed: forest size limit (0: shared-memory capacity)
     bool useGraph = true;
     uint32_t nWarps = 0, nCtas = 0;
     uint32_t *dWarpPtr = nullptr, *dWarpCells = nullptr;
+    // mixed: forests per CTA, shared-memory forest capacity
+    uint32_t *dCtaPtr = nullptr, *dCtaForests = nullptr;
+    uint32_t mixCap = 0, mixSmem = 0;
     DevBuf buf;              // long-lived allocations
     DevBuf packBuf;          // packing arrays (replaced by retuning)
     // FP64
@@ -172,34 +175,28 @@ namespace {
 cudaError_t launchStep(HsBatch* b, uint32_t k) {
     if (b->precision == HS_PREC_FP64)
         return launchBatchStepFp64(b->dDcs, b->dWarpPtr, b->dWarpCells, b->nWarps, k, b->threadsPerCta, b->st);
-    return launchBatchStepMixed(b->mb, b->dWarpPtr, b->dWarpCells, b->nWarps, b->warpsPerTeam, b->threadsPerCta, k,
-                                b->st);
+    return launchForestStepMixed(b->mb, b->dCtaPtr, b->dCtaForests, b->nCtas, b->threadsPerCta, b->mixSmem,
+                                 b->mixCap, k, b->st);
 }
 
-// Longest-processing-time packing: cells to the CTAs of one wave, then to
-// the teams (of warpsPerTeam warps) inside each CTA.
+// Longest-processing-time packing of the FP64 batch: cells to the CTAs of one
+// wave, then to the warps inside each CTA.  (The mixed batch packs its
+// forests when its layout is built.)
 int repack(HsBatch* b) {
-    b->packBuf.freeAll();
-    b->packBuf.err = cudaSuccess;
     if (b->gexec) {
         cudaGraphExecDestroy(b->gexec);
         b->gexec = nullptr;
     }
-    const uint32_t W = b->precision == HS_PREC_FP64 ? 1 : b->warpsPerTeam;
-    const uint32_t teamsPerCta = b->threadsPerCta / (32 * W);
-    if (teamsPerCta == 0 || teamsPerCta > 15 || b->threadsPerCta % (32 * W))
-        return berr(HS_EINVAL, "threads_per_cta must hold 1..15 teams of warps_per_team warps");
+    if (b->precision != HS_PREC_FP64) return HS_OK;
+    b->packBuf.freeAll();
+    b->packBuf.err = cudaSuccess;
+    const uint32_t teamsPerCta = b->threadsPerCta / 32;
     b->nCtas = std::max<uint32_t>(1, b->nSm * b->ctasPerSm);
-    b->nWarps = b->nCtas * teamsPerCta;     // teams (a team is one warp for FP64)
+    b->nWarps = b->nCtas * teamsPerCta;
     std::vector<double> cost(b->nCells);
     for (uint32_t c = 0; c < b->nCells; ++c) {
-        if (b->precision == HS_PREC_FP64) {
-            const CellPlan& P = b->plans[c];
-            cost[c] = P.N + 0.3 * P.C + 0.5 * P.S + 2.0 * (P.fLevelPtr.size() + P.bLevelPtr.size());
-        } else {
-            const MixCellRange& R = b->mh.cells[c];
-            cost[c] = std::ceil(R.nNodes / (32.0 * W)) * 8.0 + b->mh.elimCost[c];
-        }
+        const CellPlan& P = b->plans[c];
+        cost[c] = P.N + 0.3 * P.C + 0.5 * P.S + 2.0 * (P.fLevelPtr.size() + P.bLevelPtr.size());
     }
     std::vector<uint32_t> order(b->nCells);
     for (uint32_t c = 0; c < b->nCells; ++c) order[c] = c;
@@ -350,109 +347,84 @@ int8_t powCode(double p, float& pf) {
     return -1;
 }
 
-// Elimination schedule of one tree (see MixCellRange).  Maximal subtrees of
-// at most S nodes become level-0 units in post-order; the nodes above them are
-// cut into unbranched chains, bottom to top, a chain one level above the
-// highest chain hanging below it.  S = 0 gives chains only; S >= T one serial
-// unit.  The estimated time of a level is the serial node count of its
-// busiest thread (units dealt round-robin, longest first, over `nth` threads)
-// plus `levelCost` for the barrier and memory round trip that ends it.
-struct UnitPlan {
-    std::vector<uint32_t> order;                       // tree node of each new index
-    std::vector<uint32_t> levelPtr;                    // unit offsets per level
-    std::vector<std::pair<uint32_t, uint32_t>> units;  // new-index ranges
-    double cost = 0;
+// Star-form tree of one cell (hs_mixed.cuh): compartments 0..N-1 in the
+// plan's Hines numbering, junction nodes N..T-1; children in CSR.
+struct StarTree {
+    uint32_t N = 0, T = 0, root = 0;
+    std::vector<uint32_t> chPtr, ch;
+    std::vector<double> diag, off;
 };
 
-UnitPlan planUnits(const std::vector<std::vector<uint32_t>>& tk, const std::vector<uint32_t>& bfs, uint32_t S,
-                   uint32_t nth, double levelCost) {
-    const uint32_t T = (uint32_t)tk.size();
-    std::vector<uint32_t> sz(T, 1), par(T, ~0u);
-    for (uint32_t t = 0; t < T; ++t)
-        for (uint32_t c : tk[t]) par[c] = t;
-    for (uint32_t k = T; k-- > 0;) {
-        const uint32_t t = bfs[k];
-        if (par[t] != ~0u) sz[par[t]] += sz[t];
+int starTree(const CellPlan& P, StarTree& S) {
+    const uint32_t N = P.N;
+    std::vector<int64_t> mparent(N, -1);
+    for (uint32_t i = 0; i < N; ++i)
+        for (uint32_t c : P.children[i]) mparent[c] = i;
+    int64_t root = -1;
+    for (uint32_t i = 0; i < N; ++i)
+        if (mparent[i] < 0) root = i;
+    if (root < 0) return berr(HS_EINVAL, "mixed batch: no root compartment");
+    std::vector<double> Ga(N), diag(N);
+    for (uint32_t i = 0; i < N; ++i) {
+        Ga[i] = 2.0 / P.Ra[i];
+        diag[i] = P.Cm[i] / (P.dtSetup / 2.0) + 1.0 / P.Rm[i];
     }
-    auto small = [&](uint32_t t) { return sz[t] <= S; };
-    std::vector<std::vector<uint32_t>> unitNodes;
-    std::vector<uint32_t> unitLevel;
-    std::vector<uint32_t> stack;
-    for (uint32_t t : bfs) {
-        if (!small(t) || (par[t] != ~0u && small(par[t]))) continue;
-        // post-order of the subtree at t: children before their parent
-        std::vector<uint32_t> post;
-        stack.assign(1, t);
-        while (!stack.empty()) {
-            uint32_t u = stack.back();
-            stack.pop_back();
-            post.push_back(u);
-            for (uint32_t c : tk[u]) stack.push_back(c);
-        }
-        std::reverse(post.begin(), post.end());
-        unitNodes.push_back(std::move(post));
-        unitLevel.push_back(0);
-    }
-    std::vector<uint32_t> chainOf(T, ~0u);
-    for (uint32_t k = T; k-- > 0;) {
-        const uint32_t t = bfs[k];
-        if (small(t)) continue;
-        uint32_t nTop = 0, top = 0, lvl = 1;
-        for (uint32_t c : tk[t])
-            if (!small(c)) {
-                ++nTop;
-                top = c;
-                lvl = std::max(lvl, unitLevel[chainOf[c]] + 1);
+    std::vector<std::vector<uint32_t>> tk(N);
+    std::vector<double> toff(N, 0.0);
+    for (uint32_t p = 0; p < N; ++p) {
+        const std::vector<uint32_t>& chs = P.children[p];
+        if (chs.size() == 1) {
+            const uint32_t c = chs[0];
+            const double g = Ga[p] * Ga[c] / (Ga[p] + Ga[c]);
+            diag[p] += g;
+            diag[c] += g;
+            tk[p].push_back(c);
+            toff[c] = -g;
+        } else if (chs.size() >= 2) {
+            const uint32_t J = (uint32_t)diag.size();
+            double gsum = Ga[p];
+            for (uint32_t c : chs) gsum += Ga[c];
+            diag.push_back(gsum);
+            toff.push_back(-Ga[p]);
+            tk.push_back(std::vector<uint32_t>(chs.begin(), chs.end()));
+            diag[p] += Ga[p];
+            tk[p].push_back(J);
+            for (uint32_t c : chs) {
+                diag[c] += Ga[c];
+                toff[c] = -Ga[c];
             }
-        if (nTop == 1) {
-            chainOf[t] = chainOf[top];
-            unitNodes[chainOf[t]].push_back(t);
-        } else {
-            chainOf[t] = (uint32_t)unitNodes.size();
-            unitNodes.push_back({t});
-            unitLevel.push_back(lvl);
         }
     }
-    uint32_t maxL = 0;
-    for (uint32_t l : unitLevel) maxL = std::max(maxL, l);
-    std::vector<std::vector<uint32_t>> byLevel(maxL + 1);
-    for (uint32_t u = 0; u < unitNodes.size(); ++u) byLevel[unitLevel[u]].push_back(u);
-    UnitPlan P;
-    P.levelPtr.push_back(0);
-    for (auto& L : byLevel) {
-        if (L.empty()) continue;
-        std::stable_sort(L.begin(), L.end(),
-                         [&](uint32_t x, uint32_t y) { return unitNodes[x].size() > unitNodes[y].size(); });
-        double busiest = 0;
-        for (size_t i = 0; i < L.size(); i += nth) busiest += (double)unitNodes[L[i]].size();
-        P.cost += busiest + levelCost;
-        for (uint32_t u : L) {
-            const uint32_t a = (uint32_t)P.order.size();
-            P.order.insert(P.order.end(), unitNodes[u].begin(), unitNodes[u].end());
-            P.units.push_back({a, (uint32_t)P.order.size()});
-        }
-        P.levelPtr.push_back((uint32_t)P.units.size());
-    }
-    return P;
+    const uint32_t T = (uint32_t)diag.size();
+    // every node reachable from the root exactly once
+    std::vector<uint32_t> bfs;
+    bfs.reserve(T);
+    bfs.push_back((uint32_t)root);
+    for (size_t k = 0; k < bfs.size() && bfs.size() <= T; ++k)
+        for (uint32_t c : tk[bfs[k]]) bfs.push_back(c);
+    if (bfs.size() != T) return berr(HS_EINVAL, "mixed batch: tree construction failed");
+    for (uint32_t t = 0; t < T; ++t)
+        if (tk[t].size() > 255) return berr(HS_ENOTSUP, "mixed batch: more than 255 children at a node");
+    S.N = N;
+    S.T = T;
+    S.root = (uint32_t)root;
+    S.chPtr.assign(T + 1, 0);
+    for (uint32_t t = 0; t < T; ++t) S.chPtr[t + 1] = S.chPtr[t] + (uint32_t)tk[t].size();
+    S.ch.reserve(S.chPtr[T]);
+    for (uint32_t t = 0; t < T; ++t) S.ch.insert(S.ch.end(), tk[t].begin(), tk[t].end());
+    S.diag = std::move(diag);
+    S.off = std::move(toff);
+    return HS_OK;
 }
 
-// The cheapest schedule over subtree bounds 0, 1, 2, 3, 4, 6, 8, 12, ...
-UnitPlan bestUnits(const std::vector<std::vector<uint32_t>>& tk, const std::vector<uint32_t>& bfs, uint32_t nth,
-                   double levelCost) {
-    const uint32_t T = (uint32_t)tk.size();
-    UnitPlan best = planUnits(tk, bfs, 0, nth, levelCost);
-    for (uint32_t p = 1; p < 2 * T; p *= 2)
-        for (uint32_t S : {p, p + p / 2}) {
-            if (S == 0 || S > T) continue;
-            UnitPlan u = planUnits(tk, bfs, S, nth, levelCost);
-            if (u.cost < best.cost) best = std::move(u);
-        }
-    return best;
-}
+// Shared-memory bytes per forest node: D, R, OFF (8 B), TOPO (4 B), PAR (2 B);
+// the kernel also keeps kSmemLevels level offsets (4 B) there.
+constexpr uint32_t kForestNodeBytes = 30;
 
 int buildMixed(HsBatch* b) {
     const uint32_t nC = b->nCells;
     MixHost& H = b->mh;
+    H = MixHost();
     // one shared V table and Ca table for the batch
     const Table& V0 = b->plans[0].vTable;
     const Table& C0 = b->plans[0].caTable;
@@ -462,6 +434,181 @@ int buildMixed(HsBatch* b) {
         if (V.data != V0.data || V.min != V0.min || V.max != V0.max || Ca.data != C0.data)
             return berr(HS_ENOTSUP, "mixed batch: all cells must share one rate-table set");
     }
+    // forest capacity from the shared memory of a CTA
+    int optin = 0, perSm = 0;
+    cudaError_t ce = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
+    if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&perSm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, b->device);
+    if (ce != cudaSuccess) return cerr(ce, "shared memory size");
+    const uint32_t perCta =
+        std::min<uint32_t>((uint32_t)optin, (uint32_t)perSm / std::max<uint32_t>(1, b->ctasPerSm) - 1024) / 256 * 256;
+    if (perCta < kSmemLevels * 4 + 8 * kForestNodeBytes) return berr(HS_EINVAL, "too many CTAs per SM");
+    uint32_t cap = std::min<uint32_t>(kMaxForestNodes, (perCta - kSmemLevels * 4) / kForestNodeBytes) / 8 * 8;
+    if (b->forestNodes) cap = std::min(cap, b->forestNodes / 8 * 8);
+    if (cap < 8) return berr(HS_EINVAL, "forest_nodes too small");
+    b->mixCap = cap;
+    b->mixSmem = (kSmemLevels * 4 + cap * kForestNodeBytes + 15) / 16 * 16;
+
+    // 1. star trees
+    std::vector<StarTree> trees(nC);
+    for (uint32_t c = 0; c < nC; ++c) {
+        int rc = starTree(b->plans[c], trees[c]);
+        if (rc != HS_OK) return rc;
+        if (trees[c].T > kMaxForestNodes) return berr(HS_ENOTSUP, "mixed batch: a cell has more than 65535 nodes");
+    }
+    // 2. packing: cells to the CTAs of one wave by node count (longest
+    // processing time first), then within a CTA into forests: cells that fit
+    // the shared-memory capacity first-fit decreasing into shared forests,
+    // larger cells into global forests of up to 65535 nodes
+    const uint32_t nCtas = std::max<uint32_t>(1, b->nSm * b->ctasPerSm);
+    std::vector<uint32_t> order(nC);
+    for (uint32_t c = 0; c < nC; ++c) order[c] = c;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return trees[x].T > trees[y].T; });
+    using Item = std::pair<double, uint32_t>;
+    std::priority_queue<Item, std::vector<Item>, std::greater<Item>> pq;
+    for (uint32_t k = 0; k < nCtas; ++k) pq.push({0.0, k});
+    std::vector<std::vector<uint32_t>> ctaCells(nCtas);
+    for (uint32_t c : order) {
+        Item it = pq.top();
+        pq.pop();
+        ctaCells[it.second].push_back(c);
+        pq.push({it.first + trees[c].T * (trees[c].T > cap ? 1.5 : 1.0), it.second});
+    }
+    struct ForestPlan {
+        std::vector<uint32_t> cells;
+        uint32_t nodes = 0;
+        bool shared = true;
+    };
+    std::vector<ForestPlan> forests;
+    std::vector<uint32_t> ctaPtr(nCtas + 1, 0), ctaForests;
+    for (uint32_t k = 0; k < nCtas; ++k) {
+        std::vector<ForestPlan> fs;
+        for (uint32_t c : ctaCells[k]) {      // decreasing size
+            const uint32_t T = trees[c].T;
+            const bool sh = T <= cap;
+            const uint32_t lim = sh ? cap : kMaxForestNodes;
+            size_t f = 0;
+            while (f < fs.size() && (fs[f].shared != sh || fs[f].nodes + T > lim)) ++f;
+            if (f == fs.size()) {
+                fs.emplace_back();
+                fs.back().shared = sh;
+            }
+            fs[f].cells.push_back(c);
+            fs[f].nodes += T;
+        }
+        for (ForestPlan& f : fs) {
+            ctaForests.push_back((uint32_t)forests.size());
+            forests.push_back(std::move(f));
+        }
+        ctaPtr[k + 1] = (uint32_t)ctaForests.size();
+    }
+    // 3. node numbering: forest after forest, level-major inside a forest
+    std::vector<std::vector<uint32_t>> posOf(nC);
+    std::vector<std::pair<uint32_t, uint32_t>> nodeCT;    // (cell, tree node) of each global node
+    std::vector<MixForest> fdev(forests.size());
+    std::vector<uint32_t> levelPtr, forestCells;
+    for (size_t fi = 0; fi < forests.size(); ++fi) {
+        const ForestPlan& FP = forests[fi];
+        MixForest& F = fdev[fi];
+        std::memset(&F, 0, sizeof(F));
+        F.node0 = (uint32_t)nodeCT.size();
+        F.nNodes = FP.nodes;
+        F.level0 = (uint32_t)levelPtr.size();
+        F.cell0 = (uint32_t)forestCells.size();
+        F.nCells = (uint32_t)FP.cells.size();
+        F.shared = FP.shared ? 1 : 0;
+        forestCells.insert(forestCells.end(), FP.cells.begin(), FP.cells.end());
+        std::vector<std::pair<uint32_t, uint32_t>> cur, next;
+        for (uint32_t c : FP.cells) {
+            cur.push_back({c, trees[c].root});
+            posOf[c].assign(trees[c].T, 0);
+        }
+        levelPtr.push_back(0);
+        while (!cur.empty()) {
+            for (auto& ct : cur) {
+                posOf[ct.first][ct.second] = (uint32_t)nodeCT.size();
+                nodeCT.push_back(ct);
+            }
+            levelPtr.push_back((uint32_t)(nodeCT.size() - F.node0));
+            next.clear();
+            for (auto& ct : cur) {
+                const StarTree& S = trees[ct.first];
+                for (uint32_t k = S.chPtr[ct.second]; k < S.chPtr[ct.second + 1]; ++k) next.push_back({ct.first, S.ch[k]});
+            }
+            // junction nodes after compartments; a node's children keep
+            // their order and stay contiguous (they are all of one kind)
+            std::stable_partition(next.begin(), next.end(),
+                                  [&](const std::pair<uint32_t, uint32_t>& ct) { return ct.second < trees[ct.first].N; });
+            cur.swap(next);
+        }
+        F.nLevels = (uint32_t)(levelPtr.size() - F.level0 - 1);
+        if (nodeCT.size() - F.node0 != F.nNodes) return berr(HS_EINVAL, "mixed batch: forest layout failed");
+    }
+    const uint32_t nN = (uint32_t)nodeCT.size();
+    // 4. per-cell lists: inject entries, stimulus, SpikeGens; model maps
+    H.cells.resize(nC);
+    H.nodeOf.resize(nC);
+    H.poolOf.resize(nC);
+    b->injEntryOf.clear();
+    std::vector<double> injVal, stimValue;
+    std::vector<uint32_t> stimStep, stimEntry, sgNode;
+    std::vector<float> sgThresh, sgRefract;
+    std::vector<int32_t> sgEdge;
+    std::vector<std::vector<int32_t>> injAt(nC), c2dAt(nC);
+    std::vector<std::vector<uint32_t>> synPtr(nC), synIdx(nC);
+    for (uint32_t ci = 0; ci < nC; ++ci) {
+        const CellPlan& P = b->plans[ci];
+        const uint32_t N = P.N;
+        MixCellRange& R = H.cells[ci];
+        std::memset(&R, 0, sizeof(R));
+        H.nodeOf[ci].assign(P.hinesOf.size(), -1);
+        for (size_t m = 0; m < P.hinesOf.size(); ++m)
+            if (P.hinesOf[m] >= 0) H.nodeOf[ci][m] = posOf[ci][P.hinesOf[m]];
+        H.poolOf[ci].assign(P.poolSolverOf.size(), -1);
+        injAt[ci].assign(N, -1);
+        R.inj0 = (uint32_t)injVal.size();
+        for (uint32_t i = 0; i < N; ++i)
+            if (P.injPresent[i]) {
+                injAt[ci][i] = (int32_t)(injVal.size() - R.inj0);
+                injVal.push_back(P.injBasal[i]);
+            }
+        for (uint32_t k = 0; k < P.stimCompt.size(); ++k)
+            if (injAt[ci][P.stimCompt[k]] < 0) {
+                injAt[ci][P.stimCompt[k]] = (int32_t)(injVal.size() - R.inj0);
+                injVal.push_back(0.0);
+            }
+        R.nInj = (uint32_t)injVal.size() - R.inj0;
+        b->injEntryOf.emplace_back(P.hinesOf.size(), -1);
+        for (uint32_t i = 0; i < N; ++i)
+            if (injAt[ci][i] >= 0) b->injEntryOf.back()[P.modelOf[i]] = (int32_t)R.inj0 + injAt[ci][i];
+        R.stim0 = (uint32_t)stimStep.size();
+        for (uint32_t k = 0; k < P.stimCompt.size(); ++k) {
+            stimStep.push_back(P.stimStep[k]);
+            stimEntry.push_back((uint32_t)injAt[ci][P.stimCompt[k]]);
+            stimValue.push_back(P.stimValue[k]);
+        }
+        R.nStim = (uint32_t)stimStep.size() - R.stim0;
+        R.sg0 = (uint32_t)sgNode.size();
+        for (uint32_t k = 0; k < P.SG; ++k) {
+            sgNode.push_back(posOf[ci][P.sgCompt[k]]);
+            sgThresh.push_back((float)P.sgThreshold[k]);
+            sgRefract.push_back((float)P.sgRefract[k]);
+            sgEdge.push_back(P.sgEdge[k]);
+        }
+        R.nSg = P.SG;
+        c2dAt[ci].assign(N, -1);
+        for (uint32_t k = 0; k < P.K2; ++k) {
+            if (c2dAt[ci][P.c2dCompt[k]] >= 0)
+                return berr(HS_ENOTSUP, "mixed batch: more than one HHChannel2D in a compartment");
+            c2dAt[ci][P.c2dCompt[k]] = (int32_t)k;
+        }
+        synPtr[ci].assign(N + 1, 0);
+        for (uint32_t k = 0; k < P.S; ++k) synPtr[ci][P.synCompt[k] + 1]++;
+        for (uint32_t i = 0; i < N; ++i) synPtr[ci][i + 1] += synPtr[ci][i];
+        synIdx[ci].assign(P.S, 0);
+        std::vector<uint32_t> fill(synPtr[ci].begin(), synPtr[ci].end() - 1);
+        for (uint32_t k = 0; k < P.S; ++k) synIdx[ci][fill[P.synCompt[k]]++] = k;   // creation order per compartment
+    }
+    // 5. per-node arrays in global node order
     std::vector<float> vtab(V0.data.begin(), V0.data.end()), catab(C0.data.begin(), C0.data.end());
     std::map<std::tuple<const double*, const double*, uint32_t, uint32_t>, int> g2dIndex;
     std::vector<float> g2d, g2dGeom;
@@ -469,162 +616,49 @@ int buildMixed(HsBatch* b) {
     std::vector<uint32_t> g2dN;
     std::vector<ChanType> ctypes;
     std::vector<C2dType> ktypes;
-    // node-major staging
-    std::vector<uint32_t> unitPtr, childList, nodeInfo, ctype4, childStart, parent, syn0;
-    std::vector<uint2> units;
-    const uint32_t nth = 32 * std::max<uint32_t>(1, b->warpsPerTeam);
-    H.elimCost.assign(nC, 0.0);
-    std::vector<double> off, offsq, HS2, CmByDt, EmByRm, Vinit;
-    std::vector<float> gbar4, state12;    // 4 and 12 values per node
-    std::vector<float> poolBasal, poolG1, poolF2, poolCeil, poolFloor, k2gbar, k2x0;
+    const uint64_t ld = (nN + 31) / 32 * 32;
+    std::vector<uint32_t> nodeInfo(nN), ctype4(nN), topo(nN), injIdx(nN, 0), syn0;
+    std::vector<uint16_t> par(nN, (uint16_t)kNoParent);
+    std::vector<double> off(nN), HS2(nN), CmByDt(nN), EmByRm(nN);
+    std::vector<float> gbarS((size_t)kMaxChan * ld, 0.f), stateS((size_t)3 * kMaxChan * ld, 0.f);
+    std::vector<float> poolBasal(nN, 0.f), poolG1(nN, 0.f), poolF2(nN, 0.f), poolCeil(nN, 0.f), poolFloor(nN, 0.f);
+    std::vector<float> k2gbar(nN, 0.f), k2x0(nN, 0.f);
     std::vector<uint8_t> synTypeV;
-    std::vector<uint32_t> injNode, stimStep, stimEntry, sgNode;
-    std::vector<double> injVal, stimValue;
-    std::vector<float> sgThresh, sgRefract;
-    std::vector<int32_t> sgEdge;
-    H.cells.resize(nC);
-    H.nodeOf.resize(nC);
-    H.poolOf.resize(nC);
-    b->injEntryOf.clear();
-    for (uint32_t ci = 0; ci < nC; ++ci) {
-        const CellPlan& P = b->plans[ci];
-        const uint32_t N = P.N;
-        // star-form tree: junctions of >= 3 compartments get a node
-        std::vector<int64_t> mparent(N, -1);
-        for (uint32_t i = 0; i < N; ++i)
-            for (uint32_t c : P.children[i]) mparent[c] = i;
-        int64_t root = -1;
-        for (uint32_t i = 0; i < N; ++i)
-            if (mparent[i] < 0) root = i;
-        std::vector<double> Ga(N), diag(N);
-        for (uint32_t i = 0; i < N; ++i) {
-            Ga[i] = 2.0 / P.Ra[i];
-            diag[i] = P.Cm[i] / (P.dtSetup / 2.0) + 1.0 / P.Rm[i];
-        }
-        std::vector<std::vector<uint32_t>> tk(N);
-        std::vector<double> toff(N, 0.0);
-        for (uint32_t p = 0; p < N; ++p) {
-            const std::vector<uint32_t>& ch = P.children[p];
-            if (ch.size() == 1) {
-                uint32_t c = ch[0];
-                double g = Ga[p] * Ga[c] / (Ga[p] + Ga[c]);
-                diag[p] += g;
-                diag[c] += g;
-                tk[p].push_back(c);
-                toff[c] = -g;
-            } else if (ch.size() >= 2) {
-                uint32_t J = (uint32_t)diag.size();
-                double gsum = Ga[p];
-                for (uint32_t c : ch) gsum += Ga[c];
-                diag.push_back(gsum);
-                toff.push_back(-Ga[p]);
-                tk.push_back(std::vector<uint32_t>(ch.begin(), ch.end()));
-                diag[p] += Ga[p];
-                tk[p].push_back(J);
-                for (uint32_t c : ch) {
-                    diag[c] += Ga[c];
-                    toff[c] = -Ga[c];
-                }
-            }
-        }
-        const uint32_t T = (uint32_t)diag.size();
-        std::vector<uint32_t> bfs;
-        bfs.reserve(T);
-        bfs.push_back((uint32_t)root);
-        for (size_t k = 0; k < bfs.size(); ++k)
-            for (uint32_t c : tk[bfs[k]]) bfs.push_back(c);
-        if (bfs.size() != T) return berr(HS_EINVAL, "mixed batch: tree construction failed");
-        UnitPlan U = bestUnits(tk, bfs, nth, (double)b->levelCost);
-        H.elimCost[ci] = 2.0 * U.cost;
-        const std::vector<uint32_t>& order = U.order;
-        std::vector<uint32_t> pos(T);
-        for (uint32_t k = 0; k < T; ++k) pos[order[k]] = k;
-        MixCellRange& R = H.cells[ci];
-        const uint32_t node0 = (uint32_t)nodeInfo.size();
-        R.node0 = node0;
-        R.nNodes = T;
-        R.level0 = (uint32_t)unitPtr.size();
-        R.nLevels = (uint32_t)U.levelPtr.size() - 1;
-        R.unit0 = (uint32_t)units.size();
-        R.child0 = (uint32_t)childList.size();
-        unitPtr.insert(unitPtr.end(), U.levelPtr.begin(), U.levelPtr.end());
-        for (auto& u : U.units) units.push_back(make_uint2(u.first, u.second));
-        H.nodeOf[ci].assign(P.hinesOf.size(), -1);
-        for (size_t m = 0; m < P.hinesOf.size(); ++m)
-            if (P.hinesOf[m] >= 0) H.nodeOf[ci][m] = node0 + pos[P.hinesOf[m]];
-        H.poolOf[ci].assign(P.poolSolverOf.size(), -1);
-        // inject entries: basal injects and stimulus targets
-        std::map<uint32_t, uint32_t> injEntry;
-        R.inj0 = (uint32_t)injNode.size();
-        for (uint32_t i = 0; i < N; ++i)
-            if (P.injPresent[i]) {
-                injEntry[i] = (uint32_t)(injNode.size() - R.inj0);
-                injNode.push_back(pos[i]);
-                injVal.push_back(P.injBasal[i]);
-            }
-        for (uint32_t k = 0; k < P.stimCompt.size(); ++k)
-            if (!injEntry.count(P.stimCompt[k])) {
-                injEntry[P.stimCompt[k]] = (uint32_t)(injNode.size() - R.inj0);
-                injNode.push_back(pos[P.stimCompt[k]]);
-                injVal.push_back(0.0);
-            }
-        R.nInj = (uint32_t)injNode.size() - R.inj0;
-        b->injEntryOf.emplace_back(P.hinesOf.size(), -1);
-        for (auto& kv : injEntry) b->injEntryOf.back()[P.modelOf[kv.first]] = (int32_t)(R.inj0 + kv.second);
-        R.stim0 = (uint32_t)stimStep.size();
-        for (uint32_t k = 0; k < P.stimCompt.size(); ++k) {
-            stimStep.push_back(P.stimStep[k]);
-            stimEntry.push_back(injEntry[P.stimCompt[k]]);
-            stimValue.push_back(P.stimValue[k]);
-        }
-        R.nStim = (uint32_t)stimStep.size() - R.stim0;
-        R.sg0 = (uint32_t)sgNode.size();
-        for (uint32_t k = 0; k < P.SG; ++k) {
-            sgNode.push_back(pos[P.sgCompt[k]]);
-            sgThresh.push_back((float)P.sgThreshold[k]);
-            sgRefract.push_back((float)P.sgRefract[k]);
-            sgEdge.push_back(P.sgEdge[k]);
-        }
-        R.nSg = P.SG;
-        R.rec0 = 0;
-        R.nRec = 0;
-        std::vector<std::vector<uint32_t>> c2dOf(N), synOf(N);
-        for (uint32_t k = 0; k < P.K2; ++k) c2dOf[P.c2dCompt[k]].push_back(k);
-        for (uint32_t k = 0; k < P.S; ++k) synOf[P.synCompt[k]].push_back(k);
-        for (uint32_t k = 0; k < T; ++k) {
-            const uint32_t t = order[k];
-            const bool center = t >= N;
-            const uint32_t nch = (uint32_t)tk[t].size();
-            if (nch > 255) return berr(HS_ENOTSUP, "mixed batch: more than 255 children at a node");
-            uint32_t info = (center ? kNodeCenter : 0) | (nch << 16) | ((uint32_t)kNoType << 8);
+    H.initVm.assign(nN, 0.0);
+    syn0.reserve(nN + 1);
+    for (size_t fi = 0; fi < forests.size(); ++fi) {
+        const MixForest& F = fdev[fi];
+        for (uint32_t g = F.node0; g < F.node0 + F.nNodes; ++g) {
+            const uint32_t ci = nodeCT[g].first, t = nodeCT[g].second;
+            const CellPlan& P = b->plans[ci];
+            const StarTree& S = trees[ci];
+            const bool center = t >= S.N;
+            const uint32_t nch = S.chPtr[t + 1] - S.chPtr[t];
+            topo[g] = (nch ? posOf[ci][S.ch[S.chPtr[t]]] - F.node0 : 0) | (nch << 16);
+            for (uint32_t k = S.chPtr[t]; k < S.chPtr[t + 1]; ++k) par[posOf[ci][S.ch[k]]] = (uint16_t)(g - F.node0);
+            off[g] = S.off[t];
+            HS2[g] = S.diag[t];
+            uint32_t info = (center ? kNodeCenter : 0) | ((uint32_t)kNoType << 8);
             uint32_t types = 0xFFFFFFFFu;
-            childStart.push_back((uint32_t)childList.size() - R.child0);
-            for (uint32_t c : tk[t]) childList.push_back(pos[c]);
-            parent.push_back(k == 0 ? ~0u : 0);      // filled below
-            off.push_back(toff[t]);
-            offsq.push_back(toff[t] * toff[t]);
-            HS2.push_back(diag[t]);
-            CmByDt.push_back(center ? 0.0 : P.CmByDt[t]);
-            EmByRm.push_back(center ? 0.0 : P.EmByRm[t]);
-            Vinit.push_back(center ? 0.0 : P.initVm[t]);
-            H.initVm.push_back(center ? 0.0 : P.initVm[t]);
-            size_t g0 = gbar4.size(), s0 = state12.size();
-            gbar4.resize(g0 + kMaxChan, 0.f);
-            state12.resize(s0 + 3 * kMaxChan, 0.f);
-            float pb = 0.f, pg1 = 0.f, pf2 = 0.f, pce = 0.f, pfl = 0.f, kg = 0.f, kx = 0.f;
             syn0.push_back((uint32_t)synTypeV.size());
             if (!center) {
-                if (injEntry.count(t)) info |= kNodeInject;
+                CmByDt[g] = P.CmByDt[t];
+                EmByRm[g] = P.EmByRm[t];
+                H.initVm[g] = P.initVm[t];
+                if (injAt[ci][t] >= 0) {
+                    info |= kNodeInject;
+                    injIdx[g] = H.cells[ci].inj0 + (uint32_t)injAt[ci][t];
+                }
                 const uint32_t pb0 = P.poolPtr[t], pe0 = P.poolPtr[t + 1];
                 if (pe0 - pb0 > 1) return berr(HS_ENOTSUP, "mixed batch: more than one Ca pool in a compartment");
                 if (pe0 > pb0) {
                     info |= kNodePool;
-                    H.poolOf[ci][P.poolModel[pb0]] = node0 + k;
-                    pb = (float)P.CaBasal[pb0];
-                    pg1 = (float)(1.0 - P.f1[pb0]);     // decay per step, from FP64
-                    pf2 = (float)P.f2[pb0];
-                    pce = (float)P.ceiling[pb0];
-                    pfl = (float)P.floor_[pb0];
+                    H.poolOf[ci][P.poolModel[pb0]] = g;
+                    poolBasal[g] = (float)P.CaBasal[pb0];
+                    poolG1[g] = (float)(1.0 - P.f1[pb0]);     // decay per step, from FP64
+                    poolF2[g] = (float)P.f2[pb0];
+                    poolCeil[g] = (float)P.ceiling[pb0];
+                    poolFloor[g] = (float)P.floor_[pb0];
                 }
                 const uint32_t q0 = P.chanPtr[t], q1 = P.chanPtr[t + 1];
                 if (q1 - q0 > (uint32_t)kMaxChan)
@@ -650,27 +684,30 @@ int buildMixed(HsBatch* b) {
                             return berr(HS_ENOTSUP, "mixed batch: channel feeds another compartment's pool");
                         ty.caTarget = 1;
                     }
-                    int ti = typeIndex(ctypes, ty, kMaxChanTypes - 1);
+                    const int ti = typeIndex(ctypes, ty, kMaxChanTypes - 1);
                     if (ti < 0) return berr(HS_ENOTSUP, "mixed batch: too many channel types");
                     const uint32_t j = q - q0;
                     types = (types & ~(0xFFu << (8 * j))) | ((uint32_t)ti << (8 * j));
-                    gbar4[g0 + j] = (float)(P.Gbar[q] * P.modulation[q]);
+                    gbarS[(size_t)j * ld + g] = (float)(P.Gbar[q] * P.modulation[q]);
                     int s = P.stateOff[q];
-                    if (P.Xpow[q] > 0.0) state12[s0 + 3 * j] = (float)P.state0[s++];
-                    if (P.Ypow[q] > 0.0) state12[s0 + 3 * j + 1] = (float)P.state0[s++];
-                    if (P.Zpow[q] > 0.0) state12[s0 + 3 * j + 2] = (float)P.state0[s++];
+                    if (P.Xpow[q] > 0.0) stateS[(size_t)(3 * j) * ld + g] = (float)P.state0[s++];
+                    if (P.Ypow[q] > 0.0) stateS[(size_t)(3 * j + 1) * ld + g] = (float)P.state0[s++];
+                    if (P.Zpow[q] > 0.0) stateS[(size_t)(3 * j + 2) * ld + g] = (float)P.state0[s++];
+                    if (P.Xpow[q] > 0.0) info |= 1u << (kNodeGateShift + 3 * j);
+                    if (P.Ypow[q] > 0.0) info |= 1u << (kNodeGateShift + 3 * j + 1);
+                    if (P.Zpow[q] > 0.0) info |= 1u << (kNodeGateShift + 3 * j + 2);
                 }
-                if (c2dOf[t].size() > 1) return berr(HS_ENOTSUP, "mixed batch: more than one HHChannel2D in a compartment");
-                for (uint32_t kk : c2dOf[t]) {
+                const int32_t kk = c2dAt[ci][t];
+                if (kk >= 0) {
                     const Gate2D& G = P.gates2d[P.c2dGate[kk]];
                     auto key = std::make_tuple(G.srcA, G.srcB, G.nx, G.ny);
                     auto it = g2dIndex.find(key);
                     if (it == g2dIndex.end()) {
                         if (g2dIndex.size() >= 127) return berr(HS_ENOTSUP, "mixed batch: too many 2-D tables");
-                        int gi = (int)g2dN.size() / 2;
-                        size_t nn = (size_t)G.nx * G.ny;
+                        const int gi = (int)g2dN.size() / 2;
+                        const size_t nn = (size_t)G.nx * G.ny;
                         g2dOff.push_back(g2d.size());
-                        size_t o = g2d.size();
+                        const size_t o = g2d.size();
                         g2d.resize(o + 2 * nn);
                         for (size_t i = 0; i < nn; ++i) {
                             g2d[o + 2 * i] = (float)G.srcA[i];
@@ -686,28 +723,25 @@ int buildMixed(HsBatch* b) {
                     std::memset(&ky, 0, sizeof(ky));
                     ky.ek = (float)P.c2dEk[kk];
                     ky.xp = powCode(P.c2dXpow[kk], ky.xpf);
-                    auto dep = [&](int d) -> int8_t {
-                        if (d == 0) return 0;
-                        if (d == 1) return 1;
-                        return -2;
-                    };
                     if (P.c2dConc2[kk] >= 0 || P.c2dDep0[kk] == 2 || P.c2dDep1[kk] == 2)
                         return berr(HS_ENOTSUP, "mixed batch: HHChannel2D on a second concentration");
                     if (P.c2dConc1[kk] >= 0 && (P.c2dConc1[kk] != (int32_t)pb0 || pe0 == pb0))
                         return berr(HS_ENOTSUP, "mixed batch: HHChannel2D reads another compartment's pool");
-                    ky.dep0 = P.c2dDep0[kk] < 0 ? -1 : dep(P.c2dDep0[kk]);
-                    ky.dep1 = P.c2dDep1[kk] < 0 ? -1 : dep(P.c2dDep1[kk]);
+                    auto dep = [](int32_t d) -> int8_t { return d < 0 ? -1 : d == 0 ? 0 : d == 1 ? 1 : -2; };
+                    ky.dep0 = dep(P.c2dDep0[kk]);
+                    ky.dep1 = dep(P.c2dDep1[kk]);
                     ky.instant = (int8_t)P.c2dInstant[kk];
                     ky.gate = (int8_t)it->second;
-                    int ti = typeIndex(ktypes, ky, kMaxC2dTypes - 1);
+                    const int ti = typeIndex(ktypes, ky, kMaxC2dTypes - 1);
                     if (ti < 0) return berr(HS_ENOTSUP, "mixed batch: too many HHChannel2D types");
                     info = (info & ~(0xFFu << 8)) | ((uint32_t)ti << 8);
-                    kg = (float)(P.c2dGbar[kk] * P.c2dMod[kk]);
-                    kx = (float)P.c2dX0[kk];
+                    k2gbar[g] = (float)(P.c2dGbar[kk] * P.c2dMod[kk]);
+                    k2x0[g] = (float)P.c2dX0[kk];
                 }
-                if (!synOf[t].empty()) info |= kNodeSyn;
-                for (uint32_t kk : synOf[t]) {
-                    auto key = std::make_tuple(P.synTau1[kk], P.synTau2[kk], P.synEk[kk]);
+                if (synPtr[ci][t + 1] > synPtr[ci][t]) info |= kNodeSyn;
+                for (uint32_t q = synPtr[ci][t]; q < synPtr[ci][t + 1]; ++q) {
+                    const uint32_t kk2 = synIdx[ci][q];
+                    auto key = std::make_tuple(P.synTau1[kk2], P.synTau2[kk2], P.synEk[kk2]);
                     size_t ti = 0;
                     while (ti < H.synTypeKey.size() && H.synTypeKey[ti] != key) ++ti;
                     if (ti == H.synTypeKey.size()) {
@@ -715,44 +749,30 @@ int buildMixed(HsBatch* b) {
                         H.synTypeKey.push_back(key);
                     }
                     synTypeV.push_back((uint8_t)ti);
-                    H.synGbar.push_back(P.synGbar[kk]);
-                    H.synTau1.push_back(P.synTau1[kk]);
-                    H.synTau2.push_back(P.synTau2[kk]);
-                    H.synMod.push_back(P.synMod[kk]);
+                    H.synGbar.push_back(P.synGbar[kk2]);
+                    H.synTau1.push_back(P.synTau1[kk2]);
+                    H.synTau2.push_back(P.synTau2[kk2]);
+                    H.synMod.push_back(P.synMod[kk2]);
                     H.evStart.push_back((uint32_t)H.evTime.size());
-                    for (uint32_t e = P.evPtr[kk]; e < P.evPtr[kk + 1]; ++e) {
+                    for (uint32_t e = P.evPtr[kk2]; e < P.evPtr[kk2 + 1]; ++e) {
                         H.evTime.push_back(P.evTime[e]);
                         H.evW.push_back(P.evW[e]);
                     }
                     H.evEnd.push_back((uint32_t)H.evTime.size());
                 }
             }
-            nodeInfo.push_back(info);
-            ctype4.push_back(types);
-            poolBasal.push_back(pb);
-            poolG1.push_back(pg1);
-            poolF2.push_back(pf2);
-            poolCeil.push_back(pce);
-            poolFloor.push_back(pfl);
-            k2gbar.push_back(kg);
-            k2x0.push_back(kx);
+            nodeInfo[g] = info;
+            ctype4[g] = types;
         }
-        for (uint32_t k = 0; k < T; ++k)
-            for (uint32_t c : tk[order[k]]) parent[node0 + pos[c]] = k;
     }
-    const uint32_t nN = (uint32_t)nodeInfo.size();
     syn0.push_back((uint32_t)synTypeV.size());
-    const uint64_t ld = (nN + 31) / 32 * 32;
     H.nNodes = nN;
-    // slot-major arrays [slot][ld]
-    std::vector<float> gbarS((size_t)kMaxChan * ld, 0.f), stateS((size_t)3 * kMaxChan * ld, 0.f);
-    for (uint32_t n = 0; n < nN; ++n) {
-        for (int j = 0; j < kMaxChan; ++j) gbarS[(size_t)j * ld + n] = gbar4[(size_t)n * kMaxChan + j];
-        for (int j = 0; j < 3 * kMaxChan; ++j) stateS[(size_t)j * ld + n] = state12[(size_t)n * 3 * kMaxChan + j];
-    }
-    gbar4.clear();
-    state12.clear();
     H.c2dX0 = k2x0;
+    H.nForests = (uint32_t)forests.size();
+    H.nShared = 0;
+    for (const ForestPlan& f : forests) H.nShared += f.shared ? 1 : 0;
+    trees.clear();
+    // 6. upload
     DevBuf& D = b->buf;
     cudaStream_t st = b->st;
     MixBatch& m = b->mb;
@@ -760,22 +780,23 @@ int buildMixed(HsBatch* b) {
     m.nCells = nC;
     m.ld = ld;
     m.cells = D.up(H.cells, st);
-    m.unitPtr = D.up(unitPtr, st);
-    m.units = D.up(units, st);
-    m.childList = D.up(childList, st);
+    m.forests = D.up(fdev, st);
+    m.forestCells = D.up(forestCells, st);
+    m.levelPtr = D.up(levelPtr, st);
     m.nodeInfo = D.up(nodeInfo, st);
     m.ctype4 = D.up(ctype4, st);
-    m.childStart = D.up(childStart, st);
-    m.parent = D.up(parent, st);
+    m.topo = D.up(topo, st);
+    m.par = D.up(par, st);
+    m.injIdx = D.up(injIdx, st);
     m.off = D.up(off, st);
-    m.offsq = D.up(offsq, st);
     m.HS2 = D.up(HS2, st);
     m.CmByDt = D.up(CmByDt, st);
     m.EmByRm = D.up(EmByRm, st);
-    m.V = D.up(Vinit, st);
-    m.inv = D.zeros<double>(nN, st);
-    m.gEl = D.zeros<double>(nN, st);
-    m.VMid = D.zeros<double>(nN, st);
+    m.V = D.up(H.initVm, st);
+    if (H.nShared < H.nForests) {
+        m.elimD = D.zeros<double>(nN, st);
+        m.elimR = D.zeros<double>(nN, st);
+    }
     m.caG = D.zeros<float>(nN, st);
     m.caGE = D.zeros<float>(nN, st);
     m.gbar = D.up(gbarS, st);
@@ -805,7 +826,6 @@ int buildMixed(HsBatch* b) {
     m.evStep = b->dEvStep;
     m.evAct = b->dEvAct;
     m.synNorm = b->dSynNorm;
-    m.injNode = D.up(injNode, st);
     m.injVal = D.up(injVal, st);
     m.stimStep = D.up(stimStep, st);
     m.stimEntry = D.up(stimEntry, st);
@@ -838,6 +858,9 @@ int buildMixed(HsBatch* b) {
     b->dMixInitVm = D.up(H.initVm, st);
     b->dMixC2dX0 = D.up(H.c2dX0, st);
     b->dEvStart = D.up(H.evStart, st);
+    b->dCtaPtr = D.up(ctaPtr, st);
+    b->dCtaForests = D.up(ctaForests, st);
+    b->nCtas = nCtas;
     if (D.err != cudaSuccess) return cerr(D.err, "mixed batch upload");
     cudaError_t e = uploadMixedTypes(ctypes.data(), (int)ctypes.size(), ktypes.data(), (int)ktypes.size(),
                                      nullptr, 0, st);
@@ -901,18 +924,21 @@ int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds, uint32_t n_c
         delete b;
         return cerr(e, "batch stream");
     }
+    if (precision == HS_PREC_MIXED) {
+        b->threadsPerCta = 512;
+        b->ctasPerSm = 1;
+    }
     if (tuning) {
         if (tuning->threads_per_cta) b->threadsPerCta = tuning->threads_per_cta;
         if (tuning->ctas_per_sm) b->ctasPerSm = tuning->ctas_per_sm;
-        if (tuning->warps_per_team) b->warpsPerTeam = tuning->warps_per_team;
         if (tuning->steps_per_launch) b->stepsPerLaunch = tuning->steps_per_launch;
-        if (tuning->level_cost) b->levelCost = tuning->level_cost;
+        b->forestNodes = tuning->forest_nodes;
         b->useGraph = tuning->use_graph != 0;
     }
-    if (b->threadsPerCta % 32 || b->threadsPerCta > 512 ||
-        (precision == HS_PREC_FP64 && b->threadsPerCta > 256)) {
+    const uint32_t maxTpc = precision == HS_PREC_FP64 ? 256 : 1024;
+    if (b->threadsPerCta % 32 || b->threadsPerCta == 0 || b->threadsPerCta > maxTpc) {
         hs_batch_destroy(b);
-        return berr(HS_EINVAL, "threads_per_cta must be a multiple of 32, at most 512 (256 for FP64)");
+        return berr(HS_EINVAL, "threads_per_cta must be a multiple of 32, at most 256 (FP64) or 1024 (mixed)");
     }
     int rc = precision == HS_PREC_FP64 ? buildFp64(b, cells) : buildMixed(b);
     if (rc == HS_OK && precision == HS_PREC_FP64) rc = uploadDcs(b);
@@ -946,16 +972,40 @@ int hs_batch_destroy(HsBatch* b) {
 
 int hs_batch_tune(HsBatch* b, const HsBatchTuning* t) {
     if (!b || !t) return berr(HS_EINVAL, "null argument");
+    const uint32_t maxTpc = b->precision == HS_PREC_FP64 ? 256 : 1024;
     if (t->threads_per_cta) {
-        if (t->threads_per_cta % 32 || t->threads_per_cta > 512)
-            return berr(HS_EINVAL, "threads_per_cta must be a multiple of 32, at most 512");
+        if (t->threads_per_cta % 32 || t->threads_per_cta > maxTpc)
+            return berr(HS_EINVAL, "threads_per_cta must be a multiple of 32, at most 256 (FP64) or 1024 (mixed)");
         b->threadsPerCta = t->threads_per_cta;
     }
-    if (t->ctas_per_sm) b->ctasPerSm = t->ctas_per_sm;
-    if (t->warps_per_team) b->warpsPerTeam = t->warps_per_team;
+    cudaError_t e = cudaStreamSynchronize(b->st);
+    if (e != cudaSuccess) return cerr(e, "batch tune");
+    const uint32_t cps = t->ctas_per_sm ? t->ctas_per_sm : b->ctasPerSm;
+    const bool relayout = b->precision == HS_PREC_MIXED && (cps != b->ctasPerSm || t->forest_nodes != b->forestNodes);
+    b->ctasPerSm = cps;
+    b->forestNodes = t->forest_nodes;
     if (t->steps_per_launch) b->stepsPerLaunch = t->steps_per_launch;
     b->useGraph = t->use_graph != 0;
-    cudaStreamSynchronize(b->st);
+    if (relayout) {
+        // a new forest packing renumbers every node: rebuild the layout; the
+        // state, recording and inject targets start over
+        if (b->gexec) {
+            cudaGraphExecDestroy(b->gexec);
+            b->gexec = nullptr;
+        }
+        b->buf.freeAll();
+        b->buf.err = cudaSuccess;
+        b->recBuf.freeAll();
+        b->recBuf.err = cudaSuccess;
+        b->rec.clear();
+        b->recBase = nullptr;
+        b->injBuf.freeAll();
+        b->injBuf.err = cudaSuccess;
+        b->nInjTargets = 0;
+        b->reinited = false;
+        int rc = buildMixed(b);
+        if (rc != HS_OK) return rc;
+    }
     return repack(b);
 }
 
@@ -1017,7 +1067,8 @@ int hs_batch_reinit(HsBatch* b, double clock_dt) {
         b->mb.dt = clock_dt;
         b->mb.dtf = (float)clock_dt;
         b->mb.caAdvance = b->caAdvance;
-        if (e == cudaSuccess) e = launchBatchReinitMixed(b->mb, b->dMixInitVm, b->dMixC2dX0, b->dEvStart, b->st);
+        if (e == cudaSuccess)
+            e = launchBatchReinitMixed(b->mb, (uint32_t)H.nNodes, b->dMixInitVm, b->dMixC2dX0, b->dEvStart, b->st);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
     if (e != cudaSuccess) return cerr(e, "batch reinit");
@@ -1131,14 +1182,19 @@ int hs_batch_read_vm(HsBatch* b, uint32_t cell, double* out, uint32_t n) {
         if (e != cudaSuccess) return cerr(e, "batch read vm");
         for (uint32_t m = 0; m < n; ++m) out[m] = P.hinesOf[m] < 0 ? NAN : v[P.hinesOf[m]];
     } else {
-        const MixCellRange& R = b->mh.cells[cell];
-        std::vector<double> v(R.nNodes);
-        if (e == cudaSuccess) e = cudaMemcpy(v.data(), b->mb.V + R.node0, R.nNodes * 8, cudaMemcpyDeviceToHost);
+        // the cell's nodes lie inside one forest: copy their index range
+        const std::vector<int64_t>& no = b->mh.nodeOf[cell];
+        int64_t lo = INT64_MAX, hi = -1;
+        for (int64_t g : no)
+            if (g >= 0) {
+                lo = std::min(lo, g);
+                hi = std::max(hi, g);
+            }
+        std::vector<double> v(hi >= lo ? (size_t)(hi - lo + 1) : 0);
+        if (e == cudaSuccess && !v.empty())
+            e = cudaMemcpy(v.data(), b->mb.V + lo, v.size() * 8, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return cerr(e, "batch read vm");
-        for (uint32_t m = 0; m < n; ++m) {
-            int64_t g = b->mh.nodeOf[cell][m];
-            out[m] = g < 0 ? NAN : v[g - R.node0];
-        }
+        for (uint32_t m = 0; m < n; ++m) out[m] = no[m] < 0 ? NAN : v[no[m] - lo];
     }
     return HS_OK;
 }
@@ -1222,7 +1278,7 @@ int hs_batch_record(HsBatch* b, const uint32_t* cell, const uint32_t* compt, uin
         R.rec0 = col;
         R.nRec = (uint32_t)per[c].size();
         for (uint32_t m : per[c]) {
-            nodes.push_back((uint32_t)(b->mh.nodeOf[c][m] - R.node0));
+            nodes.push_back((uint32_t)b->mh.nodeOf[c][m]);
             b->rec.push_back({c, m});
         }
         col += R.nRec;

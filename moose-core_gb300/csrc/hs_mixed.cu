@@ -1,20 +1,19 @@
 // hs_mixed.cu -- mixed-precision batched HSolve step (sm_103a).
 //
-// A team of W warps steps one cell at a time; every team owns a list of
-// cells (packed by cost on the host) and runs each for `nsteps` steps before
-// moving on.  A team synchronises with a named barrier (bar.sync id, 32*W),
-// or __syncwarp when W = 1.  Per step:
-//   tick 0    stimulus schedule
-//   assembly  every compartment node, in parallel over the team: FP32 rate
-//             lookup and gate update for each channel slot, conductances,
-//             the K(Ca) 2-D gate, SynChans; FP64 matrix row.
-//   forward   work units level by level (hs_mixed.cuh), each unit serially
-//             by one thread: pull the children's eliminated rows
-//             (diag -= off^2/pivot_c, rhs -= off*g_c), keep 1/pivot and
-//             g = rhs/pivot (FP64).
-//   backward  the same units in reverse: VMid = g - (off/pivot)*VMid[parent],
-//             V = 2*VMid - V, then the node's Ca pool (FP32).
-//   SpikeGens, trace record.
+// A persistent kernel: each CTA owns a list of forests (groups of cells,
+// hs_mixed.cuh) packed by size on the host and steps each forest for
+// `nsteps` steps before moving on.  Per step, the whole CTA:
+//   tick 0    stimulus schedule (a thread per cell)
+//   assembly  every node in parallel: FP32 rate lookup and gate update for
+//             each channel slot, conductances, the K(Ca) 2-D gate, SynChans;
+//             FP64 matrix row into the elimination arrays
+//   forward   levels deepest first, a barrier per level: pull the children's
+//             eliminated rows, FP64 pivot reciprocal
+//   backward  levels root first: VMid = g - f * VMid[parent] (FP64)
+//   update    V = 2 VMid - V, Ca pools (FP32)
+//   outputs   SpikeGens, trace samples (a thread per cell).
+// The update and outputs of a step are done at the start of the next step's
+// assembly (and after the last step), which saves a pass over the nodes.
 // Reference routines: hsolve/HSolveActive.cpp:45-332, hsolve/HSolvePassive.cpp:
 // 246-401 (the same elimination, tree form), biophysics/HHChannel2D.cpp:327-369,
 // biophysics/SynChan.cpp:200-224, synapse/SimpleSynHandler.cpp:98-113,
@@ -29,15 +28,14 @@ __constant__ ChanType c_chanTypes[kMaxChanTypes];
 __constant__ C2dType c_c2dTypes[kMaxC2dTypes];
 __constant__ SynType c_synTypes[kMaxSynTypes];
 
-// Reciprocal of a positive FP64 pivot: the FP32 hardware approximation
-// (relative error below 2^-22) refined by one Newton-Raphson step
-// x <- x + x(1 - d x) in FP64, which squares the error (below 2^-44).
-__device__ __forceinline__ double rcpNewton(double d) {
-    float f = __double2float_rn(d);
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(f));
-    double x = (double)r;
-    double e = fma(-d, x, 1.0);
+// Reciprocal of a positive FP64 pivot: the hardware FP64 reciprocal
+// estimate (rcp.approx.ftz.f64, relative error about 1e-6 measured over
+// 1e-9..1e9) refined by one Newton-Raphson step x <- x + x(1 - d x), which
+// squares the error (about 1e-12).
+__device__ __forceinline__ double rcpPivot(double d) {
+    double x;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(x) : "d"(d));
+    const double e = fma(-d, x, 1.0);
     return fma(x, e, x);
 }
 
@@ -104,16 +102,91 @@ __device__ __forceinline__ void interp2dF(const float* T, const float* geom, uin
     B = z00.y * w00 + z10.y * w10 + z01.y * w01 + z11.y * xFyF;
 }
 
-// Channels, K(Ca), SynChans and FP64 matrix row of one compartment node.
-__device__ __forceinline__ void nodeRow(const MixBatch& b, uint32_t n, uint32_t info,
-                                        unsigned long long step, double& diag, double& rhs) {
+// Exact widening of an FP32 value to FP64 with integer operations (the
+// FP32-to-FP64 conversion instruction issues at the FP64 rate on this GPU,
+// integer operations at the full rate).  IEEE binary32 -> binary64: sign
+// kept, exponent rebiased by 1023 - 127 = 896, fraction shifted left by 29;
+// zero and subnormal inputs give a signed zero, Inf/NaN stay Inf/NaN.
+__device__ __forceinline__ double widenF(float x) {
+    const uint32_t u = __float_as_uint(x);
+    const uint32_t e = (u >> 23) & 0xFFu;
+    const uint32_t sign = u & 0x80000000u;
+    const uint32_t e64 = e == 0xFFu ? 0x7FFu : e + 896u;
+    const uint32_t hi = e == 0 ? sign : (sign | (e64 << 20) | ((u >> 3) & 0xFFFFFu));
+    const uint32_t lo = e == 0 ? 0u : (u << 29);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// One compartment node of the assembly: first the update left over from the
+// previous step (V = 2 VMid - V, then the node's Ca pool; `update`), then
+// channels, K(Ca), SynChans and the FP64 matrix row.  Every load that depends
+// only on the node index is issued before any arithmetic, so a thread's
+// memory round trips per node are: node data, then rate tables and synapse
+// state, then (synapses only) event times.
+__device__ __forceinline__ void assembleNode(const MixBatch& b, uint32_t n, uint32_t info, bool update,
+                                             double vmPrev, unsigned long long step, double& diag, double& rhs) {
     const uint64_t ld = b.ld;
-    const double V = b.V[n];
-    const uint32_t types = b.ctype4[n];
-    const float v = (float)V;
     const float dt = b.dtf, hdt = 0.5f * b.dtf;
-    const float ca = (info & kNodePool) ? b.poolCa[n] : 0.f;
-    RowF vr = rowF(b.vTab, b.vCol, b.vRows, v, b.vMin, b.vMax, b.vInvDx);
+    // ---- node data
+    double V = b.V[n];
+    const uint32_t types = __ldg(b.ctype4 + n);
+    const double hs2 = __ldg(b.HS2 + n), cmdt = __ldg(b.CmByDt + n), emrm = __ldg(b.EmByRm + n);
+    float xs[3 * kMaxChan];
+#pragma unroll
+    for (int k = 0; k < 3 * kMaxChan; ++k)
+        xs[k] = (info >> (kNodeGateShift + k)) & 1u ? b.state[(uint64_t)k * ld + n] : 0.f;
+    float gb[kMaxChan];
+#pragma unroll
+    for (int j = 0; j < kMaxChan; ++j) gb[j] = ((types >> (8 * j)) & 0xFF) != kNoType ? __ldg(b.gbar + (uint64_t)j * ld + n) : 0.f;
+    const bool pool = info & kNodePool;
+    float ca = 0.f, c0v = 0.f, pg1 = 0.f, pf2 = 0.f, pbas = 0.f, pceil = 0.f, pfloor = 0.f, cgP = 0.f, cgeP = 0.f;
+    if (pool) {
+        ca = b.poolCa[n];
+        if (update) {
+            c0v = b.poolC[n];
+            pg1 = __ldg(b.poolG1 + n);
+            pf2 = __ldg(b.poolF2 + n);
+            pbas = __ldg(b.poolBasal + n);
+            pceil = __ldg(b.poolCeil + n);
+            pfloor = __ldg(b.poolFloor + n);
+            cgP = b.caG[n];
+            cgeP = b.caGE[n];
+        }
+    }
+    const uint32_t k2 = (info >> 8) & 0xFF;
+    float k2x = 0.f, k2g = 0.f;
+    if (k2 != kNoType) {
+        k2x = b.k2x[n];
+        k2g = __ldg(b.k2gbar + n);
+    }
+    uint32_t s0 = 0, s1 = 0;
+    if (info & kNodeSyn) {
+        s0 = __ldg(b.syn0 + n);
+        s1 = __ldg(b.syn0 + n + 1);
+    }
+    double inj = 0.0;
+    if (info & kNodeInject) inj = b.injVal[__ldg(b.injIdx + n)];
+    // ---- the previous step's update
+    if (update) {
+        const double Vold = V;
+        V = fma(2.0, vmPrev, -Vold);
+        b.V[n] = V;
+        if (pool) {
+            const float vca = (float)(b.caAdvance == 1 ? vmPrev : fma(2.0, vmPrev, -V));
+            const float act = fmaf(-cgP, vca, cgeP);
+            // c f1 + f2 act with f1 = 1 - g1 (g1 = 1 - f1 from FP64)
+            float c = fmaf(-pg1, c0v, c0v) + pf2 * act;
+            float cav = pbas + c;
+            if (pceil > 0.f && cav > pceil) { cav = pceil; c = cav - pbas; }
+            if (cav < pfloor) { cav = pfloor; c = cav - pbas; }
+            b.poolC[n] = c;
+            b.poolCa[n] = cav;
+            ca = cav;
+        }
+    }
+    // ---- HHChannels: trapezoidal gates on the V (or Ca) table rows
+    const float v = (float)V;
+    const RowF vr = rowF(b.vTab, b.vCol, b.vRows, v, b.vMin, b.vMax, b.vInvDx);
     float G = 0.f, GE = 0.f, cg = 0.f, cge = 0.f;
 #pragma unroll
     for (int j = 0; j < kMaxChan; ++j) {
@@ -123,27 +196,27 @@ __device__ __forceinline__ void nodeRow(const MixBatch& b, uint32_t n, uint32_t 
         float frac = 1.f;
         float* st = b.state + (uint64_t)(3 * j) * ld + n;
         if (t.xp) {
-            float x = gateF(vr, b.vCol, t.colX, st[0], dt, hdt, t.instant & 1);
+            const float x = gateF(vr, b.vCol, t.colX, xs[3 * j], dt, hdt, t.instant & 1);
             st[0] = x;
             frac *= powi(x, t.xp, t.xpf);
         }
         if (t.yp) {
-            float y = gateF(vr, b.vCol, t.colY, st[ld], dt, hdt, t.instant & 2);
+            const float y = gateF(vr, b.vCol, t.colY, xs[3 * j + 1], dt, hdt, t.instant & 2);
             st[ld] = y;
             frac *= powi(y, t.yp, t.ypf);
         }
         if (t.zp) {
             float z;
             if (t.zCa) {
-                RowF cr = rowF(b.caTab, b.caCol, b.caRows, ca, b.caMin, b.caMax, b.caInvDx);
-                z = gateF(cr, b.caCol, t.colZ, st[2 * ld], dt, hdt, t.instant & 4);
+                const RowF cr = rowF(b.caTab, b.caCol, b.caRows, ca, b.caMin, b.caMax, b.caInvDx);
+                z = gateF(cr, b.caCol, t.colZ, xs[3 * j + 2], dt, hdt, t.instant & 4);
             } else {
-                z = gateF(vr, b.vCol, t.colZ, st[2 * ld], dt, hdt, t.instant & 4);
+                z = gateF(vr, b.vCol, t.colZ, xs[3 * j + 2], dt, hdt, t.instant & 4);
             }
             st[2 * ld] = z;
             frac *= powi(z, t.zp, t.zpf);
         }
-        const float gk = b.gbar[(uint64_t)j * ld + n] * frac;
+        const float gk = gb[j] * frac;
         G += gk;
         GE = fmaf(gk, t.ek, GE);
         if (t.caTarget) {
@@ -151,275 +224,295 @@ __device__ __forceinline__ void nodeRow(const MixBatch& b, uint32_t n, uint32_t 
             cge = fmaf(gk, t.ek, cge);
         }
     }
-    if (info & kNodePool) {
+    if (pool) {
         b.caG[n] = cg;
         b.caGE[n] = cge;
     }
-    // HHChannel2D (K(Ca)): inputs are Vm and Ca of the previous step
-    const uint32_t k2 = (info >> 8) & 0xFF;
+    // ---- HHChannel2D (K(Ca)) on this step's Vm and Ca
     if (k2 != kNoType) {
         const C2dType& t = c_c2dTypes[k2];
-        float x = t.dep0 == 0 ? v : t.dep0 == 1 ? ca : 0.f;
-        float y = t.dep1 == 0 ? v : t.dep1 == 1 ? ca : 0.f;
+        const float x = t.dep0 == 0 ? v : t.dep0 == 1 ? ca : 0.f;
+        const float y = t.dep1 == 0 ? v : t.dep1 == 1 ? ca : 0.f;
         float A, B;
-        interp2dF(b.g2d + b.g2dOff[t.gate], b.g2dGeom + 6 * t.gate, b.g2dN[2 * t.gate],
-                  b.g2dN[2 * t.gate + 1], x, y, A, B);
-        float X = b.k2x[n];
+        interp2dF(b.g2d + b.g2dOff[t.gate], b.g2dGeom + 6 * t.gate, b.g2dN[2 * t.gate], b.g2dN[2 * t.gate + 1], x,
+                  y, A, B);
+        float X = k2x;
         if (t.instant & 1) X = __fdividef(A, B);
         else if (B > 1.0e-10f) {
             // HHChannelBase::integrate, X e + (A/B)(1 - e) with e = exp(-B dt),
             // as X + (A/B - X)(1 - e), 1 - e = -expm1(-B dt) (no cancellation)
-            float em = -expm1f(-B * dt);
+            const float em = -expm1f(-B * dt);
             X = fmaf(__fdividef(A, B) - X, em, X);
         } else X = fmaf(A, dt, X);
         b.k2x[n] = X;
-        float gk = b.k2gbar[n] * powi(X, t.xp, t.xpf);
+        const float gk = k2g * powi(X, t.xp, t.xpf);
         G += gk;
         GE = fmaf(gk, t.ek, GE);
     }
-    // SynChans: events delivered this step (SimpleSynHandler), dual exponential
-    if (info & kNodeSyn) {
-        for (uint32_t k = b.syn0[n]; k < b.syn0[n + 1]; ++k) {
-            const SynType& t = c_synTypes[b.synType[k]];
-            uint32_t e = b.evCur[k];
-            const uint32_t end = b.evEnd[k];
-            float act = 0.f;
-            while (e < end && b.evStep[e] <= step) act += b.evAct[e++];
-            b.evCur[k] = e;
-            float X = fmaf(act, t.xc1, b.synX[k] * t.xc2);
-            float Y = fmaf(X, t.yc1, b.synY[k] * t.yc2);
-            b.synX[k] = X;
-            b.synY[k] = Y;
-            float gk = Y * b.synNorm[k];
-            G += gk;
-            GE = fmaf(gk, t.ek, GE);
-        }
+    // ---- SynChans: events delivered this step (SimpleSynHandler), dual exponential
+    for (uint32_t k = s0; k < s1; ++k) {
+        const SynType& t = c_synTypes[__ldg(b.synType + k)];
+        uint32_t e = b.evCur[k];
+        const uint32_t end = __ldg(b.evEnd + k);
+        const float sx = b.synX[k], sy = b.synY[k], nm = __ldg(b.synNorm + k);
+        float act = 0.f;
+        while (e < end && __ldg(b.evStep + e) <= step) act += __ldg(b.evAct + e++);
+        b.evCur[k] = e;
+        const float X = fmaf(act, t.xc1, sx * t.xc2);
+        const float Y = fmaf(X, t.yc1, sy * t.yc2);
+        b.synX[k] = X;
+        b.synY[k] = Y;
+        const float gk = Y * nm;
+        G += gk;
+        GE = fmaf(gk, t.ek, GE);
     }
-    diag = b.HS2[n] + (double)G;
-    rhs = fma(V, b.CmByDt[n], b.EmByRm[n]) + (double)GE;
+    diag = hs2 + widenF(G);
+    rhs = fma(V, cmdt, emrm) + widenF(GE) + inj;
 }
 
-struct Team {
-    uint32_t tid, nth, bar;
+// Elimination arrays of a forest: pivots/couplings D, right-hand sides R,
+// off-diagonals OFF, topology TOPO and PAR (forest-local indices).
+struct Elim {
+    double *D, *R;
+    const double* OFF;
+    const uint32_t* TOPO;
+    const uint16_t* PAR;
 };
 
-__device__ __forceinline__ void teamSync(const Team& t) {
-    if (t.nth == 32) __syncwarp();
-    else asm volatile("bar.sync %0, %1;" ::"r"(t.bar), "r"(t.nth) : "memory");
+// Per-cell work of tick 0 (stimulus schedule) for the forest's cells.
+__device__ __forceinline__ void forestStimulus(const MixBatch& b, const MixForest& F, unsigned long long step) {
+    for (uint32_t k = threadIdx.x; k < F.nCells; k += blockDim.x) {
+        const uint32_t cell = b.forestCells[F.cell0 + k];
+        const MixCellRange cr = b.cells[cell];
+        if (!cr.nStim) continue;
+        uint32_t cur = b.stimCur[cell];
+        while (cur < cr.nStim && b.stimStep[cr.stim0 + cur] <= step) {
+            b.injVal[cr.inj0 + b.stimEntry[cr.stim0 + cur]] = b.stimValue[cr.stim0 + cur];
+            ++cur;
+        }
+        b.stimCur[cell] = cur;
+    }
 }
 
-__device__ void stepCell(const MixBatch& b, uint32_t cell, uint32_t nsteps, const Team& tm) {
-    const MixCellRange cr = b.cells[cell];
-    const uint32_t base = cr.node0;
-    unsigned long long step = b.stepCount[cell];
-    uint32_t stimCur = b.stimCur[cell];
-    uint32_t spk = b.spikeCount[cell];
-    for (uint32_t s = 0; s < nsteps; ++s, ++step) {
-        if (tm.tid == 0) {
-            while (stimCur < cr.nStim && b.stimStep[cr.stim0 + stimCur] <= step) {
-                b.injVal[cr.inj0 + b.stimEntry[cr.stim0 + stimCur]] = b.stimValue[cr.stim0 + stimCur];
-                ++stimCur;
-            }
-        }
-        teamSync(tm);
-        // assembly, all compartment nodes in parallel; rows staged in inv/gEl
-        for (uint32_t i = tm.tid; i < cr.nNodes; i += tm.nth) {
-            const uint32_t n = base + i;
-            const uint32_t info = b.nodeInfo[n];
-            if (info & kNodeCenter) {
-                b.inv[n] = b.HS2[n];
-                b.gEl[n] = 0.0;
-                continue;
-            }
-            double d, r;
-            nodeRow(b, n, info, step, d, r);
-            if (info & kNodeInject)
-                for (uint32_t k = 0; k < cr.nInj; ++k)
-                    if (b.injNode[cr.inj0 + k] == i) r += b.injVal[cr.inj0 + k];
-            b.inv[n] = d;
-            b.gEl[n] = r;
-        }
-        teamSync(tm);
-        // forward elimination: units level by level, each unit serially;
-        // every node pulls its children (diag -= off^2/pivot_c, rhs -= off*g_c)
-        const uint32_t* up = b.unitPtr + cr.level0;
-        const uint2* un = b.units + cr.unit0;
-        const uint32_t* cl = b.childList + cr.child0;
-        for (uint32_t L = 0; L < cr.nLevels; ++L) {
-            for (uint32_t u = up[L] + tm.tid; u < up[L + 1]; u += tm.nth) {
-                const uint2 rg = un[u];
-                // the node eliminated just before is the last child in
-                // post-order and the lower neighbour in a chain: its pivot
-                // and g stay in registers
-                double pIv = 0.0, pG = 0.0;
-                for (uint32_t v = rg.x; v < rg.y; ++v) {
-                    const uint32_t n = base + v;
-                    double d = b.inv[n], r = b.gEl[n];
-                    const uint32_t cs = b.childStart[n], nc = (b.nodeInfo[n] >> 16) & 0xFF;
-                    for (uint32_t k = cs; k < cs + nc; ++k) {
-                        const uint32_t cv = cl[k];
-                        const uint32_t c = base + cv;
-                        const bool prev = cv + 1 == v && v > rg.x;
-                        const double ivc = prev ? pIv : b.inv[c];
-                        const double gc = prev ? pG : b.gEl[c];
-                        d = fma(-b.offsq[c], ivc, d);
-                        r = fma(-b.off[c], gc, r);
+// SpikeGens (SpikeGen::process with the solver's V and currTime = dt (step+1))
+// and trace samples, one thread per cell.
+__device__ __forceinline__ void forestOutputs(const MixBatch& b, const MixForest& F, unsigned long long step) {
+    const double currTime = b.dt * (double)(step + 1);
+    const bool sample = ((step + 1) % b.recStride) == 0;
+    for (uint32_t k = threadIdx.x; k < F.nCells; k += blockDim.x) {
+        const uint32_t cell = b.forestCells[F.cell0 + k];
+        const MixCellRange cr = b.cells[cell];
+        for (uint32_t g = cr.sg0; g < cr.sg0 + cr.nSg; ++g) {
+            const double Vs = b.V[b.sgNode[g]];
+            if (Vs > (double)b.sgThresh[g]) {
+                if ((float)(currTime + b.dt / 2.0) >= b.sgLast[g] + b.sgRefract[g] && !(b.sgEdge[g] && b.sgFired[g])) {
+                    const uint32_t spk = b.spikeCount[cell];
+                    if (spk < b.spikeCap) {
+                        b.spikeGen[(size_t)cell * b.spikeCap + spk] = g - cr.sg0;
+                        b.spikeTime[(size_t)cell * b.spikeCap + spk] = (float)currTime;
                     }
-                    pIv = rcpNewton(d);
-                    pG = r * pIv;
-                    b.inv[n] = pIv;
-                    b.gEl[n] = pG;
+                    b.spikeCount[cell] = spk + 1;
+                    b.sgLast[g] = (float)currTime;
+                    b.sgFired[g] = 1;
                 }
-            }
-            teamSync(tm);
-        }
-        // back substitution in the reverse order: VMid = g - (off/pivot) VMid[parent],
-        // V = 2 VMid - V, then the node's Ca pool
-        for (int L = (int)cr.nLevels - 1; L >= 0; --L) {
-            for (uint32_t u = up[L] + tm.tid; u < up[L + 1]; u += tm.nth) {
-                const uint2 rg = un[u];
-                double pVm = 0.0;   // VMid of the node substituted just before
-                for (uint32_t v = rg.y; v-- > rg.x;) {
-                    const uint32_t n = base + v;
-                    double vm = b.gEl[n];
-                    const uint32_t pa = b.parent[n];
-                    if (pa != ~0u) {
-                        const double vp = (pa == v + 1 && v + 1 < rg.y) ? pVm : b.VMid[base + pa];
-                        vm = fma(-(b.off[n] * b.inv[n]), vp, vm);
-                    }
-                    pVm = vm;
-                    b.VMid[n] = vm;
-                    const uint32_t info = b.nodeInfo[n];
-                    if (!(info & kNodeCenter)) {
-                        const double Vold = b.V[n];
-                        const double Vnew = fma(2.0, vm, -Vold);
-                        b.V[n] = Vnew;
-                        if (info & kNodePool) {
-                            const float vca = (float)(b.caAdvance == 1 ? vm : fma(2.0, vm, -Vnew));
-                            float act = fmaf(-b.caG[n], vca, b.caGE[n]);
-                            // c f1 + f2 act with f1 = 1 - g1 (g1 = 1 - f1 from FP64)
-                            float c0v = b.poolC[n];
-                            float c = fmaf(-b.poolG1[n], c0v, c0v) + b.poolF2[n] * act;
-                            float cav = b.poolBasal[n] + c;
-                            if (b.poolCeil[n] > 0.f && cav > b.poolCeil[n]) { cav = b.poolCeil[n]; c = cav - b.poolBasal[n]; }
-                            if (cav < b.poolFloor[n]) { cav = b.poolFloor[n]; c = cav - b.poolBasal[n]; }
-                            b.poolC[n] = c;
-                            b.poolCa[n] = cav;
-                        }
-                    }
-                }
-            }
-            teamSync(tm);
-        }
-        // SpikeGens (SpikeGen::process with the solver's V and currTime)
-        if (tm.tid == 0) {
-            const double currTime = b.dt * (double)(step + 1);
-            for (uint32_t k = cr.sg0; k < cr.sg0 + cr.nSg; ++k) {
-                double Vs = b.V[base + b.sgNode[k]];
-                if (Vs > (double)b.sgThresh[k]) {
-                    if ((float)(currTime + b.dt / 2.0) >= b.sgLast[k] + b.sgRefract[k]) {
-                        if (!(b.sgEdge[k] && b.sgFired[k])) {
-                            if (spk < b.spikeCap) {
-                                b.spikeGen[(size_t)cell * b.spikeCap + spk] = k - cr.sg0;
-                                b.spikeTime[(size_t)cell * b.spikeCap + spk] = (float)currTime;
-                            }
-                            ++spk;
-                            b.sgLast[k] = (float)currTime;
-                            b.sgFired[k] = 1;
-                        }
-                    }
-                } else {
-                    b.sgFired[k] = 0;
-                }
+            } else {
+                b.sgFired[g] = 0;
             }
         }
-        if (cr.nRec && ((step + 1) % b.recStride) == 0) {
-            uint32_t smp = (uint32_t)((step + 1) / b.recStride);
+        if (cr.nRec && sample) {
+            const uint64_t smp = (step + 1) / b.recStride;
             if (smp < b.recCap)
-                for (uint32_t r = tm.tid; r < cr.nRec; r += tm.nth)
-                    b.recBuf[(size_t)smp * b.recLd + cr.rec0 + r] = b.V[base + b.recNode[cr.rec0 + r]];
+                for (uint32_t r = cr.rec0; r < cr.rec0 + cr.nRec; ++r)
+                    b.recBuf[smp * b.recLd + r] = b.V[b.recNode[r]];
         }
-        teamSync(tm);
-    }
-    if (tm.tid == 0) {
-        b.stepCount[cell] = step;
-        b.stimCur[cell] = stimCur;
-        b.spikeCount[cell] = spk;
     }
 }
 
-__global__ void __launch_bounds__(512) hsBatchStepMixed(MixBatch b, const uint32_t* __restrict__ teamCellPtr,
-                                                        const uint32_t* __restrict__ teamCells, uint32_t nTeams,
-                                                        uint32_t warpsPerTeam, uint32_t nsteps) {
-    const uint32_t teamsPerCta = blockDim.x / (32 * warpsPerTeam);
-    const uint32_t teamInCta = threadIdx.x / (32 * warpsPerTeam);
-    const uint32_t team = blockIdx.x * teamsPerCta + teamInCta;
-    if (team >= nTeams) return;     // whole teams leave together
-    Team tm;
-    tm.nth = 32 * warpsPerTeam;
-    tm.tid = threadIdx.x - teamInCta * tm.nth;
-    tm.bar = teamInCta + 1;
-    for (uint32_t k = teamCellPtr[team]; k < teamCellPtr[team + 1]; ++k) stepCell(b, teamCells[k], nsteps, tm);
+// `nsteps` steps of one forest by the whole CTA.  The V/Ca update and the
+// outputs (SpikeGens, trace samples) of a step run at the start of the next
+// step's assembly, and after the last step.
+__device__ void stepForest(const MixBatch& b, const MixForest& F, const Elim& E, const uint32_t* lp,
+                           uint32_t nsteps) {
+    const uint32_t tid = threadIdx.x, nth = blockDim.x;
+    if (nsteps == 0) return;
+    unsigned long long step = b.stepCount[b.forestCells[F.cell0]];
+    for (uint32_t s = 0; s < nsteps; ++s, ++step) {
+        forestStimulus(b, F, step);
+        __syncthreads();
+        // assembly: every node's FP64 row (junction nodes: their diagonal)
+        for (uint32_t i = tid; i < F.nNodes; i += nth) {
+            const uint32_t n = F.node0 + i;
+            const uint32_t info = __ldg(b.nodeInfo + n);
+            double d, r;
+            if (info & kNodeCenter) {
+                d = __ldg(b.HS2 + n);
+                r = 0.0;
+            } else {
+                assembleNode(b, n, info, s > 0, s > 0 ? E.R[i] : 0.0, step, d, r);
+            }
+            E.D[i] = d;
+            E.R[i] = r;
+        }
+        __syncthreads();
+        if (s > 0) forestOutputs(b, F, step - 1);
+        // forward elimination, deepest level first: pull the children's
+        // eliminated rows (diag -= off_c * f_c, rhs -= off_c * g_c), then keep
+        // g = rhs/pivot in R and f = off/pivot in D
+        for (int L = (int)F.nLevels - 1; L >= 0; --L) {
+            const uint32_t e = lp[L + 1];
+            for (uint32_t i = lp[L] + tid; i < e; i += nth) {
+                const uint32_t t = E.TOPO[i];
+                const uint32_t c0 = t & 0xFFFF, c1 = c0 + (t >> 16);
+                double d = E.D[i], r = E.R[i];
+                for (uint32_t c = c0; c < c1; ++c) {
+                    const double oc = E.OFF[c];
+                    d = fma(-oc, E.D[c], d);
+                    r = fma(-oc, E.R[c], r);
+                }
+                const double iv = rcpPivot(d);
+                E.R[i] = r * iv;
+                E.D[i] = E.OFF[i] * iv;
+            }
+            __syncthreads();
+        }
+        // back substitution, root level first: VMid = g - f * VMid[parent]
+        for (uint32_t L = 0; L < F.nLevels; ++L) {
+            const uint32_t e = lp[L + 1];
+            for (uint32_t i = lp[L] + tid; i < e; i += nth) {
+                const uint32_t p = E.PAR[i];
+                double vm = E.R[i];
+                if (p != kNoParent) vm = fma(-E.D[i], E.R[p], vm);
+                E.R[i] = vm;
+            }
+            __syncthreads();
+        }
+    }
+    // the last step's update and outputs
+    for (uint32_t i = tid; i < F.nNodes; i += nth) {
+        const uint32_t n = F.node0 + i;
+        const uint32_t info = __ldg(b.nodeInfo + n);
+        if (info & kNodeCenter) continue;
+        const double vm = E.R[i];
+        const double Vnew = fma(2.0, vm, -b.V[n]);
+        b.V[n] = Vnew;
+        if (info & kNodePool) {
+            const float vca = (float)(b.caAdvance == 1 ? vm : fma(2.0, vm, -Vnew));
+            const float act = fmaf(-b.caG[n], vca, b.caGE[n]);
+            const float c0v = b.poolC[n];
+            float c = fmaf(-b.poolG1[n], c0v, c0v) + b.poolF2[n] * act;
+            float cav = b.poolBasal[n] + c;
+            if (b.poolCeil[n] > 0.f && cav > b.poolCeil[n]) { cav = b.poolCeil[n]; c = cav - b.poolBasal[n]; }
+            if (cav < b.poolFloor[n]) { cav = b.poolFloor[n]; c = cav - b.poolBasal[n]; }
+            b.poolC[n] = c;
+            b.poolCa[n] = cav;
+        }
+    }
+    __syncthreads();
+    forestOutputs(b, F, step - 1);
+    for (uint32_t k = tid; k < F.nCells; k += nth) b.stepCount[b.forestCells[F.cell0 + k]] = step;
+    __syncthreads();
 }
 
-// Reinit: V = initVm, gates at their steady state, Ca = CaBasal, synapses,
-// K(Ca) X, spike and stimulus state.  One warp per cell.
-__global__ void hsBatchReinitMixed(MixBatch b, const double* __restrict__ initVm,
+// One CTA steps its forests one after the other, each for `nsteps` steps.
+// Dynamic shared memory: kSmemLevels level offsets, then for shared forests
+// the elimination arrays of `cap` nodes: D, R, OFF (8 B each), TOPO (4 B),
+// PAR (2 B).
+__global__ void __launch_bounds__(1024, 1) hsForestStepMixed(MixBatch b, const uint32_t* __restrict__ ctaPtr,
+                                                             const uint32_t* __restrict__ ctaForests, uint32_t cap,
+                                                             uint32_t nsteps) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t* sLp = reinterpret_cast<uint32_t*>(smem);
+    double* sD = reinterpret_cast<double*>(smem + kSmemLevels * 4);
+    for (uint32_t k = ctaPtr[blockIdx.x]; k < ctaPtr[blockIdx.x + 1]; ++k) {
+        const MixForest F = b.forests[ctaForests[k]];
+        const uint32_t* lp = b.levelPtr + F.level0;
+        if (F.nLevels < kSmemLevels) {
+            for (uint32_t i = threadIdx.x; i <= F.nLevels; i += blockDim.x) sLp[i] = lp[i];
+            lp = sLp;
+        }
+        Elim E;
+        if (F.shared) {
+            double* sR = sD + cap;
+            double* sOff = sR + cap;
+            uint32_t* sTopo = reinterpret_cast<uint32_t*>(sOff + cap);
+            uint16_t* sPar = reinterpret_cast<uint16_t*>(sTopo + cap);
+            for (uint32_t i = threadIdx.x; i < F.nNodes; i += blockDim.x) {
+                sOff[i] = b.off[F.node0 + i];
+                sTopo[i] = b.topo[F.node0 + i];
+                sPar[i] = b.par[F.node0 + i];
+            }
+            E.D = sD;
+            E.R = sR;
+            E.OFF = sOff;
+            E.TOPO = sTopo;
+            E.PAR = sPar;
+        } else {
+            E.D = b.elimD + F.node0;
+            E.R = b.elimR + F.node0;
+            E.OFF = b.off + F.node0;
+            E.TOPO = b.topo + F.node0;
+            E.PAR = b.par + F.node0;
+        }
+        __syncthreads();
+        stepForest(b, F, E, lp, nsteps);
+    }
+}
+
+// Reinit, per node: V = initVm, gates at their steady state, Ca = CaBasal,
+// synapses, K(Ca) X.
+__global__ void hsReinitNodesMixed(MixBatch b, uint32_t nNodes, const double* __restrict__ initVm,
                                    const float* __restrict__ k2x0, const uint32_t* __restrict__ evStart) {
-    uint32_t cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t lane = threadIdx.x & 31;
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nNodes) return;
+    const uint64_t ld = b.ld;
+    const uint32_t info = b.nodeInfo[n];
+    b.V[n] = initVm[n];
+    if (info & kNodeCenter) return;
+    if (info & kNodePool) {
+        b.poolC[n] = 0.f;
+        b.poolCa[n] = b.poolBasal[n];
+    }
+    const float ca = (info & kNodePool) ? b.poolCa[n] : 0.f;
+    RowF vr = rowF(b.vTab, b.vCol, b.vRows, (float)initVm[n], b.vMin, b.vMax, b.vInvDx);
+    const uint32_t types = b.ctype4[n];
+    for (int j = 0; j < kMaxChan; ++j) {
+        const uint32_t tj = (types >> (8 * j)) & 0xFF;
+        if (tj == kNoType) break;
+        const ChanType& t = c_chanTypes[tj];
+        float* st = b.state + (uint64_t)(3 * j) * ld + n;
+        if (t.xp) st[0] = gateF(vr, b.vCol, t.colX, 0.f, 0.f, 0.f, true);
+        if (t.yp) st[ld] = gateF(vr, b.vCol, t.colY, 0.f, 0.f, 0.f, true);
+        if (t.zp) {
+            if (t.zCa) {
+                RowF cr2 = rowF(b.caTab, b.caCol, b.caRows, ca, b.caMin, b.caMax, b.caInvDx);
+                st[2 * ld] = gateF(cr2, b.caCol, t.colZ, 0.f, 0.f, 0.f, true);
+            } else {
+                st[2 * ld] = gateF(vr, b.vCol, t.colZ, 0.f, 0.f, 0.f, true);
+            }
+        }
+    }
+    if (((info >> 8) & 0xFF) != kNoType) b.k2x[n] = k2x0[n];
+    if (info & kNodeSyn)
+        for (uint32_t k = b.syn0[n]; k < b.syn0[n + 1]; ++k) {
+            b.synX[k] = 0.f;
+            b.synY[k] = 0.f;
+            b.evCur[k] = evStart[k];
+        }
+}
+
+// Reinit, per cell: SpikeGens, counters, trace sample 0 (after the nodes).
+__global__ void hsReinitCellsMixed(MixBatch b) {
+    const uint32_t cell = blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= b.nCells) return;
     const MixCellRange cr = b.cells[cell];
-    const uint64_t ld = b.ld;
-    for (uint32_t i = lane; i < cr.nNodes; i += 32) {
-        const uint32_t n = cr.node0 + i;
-        const uint32_t info = b.nodeInfo[n];
-        b.V[n] = initVm[n];
-        if (info & kNodeCenter) continue;
-        if (info & kNodePool) {
-            b.poolC[n] = 0.f;
-            b.poolCa[n] = b.poolBasal[n];
-        }
-        const float ca = (info & kNodePool) ? b.poolCa[n] : 0.f;
-        RowF vr = rowF(b.vTab, b.vCol, b.vRows, (float)b.V[n], b.vMin, b.vMax, b.vInvDx);
-        const uint32_t types = b.ctype4[n];
-        for (int j = 0; j < kMaxChan; ++j) {
-            const uint32_t tj = (types >> (8 * j)) & 0xFF;
-            if (tj == kNoType) break;
-            const ChanType& t = c_chanTypes[tj];
-            float* st = b.state + (uint64_t)(3 * j) * ld + n;
-            if (t.xp) st[0] = gateF(vr, b.vCol, t.colX, 0.f, 0.f, 0.f, true);
-            if (t.yp) st[ld] = gateF(vr, b.vCol, t.colY, 0.f, 0.f, 0.f, true);
-            if (t.zp) {
-                if (t.zCa) {
-                    RowF cr2 = rowF(b.caTab, b.caCol, b.caRows, ca, b.caMin, b.caMax, b.caInvDx);
-                    st[2 * ld] = gateF(cr2, b.caCol, t.colZ, 0.f, 0.f, 0.f, true);
-                } else {
-                    st[2 * ld] = gateF(vr, b.vCol, t.colZ, 0.f, 0.f, 0.f, true);
-                }
-            }
-        }
-        if (((info >> 8) & 0xFF) != kNoType) b.k2x[n] = k2x0[n];
-        if (info & kNodeSyn)
-            for (uint32_t k = b.syn0[n]; k < b.syn0[n + 1]; ++k) {
-                b.synX[k] = 0.f;
-                b.synY[k] = 0.f;
-                b.evCur[k] = evStart[k];
-            }
+    for (uint32_t g = cr.sg0; g < cr.sg0 + cr.nSg; ++g) {
+        b.sgLast[g] = -b.sgRefract[g];
+        b.sgFired[g] = 0;
     }
-    for (uint32_t k = cr.sg0 + lane; k < cr.sg0 + cr.nSg; k += 32) {
-        b.sgLast[k] = -b.sgRefract[k];
-        b.sgFired[k] = 0;
-    }
-    if (lane == 0) {
-        b.stepCount[cell] = 0;
-        b.stimCur[cell] = 0;
-        b.spikeCount[cell] = 0;
-    }
-    __syncwarp();
-    if (cr.nRec)
-        for (uint32_t r = lane; r < cr.nRec; r += 32)
-            b.recBuf[cr.rec0 + r] = b.V[cr.node0 + b.recNode[cr.rec0 + r]];
+    b.stepCount[cell] = 0;
+    b.stimCur[cell] = 0;
+    b.spikeCount[cell] = 0;
+    for (uint32_t r = cr.rec0; r < cr.rec0 + cr.nRec; ++r) b.recBuf[r] = b.V[b.recNode[r]];
 }
 
 // Scatter of host-supplied inject values to their solver slots.
@@ -449,19 +542,21 @@ cudaError_t uploadMixedTypes(const ChanType* ct, int nct, const C2dType* kt, int
     return e;
 }
 
-cudaError_t launchBatchStepMixed(const MixBatch& b, const uint32_t* teamCellPtr, const uint32_t* teamCells,
-                                 uint32_t nTeams, uint32_t warpsPerTeam, uint32_t threadsPerCta, uint32_t nsteps,
-                                 cudaStream_t st) {
-    uint32_t teamsPerCta = threadsPerCta / (32 * warpsPerTeam);
-    uint32_t blocks = (nTeams + teamsPerCta - 1) / teamsPerCta;
-    hsBatchStepMixed<<<blocks, threadsPerCta, 0, st>>>(b, teamCellPtr, teamCells, nTeams, warpsPerTeam, nsteps);
+cudaError_t launchForestStepMixed(const MixBatch& b, const uint32_t* ctaPtr, const uint32_t* ctaForests,
+                                  uint32_t nCtas, uint32_t threadsPerCta, uint32_t smemBytes, uint32_t cap,
+                                  uint32_t nsteps, cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(hsForestStepMixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes);
+    if (e != cudaSuccess) return e;
+    hsForestStepMixed<<<nCtas, threadsPerCta, smemBytes, st>>>(b, ctaPtr, ctaForests, cap, nsteps);
     return cudaGetLastError();
 }
 
-cudaError_t launchBatchReinitMixed(const MixBatch& b, const double* initVm, const float* k2x0,
+cudaError_t launchBatchReinitMixed(const MixBatch& b, uint32_t nNodes, const double* initVm, const float* k2x0,
                                    const uint32_t* evStart, cudaStream_t st) {
-    uint32_t blocks = (b.nCells * 32 + 255) / 256;
-    hsBatchReinitMixed<<<blocks ? blocks : 1, 256, 0, st>>>(b, initVm, k2x0, evStart);
+    hsReinitNodesMixed<<<(nNodes + 255) / 256, 256, 0, st>>>(b, nNodes, initVm, k2x0, evStart);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    hsReinitCellsMixed<<<(b.nCells + 127) / 128, 128, 0, st>>>(b);
     return cudaGetLastError();
 }
 

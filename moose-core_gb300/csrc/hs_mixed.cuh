@@ -1,16 +1,25 @@
 // hs_mixed.cuh -- device layout of the mixed-precision batched HSolve.
 //
-// All cells of a batch are concatenated.  Each cell's compartments are nodes
-// of a tree in breadth-first order from the morphological root; every
-// junction of three or more compartments (a `coupled_` group of
-// hsolve/HinesMatrix.cpp:84-130) becomes one extra node without membrane: the
-// reference's clique of conductances Ga_i*Ga_j/sum(Ga) between the members is
-// exactly the star with conductance Ga_i from each member to that node, once
-// the node is eliminated (Y-Delta transform), so the voltages are the same.
-// The matrix is then a plain tree: each node has one coupling to its parent.
+// Matrix.  Each cell's compartments are nodes of a tree rooted at the
+// morphological root; every junction of three or more compartments (a
+// `coupled_` group of hsolve/HinesMatrix.cpp:84-130) becomes one extra node
+// without membrane: the reference's clique of conductances Ga_i*Ga_j/sum(Ga)
+// between the members is exactly the star with conductance Ga_i from each
+// member to that node, once the node is eliminated (Y-Delta transform), so the
+// voltages are the same.  The matrix is then a plain tree: each node has one
+// coupling (off) to its parent.
 //
-// Layout: structure of arrays indexed by node, with fixed "slots" so that all
-// of a node's loads are independent and coalesced across the lanes of a warp:
+// Forests.  Cells are grouped into forests that one CTA steps together.  A
+// forest's nodes are numbered level-major: level 0 holds the roots of all its
+// cells, level d+1 the children of level d, the children of one node
+// contiguous and junction nodes after compartments.  A level is one parallel
+// step of the elimination, so narrow levels of one cell fill up with the
+// levels of the others.  During elimination a forest keeps its pivots, right
+// hand sides and coupling topology in shared memory when it fits ("shared
+// forest"); otherwise in global scratch ("global forest").
+//
+// Per-node arrays: structure of arrays over all nodes (forest after forest),
+// with fixed "slots" so that a warp's loads are coalesced:
 //   channel slot j (< kMaxChan): type byte j of ctype4[n], gbar[j*ld + n]
 //   gate state of channel j, gate g (X,Y,Z): state[(3*j+g)*ld + n]
 //   at most one Ca pool, one HHChannel2D per compartment; SynChans in CSR.
@@ -36,6 +45,8 @@ constexpr uint32_t kNodeInject = 1u << 1;    // has an inject entry
 constexpr uint32_t kNodePool = 1u << 2;      // has a Ca pool
 constexpr uint32_t kNodeSyn = 1u << 3;       // has SynChans
 // bits 8..15: HHChannel2D type (kNoType: none)
+// bits 16..27: gate present, bit kNodeGateShift + 3*slot + gate (X, Y, Z)
+constexpr uint32_t kNodeGateShift = 16;
 
 struct ChanType {          // one HHChannel prototype (hsolve/HSolveStruct.h:55-108)
     float ek;
@@ -61,17 +72,23 @@ struct SynType {           // SynChan constants at the clock dt
     float xc1, xc2, yc1, yc2, ek;
 };
 
-// Elimination schedule of a cell: its nodes are numbered unit by unit.  A
-// unit is eliminated serially by one thread: a whole small subtree in
-// post-order (level 0) or an unbranched chain of the tree above those
-// subtrees, bottom to top (levels >= 1).  Units of one level are independent;
-// a unit's children lie in lower levels or earlier in the same unit.
+constexpr uint32_t kNoParent = 0xFFFF;   // MixBatch::par of a root
+constexpr uint32_t kMaxForestNodes = 0xFFFF;
+constexpr uint32_t kSmemLevels = 1024;      // level offsets kept in shared memory
+
+// A forest: nodes [node0, node0 + nNodes), level offsets (forest-local)
+// levelPtr[level0 .. level0 + nLevels], cells forestCells[cell0 ..].
+struct MixForest {
+    uint32_t node0, nNodes;
+    uint32_t level0, nLevels;
+    uint32_t cell0, nCells;
+    uint32_t shared;             // 1: elimination arrays staged in shared memory
+    uint32_t pad;
+};
+
+// Per-cell entries of the inject, stimulus, SpikeGen and recording lists.
 struct MixCellRange {
-    uint32_t node0, nNodes;      // global first node, count
-    uint32_t level0, nLevels;    // offset into unitPtr (nLevels+1 entries)
-    uint32_t unit0;              // offset into units
-    uint32_t child0;             // offset into childList
-    uint32_t inj0, nInj;         // inject entries
+    uint32_t inj0, nInj;         // inject entries (injVal)
     uint32_t stim0, nStim;       // stimulus schedule entries
     uint32_t sg0, nSg;           // SpikeGens
     uint32_t rec0, nRec;         // recorded nodes (columns rec0..)
@@ -84,17 +101,18 @@ struct MixBatch {
     double dt;
     int caAdvance;
     const MixCellRange* cells;
-    const uint32_t* unitPtr;     // cell-local unit offsets per level
-    const uint2* units;          // cell-local node range [x, y) of each unit
-    const uint32_t* childList;   // cell-local children, per cell from child0
+    const MixForest* forests;
+    const uint32_t* forestCells;
+    const uint32_t* levelPtr;
     // per node (global index)
-    const uint32_t* nodeInfo;    // flags; bits 8-15 K(Ca) type; bits 16-23 child count
+    const uint32_t* nodeInfo;    // flags, K(Ca) type, gate mask (bits above)
     const uint32_t* ctype4;      // 4 channel type bytes
-    const uint32_t* childStart;  // into the cell's childList
-    const uint32_t* parent;      // cell-local node index, ~0u for the root
-    const double *off, *offsq, *HS2, *CmByDt, *EmByRm;
+    const uint32_t* topo;        // forest-local first child | child count << 16
+    const uint16_t* par;         // forest-local parent, kNoParent for a root
+    const uint32_t* injIdx;      // inject entry of a kNodeInject node
+    const double *off, *HS2, *CmByDt, *EmByRm;
     double* V;
-    double *inv, *gEl, *VMid;    // elimination temporaries
+    double *elimD, *elimR;       // elimination scratch of global forests
     float *caG, *caGE;           // Ca-feeding conductance of the step
     const float* gbar;           // [kMaxChan][ld]  Gbar * modulation
     float* state;                // [3*kMaxChan][ld]
@@ -119,13 +137,12 @@ struct MixBatch {
     const uint32_t* evStep;      // delivery step of each event
     const float* evAct;          // weight / dt
     // inject / stimulus
-    const uint32_t* injNode;
     double* injVal;
     const uint32_t *stimStep, *stimEntry;
     const double* stimValue;
     uint32_t* stimCur;
     // spike gens
-    const uint32_t* sgNode;
+    const uint32_t* sgNode;      // global node
     const float *sgThresh, *sgRefract;
     const int32_t* sgEdge;
     float* sgLast;
@@ -142,7 +159,7 @@ struct MixBatch {
     uint32_t caCol, caRows;
     float caMin, caMax, caInvDx;
     // recording
-    const uint32_t* recNode;
+    const uint32_t* recNode;     // global node of each column
     double* recBuf;
     uint32_t recLd, recCap, recStride;
     unsigned long long* stepCount;

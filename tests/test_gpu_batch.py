@@ -92,7 +92,8 @@ def test_mixed_recording_and_tuning():
     b.record([0, 0, 3, 5], [0, 4, 0, 2], 10, 51)
     b.reinit(DT)
     b.process(200)
-    b.tune(threads_per_cta=128, ctas_per_sm=2, steps_per_launch=25)
+    # a new launch shape without a new packing keeps the state
+    b.tune(threads_per_cta=128, steps_per_launch=25)
     b.process(300)
     tr, cols = b.trace()
     assert tr.shape == (51, 4)
@@ -100,3 +101,27 @@ def test_mixed_recording_and_tuning():
     assert np.array_equal(tr[-1], [b.vm(c)[m] for c, m in cols])
     ms, n = b.kernel_time()
     assert n >= 1 and ms > 0
+
+
+def test_mixed_results_do_not_depend_on_packing():
+    """A cell's result is the same alone, in a large mix, in small shared
+    forests, in global forests and under any launch shape (bit-identical:
+    every node's arithmetic is fixed by its own cell)."""
+    cells = small_population(12, 7, n_syn=4)
+    a = Batch(cells, DT, HS_PREC_MIXED)
+    c = Batch(cells, DT, HS_PREC_MIXED, threads_per_cta=256, ctas_per_sm=2, forest_nodes=64)
+    alone = Batch([cells[3]], DT, HS_PREC_MIXED, threads_per_cta=96)
+    for x in (a, c, alone):
+        x.reinit(DT)
+        x.process(500)
+    for i in range(len(cells)):
+        assert np.array_equal(a.vm(i), c.vm(i)), i
+    assert np.array_equal(alone.vm(0), a.vm(3))
+    # repacking an existing batch starts it over
+    a.tune(ctas_per_sm=2, forest_nodes=128)
+    with pytest.raises(Exception):
+        a.process(10)
+    a.reinit(DT)
+    a.process(500)
+    for i in range(len(cells)):
+        assert np.array_equal(a.vm(i), c.vm(i)), i
