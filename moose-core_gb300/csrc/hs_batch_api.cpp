@@ -858,6 +858,45 @@ int buildMixed(HsBatch* b) {
     b->dMixInitVm = D.up(H.initVm, st);
     b->dMixC2dX0 = D.up(H.c2dX0, st);
     b->dEvStart = D.up(H.evStart, st);
+    // per-node arrays the assembly reads, for the L2 prefetch
+    {
+        uint32_t gateUse = 0, slotUse = 0, anyPool = 0, anyK2 = 0, anySyn = 0;
+        for (uint32_t g = 0; g < nN; ++g) {
+            gateUse |= nodeInfo[g] >> kNodeGateShift;
+            for (int j = 0; j < kMaxChan; ++j)
+                if (((ctype4[g] >> (8 * j)) & 0xFF) != kNoType) slotUse |= 1u << j;
+            anyPool |= nodeInfo[g] & kNodePool;
+            anyK2 |= ((nodeInfo[g] >> 8) & 0xFF) != kNoType;
+            anySyn |= nodeInfo[g] & kNodeSyn;
+        }
+        auto add = [&](const void* p, uint32_t elem, uint64_t n) {
+            if (m.nPf < (uint32_t)kMaxPrefetch) m.pf[m.nPf++] = PrefetchArr{p, elem, (uint32_t)n};
+        };
+        add(m.nodeInfo, 4, nN);
+        add(m.ctype4, 4, nN);
+        add(m.V, 8, nN);
+        add(m.HS2, 8, nN);
+        add(m.CmByDt, 8, nN);
+        add(m.EmByRm, 8, nN);
+        for (int k = 0; k < 3 * kMaxChan; ++k)
+            if ((gateUse >> k) & 1u) add(m.state + (size_t)k * ld, 4, ld);
+        for (int j = 0; j < kMaxChan; ++j)
+            if ((slotUse >> j) & 1u) add(m.gbar + (size_t)j * ld, 4, ld);
+        if (anyPool) {
+            add(m.poolC, 4, nN);
+            add(m.poolCa, 4, nN);
+            add(m.poolG1, 4, nN);
+            add(m.poolF2, 4, nN);
+            add(m.poolBasal, 4, nN);
+            add(m.caG, 4, nN);
+            add(m.caGE, 4, nN);
+        }
+        if (anyK2) {
+            add(m.k2x, 4, nN);
+            add(m.k2gbar, 4, nN);
+        }
+        if (anySyn) add(m.syn0, 4, nN + 1);
+    }
     b->dCtaPtr = D.up(ctaPtr, st);
     b->dCtaForests = D.up(ctaForests, st);
     b->nCtas = nCtas;

@@ -68,8 +68,8 @@ __device__ __forceinline__ RowF rowF(const float* T, uint32_t nCol, uint32_t nRo
 __device__ __forceinline__ float gateF(const RowF& r, uint32_t nCol, int col, float x, float dt,
                                        float hdt, bool inst) {
     const float* ap = r.p + col;
-    float2 a = *reinterpret_cast<const float2*>(ap);
-    float2 b = *reinterpret_cast<const float2*>(ap + nCol);
+    const float2 a = __ldg(reinterpret_cast<const float2*>(ap));
+    const float2 b = __ldg(reinterpret_cast<const float2*>(ap + nCol));
     float C1 = fmaf(b.x - a.x, r.frac, a.x);
     float C2 = fmaf(b.y - a.y, r.frac, a.y);
     if (inst) return __fdividef(C1, C2);
@@ -91,11 +91,11 @@ __device__ __forceinline__ void interp2dF(const float* T, const float* geom, uin
     float xF = xv - (float)xi, yF = yv - (float)yi;
     bool endX = xi == nx - 1, endY = yi == ny - 1;
     const float* p00 = T + 2 * ((size_t)xi * ny + yi);
-    float2 z00 = *reinterpret_cast<const float2*>(p00);
+    const float2 z00 = __ldg(reinterpret_cast<const float2*>(p00));
     float2 z10 = make_float2(0.f, 0.f), z01 = z10, z11 = z10;
-    if (!endX) z10 = *reinterpret_cast<const float2*>(p00 + 2 * ny);
-    if (!endY) z01 = *reinterpret_cast<const float2*>(p00 + 2);
-    if (!endX && !endY) z11 = *reinterpret_cast<const float2*>(p00 + 2 * ny + 2);
+    if (!endX) z10 = __ldg(reinterpret_cast<const float2*>(p00 + 2 * ny));
+    if (!endY) z01 = __ldg(reinterpret_cast<const float2*>(p00 + 2));
+    if (!endX && !endY) z11 = __ldg(reinterpret_cast<const float2*>(p00 + 2 * ny + 2));
     float xFyF = xF * yF;
     float w00 = 1.f - xF - yF + xFyF, w10 = xF - xFyF, w01 = yF - xFyF;
     A = z00.x * w00 + z10.x * w10 + z01.x * w01 + z11.x * xFyF;
@@ -188,33 +188,30 @@ __device__ __forceinline__ void assembleNode(const MixBatch& b, uint32_t n, uint
     const float v = (float)V;
     const RowF vr = rowF(b.vTab, b.vCol, b.vRows, v, b.vMin, b.vMax, b.vInvDx);
     float G = 0.f, GE = 0.f, cg = 0.f, cge = 0.f;
+    // new gate values replace xs[] and are stored after all lookups, so that
+    // the table loads of every gate can be in flight together
 #pragma unroll
     for (int j = 0; j < kMaxChan; ++j) {
         const uint32_t tj = (types >> (8 * j)) & 0xFF;
-        if (tj == kNoType) break;
+        if (tj == kNoType) continue;
         const ChanType& t = c_chanTypes[tj];
         float frac = 1.f;
-        float* st = b.state + (uint64_t)(3 * j) * ld + n;
         if (t.xp) {
-            const float x = gateF(vr, b.vCol, t.colX, xs[3 * j], dt, hdt, t.instant & 1);
-            st[0] = x;
-            frac *= powi(x, t.xp, t.xpf);
+            xs[3 * j] = gateF(vr, b.vCol, t.colX, xs[3 * j], dt, hdt, t.instant & 1);
+            frac *= powi(xs[3 * j], t.xp, t.xpf);
         }
         if (t.yp) {
-            const float y = gateF(vr, b.vCol, t.colY, xs[3 * j + 1], dt, hdt, t.instant & 2);
-            st[ld] = y;
-            frac *= powi(y, t.yp, t.ypf);
+            xs[3 * j + 1] = gateF(vr, b.vCol, t.colY, xs[3 * j + 1], dt, hdt, t.instant & 2);
+            frac *= powi(xs[3 * j + 1], t.yp, t.ypf);
         }
         if (t.zp) {
-            float z;
             if (t.zCa) {
                 const RowF cr = rowF(b.caTab, b.caCol, b.caRows, ca, b.caMin, b.caMax, b.caInvDx);
-                z = gateF(cr, b.caCol, t.colZ, xs[3 * j + 2], dt, hdt, t.instant & 4);
+                xs[3 * j + 2] = gateF(cr, b.caCol, t.colZ, xs[3 * j + 2], dt, hdt, t.instant & 4);
             } else {
-                z = gateF(vr, b.vCol, t.colZ, xs[3 * j + 2], dt, hdt, t.instant & 4);
+                xs[3 * j + 2] = gateF(vr, b.vCol, t.colZ, xs[3 * j + 2], dt, hdt, t.instant & 4);
             }
-            st[2 * ld] = z;
-            frac *= powi(z, t.zp, t.zpf);
+            frac *= powi(xs[3 * j + 2], t.zp, t.zpf);
         }
         const float gk = gb[j] * frac;
         G += gk;
@@ -224,6 +221,9 @@ __device__ __forceinline__ void assembleNode(const MixBatch& b, uint32_t n, uint
             cge = fmaf(gk, t.ek, cge);
         }
     }
+#pragma unroll
+    for (int k = 0; k < 3 * kMaxChan; ++k)
+        if ((info >> (kNodeGateShift + k)) & 1u) b.state[(uint64_t)k * ld + n] = xs[k];
     if (pool) {
         b.caG[n] = cg;
         b.caGE[n] = cge;
@@ -328,6 +328,20 @@ __device__ __forceinline__ void forestOutputs(const MixBatch& b, const MixForest
     }
 }
 
+// Bulk prefetch into L2 (cp.async.bulk.prefetch) of forest nodes
+// [first, first + count) of per-node array `k`, clamped to the array and
+// aligned to 16 bytes; called by one thread per array.
+__device__ __forceinline__ void prefetchNodes(const MixBatch& b, uint32_t k, uint64_t first, uint32_t count) {
+    const PrefetchArr a = b.pf[k];
+    const uint64_t total = (uint64_t)a.n * a.elem / 16 * 16;
+    uint64_t lo = first * a.elem / 16 * 16;
+    uint64_t hi = ((first + count) * a.elem + 15) / 16 * 16;
+    if (hi > total) hi = total;
+    if (lo >= hi) return;
+    const char* p = static_cast<const char*>(a.base) + lo;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"((uint32_t)(hi - lo)) : "memory");
+}
+
 // `nsteps` steps of one forest by the whole CTA.  The V/Ca update and the
 // outputs (SpikeGens, trace samples) of a step run at the start of the next
 // step's assembly, and after the last step.
@@ -337,10 +351,13 @@ __device__ void stepForest(const MixBatch& b, const MixForest& F, const Elim& E,
     if (nsteps == 0) return;
     unsigned long long step = b.stepCount[b.forestCells[F.cell0]];
     for (uint32_t s = 0; s < nsteps; ++s, ++step) {
+        if (tid < b.nPf) prefetchNodes(b, tid, F.node0, nth);
         forestStimulus(b, F, step);
         __syncthreads();
-        // assembly: every node's FP64 row (junction nodes: their diagonal)
+        // assembly: every node's FP64 row (junction nodes: their diagonal);
+        // the next chunk of nth nodes is prefetched into L2 meanwhile
         for (uint32_t i = tid; i < F.nNodes; i += nth) {
+            if (tid < b.nPf && i + nth - tid < F.nNodes) prefetchNodes(b, tid, F.node0 + i + nth - tid, nth);
             const uint32_t n = F.node0 + i;
             const uint32_t info = __ldg(b.nodeInfo + n);
             double d, r;

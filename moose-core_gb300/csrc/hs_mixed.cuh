@@ -94,6 +94,15 @@ struct MixCellRange {
     uint32_t rec0, nRec;         // recorded nodes (columns rec0..)
 };
 
+// A per-node array prefetched into L2 ahead of the assembly: `n` elements
+// of `elem` bytes from `base`, node k at base + k * elem.
+constexpr int kMaxPrefetch = 32;
+struct PrefetchArr {
+    const void* base;
+    uint32_t elem;
+    uint32_t n;
+};
+
 struct MixBatch {
     uint32_t nCells;
     uint64_t ld;                 // slot stride (number of nodes, padded)
@@ -163,6 +172,9 @@ struct MixBatch {
     double* recBuf;
     uint32_t recLd, recCap, recStride;
     unsigned long long* stepCount;
+    // arrays the assembly reads per node (L2 prefetch)
+    PrefetchArr pf[kMaxPrefetch];
+    uint32_t nPf;
 };
 
 }  // namespace hsg
