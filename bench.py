@@ -151,7 +151,7 @@ class ClockSampler:
 def _traffic_from_profiles():
     """DRAM bytes per stepping launch per compartment-step from the committed
     ncu summary, if there is one."""
-    path = os.path.join(ROOT, "profiles", "hsBatchStepMixed_4096cells.md")
+    path = os.path.join(ROOT, "profiles", "hsForestStepMixed_4096cells.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -297,7 +297,7 @@ def run_ours(args, rank, world, cpu_pool):
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if achieved else None,
                 "traffic": tpc * ncomp * spl if tpc else None,
-                "kernel": "hsBatchStepMixed", "algorithmic_bytes_per_compartment_step": round(bpc, 1),
+                "kernel": "hsForestStepMixed", "algorithmic_bytes_per_compartment_step": round(bpc, 1),
                 "launch_ms": k_ms, "launches_timed": k_n, "peak_source": peak_kind}
         # plain FP64 drop-in on a sample of the same cells: one HSolve per cell
         dropin = None
@@ -374,7 +374,8 @@ def run_ours(args, rank, world, cpu_pool):
                "data": "synthetic (seeded cells; working set larger than L2, no flush)",
                "config": {"workload": "hsolve_4096cells_mixed_syn200", "cells": args.cells,
                           "compartments": ncomp, "dt_s": DT, "chunk_dt_steps": args.chunk,
-                          "steps_per_launch": spl, "synchans_per_cell": 200, "parallelism": "replicas"},
+                          "steps_per_launch": spl, "threads_per_cta": b.info()["threads_per_cta"],
+                          "ctas": b.info()["n_ctas"], "synchans_per_cell": 200, "parallelism": "replicas"},
                "e2e": {"value": e2e_value, "unit": "compartment-steps/s",
                        "h2d_bytes_per_step": args.cells * 8,
                        "d2h_bytes_per_step": (args.chunk // stride) * args.cells * 8},

@@ -300,7 +300,7 @@ typedef struct HsBatch HsBatch;
  * targets start over and hs_batch_reinit must follow. */
 typedef struct HsBatchTuning {
     uint32_t threads_per_cta;   /* multiple of 32; FP64 <= 256 (default 256),
-                                   mixed <= 1024 (default 512) */
+                                   mixed <= 1024 (default 1024) */
     uint32_t ctas_per_sm;       /* CTAs per SM (default 4 FP64, 1 mixed) */
     uint32_t steps_per_launch;  /* dt steps per kernel launch (default 100) */
     uint32_t use_graph;         /* capture a process() call as a CUDA graph */

@@ -620,7 +620,8 @@ int buildMixed(HsBatch* b) {
     std::vector<uint32_t> nodeInfo(nN), ctype4(nN), topo(nN), injIdx(nN, 0), syn0;
     std::vector<uint16_t> par(nN, (uint16_t)kNoParent);
     std::vector<double> off(nN), HS2(nN), CmByDt(nN), EmByRm(nN);
-    std::vector<float> gbarS((size_t)kMaxChan * ld, 0.f), stateS((size_t)3 * kMaxChan * ld, 0.f);
+    std::vector<float> gbarS((size_t)kMaxChan * ld, 0.f);
+    std::vector<double> stateS((size_t)3 * kMaxChan * ld, 0.0);
     std::vector<float> poolBasal(nN, 0.f), poolG1(nN, 0.f), poolF2(nN, 0.f), poolCeil(nN, 0.f), poolFloor(nN, 0.f);
     std::vector<float> k2gbar(nN, 0.f), k2x0(nN, 0.f);
     std::vector<uint8_t> synTypeV;
@@ -690,9 +691,9 @@ int buildMixed(HsBatch* b) {
                     types = (types & ~(0xFFu << (8 * j))) | ((uint32_t)ti << (8 * j));
                     gbarS[(size_t)j * ld + g] = (float)(P.Gbar[q] * P.modulation[q]);
                     int s = P.stateOff[q];
-                    if (P.Xpow[q] > 0.0) stateS[(size_t)(3 * j) * ld + g] = (float)P.state0[s++];
-                    if (P.Ypow[q] > 0.0) stateS[(size_t)(3 * j + 1) * ld + g] = (float)P.state0[s++];
-                    if (P.Zpow[q] > 0.0) stateS[(size_t)(3 * j + 2) * ld + g] = (float)P.state0[s++];
+                    if (P.Xpow[q] > 0.0) stateS[(size_t)(3 * j) * ld + g] = P.state0[s++];
+                    if (P.Ypow[q] > 0.0) stateS[(size_t)(3 * j + 1) * ld + g] = P.state0[s++];
+                    if (P.Zpow[q] > 0.0) stateS[(size_t)(3 * j + 2) * ld + g] = P.state0[s++];
                     if (P.Xpow[q] > 0.0) info |= 1u << (kNodeGateShift + 3 * j);
                     if (P.Ypow[q] > 0.0) info |= 1u << (kNodeGateShift + 3 * j + 1);
                     if (P.Zpow[q] > 0.0) info |= 1u << (kNodeGateShift + 3 * j + 2);
@@ -879,7 +880,7 @@ int buildMixed(HsBatch* b) {
         add(m.CmByDt, 8, nN);
         add(m.EmByRm, 8, nN);
         for (int k = 0; k < 3 * kMaxChan; ++k)
-            if ((gateUse >> k) & 1u) add(m.state + (size_t)k * ld, 4, ld);
+            if ((gateUse >> k) & 1u) add(m.state + (size_t)k * ld, 8, ld);
         for (int j = 0; j < kMaxChan; ++j)
             if ((slotUse >> j) & 1u) add(m.gbar + (size_t)j * ld, 4, ld);
         if (anyPool) {
@@ -964,7 +965,7 @@ int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds, uint32_t n_c
         return cerr(e, "batch stream");
     }
     if (precision == HS_PREC_MIXED) {
-        b->threadsPerCta = 512;
+        b->threadsPerCta = 1024;
         b->ctasPerSm = 1;
     }
     if (tuning) {

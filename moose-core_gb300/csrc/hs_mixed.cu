@@ -65,20 +65,53 @@ __device__ __forceinline__ RowF rowF(const float* T, uint32_t nCol, uint32_t nRo
     return r;
 }
 
-__device__ __forceinline__ float gateF(const RowF& r, uint32_t nCol, int col, float x, float dt,
-                                       float hdt, bool inst) {
+// Exact widening of an FP32 value to FP64 with integer operations (the
+// FP32-to-FP64 conversion instruction issues at the FP64 rate on this GPU,
+// integer operations at the full rate).  IEEE binary32 -> binary64: sign
+// kept, exponent rebiased by 1023 - 127 = 896, fraction shifted left by 29;
+// zero and subnormal inputs give a signed zero, Inf/NaN stay Inf/NaN.
+__device__ __forceinline__ double widenF(float x) {
+    const uint32_t u = __float_as_uint(x);
+    const uint32_t e = (u >> 23) & 0xFFu;
+    const uint32_t sign = u & 0x80000000u;
+    const uint32_t e64 = e == 0xFFu ? 0x7FFu : e + 896u;
+    const uint32_t hi = e == 0 ? sign : (sign | (e64 << 20) | ((u >> 3) & 0xFFFFFu));
+    const uint32_t lo = e == 0 ? 0u : (u << 29);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// FP64 to FP32 by truncation with integer operations (for values used only
+// as FP32 inputs: gate states in [0, 1]): exponent rebiased by -896, the top
+// 23 fraction bits kept; magnitudes below the FP32 normal range give zero.
+__device__ __forceinline__ float narrowF(double x) {
+    const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+    const uint32_t e = (hi >> 20) & 0x7FFu;
+    const uint32_t sign = hi & 0x80000000u;
+    if (e <= 896u) return __uint_as_float(sign);
+    if (e >= 1151u) return __uint_as_float(sign | 0x7F800000u | (e == 0x7FFu && ((hi & 0xFFFFFu) | lo) ? 1u : 0u));
+    return __uint_as_float(sign | ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
+}
+
+// Lerp of the table row pair for column `col` (A at col, B at col + 1).
+__device__ __forceinline__ float2 lookupF(const RowF& r, uint32_t nCol, int col) {
     const float* ap = r.p + col;
     const float2 a = __ldg(reinterpret_cast<const float2*>(ap));
     const float2 b = __ldg(reinterpret_cast<const float2*>(ap + nCol));
-    float C1 = fmaf(b.x - a.x, r.frac, a.x);
-    float C2 = fmaf(b.y - a.y, r.frac, a.y);
-    if (inst) return __fdividef(C1, C2);
-    // The reference's trapezoidal step (x(2-T) + dt C1)/T with T = 1 + h,
-    // h = dt/2 C2 (hsolve/HSolveActive.cpp:272-273), written as the
-    // increment x + (dt C1 - 2 h x)/(1 + h): the same number in exact
-    // arithmetic, but FP32 keeps the small h instead of rounding it into 1 + h.
-    float h = hdt * C2;
-    return x + __fdividef(fmaf(-2.0f * h, x, dt * C1), 1.0f + h);
+    return make_float2(fmaf(b.x - a.x, r.frac, a.x), fmaf(b.y - a.y, r.frac, a.y));
+}
+
+// New value of a gate with state x (FP64) over one step, from C1, C2 of
+// its table row.  The reference's trapezoidal step (x(2-T) + dt C1)/T with
+// T = 1 + h, h = dt/2 C2 (hsolve/HSolveActive.cpp:272-273) is the same
+// number as x + (dt C1 - 2 h x)/(1 + h); the increment is computed in FP32
+// and accumulated into the FP64 state, so that the small per-step changes
+// of slow gates are not lost to FP32 rounding of the state itself.
+// Instantaneous gates: x = C1/C2.
+__device__ __forceinline__ double gateStep(float2 C, double x, float dt, float hdt, bool inst) {
+    if (inst) return widenF(__fdividef(C.x, C.y));
+    const float xf = narrowF(x);
+    const float h = hdt * C.y;
+    return x + widenF(__fdividef(fmaf(-2.0f * h, xf, dt * C.x), 1.0f + h));
 }
 
 __device__ __forceinline__ void interp2dF(const float* T, const float* geom, uint32_t nx, uint32_t ny,
@@ -102,21 +135,6 @@ __device__ __forceinline__ void interp2dF(const float* T, const float* geom, uin
     B = z00.y * w00 + z10.y * w10 + z01.y * w01 + z11.y * xFyF;
 }
 
-// Exact widening of an FP32 value to FP64 with integer operations (the
-// FP32-to-FP64 conversion instruction issues at the FP64 rate on this GPU,
-// integer operations at the full rate).  IEEE binary32 -> binary64: sign
-// kept, exponent rebiased by 1023 - 127 = 896, fraction shifted left by 29;
-// zero and subnormal inputs give a signed zero, Inf/NaN stay Inf/NaN.
-__device__ __forceinline__ double widenF(float x) {
-    const uint32_t u = __float_as_uint(x);
-    const uint32_t e = (u >> 23) & 0xFFu;
-    const uint32_t sign = u & 0x80000000u;
-    const uint32_t e64 = e == 0xFFu ? 0x7FFu : e + 896u;
-    const uint32_t hi = e == 0 ? sign : (sign | (e64 << 20) | ((u >> 3) & 0xFFFFFu));
-    const uint32_t lo = e == 0 ? 0u : (u << 29);
-    return __hiloint2double((int)hi, (int)lo);
-}
-
 // One compartment node of the assembly: first the update left over from the
 // previous step (V = 2 VMid - V, then the node's Ca pool; `update`), then
 // channels, K(Ca), SynChans and the FP64 matrix row.  Every load that depends
@@ -131,10 +149,6 @@ __device__ __forceinline__ void assembleNode(const MixBatch& b, uint32_t n, uint
     double V = b.V[n];
     const uint32_t types = __ldg(b.ctype4 + n);
     const double hs2 = __ldg(b.HS2 + n), cmdt = __ldg(b.CmByDt + n), emrm = __ldg(b.EmByRm + n);
-    float xs[3 * kMaxChan];
-#pragma unroll
-    for (int k = 0; k < 3 * kMaxChan; ++k)
-        xs[k] = (info >> (kNodeGateShift + k)) & 1u ? b.state[(uint64_t)k * ld + n] : 0.f;
     float gb[kMaxChan];
 #pragma unroll
     for (int j = 0; j < kMaxChan; ++j) gb[j] = ((types >> (8 * j)) & 0xFF) != kNoType ? __ldg(b.gbar + (uint64_t)j * ld + n) : 0.f;
@@ -188,30 +202,30 @@ __device__ __forceinline__ void assembleNode(const MixBatch& b, uint32_t n, uint
     const float v = (float)V;
     const RowF vr = rowF(b.vTab, b.vCol, b.vRows, v, b.vMin, b.vMax, b.vInvDx);
     float G = 0.f, GE = 0.f, cg = 0.f, cge = 0.f;
-    // new gate values replace xs[] and are stored after all lookups, so that
-    // the table loads of every gate can be in flight together
 #pragma unroll
     for (int j = 0; j < kMaxChan; ++j) {
         const uint32_t tj = (types >> (8 * j)) & 0xFF;
         if (tj == kNoType) continue;
         const ChanType& t = c_chanTypes[tj];
+        double* st = b.state + (uint64_t)(3 * j) * ld + n;
         float frac = 1.f;
         if (t.xp) {
-            xs[3 * j] = gateF(vr, b.vCol, t.colX, xs[3 * j], dt, hdt, t.instant & 1);
-            frac *= powi(xs[3 * j], t.xp, t.xpf);
+            const double x = gateStep(lookupF(vr, b.vCol, t.colX), st[0], dt, hdt, t.instant & 1);
+            st[0] = x;
+            frac *= powi(narrowF(x), t.xp, t.xpf);
         }
         if (t.yp) {
-            xs[3 * j + 1] = gateF(vr, b.vCol, t.colY, xs[3 * j + 1], dt, hdt, t.instant & 2);
-            frac *= powi(xs[3 * j + 1], t.yp, t.ypf);
+            const double y = gateStep(lookupF(vr, b.vCol, t.colY), st[ld], dt, hdt, t.instant & 2);
+            st[ld] = y;
+            frac *= powi(narrowF(y), t.yp, t.ypf);
         }
         if (t.zp) {
-            if (t.zCa) {
-                const RowF cr = rowF(b.caTab, b.caCol, b.caRows, ca, b.caMin, b.caMax, b.caInvDx);
-                xs[3 * j + 2] = gateF(cr, b.caCol, t.colZ, xs[3 * j + 2], dt, hdt, t.instant & 4);
-            } else {
-                xs[3 * j + 2] = gateF(vr, b.vCol, t.colZ, xs[3 * j + 2], dt, hdt, t.instant & 4);
-            }
-            frac *= powi(xs[3 * j + 2], t.zp, t.zpf);
+            float2 C;
+            if (t.zCa) C = lookupF(rowF(b.caTab, b.caCol, b.caRows, ca, b.caMin, b.caMax, b.caInvDx), b.caCol, t.colZ);
+            else C = lookupF(vr, b.vCol, t.colZ);
+            const double z = gateStep(C, st[2 * ld], dt, hdt, t.instant & 4);
+            st[2 * ld] = z;
+            frac *= powi(narrowF(z), t.zp, t.zpf);
         }
         const float gk = gb[j] * frac;
         G += gk;
@@ -221,9 +235,6 @@ __device__ __forceinline__ void assembleNode(const MixBatch& b, uint32_t n, uint
             cge = fmaf(gk, t.ek, cge);
         }
     }
-#pragma unroll
-    for (int k = 0; k < 3 * kMaxChan; ++k)
-        if ((info >> (kNodeGateShift + k)) & 1u) b.state[(uint64_t)k * ld + n] = xs[k];
     if (pool) {
         b.caG[n] = cg;
         b.caGE[n] = cge;
@@ -496,16 +507,15 @@ __global__ void hsReinitNodesMixed(MixBatch b, uint32_t nNodes, const double* __
         const uint32_t tj = (types >> (8 * j)) & 0xFF;
         if (tj == kNoType) break;
         const ChanType& t = c_chanTypes[tj];
-        float* st = b.state + (uint64_t)(3 * j) * ld + n;
-        if (t.xp) st[0] = gateF(vr, b.vCol, t.colX, 0.f, 0.f, 0.f, true);
-        if (t.yp) st[ld] = gateF(vr, b.vCol, t.colY, 0.f, 0.f, 0.f, true);
+        double* st = b.state + (uint64_t)(3 * j) * ld + n;
+        if (t.xp) st[0] = gateStep(lookupF(vr, b.vCol, t.colX), 0.0, 0.f, 0.f, true);
+        if (t.yp) st[ld] = gateStep(lookupF(vr, b.vCol, t.colY), 0.0, 0.f, 0.f, true);
         if (t.zp) {
-            if (t.zCa) {
-                RowF cr2 = rowF(b.caTab, b.caCol, b.caRows, ca, b.caMin, b.caMax, b.caInvDx);
-                st[2 * ld] = gateF(cr2, b.caCol, t.colZ, 0.f, 0.f, 0.f, true);
-            } else {
-                st[2 * ld] = gateF(vr, b.vCol, t.colZ, 0.f, 0.f, 0.f, true);
-            }
+            if (t.zCa)
+                st[2 * ld] = gateStep(lookupF(rowF(b.caTab, b.caCol, b.caRows, ca, b.caMin, b.caMax, b.caInvDx),
+                                              b.caCol, t.colZ), 0.0, 0.f, 0.f, true);
+            else
+                st[2 * ld] = gateStep(lookupF(vr, b.vCol, t.colZ), 0.0, 0.f, 0.f, true);
         }
     }
     if (((info >> 8) & 0xFF) != kNoType) b.k2x[n] = k2x0[n];

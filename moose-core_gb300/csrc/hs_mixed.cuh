@@ -24,9 +24,10 @@
 //   gate state of channel j, gate g (X,Y,Z): state[(3*j+g)*ld + n]
 //   at most one Ca pool, one HHChannel2D per compartment; SynChans in CSR.
 //
-// Precision: gate states, rate tables, channel conductances, K(Ca), Ca pools
-// and synapses are FP32; Vm, matrix assembly, forward elimination and back
-// substitution are FP64.
+// Precision: rate tables, gate increments, channel conductances, K(Ca), Ca
+// pools and synapses are FP32; gate states accumulate the FP32 increments in
+// FP64; Vm, matrix assembly, forward elimination and back substitution are
+// FP64.
 #pragma once
 
 #include <cstdint>
@@ -124,8 +125,7 @@ struct MixBatch {
     double *elimD, *elimR;       // elimination scratch of global forests
     float *caG, *caGE;           // Ca-feeding conductance of the step
     const float* gbar;           // [kMaxChan][ld]  Gbar * modulation
-    float* state;                // [3*kMaxChan][ld]
-    float* chanGk;               // [kMaxChan][ld] last conductance
+    double* state;               // [3*kMaxChan][ld] gate states (FP64 accumulators)
     // pool (one per node)
     float *poolC, *poolCa;
     const float *poolG1, *poolF2, *poolBasal, *poolCeil, *poolFloor;   // poolG1 = 1 - factor1

@@ -6,7 +6,7 @@ quantity the step needs were read once and every piece of state written once
 per step, with rate tables and elimination temporaries on chip:
 
   V (FP64)                         read + write          16 B
-  each gate state                  read + write          2 x state size
+  each gate state                  read + write          16 B (FP64 in both paths)
   each channel Gbar                read                  param size
   passive row: diag, off-diagonal,
       2C/dt, Em/Rm (FP64)          read                  32 B
@@ -17,7 +17,8 @@ per step, with rate tables and elimination temporaries on chip:
   each SynChan: X, Y               read + write          4 x state size
       norm                         read                  param size
 
-state/param size is 8 B in FP64 and 4 B in the mixed-precision path.
+state/param size is 8 B in FP64 and 4 B in the mixed-precision path, except
+the HH gate states, which accumulate in FP64 in both.
 """
 import numpy as np
 
@@ -29,7 +30,7 @@ def bytes_per_cell_step(m, precision):
     n = m.n_compt
     gates = int((m.chan_Xpower > 0).sum() + (m.chan_Ypower > 0).sum() + (m.chan_Zpower > 0).sum())
     total = 16 * n + 32 * n
-    total += gates * 2 * s + len(m.chan_compt) * s
+    total += gates * 16 + len(m.chan_compt) * s
     total += len(m.pool_compt) * (2 * s + 2 * s)
     total += len(m.c2d_compt) * (2 * s + s)
     total += len(m.syn_compt) * (4 * s + s)
