@@ -337,6 +337,22 @@ int hs_batch_inject_targets(HsBatch* b, const uint32_t* cell, const uint32_t* co
 int hs_batch_set_inject(HsBatch* b, const double* values, uint32_t n);
 int hs_batch_read_spikes(HsBatch* b, uint32_t* cell, uint32_t* gen,
                          double* time, uint32_t capacity, uint32_t* n);
+/* Serving support (mixed batch).  Cell c advances only while its step count
+ * is below stop[c] (UINT64_MAX: no limit; set before or between process()
+ * calls); a stopped cell keeps its final state, trace and spikes.  n equals
+ * the number of cells.  No counterpart in the reference, which steps every
+ * compartment on every tick. */
+int hs_batch_set_stop_steps(HsBatch* b, const uint64_t* stop, uint32_t n);
+/* dt steps each cell has advanced (at most its stop step). */
+int hs_batch_read_steps(HsBatch* b, uint64_t* out, uint32_t n);
+/* Spikes recorded so far by each cell. */
+int hs_batch_read_spike_counts(HsBatch* b, uint32_t* out, uint32_t n);
+/* Device memory held by the batch, in bytes. */
+int hs_batch_device_bytes(HsBatch* b, uint64_t* out);
+/* Spikes of one cell from its `first`-th on; *n = the cell's total count.
+ * Returns HS_ECAPACITY if the per-cell spike buffer overflowed. */
+int hs_batch_read_cell_spikes(HsBatch* b, uint32_t cell, uint32_t first, uint32_t* gen,
+                              double* time, uint32_t capacity, uint32_t* n);
 /* The CUDA stream (a cudaStream_t) the batch runs on, for event timing. */
 int hs_batch_stream(HsBatch* b, void** stream);
 /* Statistics of the packing: compartments, cells, CTAs, launches/step. */

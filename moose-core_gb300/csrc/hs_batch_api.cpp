@@ -61,11 +61,15 @@ uint64_t fnv(const void* p, size_t n, uint64_t h = 1469598103934665603ull) {
 struct DevBuf {
     std::vector<void*> ptrs;
     cudaError_t err = cudaSuccess;
+    uint64_t bytes = 0;
     template <class T>
     T* alloc(size_t n) {
         void* p = nullptr;
         if (err == cudaSuccess) err = cudaMalloc(&p, (n ? n : 1) * sizeof(T));
-        if (err == cudaSuccess) ptrs.push_back(p);
+        if (err == cudaSuccess) {
+            ptrs.push_back(p);
+            bytes += (n ? n : 1) * sizeof(T);
+        }
         return (T*)p;
     }
     template <class T>
@@ -84,6 +88,7 @@ struct DevBuf {
     void freeAll() {
         for (void* p : ptrs) cudaFree(p);
         ptrs.clear();
+        bytes = 0;
     }
 };
 
@@ -127,6 +132,7 @@ struct HsBatch {
     // mixed: forests per CTA, shared-memory forest capacity
     uint32_t *dCtaPtr = nullptr, *dCtaForests = nullptr;
     uint32_t mixCap = 0, mixSmem = 0;
+    unsigned long long* dStopStep = nullptr;    // mixed: per-cell stop steps
     DevBuf buf;              // long-lived allocations
     DevBuf packBuf;          // packing arrays (replaced by retuning)
     // FP64
@@ -779,9 +785,18 @@ int buildMixed(HsBatch* b) {
     MixBatch& m = b->mb;
     std::memset(&m, 0, sizeof(m));
     m.nCells = nC;
+    m.nForests = (uint32_t)fdev.size();
     m.ld = ld;
     m.cells = D.up(H.cells, st);
     m.forests = D.up(fdev, st);
+    m.forestStep = D.zeros<unsigned long long>(fdev.size(), st);
+    {
+        std::vector<uint32_t> cellOf(nN);
+        for (uint32_t g = 0; g < nN; ++g) cellOf[g] = nodeCT[g].first;
+        m.cellOf = D.up(cellOf, st);
+        b->dStopStep = D.up(std::vector<unsigned long long>(nC, ~0ull), st);
+        m.stopStep = b->dStopStep;
+    }
     m.forestCells = D.up(forestCells, st);
     m.levelPtr = D.up(levelPtr, st);
     m.nodeInfo = D.up(nodeInfo, st);
@@ -1121,6 +1136,19 @@ int hs_batch_process(HsBatch* b, uint32_t nsteps) {
     if (!b->reinited) return berr(HS_ESTATE, "reinit before process");
     if (nsteps == 0) return HS_OK;
     const uint32_t K = b->stepsPerLaunch;
+    if (b->evUsed >= 1024) {
+        // fold the timings recorded so far, so that a long-running caller
+        // that never asks for them keeps a bounded event list
+        cudaError_t e0 = cudaStreamSynchronize(b->st);
+        if (e0 != cudaSuccess) return cerr(e0, "batch process");
+        for (size_t i = 0; i < b->evUsed; ++i) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, b->evs[i].first, b->evs[i].second);
+            b->timedMs += ms;
+            b->timedLaunches += 1;
+        }
+        b->evUsed = 0;
+    }
     auto timedLaunch = [&](uint32_t k) -> cudaError_t {
         if (b->evUsed == b->evs.size()) {
             cudaEvent_t a, z;
@@ -1207,6 +1235,69 @@ int hs_batch_info(HsBatch* b, uint64_t* n_compt, uint32_t* n_ctas, uint32_t* thr
     if (n_ctas) *n_ctas = b->nCtas;
     if (threads_per_cta) *threads_per_cta = b->threadsPerCta;
     if (steps_per_launch) *steps_per_launch = b->stepsPerLaunch;
+    return HS_OK;
+}
+
+int hs_batch_set_stop_steps(HsBatch* b, const uint64_t* stop, uint32_t n) {
+    if (!b || !stop) return berr(HS_EINVAL, "null argument");
+    if (b->precision != HS_PREC_MIXED) return berr(HS_ENOTSUP, "stop steps are a mixed-batch feature");
+    if (n != b->nCells) return berr(HS_EINVAL, "n must equal the number of cells");
+    static_assert(sizeof(unsigned long long) == sizeof(uint64_t), "64-bit step counts");
+    cudaError_t e = cudaMemcpyAsync(b->dStopStep, stop, (size_t)n * 8, cudaMemcpyHostToDevice, b->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    return e == cudaSuccess ? HS_OK : cerr(e, "stop steps");
+}
+
+int hs_batch_read_steps(HsBatch* b, uint64_t* out, uint32_t n) {
+    if (!b || !out) return berr(HS_EINVAL, "null argument");
+    if (b->precision != HS_PREC_MIXED) return berr(HS_ENOTSUP, "per-cell step counts are a mixed-batch feature");
+    if (n != b->nCells) return berr(HS_EINVAL, "n must equal the number of cells");
+    cudaError_t e = cudaStreamSynchronize(b->st);
+    if (e == cudaSuccess) e = cudaMemcpy(out, b->mb.stepCount, (size_t)n * 8, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? HS_OK : cerr(e, "read steps");
+}
+
+int hs_batch_read_spike_counts(HsBatch* b, uint32_t* out, uint32_t n) {
+    if (!b || !out) return berr(HS_EINVAL, "null argument");
+    if (b->precision != HS_PREC_MIXED) return berr(HS_ENOTSUP, "per-cell spike counts are a mixed-batch feature");
+    if (n != b->nCells) return berr(HS_EINVAL, "n must equal the number of cells");
+    cudaError_t e = cudaStreamSynchronize(b->st);
+    if (e == cudaSuccess) e = cudaMemcpy(out, b->mb.spikeCount, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? HS_OK : cerr(e, "spike counts");
+}
+
+int hs_batch_device_bytes(HsBatch* b, uint64_t* out) {
+    if (!b || !out) return berr(HS_EINVAL, "null argument");
+    *out = b->buf.bytes + b->packBuf.bytes + b->recBuf.bytes + b->injBuf.bytes + b->arena.size;
+    return HS_OK;
+}
+
+int hs_batch_read_cell_spikes(HsBatch* b, uint32_t cell, uint32_t first, uint32_t* gen, double* time,
+                              uint32_t capacity, uint32_t* n) {
+    if (!b || !n) return berr(HS_EINVAL, "null argument");
+    if (b->precision != HS_PREC_MIXED) return berr(HS_ENOTSUP, "per-cell spike reads are a mixed-batch feature");
+    if (cell >= b->nCells) return berr(HS_EINVAL, "cell index out of range");
+    cudaError_t e = cudaStreamSynchronize(b->st);
+    uint32_t cnt = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&cnt, b->mb.spikeCount + cell, 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cerr(e, "cell spikes");
+    *n = cnt;
+    const uint32_t stored = std::min(cnt, b->spikeCap);
+    const uint32_t k = first < stored ? std::min(stored - first, capacity) : 0;
+    if (k && (gen || time)) {
+        std::vector<uint32_t> g(k);
+        std::vector<float> t(k);
+        e = cudaMemcpy(g.data(), b->mb.spikeGen + (size_t)cell * b->spikeCap + first, k * 4, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(t.data(), b->mb.spikeTime + (size_t)cell * b->spikeCap + first, k * 4,
+                           cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cerr(e, "cell spikes");
+        for (uint32_t i = 0; i < k; ++i) {
+            if (gen) gen[i] = g[i];
+            if (time) time[i] = t[i];
+        }
+    }
+    if (cnt > b->spikeCap) return berr(HS_ECAPACITY, "spike buffer overflow");
     return HS_OK;
 }
 

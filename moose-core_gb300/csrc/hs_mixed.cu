@@ -295,7 +295,7 @@ __device__ __forceinline__ void forestStimulus(const MixBatch& b, const MixFores
     for (uint32_t k = threadIdx.x; k < F.nCells; k += blockDim.x) {
         const uint32_t cell = b.forestCells[F.cell0 + k];
         const MixCellRange cr = b.cells[cell];
-        if (!cr.nStim) continue;
+        if (!cr.nStim || step >= b.stopStep[cell]) continue;
         uint32_t cur = b.stimCur[cell];
         while (cur < cr.nStim && b.stimStep[cr.stim0 + cur] <= step) {
             b.injVal[cr.inj0 + b.stimEntry[cr.stim0 + cur]] = b.stimValue[cr.stim0 + cur];
@@ -312,6 +312,7 @@ __device__ __forceinline__ void forestOutputs(const MixBatch& b, const MixForest
     const bool sample = ((step + 1) % b.recStride) == 0;
     for (uint32_t k = threadIdx.x; k < F.nCells; k += blockDim.x) {
         const uint32_t cell = b.forestCells[F.cell0 + k];
+        if (step >= b.stopStep[cell]) continue;
         const MixCellRange cr = b.cells[cell];
         for (uint32_t g = cr.sg0; g < cr.sg0 + cr.nSg; ++g) {
             const double Vs = b.V[b.sgNode[g]];
@@ -353,14 +354,33 @@ __device__ __forceinline__ void prefetchNodes(const MixBatch& b, uint32_t k, uin
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"((uint32_t)(hi - lo)) : "memory");
 }
 
+// V = 2 VMid - V, then the node's Ca pool: the end of a step of one node.
+__device__ __forceinline__ void updateNode(const MixBatch& b, uint32_t n, uint32_t info, double vm) {
+    const double Vnew = fma(2.0, vm, -b.V[n]);
+    b.V[n] = Vnew;
+    if (info & kNodePool) {
+        const float vca = (float)(b.caAdvance == 1 ? vm : fma(2.0, vm, -Vnew));
+        const float act = fmaf(-b.caG[n], vca, b.caGE[n]);
+        const float c0v = b.poolC[n];
+        float c = fmaf(-b.poolG1[n], c0v, c0v) + b.poolF2[n] * act;
+        float cav = b.poolBasal[n] + c;
+        if (b.poolCeil[n] > 0.f && cav > b.poolCeil[n]) { cav = b.poolCeil[n]; c = cav - b.poolBasal[n]; }
+        if (cav < b.poolFloor[n]) { cav = b.poolFloor[n]; c = cav - b.poolBasal[n]; }
+        b.poolC[n] = c;
+        b.poolCa[n] = cav;
+    }
+}
+
 // `nsteps` steps of one forest by the whole CTA.  The V/Ca update and the
 // outputs (SpikeGens, trace samples) of a step run at the start of the next
-// step's assembly, and after the last step.
-__device__ void stepForest(const MixBatch& b, const MixForest& F, const Elim& E, const uint32_t* lp,
+// step's assembly, and after the last step.  A cell whose stop step is
+// reached stays as it is: its nodes get a neutral row (pivot 1, rhs 0) so
+// that the elimination of the forest goes on around them.
+__device__ void stepForest(const MixBatch& b, const MixForest& F, uint32_t f, const Elim& E, const uint32_t* lp,
                            uint32_t nsteps) {
     const uint32_t tid = threadIdx.x, nth = blockDim.x;
     if (nsteps == 0) return;
-    unsigned long long step = b.stepCount[b.forestCells[F.cell0]];
+    unsigned long long step = b.forestStep[f];
     for (uint32_t s = 0; s < nsteps; ++s, ++step) {
         if (tid < b.nPf) prefetchNodes(b, tid, F.node0, nth);
         forestStimulus(b, F, step);
@@ -371,12 +391,16 @@ __device__ void stepForest(const MixBatch& b, const MixForest& F, const Elim& E,
             if (tid < b.nPf && i + nth - tid < F.nNodes) prefetchNodes(b, tid, F.node0 + i + nth - tid, nth);
             const uint32_t n = F.node0 + i;
             const uint32_t info = __ldg(b.nodeInfo + n);
-            double d, r;
+            const unsigned long long stop = b.stopStep[__ldg(b.cellOf + n)];
+            const bool live = step < stop;                  // this step advances the cell
+            const bool pending = s > 0 && step - 1 < stop;  // the previous step's update
+            double d = 1.0, r = 0.0;
             if (info & kNodeCenter) {
-                d = __ldg(b.HS2 + n);
-                r = 0.0;
-            } else {
-                assembleNode(b, n, info, s > 0, s > 0 ? E.R[i] : 0.0, step, d, r);
+                if (live) d = __ldg(b.HS2 + n);
+            } else if (live) {
+                assembleNode(b, n, info, pending, pending ? E.R[i] : 0.0, step, d, r);
+            } else if (pending) {
+                updateNode(b, n, info, E.R[i]);
             }
             E.D[i] = d;
             E.R[i] = r;
@@ -420,24 +444,15 @@ __device__ void stepForest(const MixBatch& b, const MixForest& F, const Elim& E,
         const uint32_t n = F.node0 + i;
         const uint32_t info = __ldg(b.nodeInfo + n);
         if (info & kNodeCenter) continue;
-        const double vm = E.R[i];
-        const double Vnew = fma(2.0, vm, -b.V[n]);
-        b.V[n] = Vnew;
-        if (info & kNodePool) {
-            const float vca = (float)(b.caAdvance == 1 ? vm : fma(2.0, vm, -Vnew));
-            const float act = fmaf(-b.caG[n], vca, b.caGE[n]);
-            const float c0v = b.poolC[n];
-            float c = fmaf(-b.poolG1[n], c0v, c0v) + b.poolF2[n] * act;
-            float cav = b.poolBasal[n] + c;
-            if (b.poolCeil[n] > 0.f && cav > b.poolCeil[n]) { cav = b.poolCeil[n]; c = cav - b.poolBasal[n]; }
-            if (cav < b.poolFloor[n]) { cav = b.poolFloor[n]; c = cav - b.poolBasal[n]; }
-            b.poolC[n] = c;
-            b.poolCa[n] = cav;
-        }
+        if (step - 1 < b.stopStep[__ldg(b.cellOf + n)]) updateNode(b, n, info, E.R[i]);
     }
     __syncthreads();
     forestOutputs(b, F, step - 1);
-    for (uint32_t k = tid; k < F.nCells; k += nth) b.stepCount[b.forestCells[F.cell0 + k]] = step;
+    for (uint32_t k = tid; k < F.nCells; k += nth) {
+        const uint32_t cell = b.forestCells[F.cell0 + k];
+        b.stepCount[cell] = step < b.stopStep[cell] ? step : b.stopStep[cell];
+    }
+    if (tid == 0) b.forestStep[f] = step;
     __syncthreads();
 }
 
@@ -482,7 +497,7 @@ __global__ void __launch_bounds__(1024, 1) hsForestStepMixed(MixBatch b, const u
             E.PAR = b.par + F.node0;
         }
         __syncthreads();
-        stepForest(b, F, E, lp, nsteps);
+        stepForest(b, F, ctaForests[k], E, lp, nsteps);
     }
 }
 
@@ -536,6 +551,7 @@ __global__ void hsReinitCellsMixed(MixBatch b) {
         b.sgLast[g] = -b.sgRefract[g];
         b.sgFired[g] = 0;
     }
+    if (cell < b.nForests) b.forestStep[cell] = 0;
     b.stepCount[cell] = 0;
     b.stimCur[cell] = 0;
     b.spikeCount[cell] = 0;
@@ -583,7 +599,8 @@ cudaError_t launchBatchReinitMixed(const MixBatch& b, uint32_t nNodes, const dou
     hsReinitNodesMixed<<<(nNodes + 255) / 256, 256, 0, st>>>(b, nNodes, initVm, k2x0, evStart);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    hsReinitCellsMixed<<<(b.nCells + 127) / 128, 128, 0, st>>>(b);
+    const uint32_t n = b.nCells > b.nForests ? b.nCells : b.nForests;
+    hsReinitCellsMixed<<<(n + 127) / 128, 128, 0, st>>>(b);
     return cudaGetLastError();
 }
 

@@ -110,8 +110,12 @@ struct MixBatch {
     float dtf;
     double dt;
     int caAdvance;
+    uint32_t nForests;
     const MixCellRange* cells;
     const MixForest* forests;
+    unsigned long long* forestStep;      // steps done by each forest
+    const unsigned long long* stopStep;  // per cell: no step at or after this one
+    const uint32_t* cellOf;              // per node: its cell
     const uint32_t* forestCells;
     const uint32_t* levelPtr;
     // per node (global index)

@@ -71,6 +71,11 @@ def load(build_if_missing=True):
         "hs_batch_info": (i32, [vp, C.POINTER(u64), pu, pu, pu]),
         "hs_batch_stream": (i32, [vp, C.POINTER(vp)]),
         "hs_batch_kernel_time": (i32, [vp, pd, pu]),
+        "hs_batch_set_stop_steps": (i32, [vp, C.POINTER(u64), u32]),
+        "hs_batch_read_steps": (i32, [vp, C.POINTER(u64), u32]),
+        "hs_batch_device_bytes": (i32, [vp, C.POINTER(u64)]),
+        "hs_batch_read_spike_counts": (i32, [vp, pu, u32]),
+        "hs_batch_read_cell_spikes": (i32, [vp, u32, u32, pu, pd, u32, pu]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name, None)

@@ -125,6 +125,44 @@ class Batch:
                                              t.ctypes.data_as(C.POINTER(C.c_double)), n.value, C.byref(n)))
         return cells, gens, t
 
+    def set_stop_steps(self, stop):
+        """Cell c advances only while its step count is below stop[c]
+        (None or -1: no limit).  Mixed precision only."""
+        a = np.array([np.iinfo(np.uint64).max if (x is None or x < 0) else x for x in stop], np.uint64)
+        _native.check(_native.load().hs_batch_set_stop_steps(self._h, a.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                                             len(a)))
+
+    def steps(self):
+        """dt steps each cell has advanced.  Mixed precision only."""
+        out = np.empty(self.n, np.uint64)
+        _native.check(_native.load().hs_batch_read_steps(self._h, out.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                                         self.n))
+        return out
+
+    def spike_counts(self):
+        """Spikes recorded so far by each cell.  Mixed precision only."""
+        out = np.empty(self.n, np.uint32)
+        _native.check(_native.load().hs_batch_read_spike_counts(self._h, out.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                                                self.n))
+        return out
+
+    def device_bytes(self):
+        v = C.c_uint64()
+        _native.check(_native.load().hs_batch_device_bytes(self._h, C.byref(v)))
+        return v.value
+
+    def cell_spikes(self, cell, first=0, capacity=4096):
+        """(generator index, time) of the cell's spikes from its `first`-th on,
+        and the cell's total spike count.  Mixed precision only."""
+        g = np.empty(capacity, np.uint32)
+        t = np.empty(capacity)
+        n = C.c_uint32()
+        _native.check(_native.load().hs_batch_read_cell_spikes(
+            self._h, int(cell), int(first), g.ctypes.data_as(C.POINTER(C.c_uint32)),
+            t.ctypes.data_as(C.POINTER(C.c_double)), capacity, C.byref(n)))
+        k = max(0, min(n.value, capacity + first) - first)
+        return g[:k], t[:k], n.value
+
     def stream(self):
         """The cudaStream_t handle (int) the batch's kernels run on."""
         s = C.c_void_p()

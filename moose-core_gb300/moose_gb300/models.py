@@ -346,3 +346,27 @@ def population(config, seed=1, n_cells=None, t_end=1.0, kca_tables=None):
     sizes, _, _ = population_sizes(config, seed, n_cells)
     return [make_cell(config, seed, i, t_end=t_end, kca_tables=kca_tables, sizes=sizes)
             for i in range(len(sizes))]
+
+
+def serving_request(seed, i, dt=25e-6, kca_tables=None):
+    """Request i of the serving workload: (cell, dt steps to simulate).
+
+    Cells of log-uniform 100..10,000 compartments (junctions of up to 4
+    children) with HH Na/K, Ca(HVA), K(Ca) and CaConc; simulated duration
+    uniform 0.1..2 s; driven either by a somatic step current of 0.1..1 nA or
+    by 50..500 SynChans with 5 Hz Poisson trains (even odds).
+    """
+    rng = np.random.default_rng([seed, 5, i])
+    n = int(loguniform_int(rng, 100, 10000, 1)[0])
+    duration = float(rng.uniform(0.1, 2.0))
+    steps = int(round(duration / dt))
+    if kca_tables is None:
+        kca_tables = kca_2d_tables()
+    parent, d, L = branched_morphology(rng, n, 0.5, 4)
+    if rng.uniform() < 0.5:
+        cell = active_cell(parent, d, L, inject=float(rng.uniform(0.1e-9, 1e-9)), rng=rng, t_end=duration,
+                           kca_tables=kca_tables)
+    else:
+        cell = active_cell(parent, d, L, inject=0.0, n_syn=int(rng.integers(50, 501)), rng=rng, t_end=duration,
+                           kca_tables=kca_tables)
+    return cell, steps

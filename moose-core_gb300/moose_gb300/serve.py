@@ -1,0 +1,215 @@
+"""Continuous-batching serving loop over the mixed-precision batch.
+
+Simulation requests (one cell, a number of dt steps) arrive over time.  Each
+tick of the loop:
+
+  1. queues one chunk of dt steps for every running cohort (a cohort is a
+     mixed-precision ``Batch`` with its own CUDA stream whose state stays on
+     the device between chunks).  All launches are queued before any is
+     waited for, so the kernels of different cohorts run at the same time on
+     the GPU: a cohort's persistent kernel holds only the SMs its forests
+     need, the rest go to the others;
+  2. while the GPU works, admits waiting requests first come, first served,
+     while the device memory of the running cohorts plus the estimate for the
+     request stays within the HBM budget, and sets up the admitted ones as a
+     new cohort (it runs from the next tick).  Every cell stops at its own
+     step count (``Batch.set_stop_steps``), so one cohort holds requests of
+     any duration;
+  3. waits for the chunk of each cohort and streams out the new soma Vm
+     samples and spikes of its requests, completes the requests that reached
+     their step count and releases cohorts whose cells are all done.
+
+A request's latency is completion minus arrival (queueing, setup and
+simulation).  A cell's result does not depend on the cohort it runs in or on
+the other requests (every node's arithmetic depends only on its own cell):
+the tests compare each request served in a mix with the same request run
+alone.
+"""
+import dataclasses
+import time
+
+import numpy as np
+
+from .abi import HS_PREC_MIXED
+from .batch import Batch
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    cell: object            # abi.CellModel
+    n_steps: int
+    arrival: float = 0.0    # seconds after the start of the run
+
+
+@dataclasses.dataclass
+class Result:
+    rid: int
+    n_compt: int
+    n_steps: int
+    arrival: float
+    admitted: float
+    finished: float
+    vm: np.ndarray          # soma Vm every record_stride steps; sample 0 is the reinit state
+    spike_times: np.ndarray
+
+    @property
+    def latency(self):
+        return self.finished - self.arrival
+
+
+def estimate_bytes(cell, n_steps, record_stride):
+    """Device memory a request takes in a cohort: per compartment (node
+    arrays, FP64 gate states, junction nodes), per synapse and event, its
+    trace and its spike buffer.  With ``cohort_overhead`` of the cohort, an
+    upper bound of what ``Batch.device_bytes`` reports (checked by the
+    tests)."""
+    n = cell.n_compt
+    samples = n_steps // record_stride + 2
+    return 640 * n + 64 * len(cell.syn_compt) + 16 * len(cell.ev_time) + 8 * samples + 16384
+
+
+def cohort_overhead(cell):
+    """Device memory a cohort holds once whatever its size: the FP32 rate
+    tables (merged 1-D table, 2-D tables), with a margin for resampling."""
+    rows = max((len(g[2]) for g in cell.gates), default=0) + 2
+    table = rows * 2 * len(cell.gates) * 4
+    table2d = sum(np.asarray(g[4]).size * 8 for g in cell.gates2d)
+    return int(1.25 * (table + table2d)) + (1 << 20)
+
+
+class _Cohort:
+    def __init__(self, reqs, dt, record_stride, chunk, now, tuning):
+        self.reqs = reqs
+        self.admitted = now
+        n = len(reqs)
+        self.batch = Batch([r.cell for r in reqs], dt, HS_PREC_MIXED, steps_per_launch=chunk, **tuning)
+        self.stride = record_stride
+        self.cap = max(r.n_steps for r in reqs) // record_stride + 2
+        self.batch.record(np.arange(n), np.zeros(n, np.uint32), record_stride, self.cap)
+        self.batch.set_stop_steps([r.n_steps for r in reqs])
+        self.batch.reinit(dt)
+        self.launched = 0                  # dt steps queued so far
+        self.next_sample = 0               # first sample not streamed yet
+        self.vm = [[] for _ in reqs]
+        self.spikes_seen = np.zeros(n, np.int64)
+        self.spikes = [[] for _ in reqs]
+        self.done = np.zeros(n, bool)
+        self.bytes = self.batch.device_bytes()
+
+    def launch(self, chunk):
+        self.batch.process(chunk)
+        self.launched += chunk
+
+    def collect(self):
+        """Stream the samples and spikes of the last chunk; return the
+        indices of requests that completed with it."""
+        last = min(self.launched // self.stride, self.cap - 1)
+        if last >= self.next_sample:
+            rows = self.batch.trace_window(self.next_sample, last - self.next_sample + 1)
+            for i, r in enumerate(self.reqs):
+                if self.done[i]:
+                    continue
+                k_end = min(last, r.n_steps // self.stride)     # the cell's own samples
+                if k_end >= self.next_sample:
+                    self.vm[i].append(rows[: k_end - self.next_sample + 1, i].copy())
+            self.next_sample = last + 1
+        counts = self.batch.spike_counts()
+        for i in np.nonzero(counts > self.spikes_seen)[0]:
+            _, t, _ = self.batch.cell_spikes(int(i), int(self.spikes_seen[i]))
+            self.spikes[i].append(t)
+            self.spikes_seen[i] += len(t)
+        steps = self.batch.steps()
+        fresh = [i for i, r in enumerate(self.reqs) if not self.done[i] and steps[i] >= r.n_steps]
+        for i in fresh:
+            self.done[i] = True
+        return fresh
+
+    def close(self):
+        self.batch.close()
+
+
+class Server:
+    """The serving loop.  ``budget_bytes`` bounds the device memory of the
+    running cohorts; ``chunk`` is the number of dt steps per tick."""
+
+    def __init__(self, dt, budget_bytes=150 * 10**9, chunk=400, record_stride=40, max_cohort=4096,
+                 tuning=None, clock=time.perf_counter, cohort_factory=None):
+        self.dt = dt
+        self.budget = budget_bytes
+        self.chunk = chunk
+        self.stride = record_stride
+        self.max_cohort = max_cohort
+        self.tuning = dict(tuning or {})
+        self.clock = clock
+        self.cohort_factory = cohort_factory or _Cohort
+        self.cohorts = []
+        self.waiting = []
+        self.results = []
+        self.ticks = 0
+        self.peak_bytes = 0
+
+    def used_bytes(self):
+        return sum(c.bytes for c in self.cohorts)
+
+    def _admit(self, now):
+        take, est = [], 0
+        used = self.used_bytes()
+        while self.waiting and len(take) < self.max_cohort:
+            r = self.waiting[0]
+            e = estimate_bytes(r.cell, r.n_steps, self.stride)
+            if not take:
+                e += cohort_overhead(r.cell)
+            if used + est + e > self.budget:
+                break
+            take.append(self.waiting.pop(0))
+            est += e
+        if not take:
+            return None
+        return self.cohort_factory(take, self.dt, self.stride, self.chunk, now, self.tuning)
+
+    def run(self, requests, real_time=True, t0=None):
+        """Serve `requests` (sorted by arrival); returns the results in
+        completion order.  With real_time, arrivals follow the clock from t0;
+        otherwise every request is available from the start."""
+        pending = list(requests)
+        start = self.clock() if t0 is None else t0
+        while pending or self.waiting or self.cohorts:
+            now = self.clock() - start
+            for c in self.cohorts:
+                c.launch(self.chunk)
+            while pending and (not real_time or pending[0].arrival <= now):
+                self.waiting.append(pending.pop(0))
+            fresh = self._admit(now) if self.waiting else None
+            for c in list(self.cohorts):
+                done = c.collect()
+                t = self.clock() - start
+                for i in done:
+                    r = c.reqs[i]
+                    vm = np.concatenate(c.vm[i]) if c.vm[i] else np.zeros(0)
+                    sp = np.concatenate(c.spikes[i]) if c.spikes[i] else np.zeros(0)
+                    self.results.append(Result(r.rid, r.cell.n_compt, r.n_steps, r.arrival, c.admitted, t, vm, sp))
+                if c.done.all():
+                    self.cohorts.remove(c)
+                    c.close()
+            if fresh is not None:
+                self.cohorts.append(fresh)
+            self.peak_bytes = max(self.peak_bytes, self.used_bytes())
+            self.ticks += 1
+            if not self.cohorts and not self.waiting and pending and real_time:
+                # idle until the next arrival (the clock is wall time here)
+                time.sleep(max(0.0, min(0.05, pending[0].arrival - (self.clock() - start))))
+        return self.results
+
+
+def summarize(results, wall_s, offered_rate=None):
+    """p50/p99 latency, throughput in compartment-steps/s over `wall_s`."""
+    lat = np.array([r.latency for r in results])
+    work = sum(r.n_compt * r.n_steps for r in results)
+    out = {"requests": len(results), "wall_s": wall_s,
+           "p50_latency_s": float(np.percentile(lat, 50)) if len(lat) else None,
+           "p99_latency_s": float(np.percentile(lat, 99)) if len(lat) else None,
+           "compartment_steps_per_s": work / wall_s if wall_s > 0 else None}
+    if offered_rate is not None:
+        out["offered_rate_per_s"] = offered_rate
+    return out

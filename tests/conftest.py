@@ -12,6 +12,10 @@ for p in (os.path.join(ROOT, "moose-core_gb300"), os.path.join(ROOT, "oracle"),
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    # a per-test time limit when pytest-timeout is present, so that a host
+    # loop that never ends cannot hold a GPU for the whole run
+    if config.pluginmanager.hasplugin("timeout") and not getattr(config.option, "timeout", None):
+        config.option.timeout = 900
 
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
