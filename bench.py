@@ -21,6 +21,10 @@ The JSON line carries:
              FP64 path (bit-identical to the reference HSolve) on a subset;
   roofline   the stepping kernel against the measured HBM copy bandwidth;
   cpu_baseline the CPU restatement of HSolve (the oracle) on the host cores.
+  serving    the serving loop (continuous batching under a 150 GB budget)
+             on Poisson arrivals of the serving workload: p50/p99 latency
+             and compartment-steps/s at the offered 2,000 requests/s over a
+             bounded window, and at a rate the GPU sustains.
 With --impl reference the line is the CPU HSolve on all host cores instead.
 With --gpus N (torchrun) every rank runs its own replica ("replicas only").
 """
@@ -204,6 +208,46 @@ def run_reference(args, rank, world):
                     "d2h_bytes_per_step": 0}}
 
 
+def run_serving(args):
+    """The serving loop on Poisson arrivals of the serving workload (cells of
+    100..10,000 compartments, 0.1..2 s, step current or 50..500 synapses),
+    150 GB budget: once at the offered rate over a bounded window (the loop is
+    overloaded there: each request carries ~9e7 compartment-steps), once at a
+    rate the GPU sustains.  Requests are generated before the clock starts."""
+    import numpy as np
+    from moose_gb300 import models, serve
+    kca = models.kca_2d_tables()
+    out = {"workload": "serving: Poisson arrivals, cells log-uniform 100..10,000 compartments, 0.1..2 s at 25 us, "
+                       "step current 0.1..1 nA or 50..500 Poisson synapses at 5 Hz, mixed precision",
+           "budget_bytes": args.serve_budget, "chunk_dt_steps": args.serve_chunk,
+           "admit_interval_s": args.serve_admit}
+    rid = 0
+    for name, rate, window in (("offered", args.serve_rate, args.serve_window),
+                               ("sustainable", args.serve_rate_low, args.serve_window_low)):
+        rng = np.random.default_rng([SEED, 77, int(rate)])
+        t, arrivals = 0.0, []
+        while True:
+            t += rng.exponential(1.0 / rate)
+            if t > window:
+                break
+            arrivals.append(t)
+        reqs = []
+        for a in arrivals:
+            cell, steps = models.serving_request(SEED, rid, DT, kca)
+            reqs.append(serve.Request(rid, cell, steps, arrival=a))
+            rid += 1
+        srv = serve.Server(DT, budget_bytes=args.serve_budget, chunk=args.serve_chunk, admit_interval=args.serve_admit)
+        t0 = time.perf_counter()
+        res = srv.run(reqs)
+        wall = time.perf_counter() - t0
+        summ = serve.summarize(res, wall, offered_rate=rate)
+        summ.update({"arrival_window_s": window, "peak_device_bytes": srv.peak_bytes, "ticks": srv.ticks,
+                     "mean_compartments": float(np.mean([r.n_compt for r in res])) if res else None,
+                     "mean_dt_steps": float(np.mean([r.n_steps for r in res])) if res else None})
+        out[name] = summ
+    return out
+
+
 def run_ours(args, rank, world, cpu_pool):
     import numpy as np
     import torch
@@ -381,6 +425,8 @@ def run_ours(args, rank, world, cpu_pool):
                        "d2h_bytes_per_step": (args.chunk // stride) * args.cells * 8},
                "roofline": roof, "cpu_baseline": cpu, "fp64_dropin": dropin, "accuracy": acc,
                "clocks": clk, "gpu_launches": launches}
+        if not args.skip_serving:
+            out["serving"] = run_serving(args)
     b.close()
     return out
 
@@ -405,6 +451,15 @@ def main():
     ap.add_argument("--skip-dropin", action="store_true")
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-serving", action="store_true")
+    ap.add_argument("--serving-only", action="store_true", help="print only the serving measurement")
+    ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s")
+    ap.add_argument("--serve-window", type=float, default=0.5, help="s of arrivals at the offered rate")
+    ap.add_argument("--serve-rate-low", type=float, default=10.0, help="a rate the GPU sustains")
+    ap.add_argument("--serve-window-low", type=float, default=8.0)
+    ap.add_argument("--serve-chunk", type=int, default=2000)
+    ap.add_argument("--serve-admit", type=float, default=0.05, help="s between admission rounds")
+    ap.add_argument("--serve-budget", type=float, default=150e9)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -412,6 +467,11 @@ def main():
         out = run_reference(args, rank, world)
         if out is not None:
             print(json.dumps(out))
+        return 0
+    if args.serving_only:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"serving": run_serving(args)}))
         return 0
     # the CPU pool is spawned before the first GPU call
     cpu_pool = None

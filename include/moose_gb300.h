@@ -295,9 +295,9 @@ typedef struct HsBatch HsBatch;
  * FP64: one warp steps one cell; cells are packed over ctas_per_sm x
  * SM-count CTAs.  Mixed: one CTA steps a forest of cells at a time; a forest
  * holds its elimination arrays in the CTA's shared memory (30 B per node),
- * so ctas_per_sm and forest_nodes set the forest size.  Changing either on
- * a mixed batch renumbers its nodes: its state, recording and inject
- * targets start over and hs_batch_reinit must follow. */
+ * so ctas_per_sm and forest_nodes set the forest size.  Changing either (or
+ * max_ctas) on a mixed batch renumbers its nodes: its state, recording and
+ * inject targets start over and hs_batch_reinit must follow. */
 typedef struct HsBatchTuning {
     uint32_t threads_per_cta;   /* multiple of 32; FP64 <= 256 (default 256),
                                    mixed <= 1024 (default 1024) */
@@ -306,6 +306,9 @@ typedef struct HsBatchTuning {
     uint32_t use_graph;         /* capture a process() call as a CUDA graph */
     uint32_t forest_nodes;      /* mixed: most nodes per shared-memory forest
                                    (0: as many as shared memory holds) */
+    uint32_t max_ctas;          /* mixed: pack the cells into at most this many
+                                   CTAs (0: ctas_per_sm x SM count); fewer,
+                                   fuller forests leave SMs to other batches */
 } HsBatchTuning;
 
 int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds,
@@ -317,6 +320,9 @@ int hs_batch_tune(HsBatch* b, const HsBatchTuning* tuning);
 int hs_batch_reinit(HsBatch* b, double clock_dt);
 int hs_batch_process(HsBatch* b, uint32_t nsteps);
 int hs_batch_sync(HsBatch* b);
+/* *idle = 1 when all queued work of the batch has finished, else 0; does
+ * not wait. */
+int hs_batch_idle(HsBatch* b, int* idle);
 /* Vm of every compartment of cell `cell` in model order. */
 int hs_batch_read_vm(HsBatch* b, uint32_t cell, double* out, uint32_t n);
 int hs_batch_read_ca(HsBatch* b, uint32_t cell, double* out, uint32_t n);

@@ -126,6 +126,7 @@ struct HsBatch {
     // packing / tuning
     uint32_t threadsPerCta = 256, ctasPerSm = 4, stepsPerLaunch = 100;
     uint32_t forestNodes = 0;    // mixed: forest size limit (0: shared-memory capacity)
+    uint32_t maxCtas = 0;        // mixed: CTA limit of the packing (0: one wave)
     bool useGraph = true;
     uint32_t nWarps = 0, nCtas = 0;
     uint32_t *dWarpPtr = nullptr, *dWarpCells = nullptr;
@@ -465,7 +466,8 @@ int buildMixed(HsBatch* b) {
     // processing time first), then within a CTA into forests: cells that fit
     // the shared-memory capacity first-fit decreasing into shared forests,
     // larger cells into global forests of up to 65535 nodes
-    const uint32_t nCtas = std::max<uint32_t>(1, b->nSm * b->ctasPerSm);
+    uint32_t nCtas = std::max<uint32_t>(1, b->nSm * b->ctasPerSm);
+    if (b->maxCtas) nCtas = std::min(nCtas, b->maxCtas);
     std::vector<uint32_t> order(nC);
     for (uint32_t c = 0; c < nC; ++c) order[c] = c;
     std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return trees[x].T > trees[y].T; });
@@ -507,6 +509,15 @@ int buildMixed(HsBatch* b) {
         }
         ctaPtr[k + 1] = (uint32_t)ctaForests.size();
     }
+    // launch only CTAs that hold forests (a small batch leaves the other SMs
+    // to concurrent batches)
+    {
+        std::vector<uint32_t> kept(1, 0);
+        for (uint32_t k = 0; k < nCtas; ++k)
+            if (ctaPtr[k + 1] > ctaPtr[k]) kept.push_back(ctaPtr[k + 1]);
+        ctaPtr.swap(kept);
+    }
+    const uint32_t busy = (uint32_t)ctaPtr.size() - 1;
     // 3. node numbering: forest after forest, level-major inside a forest
     std::vector<std::vector<uint32_t>> posOf(nC);
     std::vector<std::pair<uint32_t, uint32_t>> nodeCT;    // (cell, tree node) of each global node
@@ -915,7 +926,7 @@ int buildMixed(HsBatch* b) {
     }
     b->dCtaPtr = D.up(ctaPtr, st);
     b->dCtaForests = D.up(ctaForests, st);
-    b->nCtas = nCtas;
+    b->nCtas = busy;
     if (D.err != cudaSuccess) return cerr(D.err, "mixed batch upload");
     cudaError_t e = uploadMixedTypes(ctypes.data(), (int)ctypes.size(), ktypes.data(), (int)ktypes.size(),
                                      nullptr, 0, st);
@@ -988,6 +999,7 @@ int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds, uint32_t n_c
         if (tuning->ctas_per_sm) b->ctasPerSm = tuning->ctas_per_sm;
         if (tuning->steps_per_launch) b->stepsPerLaunch = tuning->steps_per_launch;
         b->forestNodes = tuning->forest_nodes;
+        b->maxCtas = tuning->max_ctas;
         b->useGraph = tuning->use_graph != 0;
     }
     const uint32_t maxTpc = precision == HS_PREC_FP64 ? 256 : 1024;
@@ -1036,9 +1048,11 @@ int hs_batch_tune(HsBatch* b, const HsBatchTuning* t) {
     cudaError_t e = cudaStreamSynchronize(b->st);
     if (e != cudaSuccess) return cerr(e, "batch tune");
     const uint32_t cps = t->ctas_per_sm ? t->ctas_per_sm : b->ctasPerSm;
-    const bool relayout = b->precision == HS_PREC_MIXED && (cps != b->ctasPerSm || t->forest_nodes != b->forestNodes);
+    const bool relayout = b->precision == HS_PREC_MIXED &&
+                          (cps != b->ctasPerSm || t->forest_nodes != b->forestNodes || t->max_ctas != b->maxCtas);
     b->ctasPerSm = cps;
     b->forestNodes = t->forest_nodes;
+    b->maxCtas = t->max_ctas;
     if (t->steps_per_launch) b->stepsPerLaunch = t->steps_per_launch;
     b->useGraph = t->use_graph != 0;
     if (relayout) {
@@ -1196,6 +1210,20 @@ int hs_batch_process(HsBatch* b, uint32_t nsteps) {
     if (e != cudaSuccess) return cerr(e, "batch process");
     b->stepsDone += nsteps;
     return HS_OK;
+}
+
+int hs_batch_idle(HsBatch* b, int* idle) {
+    if (!b || !idle) return berr(HS_EINVAL, "null argument");
+    cudaError_t e = cudaStreamQuery(b->st);
+    if (e == cudaSuccess) {
+        *idle = 1;
+        return HS_OK;
+    }
+    if (e == cudaErrorNotReady) {
+        *idle = 0;
+        return HS_OK;
+    }
+    return cerr(e, "batch query");
 }
 
 int hs_batch_sync(HsBatch* b) {

@@ -1,29 +1,29 @@
 """Continuous-batching serving loop over the mixed-precision batch.
 
-Simulation requests (one cell, a number of dt steps) arrive over time.  Each
-tick of the loop:
+Simulation requests (one cell, a number of dt steps) arrive over time.  The
+loop keeps a set of running cohorts.  A cohort is a mixed-precision
+``Batch`` with its own CUDA stream, whose state stays on the device between
+chunks of dt steps; every cell in it stops at its own step count
+(``Batch.set_stop_steps``), so one cohort holds requests of any duration.
+The loop repeatedly:
 
-  1. queues one chunk of dt steps for every running cohort (a cohort is a
-     mixed-precision ``Batch`` with its own CUDA stream whose state stays on
-     the device between chunks).  All launches are queued before any is
-     waited for, so the kernels of different cohorts run at the same time on
-     the GPU: a cohort's persistent kernel holds only the SMs its forests
-     need, the rest go to the others;
-  2. while the GPU works, admits waiting requests first come, first served,
-     while the device memory of the running cohorts plus the estimate for the
-     request stays within the HBM budget, and sets up the admitted ones as a
-     new cohort (it runs from the next tick).  Every cell stops at its own
-     step count (``Batch.set_stop_steps``), so one cohort holds requests of
-     any duration;
-  3. waits for the chunk of each cohort and streams out the new soma Vm
-     samples and spikes of its requests, completes the requests that reached
-     their step count and releases cohorts whose cells are all done.
+  * admits waiting requests first come, first served (at most every
+    ``admit_interval`` seconds, to group arrivals) while the device memory of
+    the running cohorts plus the estimate for the request stays within the
+    HBM budget, sets them up as a new cohort and queues its first chunk;
+  * polls every cohort without waiting (``Batch.idle``): a cohort whose chunk
+    has finished streams out the new soma Vm samples and spikes of its
+    requests, completes the requests that reached their step count, and
+    either queues its next chunk or, when all its cells are done, releases
+    its memory.
 
-A request's latency is completion minus arrival (queueing, setup and
-simulation).  A cell's result does not depend on the cohort it runs in or on
-the other requests (every node's arithmetic depends only on its own cell):
-the tests compare each request served in a mix with the same request run
-alone.
+Cohorts thus progress independently and their kernels run at the same time
+on the GPU: a cohort's persistent kernel holds only the SMs its forests need,
+the rest go to the others.  A request's latency is completion minus arrival
+(queueing, setup and simulation).  A cell's result does not depend on the
+cohort it runs in or on the other requests (every node's arithmetic depends
+only on its own cell): the tests compare each request served in a mix with
+the same request run alone.
 """
 import dataclasses
 import time
@@ -101,6 +101,9 @@ class _Cohort:
         self.batch.process(chunk)
         self.launched += chunk
 
+    def ready(self):
+        return self.batch.idle()
+
     def collect(self):
         """Stream the samples and spikes of the last chunk; return the
         indices of requests that completed with it."""
@@ -131,15 +134,21 @@ class _Cohort:
 
 class Server:
     """The serving loop.  ``budget_bytes`` bounds the device memory of the
-    running cohorts; ``chunk`` is the number of dt steps per tick."""
+    running cohorts; ``chunk`` is the number of dt steps a cohort advances
+    between two polls of its output.  With ``dense`` a cohort is packed into
+    as few CTAs as forests of about ``forest_nodes`` nodes need."""
 
-    def __init__(self, dt, budget_bytes=150 * 10**9, chunk=400, record_stride=40, max_cohort=4096,
-                 tuning=None, clock=time.perf_counter, cohort_factory=None):
+    def __init__(self, dt, budget_bytes=150 * 10**9, chunk=2000, record_stride=40, max_cohort=4096,
+                 admit_interval=0.05, dense=True, forest_nodes=7000, tuning=None, clock=time.perf_counter,
+                 cohort_factory=None):
         self.dt = dt
         self.budget = budget_bytes
         self.chunk = chunk
         self.stride = record_stride
         self.max_cohort = max_cohort
+        self.admit_interval = admit_interval
+        self.dense = dense
+        self.forest_nodes = forest_nodes
         self.tuning = dict(tuning or {})
         self.clock = clock
         self.cohort_factory = cohort_factory or _Cohort
@@ -166,7 +175,13 @@ class Server:
             est += e
         if not take:
             return None
-        return self.cohort_factory(take, self.dt, self.stride, self.chunk, now, self.tuning)
+        tuning = dict(self.tuning)
+        if self.dense and "max_ctas" not in tuning:
+            # as few CTAs as full forests need: one forest per CTA, each SM
+            # well used, the other SMs left to the other cohorts
+            nodes = sum(int(1.3 * r.cell.n_compt) for r in take)
+            tuning["max_ctas"] = max(1, -(-nodes // self.forest_nodes))
+        return self.cohort_factory(take, self.dt, self.stride, self.chunk, now, tuning)
 
     def run(self, requests, real_time=True, t0=None):
         """Serve `requests` (sorted by arrival); returns the results in
@@ -174,14 +189,23 @@ class Server:
         otherwise every request is available from the start."""
         pending = list(requests)
         start = self.clock() if t0 is None else t0
+        last_admit = -1e30
         while pending or self.waiting or self.cohorts:
             now = self.clock() - start
-            for c in self.cohorts:
-                c.launch(self.chunk)
             while pending and (not real_time or pending[0].arrival <= now):
                 self.waiting.append(pending.pop(0))
-            fresh = self._admit(now) if self.waiting else None
+            progressed = False
+            if self.waiting and now - last_admit >= self.admit_interval:
+                fresh = self._admit(now)
+                last_admit = now
+                if fresh is not None:
+                    fresh.launch(self.chunk)
+                    self.cohorts.append(fresh)
+                    progressed = True
             for c in list(self.cohorts):
+                if not c.ready():
+                    continue
+                progressed = True
                 done = c.collect()
                 t = self.clock() - start
                 for i in done:
@@ -192,13 +216,17 @@ class Server:
                 if c.done.all():
                     self.cohorts.remove(c)
                     c.close()
-            if fresh is not None:
-                self.cohorts.append(fresh)
+                else:
+                    c.launch(self.chunk)
             self.peak_bytes = max(self.peak_bytes, self.used_bytes())
             self.ticks += 1
-            if not self.cohorts and not self.waiting and pending and real_time:
-                # idle until the next arrival (the clock is wall time here)
-                time.sleep(max(0.0, min(0.05, pending[0].arrival - (self.clock() - start))))
+            if not progressed and real_time:
+                # nothing finished and nothing to admit: wait a little (until
+                # the next arrival at most)
+                wait = 0.0005
+                if not self.cohorts and not self.waiting and pending:
+                    wait = max(0.0, min(0.05, pending[0].arrival - (self.clock() - start)))
+                time.sleep(wait)
         return self.results
 
 

@@ -35,6 +35,9 @@ class FakeCohort:
     def launch(self, chunk):
         self.steps += chunk
 
+    def ready(self):
+        return True
+
     def collect(self):
         fresh = [i for i, r in enumerate(self.reqs) if not self.done[i] and self.steps >= r.n_steps]
         for i in fresh:
