@@ -20,11 +20,12 @@ The JSON line carries:
   accuracy   max |dVm| and spike-time shift of the mixed batch against the
              FP64 path (bit-identical to the reference HSolve) on a subset;
   roofline   the stepping kernel against the measured HBM copy bandwidth;
-  cpu_baseline the CPU restatement of HSolve (the oracle) on the host cores.
+  cpu_baseline the CPU restatement of HSolve (the oracle) on the host cores;
+  config.autotuned  the packing and launch shape the autotuner picked.
   serving    the serving loop (continuous batching under a 150 GB budget)
              on Poisson arrivals of the serving workload: p50/p99 latency
              and compartment-steps/s at the offered 2,000 requests/s over a
-             bounded window, and at a rate the GPU sustains.
+             bounded window, and at a low rate (10 requests/s).
 With --impl reference the line is the CPU HSolve on all host cores instead.
 With --gpus N (torchrun) every rank runs its own replica ("replicas only").
 """
@@ -223,7 +224,7 @@ def run_serving(args):
            "admit_interval_s": args.serve_admit}
     rid = 0
     for name, rate, window in (("offered", args.serve_rate, args.serve_window),
-                               ("sustainable", args.serve_rate_low, args.serve_window_low)):
+                               ("low_rate", args.serve_rate_low, args.serve_window_low)):
         rng = np.random.default_rng([SEED, 77, int(rate)])
         t, arrivals = 0.0, []
         while True:
@@ -267,6 +268,10 @@ def run_ours(args, rank, world, cpu_pool):
              for i in range(args.cells)]
     ncomp = sum(m.n_compt for m in cells)
     b = Batch(cells, DT, HS_PREC_MIXED, steps_per_launch=args.steps_per_launch)
+    tuned = None
+    if not args.no_autotune:
+        from moose_gb300.autotune import autotune
+        tuned = autotune(b, DT, steps=200, warmup=50)
     spl = b.info()["steps_per_launch"]
     stride = 10
     cap = total_steps // stride + 2
@@ -419,7 +424,8 @@ def run_ours(args, rank, world, cpu_pool):
                "config": {"workload": "hsolve_4096cells_mixed_syn200", "cells": args.cells,
                           "compartments": ncomp, "dt_s": DT, "chunk_dt_steps": args.chunk,
                           "steps_per_launch": spl, "threads_per_cta": b.info()["threads_per_cta"],
-                          "ctas": b.info()["n_ctas"], "synchans_per_cell": 200, "parallelism": "replicas"},
+                          "ctas": b.info()["n_ctas"], "autotuned": tuned,
+                          "synchans_per_cell": 200, "parallelism": "replicas"},
                "e2e": {"value": e2e_value, "unit": "compartment-steps/s",
                        "h2d_bytes_per_step": args.cells * 8,
                        "d2h_bytes_per_step": (args.chunk // stride) * args.cells * 8},
@@ -452,10 +458,11 @@ def main():
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-serving", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--serving-only", action="store_true", help="print only the serving measurement")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s")
     ap.add_argument("--serve-window", type=float, default=0.5, help="s of arrivals at the offered rate")
-    ap.add_argument("--serve-rate-low", type=float, default=10.0, help="a rate the GPU sustains")
+    ap.add_argument("--serve-rate-low", type=float, default=10.0, help="a second, low arrival rate")
     ap.add_argument("--serve-window-low", type=float, default=8.0)
     ap.add_argument("--serve-chunk", type=int, default=2000)
     ap.add_argument("--serve-admit", type=float, default=0.05, help="s between admission rounds")
