@@ -214,7 +214,7 @@ def run_serving(args):
     100..10,000 compartments, 0.1..2 s, step current or 50..500 synapses),
     150 GB budget: once at the offered rate over a bounded window (the loop is
     overloaded there: each request carries ~9e7 compartment-steps), once at a
-    rate the GPU sustains.  Requests are generated before the clock starts."""
+    low rate.  Requests are generated before the clock starts."""
     import numpy as np
     from moose_gb300 import models, serve
     kca = models.kca_2d_tables()
