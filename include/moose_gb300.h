@@ -341,6 +341,19 @@ int hs_batch_read_trace_window(HsBatch* b, uint32_t first, uint32_t count,
 int hs_batch_inject_targets(HsBatch* b, const uint32_t* cell, const uint32_t* compt,
                             uint32_t n);
 int hs_batch_set_inject(HsBatch* b, const double* values, uint32_t n);
+/* The inject of compartment compt[k] of cell cell[k] becomes values[k], for
+ * k < n, without allocating any memory: the writes go through a fixed
+ * host staging array and a fixed device scratch array of 32768 entries
+ * (larger n: HS_ECAPACITY).  For callers that must not allocate between
+ * process() calls, such as a loop driving other batches on the same GPU
+ * (cudaMalloc/cudaFree would wait for the whole device).  The first call on
+ * a device looks up the scratch address and should come before any stream
+ * capture on it; calls share the storage, are serialised by a lock and
+ * return after the writes are done.  Same targets and rules as
+ * hs_batch_inject_targets + hs_batch_set_inject.  No counterpart in the
+ * reference. */
+int hs_batch_set_inject_at(HsBatch* b, const uint32_t* cell, const uint32_t* compt,
+                           const double* values, uint32_t n);
 int hs_batch_read_spikes(HsBatch* b, uint32_t* cell, uint32_t* gen,
                          double* time, uint32_t capacity, uint32_t* n);
 /* Serving support (mixed batch).  Cell c advances only while its step count

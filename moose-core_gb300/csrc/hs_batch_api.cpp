@@ -28,6 +28,7 @@
 #include "../../include/moose_gb300.h"
 #include "hs_cell.h"
 #include "hs_mixed.cuh"
+#include "hs_noalloc.h"
 #include "hs_plan.h"
 
 namespace hsg {
@@ -1519,6 +1520,36 @@ int hs_batch_set_inject(HsBatch* b, const double* values, uint32_t n) {
     cudaError_t e = cudaMemcpyAsync(b->dInjVal, values, (size_t)n * 8, cudaMemcpyHostToDevice, b->st);
     if (e == cudaSuccess) e = launchScatterInject(b->dInjAddr, b->dInjFlag, b->dInjVal, n, b->st);
     return e == cudaSuccess ? HS_OK : cerr(e, "set inject");
+}
+
+int hs_batch_set_inject_at(HsBatch* b, const uint32_t* cell, const uint32_t* compt, const double* values,
+                           uint32_t n) {
+    if (!b || (n && (!cell || !compt || !values))) return berr(HS_EINVAL, "null argument");
+    if (n > kInjectWriteMax)
+        return berr(HS_ECAPACITY, "hs_batch_set_inject_at takes at most 32768 writes per call");
+    if (n == 0) return HS_OK;
+    std::lock_guard<std::mutex> lock(injectStaticLock());
+    InjectWrite* w = injectStaging();
+    for (uint32_t k = 0; k < n; ++k) {
+        if (cell[k] >= b->nCells) return berr(HS_EINVAL, "inject target cell out of range");
+        const CellPlan& P = b->plans[cell[k]];
+        if (compt[k] >= P.hinesOf.size() || P.hinesOf[compt[k]] < 0)
+            return berr(HS_EINVAL, "inject target compartment not in the cell");
+        if (b->precision == HS_PREC_FP64) {
+            const uint32_t h = (uint32_t)P.hinesOf[compt[k]];
+            w[k] = InjectWrite{b->dcs[cell[k]].injBasal + h, b->dcs[cell[k]].injPresent + h, values[k]};
+        } else {
+            const int32_t e = b->injEntryOf[cell[k]][compt[k]];
+            if (e < 0) return berr(HS_ENOTSUP, "mixed batch: compartment had no inject or stimulus at setup");
+            w[k] = InjectWrite{b->mb.injVal + e, nullptr, values[k]};
+        }
+    }
+    int cur = -1;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e == cudaSuccess && cur != b->device) e = cudaSetDevice(b->device);
+    if (e == cudaSuccess) e = scatterInjectStatic(b->device, n, b->st);
+    if (cur >= 0 && cur != b->device) cudaSetDevice(cur);
+    return e == cudaSuccess ? HS_OK : cerr(e, "set inject at");
 }
 
 int hs_batch_read_spikes(HsBatch* b, uint32_t* cell, uint32_t* gen, double* time, uint32_t capacity,

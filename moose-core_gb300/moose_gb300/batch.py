@@ -122,6 +122,16 @@ class Batch:
         ptr = values.data_ptr() if hasattr(values, "data_ptr") else values.ctypes.data
         _native.check(_native.load().hs_batch_set_inject(self._h, C.c_void_p(ptr), len(self._inj[0])))
 
+    def set_inject_at(self, cells, compts, values):
+        """inject of (cells[k], compts[k]) = values[k], without allocating
+        (hs_batch_set_inject_at; at most 32768 writes per call)."""
+        c = np.ascontiguousarray(cells, np.uint32)
+        m = np.ascontiguousarray(compts, np.uint32)
+        v = np.ascontiguousarray(values, np.float64)
+        pu = C.POINTER(C.c_uint32)
+        _native.check(_native.load().hs_batch_set_inject_at(self._h, c.ctypes.data_as(pu), m.ctypes.data_as(pu),
+                                                            v.ctypes.data_as(C.POINTER(C.c_double)), len(v)))
+
     def spikes(self):
         L = _native.load()
         n = C.c_uint32()

@@ -5,6 +5,7 @@ Translation units:
     IEEE roundings, exactly as the reference CPU code computes it;
   * ``hs_mixed.cu`` -- the mixed-precision batched kernel (FMA contraction on);
   * ``hs_cell.cu``  -- device-arena upload;
+  * ``hs_noalloc.cu`` -- inject writes from fixed storage (no allocation);
   * ``hs_plan.cpp``, ``hs_api.cpp``, ``hs_batch_api.cpp`` -- host setup and
     the C ABI, ``-ffp-contract=off`` for the same reason.
 The library is built in-tree under ``moose_gb300/_lib`` (git-ignored).
@@ -35,6 +36,7 @@ UNITS = {
     "hs_fp64.cu": ["--fmad=false"],
     "hs_mixed.cu": [],
     "hs_cell.cu": ["--fmad=false"],
+    "hs_noalloc.cu": [],
     "hs_plan.cpp": None,
     "hs_api.cpp": None,
     "hs_batch_api.cpp": None,
