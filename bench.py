@@ -257,6 +257,7 @@ def run_ours(args, rank, world, cpu_pool):
     from moose_gb300.batch import Batch
     from moose_gb300.hsolve import HSolve
     from moose_gb300.perf import algorithmic_bytes
+    from moose_gb300.replicas import barrier, job_throughput, max_over_ranks
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
@@ -290,8 +291,7 @@ def run_ours(args, rank, world, cpu_pool):
     b.sync()
     b.kernel_time()
     # device-timed throughput, inputs resident
-    if world > 1:
-        torch.distributed.barrier()
+    barrier(local)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -305,8 +305,7 @@ def run_ours(args, rank, world, cpu_pool):
     dev_ms = ev0.elapsed_time(ev1)
     k_ms, k_n = b.kernel_time()
     # end to end through the C ABI: inject in from pinned memory, trace out
-    if world > 1:
-        torch.distributed.barrier()
+    barrier(local)
     done = b.info()
     first = (args.warmup + args.steps) * args.chunk // stride + 1
     t0 = time.perf_counter()
@@ -325,17 +324,10 @@ def run_ours(args, rank, world, cpu_pool):
     e2e_ms = max(e2e_ms, e2e_wall * 1e3)
     del done
 
-    def reduce_max(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
-
-    dev_ms = reduce_max(dev_ms)
-    e2e_ms = reduce_max(e2e_ms)
-    value = world * ncomp * args.chunk * args.steps / (dev_ms / 1e3)
-    e2e_value = world * ncomp * args.chunk * args.steps / (e2e_ms / 1e3)
+    dev_ms = max_over_ranks(dev_ms, "cuda")
+    e2e_ms = max_over_ranks(e2e_ms, "cuda")
+    value = job_throughput(ncomp * args.chunk * args.steps, dev_ms / 1e3, world)
+    e2e_value = job_throughput(ncomp * args.chunk * args.steps, e2e_ms / 1e3, world)
 
     out = None
     if rank == 0:
