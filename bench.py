@@ -17,6 +17,8 @@ The JSON line carries:
              reads back the somatic Vm trace of the chunk;
   fp64_dropin the plain FP64 drop-in (one HSolve instance per cell, one CTA
              each) on a sample of the same cells, and the ratio to `value`;
+  fp64_batch the FP64 batch (one warp per cell, the drop-in's arithmetic,
+             bit-identical results) on all cells of the workload;
   accuracy   max |dVm| and spike-time shift of the mixed batch against the
              FP64 path (bit-identical to the reference HSolve) on a subset;
   roofline   the stepping kernel against the measured HBM copy bandwidth;
@@ -368,6 +370,25 @@ def run_ours(args, rank, world, cpu_pool):
                       "mixed_batch_over_fp64_dropin": value / world / dv}
             for h in hs:
                 h.close()
+        # the FP64 batch (warp per cell, the drop-in's arithmetic) on the same workload
+        fp64b = None
+        if not args.skip_fp64_batch:
+            f = Batch(cells, DT, HS_PREC_FP64, steps_per_launch=100)
+            f.reinit(DT)
+            f.process(20)
+            f.sync()
+            f.kernel_time()
+            t0 = time.perf_counter()
+            f.process(args.fp64_batch_steps)
+            f.sync()
+            wall = time.perf_counter() - t0
+            fms, fn = f.kernel_time()
+            fv = ncomp * args.fp64_batch_steps / wall
+            fp64b = {"value": fv, "unit": "compartment-steps/s", "cells": args.cells,
+                     "dt_steps": args.fp64_batch_steps, "kernel_ms_per_launch": fms,
+                     "mixed_batch_over_fp64_batch": value / world / fv,
+                     "fp64_batch_over_fp64_dropin": (fv / dropin["value"]) if dropin else None}
+            f.close()
         acc = None
         if not args.skip_accuracy:
             ids = list(range(0, args.cells, max(1, args.cells // args.acc_cells)))[: args.acc_cells]
@@ -421,7 +442,8 @@ def run_ours(args, rank, world, cpu_pool):
                "e2e": {"value": e2e_value, "unit": "compartment-steps/s",
                        "h2d_bytes_per_step": args.cells * 8,
                        "d2h_bytes_per_step": (args.chunk // stride) * args.cells * 8},
-               "roofline": roof, "cpu_baseline": cpu, "fp64_dropin": dropin, "accuracy": acc,
+               "roofline": roof, "cpu_baseline": cpu, "fp64_dropin": dropin, "fp64_batch": fp64b,
+               "accuracy": acc,
                "clocks": clk, "gpu_launches": launches}
         if not args.skip_serving:
             out["serving"] = run_serving(args)
@@ -450,6 +472,8 @@ def main():
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-serving", action="store_true")
+    ap.add_argument("--skip-fp64-batch", action="store_true")
+    ap.add_argument("--fp64-batch-steps", type=int, default=100)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--serving-only", action="store_true", help="print only the serving measurement")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s")

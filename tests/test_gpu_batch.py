@@ -125,3 +125,32 @@ def test_mixed_results_do_not_depend_on_packing():
     a.process(500)
     for i in range(len(cells)):
         assert np.array_equal(a.vm(i), c.vm(i)), i
+
+
+def test_mixed_edge_cases_against_the_oracle():
+    """One- and two-compartment cells, and an unbranched 1,500-compartment
+    cable (more tree levels than the kernel keeps in shared memory), in one
+    mixed batch: within the mixed-precision tolerance of the FP64 oracle."""
+    kA, kB = models.kca_2d_tables(vdivs=300, cadivs=300)
+    cells = []
+    for n in (1, 2):
+        parent = np.arange(-1, n - 1, dtype=np.int32)
+        d = np.full(n, 2e-6)
+        L = np.full(n, 10e-6)
+        cells.append(models.active_cell(parent, d, L, inject=0.05e-9, kca_tables=(kA, kB), t_end=0.05))
+    parent, d, L = models.cable_morphology(1499)
+    cells.append(models.active_cell(parent, d, L, inject=0.8e-9, kca_tables=(kA, kB), t_end=0.05))
+    b = Batch(cells, DT, HS_PREC_MIXED, steps_per_launch=50)
+    b.reinit(DT)
+    oracles = []
+    for m in cells:
+        oc = OracleCell(m, DT)
+        oc.reinit(DT)
+        oracles.append(oc)
+    worst = 0.0
+    for _ in range(8):
+        b.process(250)
+        for i, oc in enumerate(oracles):
+            oc.step(250)
+            worst = max(worst, float(np.abs(b.vm(i) - oc.vm()).max()))
+    assert worst <= 1e-4, "max |dVm| = %g V" % worst
