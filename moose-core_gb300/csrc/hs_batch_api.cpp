@@ -846,6 +846,13 @@ int buildMixed(HsBatch* b) {
     m.synType = D.up(synTypeV, st);
     m.synX = D.zeros<float>(synTypeV.size(), st);
     m.synY = D.zeros<float>(synTypeV.size(), st);
+    m.synGk = D.zeros<float2>(synTypeV.size(), st);
+    {
+        std::vector<uint32_t> synCell(synTypeV.size());
+        for (uint32_t g = 0; g < nN; ++g)
+            for (uint32_t k = syn0[g]; k < syn0[g + 1]; ++k) synCell[k] = nodeCT[g].first;
+        m.synCell = D.up(synCell, st);
+    }
     m.evCur = D.up(H.evStart, st);
     m.evEnd = D.up(H.evEnd, st);
     b->dEvStep = D.zeros<uint32_t>(H.evTime.size(), st);

@@ -260,25 +260,35 @@ __device__ __forceinline__ void assembleNode(const MixBatch& b, uint32_t n, uint
         G += gk;
         GE = fmaf(gk, t.ek, GE);
     }
-    // ---- SynChans: events delivered this step (SimpleSynHandler), dual exponential
+    // ---- SynChans: conductances of this step, advanced beforehand (synapseStep)
     for (uint32_t k = s0; k < s1; ++k) {
-        const SynType& t = c_synTypes[__ldg(b.synType + k)];
-        uint32_t e = b.evCur[k];
-        const uint32_t end = __ldg(b.evEnd + k);
-        const float sx = b.synX[k], sy = b.synY[k], nm = __ldg(b.synNorm + k);
-        float act = 0.f;
-        while (e < end && __ldg(b.evStep + e) <= step) act += __ldg(b.evAct + e++);
-        b.evCur[k] = e;
-        const float X = fmaf(act, t.xc1, sx * t.xc2);
-        const float Y = fmaf(X, t.yc1, sy * t.yc2);
-        b.synX[k] = X;
-        b.synY[k] = Y;
-        const float gk = Y * nm;
-        G += gk;
-        GE = fmaf(gk, t.ek, GE);
+        const float2 g = b.synGk[k];
+        G += g.x;
+        GE += g.y;
     }
     diag = hs2 + widenF(G);
     rhs = fma(V, cmdt, emrm) + widenF(GE) + inj;
+}
+
+// SynChan k over step `step`: the events delivered (SimpleSynHandler, weight
+// / dt each), the dual exponential X, Y, and the conductance Gk and Gk Ek
+// the assembly of that step adds.  Needs no Vm, so it runs ahead of the
+// assembly (see stepForest).
+__device__ __forceinline__ void synapseStep(const MixBatch& b, uint32_t k, unsigned long long step) {
+    if (step >= b.stopStep[__ldg(b.synCell + k)]) return;
+    const SynType& t = c_synTypes[__ldg(b.synType + k)];
+    uint32_t e = b.evCur[k];
+    const uint32_t end = __ldg(b.evEnd + k);
+    const float sx = b.synX[k], sy = b.synY[k], nm = __ldg(b.synNorm + k);
+    float act = 0.f;
+    while (e < end && __ldg(b.evStep + e) <= step) act += __ldg(b.evAct + e++);
+    b.evCur[k] = e;
+    const float X = fmaf(act, t.xc1, sx * t.xc2);
+    const float Y = fmaf(X, t.yc1, sy * t.yc2);
+    b.synX[k] = X;
+    b.synY[k] = Y;
+    const float gk = Y * nm;
+    b.synGk[k] = make_float2(gk, gk * t.ek);
 }
 
 // Elimination arrays of a forest: pivots/couplings D, right-hand sides R,
@@ -381,6 +391,12 @@ __device__ void stepForest(const MixBatch& b, const MixForest& F, uint32_t f, co
     const uint32_t tid = threadIdx.x, nth = blockDim.x;
     if (nsteps == 0) return;
     unsigned long long step = b.forestStep[f];
+    // SynChans of the forest: [k0, k1).  Those of step 0 of the launch are
+    // advanced here; those of every later step by the threads that a level of
+    // the previous step's elimination leaves idle (whole idle warps take the
+    // next synapses in order), the rest after that elimination.
+    const uint32_t k0 = __ldg(b.syn0 + F.node0), k1 = __ldg(b.syn0 + F.node0 + F.nNodes);
+    for (uint32_t k = k0 + tid; k < k1; k += nth) synapseStep(b, k, step);
     for (uint32_t s = 0; s < nsteps; ++s, ++step) {
         if (tid < b.nPf) prefetchNodes(b, tid, F.node0, nth);
         forestStimulus(b, F, step);
@@ -410,8 +426,17 @@ __device__ void stepForest(const MixBatch& b, const MixForest& F, uint32_t f, co
         // forward elimination, deepest level first: pull the children's
         // eliminated rows (diag -= off_c * f_c, rhs -= off_c * g_c), then keep
         // g = rhs/pivot in R and f = off/pivot in D
+        const bool ahead = s + 1 < nsteps;     // advance the next step's synapses
+        uint32_t kNext = k0;
         for (int L = (int)F.nLevels - 1; L >= 0; --L) {
             const uint32_t e = lp[L + 1];
+            if (ahead && kNext < k1) {
+                const uint32_t busy = (e - lp[L] + 31) & ~31u;
+                if (busy < nth) {
+                    if (tid >= busy && kNext + (tid - busy) < k1) synapseStep(b, kNext + (tid - busy), step + 1);
+                    kNext += nth - busy;
+                }
+            }
             for (uint32_t i = lp[L] + tid; i < e; i += nth) {
                 const uint32_t t = E.TOPO[i];
                 const uint32_t c0 = t & 0xFFFF, c1 = c0 + (t >> 16);
@@ -438,6 +463,8 @@ __device__ void stepForest(const MixBatch& b, const MixForest& F, uint32_t f, co
             }
             __syncthreads();
         }
+        if (ahead)
+            for (uint32_t k = kNext + tid; k < k1; k += nth) synapseStep(b, k, step + 1);
     }
     // the last step's update and outputs
     for (uint32_t i = tid; i < F.nNodes; i += nth) {

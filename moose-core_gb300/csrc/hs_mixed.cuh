@@ -145,6 +145,8 @@ struct MixBatch {
     const uint8_t* synType;
     const float* synNorm;        // norm * modulation
     float *synX, *synY;
+    float2* synGk;               // Gk, Gk*Ek of the step the assembly adds next
+    const uint32_t* synCell;     // cell of each SynChan
     uint32_t* evCur;
     const uint32_t* evEnd;
     const uint32_t* evStep;      // delivery step of each event
