@@ -309,6 +309,9 @@ typedef struct HsBatchTuning {
     uint32_t max_ctas;          /* mixed: pack the cells into at most this many
                                    CTAs (0: ctas_per_sm x SM count); fewer,
                                    fuller forests leave SMs to other batches */
+    uint32_t elim_warps;        /* mixed: warps of a CTA that eliminate while the
+                                   others assemble (default 4; 0 keeps the
+                                   current value, 0xFFFFFFFF turns the split off) */
 } HsBatchTuning;
 
 int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds,

@@ -37,7 +37,7 @@ cudaError_t uploadMixedTypes(const ChanType* ct, int nct, const C2dType* kt, int
                              int nst, cudaStream_t s);
 cudaError_t launchForestStepMixed(const MixBatch& b, const uint32_t* ctaPtr, const uint32_t* ctaForests,
                                   uint32_t nCtas, uint32_t threadsPerCta, uint32_t smemBytes, uint32_t cap,
-                                  uint32_t nsteps, cudaStream_t st);
+                                  uint32_t elimWarps, uint32_t nsteps, cudaStream_t st);
 cudaError_t launchBatchReinitMixed(const MixBatch& b, uint32_t nNodes, const double* initVm, const float* c2dX0,
                                    const uint32_t* evStart, cudaStream_t st);
 cudaError_t launchScatterInject(double* const* addr, uint8_t* const* flag, const double* val, uint32_t n,
@@ -128,6 +128,7 @@ struct HsBatch {
     uint32_t threadsPerCta = 256, ctasPerSm = 4, stepsPerLaunch = 100;
     uint32_t forestNodes = 0;    // mixed: forest size limit (0: shared-memory capacity)
     uint32_t maxCtas = 0;        // mixed: CTA limit of the packing (0: one wave)
+    uint32_t elimWarps = 4;      // mixed: eliminator warps of the split step (0: no split)
     bool useGraph = true;
     uint32_t nWarps = 0, nCtas = 0;
     uint32_t *dWarpPtr = nullptr, *dWarpCells = nullptr;
@@ -183,8 +184,9 @@ namespace {
 cudaError_t launchStep(HsBatch* b, uint32_t k) {
     if (b->precision == HS_PREC_FP64)
         return launchBatchStepFp64(b->dDcs, b->dWarpPtr, b->dWarpCells, b->nWarps, k, b->threadsPerCta, b->st);
+    const uint32_t ew = b->elimWarps && b->threadsPerCta > 32 * b->elimWarps ? b->elimWarps : 0;
     return launchForestStepMixed(b->mb, b->dCtaPtr, b->dCtaForests, b->nCtas, b->threadsPerCta, b->mixSmem,
-                                 b->mixCap, k, b->st);
+                                 b->mixCap, ew, k, b->st);
 }
 
 // Longest-processing-time packing of the FP64 batch: cells to the CTAs of one
@@ -426,7 +428,8 @@ int starTree(const CellPlan& P, StarTree& S) {
 }
 
 // Shared-memory bytes per forest node: D, R, OFF (8 B), TOPO (4 B), PAR (2 B);
-// the kernel also keeps kSmemLevels level offsets (4 B) there.
+// the kernel also keeps kSmemLevels level offsets and kWsLevels level
+// counters (4 B each) there.
 constexpr uint32_t kForestNodeBytes = 30;
 
 int buildMixed(HsBatch* b) {
@@ -449,12 +452,13 @@ int buildMixed(HsBatch* b) {
     if (ce != cudaSuccess) return cerr(ce, "shared memory size");
     const uint32_t perCta =
         std::min<uint32_t>((uint32_t)optin, (uint32_t)perSm / std::max<uint32_t>(1, b->ctasPerSm) - 1024) / 256 * 256;
-    if (perCta < kSmemLevels * 4 + 8 * kForestNodeBytes) return berr(HS_EINVAL, "too many CTAs per SM");
-    uint32_t cap = std::min<uint32_t>(kMaxForestNodes, (perCta - kSmemLevels * 4) / kForestNodeBytes) / 8 * 8;
+    const uint32_t reserve = (kSmemLevels + kWsLevels) * 4;
+    if (perCta < reserve + 8 * kForestNodeBytes) return berr(HS_EINVAL, "too many CTAs per SM");
+    uint32_t cap = std::min<uint32_t>(kMaxForestNodes, (perCta - reserve) / kForestNodeBytes) / 8 * 8;
     if (b->forestNodes) cap = std::min(cap, b->forestNodes / 8 * 8);
     if (cap < 8) return berr(HS_EINVAL, "forest_nodes too small");
     b->mixCap = cap;
-    b->mixSmem = (kSmemLevels * 4 + cap * kForestNodeBytes + 15) / 16 * 16;
+    b->mixSmem = (reserve + cap * kForestNodeBytes + 15) / 16 * 16;
 
     // 1. star trees
     std::vector<StarTree> trees(nC);
@@ -522,6 +526,7 @@ int buildMixed(HsBatch* b) {
     // 3. node numbering: forest after forest, level-major inside a forest
     std::vector<std::vector<uint32_t>> posOf(nC);
     std::vector<std::pair<uint32_t, uint32_t>> nodeCT;    // (cell, tree node) of each global node
+    std::vector<uint8_t> nodeLevel;                       // forest level, capped at 255
     std::vector<MixForest> fdev(forests.size());
     std::vector<uint32_t> levelPtr, forestCells;
     for (size_t fi = 0; fi < forests.size(); ++fi) {
@@ -542,9 +547,11 @@ int buildMixed(HsBatch* b) {
         }
         levelPtr.push_back(0);
         while (!cur.empty()) {
+            const uint8_t lv = (uint8_t)std::min<size_t>(255, levelPtr.size() - F.level0 - 1);
             for (auto& ct : cur) {
                 posOf[ct.first][ct.second] = (uint32_t)nodeCT.size();
                 nodeCT.push_back(ct);
+                nodeLevel.push_back(lv);
             }
             levelPtr.push_back((uint32_t)(nodeCT.size() - F.node0));
             next.clear();
@@ -653,7 +660,7 @@ int buildMixed(HsBatch* b) {
             const StarTree& S = trees[ci];
             const bool center = t >= S.N;
             const uint32_t nch = S.chPtr[t + 1] - S.chPtr[t];
-            topo[g] = (nch ? posOf[ci][S.ch[S.chPtr[t]]] - F.node0 : 0) | (nch << 16);
+            topo[g] = (nch ? posOf[ci][S.ch[S.chPtr[t]]] - F.node0 : 0) | (nch << 16) | ((uint32_t)nodeLevel[g] << 24);
             for (uint32_t k = S.chPtr[t]; k < S.chPtr[t + 1]; ++k) par[posOf[ci][S.ch[k]]] = (uint16_t)(g - F.node0);
             off[g] = S.off[t];
             HS2[g] = S.diag[t];
@@ -802,6 +809,7 @@ int buildMixed(HsBatch* b) {
     m.cells = D.up(H.cells, st);
     m.forests = D.up(fdev, st);
     m.forestStep = D.zeros<unsigned long long>(fdev.size(), st);
+    m.err = D.zeros<uint32_t>(1, st);
     {
         std::vector<uint32_t> cellOf(nN);
         for (uint32_t g = 0; g < nN; ++g) cellOf[g] = nodeCT[g].first;
@@ -1008,6 +1016,7 @@ int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds, uint32_t n_c
         if (tuning->steps_per_launch) b->stepsPerLaunch = tuning->steps_per_launch;
         b->forestNodes = tuning->forest_nodes;
         b->maxCtas = tuning->max_ctas;
+        if (tuning->elim_warps) b->elimWarps = tuning->elim_warps == 0xFFFFFFFFu ? 0 : tuning->elim_warps;
         b->useGraph = tuning->use_graph != 0;
     }
     const uint32_t maxTpc = precision == HS_PREC_FP64 ? 256 : 1024;
@@ -1061,6 +1070,7 @@ int hs_batch_tune(HsBatch* b, const HsBatchTuning* t) {
     b->ctasPerSm = cps;
     b->forestNodes = t->forest_nodes;
     b->maxCtas = t->max_ctas;
+    if (t->elim_warps) b->elimWarps = t->elim_warps == 0xFFFFFFFFu ? 0 : t->elim_warps;
     if (t->steps_per_launch) b->stepsPerLaunch = t->steps_per_launch;
     b->useGraph = t->use_graph != 0;
     if (relayout) {
@@ -1237,7 +1247,14 @@ int hs_batch_idle(HsBatch* b, int* idle) {
 int hs_batch_sync(HsBatch* b) {
     if (!b) return berr(HS_EINVAL, "null batch");
     cudaError_t e = cudaStreamSynchronize(b->st);
-    return e == cudaSuccess ? HS_OK : cerr(e, "batch sync");
+    if (e != cudaSuccess) return cerr(e, "batch sync");
+    if (b->precision == HS_PREC_MIXED && b->mb.err) {
+        uint32_t flag = 0;
+        e = cudaMemcpy(&flag, b->mb.err, 4, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cerr(e, "batch sync");
+        if (flag) return berr(HS_ETIMEOUT, "a bounded wait of the split step gave up; results are invalid");
+    }
+    return HS_OK;
 }
 
 int hs_batch_kernel_time(HsBatch* b, double* avg_ms, uint32_t* launches) {

@@ -317,10 +317,11 @@ __device__ __forceinline__ void forestStimulus(const MixBatch& b, const MixFores
 
 // SpikeGens (SpikeGen::process with the solver's V and currTime = dt (step+1))
 // and trace samples, one thread per cell.
-__device__ __forceinline__ void forestOutputs(const MixBatch& b, const MixForest& F, unsigned long long step) {
+__device__ __forceinline__ void forestOutputs(const MixBatch& b, const MixForest& F, unsigned long long step,
+                                              uint32_t t0, uint32_t nt) {
     const double currTime = b.dt * (double)(step + 1);
     const bool sample = ((step + 1) % b.recStride) == 0;
-    for (uint32_t k = threadIdx.x; k < F.nCells; k += blockDim.x) {
+    for (uint32_t k = t0; k < F.nCells; k += nt) {
         const uint32_t cell = b.forestCells[F.cell0 + k];
         if (step >= b.stopStep[cell]) continue;
         const MixCellRange cr = b.cells[cell];
@@ -381,6 +382,27 @@ __device__ __forceinline__ void updateNode(const MixBatch& b, uint32_t n, uint32
     }
 }
 
+// After a forest's last step (`step` = steps done): that step's update and
+// outputs, the per-cell step counts and the forest's counter.
+__device__ void finishForest(const MixBatch& b, const MixForest& F, uint32_t f, const Elim& E,
+                             unsigned long long step) {
+    const uint32_t tid = threadIdx.x, nth = blockDim.x;
+    for (uint32_t i = tid; i < F.nNodes; i += nth) {
+        const uint32_t n = F.node0 + i;
+        const uint32_t info = __ldg(b.nodeInfo + n);
+        if (info & kNodeCenter) continue;
+        if (step - 1 < b.stopStep[__ldg(b.cellOf + n)]) updateNode(b, n, info, E.R[i]);
+    }
+    __syncthreads();
+    forestOutputs(b, F, step - 1, tid, nth);
+    for (uint32_t k = tid; k < F.nCells; k += nth) {
+        const uint32_t cell = b.forestCells[F.cell0 + k];
+        b.stepCount[cell] = step < b.stopStep[cell] ? step : b.stopStep[cell];
+    }
+    if (tid == 0) b.forestStep[f] = step;
+    __syncthreads();
+}
+
 // `nsteps` steps of one forest by the whole CTA.  The V/Ca update and the
 // outputs (SpikeGens, trace samples) of a step run at the start of the next
 // step's assembly, and after the last step.  A cell whose stop step is
@@ -422,7 +444,7 @@ __device__ void stepForest(const MixBatch& b, const MixForest& F, uint32_t f, co
             E.R[i] = r;
         }
         __syncthreads();
-        if (s > 0) forestOutputs(b, F, step - 1);
+        if (s > 0) forestOutputs(b, F, step - 1, tid, nth);
         // forward elimination, deepest level first: pull the children's
         // eliminated rows (diag -= off_c * f_c, rhs -= off_c * g_c), then keep
         // g = rhs/pivot in R and f = off/pivot in D
@@ -439,7 +461,7 @@ __device__ void stepForest(const MixBatch& b, const MixForest& F, uint32_t f, co
             }
             for (uint32_t i = lp[L] + tid; i < e; i += nth) {
                 const uint32_t t = E.TOPO[i];
-                const uint32_t c0 = t & 0xFFFF, c1 = c0 + (t >> 16);
+                const uint32_t c0 = t & 0xFFFF, c1 = c0 + ((t >> 16) & 0xFF);
                 double d = E.D[i], r = E.R[i];
                 for (uint32_t c = c0; c < c1; ++c) {
                     const double oc = E.OFF[c];
@@ -466,21 +488,115 @@ __device__ void stepForest(const MixBatch& b, const MixForest& F, uint32_t f, co
         if (ahead)
             for (uint32_t k = kNext + tid; k < k1; k += nth) synapseStep(b, k, step + 1);
     }
-    // the last step's update and outputs
-    for (uint32_t i = tid; i < F.nNodes; i += nth) {
-        const uint32_t n = F.node0 + i;
-        const uint32_t info = __ldg(b.nodeInfo + n);
-        if (info & kNodeCenter) continue;
-        if (step - 1 < b.stopStep[__ldg(b.cellOf + n)]) updateNode(b, n, info, E.R[i]);
+    finishForest(b, F, f, E, step);
+}
+
+// Named barrier over `count` threads (a multiple of 32).
+__device__ __forceinline__ void groupSync(uint32_t id, uint32_t count) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+// Spin limit of an eliminator warp waiting for a level's assembly (each
+// round sleeps ~128 ns): far longer than any assembly, short enough that a
+// lost update ends the kernel with an error instead of a hang.
+constexpr uint32_t kLevelWaitRounds = 1u << 24;
+
+// The same steps as stepForest with the CTA split into two groups.  The
+// first `elimWarps` warps eliminate; the others assemble nodes deepest level
+// first and count the finished nodes of each level in `done` (shared
+// memory).  The eliminators start a level of the forward elimination as soon
+// as its count is complete, so the elimination of the deep levels overlaps
+// the assembly of the shallow ones; then they substitute back.  Meanwhile the
+// assemblers emit the previous step's outputs and advance the next step's
+// SynChans.  Forests of at most 255 levels (the level of a node is kept in
+// the top byte of its topology word).
+__device__ void stepForestWS(const MixBatch& b, const MixForest& F, uint32_t f, const Elim& E, const uint32_t* lp,
+                             uint32_t* done, uint32_t elimWarps, uint32_t nsteps) {
+    const uint32_t tid = threadIdx.x, nth = blockDim.x;
+    if (nsteps == 0) return;
+    const uint32_t nE = 32 * elimWarps, nA = nth - nE;
+    const bool elim = tid < nE;
+    const uint32_t atid = tid - nE;
+    unsigned long long step = b.forestStep[f];
+    const uint32_t k0 = __ldg(b.syn0 + F.node0), k1 = __ldg(b.syn0 + F.node0 + F.nNodes);
+    for (uint32_t k = k0 + tid; k < k1; k += nth) synapseStep(b, k, step);
+    for (uint32_t s = 0; s < nsteps; ++s, ++step) {
+        for (uint32_t L = tid; L < F.nLevels; L += nth) done[L] = 0;
+        forestStimulus(b, F, step);
+        __syncthreads();
+        if (elim) {
+            // forward elimination, each level once the assemblers finished it
+            for (int L = (int)F.nLevels - 1; L >= 0; --L) {
+                const uint32_t b0 = lp[L], e = lp[L + 1];
+                uint32_t rounds = 0;
+                while (*(volatile uint32_t*)&done[L] < e - b0) {
+                    if (++rounds > kLevelWaitRounds) {
+                        atomicExch(b.err, 1u);
+                        break;
+                    }
+                    __nanosleep(128);
+                }
+                __threadfence_block();
+                for (uint32_t i = b0 + tid; i < e; i += nE) {
+                    const uint32_t t = E.TOPO[i];
+                    const uint32_t c0 = t & 0xFFFF, c1 = c0 + ((t >> 16) & 0xFF);
+                    double d = E.D[i], r = E.R[i];
+                    for (uint32_t c = c0; c < c1; ++c) {
+                        const double oc = E.OFF[c];
+                        d = fma(-oc, E.D[c], d);
+                        r = fma(-oc, E.R[c], r);
+                    }
+                    const double iv = rcpPivot(d);
+                    E.R[i] = r * iv;
+                    E.D[i] = E.OFF[i] * iv;
+                }
+                groupSync(1, nE);
+            }
+            // back substitution
+            for (uint32_t L = 0; L < F.nLevels; ++L) {
+                const uint32_t e = lp[L + 1];
+                for (uint32_t i = lp[L] + tid; i < e; i += nE) {
+                    const uint32_t p = E.PAR[i];
+                    double vm = E.R[i];
+                    if (p != kNoParent) vm = fma(-E.D[i], E.R[p], vm);
+                    E.R[i] = vm;
+                }
+                groupSync(1, nE);
+            }
+        } else {
+            // assembly, deepest level first (the highest node indices)
+            for (uint32_t j = atid; j < F.nNodes; j += nA) {
+                const uint32_t i = F.nNodes - 1 - j;
+                if (atid < b.nPf && j + nA - atid < F.nNodes) {
+                    const uint32_t hi = F.nNodes - (j + nA - atid);     // next chunk: [hi - nA, hi)
+                    prefetchNodes(b, atid, F.node0 + (hi > nA ? hi - nA : 0), hi > nA ? nA : hi);
+                }
+                const uint32_t n = F.node0 + i;
+                const uint32_t info = __ldg(b.nodeInfo + n);
+                const unsigned long long stop = b.stopStep[__ldg(b.cellOf + n)];
+                const bool live = step < stop;
+                const bool pending = s > 0 && step - 1 < stop;
+                double d = 1.0, r = 0.0;
+                if (info & kNodeCenter) {
+                    if (live) d = __ldg(b.HS2 + n);
+                } else if (live) {
+                    assembleNode(b, n, info, pending, pending ? E.R[i] : 0.0, step, d, r);
+                } else if (pending) {
+                    updateNode(b, n, info, E.R[i]);
+                }
+                E.D[i] = d;
+                E.R[i] = r;
+                __threadfence_block();
+                atomicAdd(&done[E.TOPO[i] >> 24], 1u);
+            }
+            groupSync(2, nA);
+            if (s > 0) forestOutputs(b, F, step - 1, atid, nA);
+            if (s + 1 < nsteps)
+                for (uint32_t k = k0 + atid; k < k1; k += nA) synapseStep(b, k, step + 1);
+        }
+        __syncthreads();
     }
-    __syncthreads();
-    forestOutputs(b, F, step - 1);
-    for (uint32_t k = tid; k < F.nCells; k += nth) {
-        const uint32_t cell = b.forestCells[F.cell0 + k];
-        b.stepCount[cell] = step < b.stopStep[cell] ? step : b.stopStep[cell];
-    }
-    if (tid == 0) b.forestStep[f] = step;
-    __syncthreads();
+    finishForest(b, F, f, E, step);
 }
 
 // One CTA steps its forests one after the other, each for `nsteps` steps.
@@ -489,10 +605,11 @@ __device__ void stepForest(const MixBatch& b, const MixForest& F, uint32_t f, co
 // PAR (2 B).
 __global__ void __launch_bounds__(1024, 1) hsForestStepMixed(MixBatch b, const uint32_t* __restrict__ ctaPtr,
                                                              const uint32_t* __restrict__ ctaForests, uint32_t cap,
-                                                             uint32_t nsteps) {
+                                                             uint32_t elimWarps, uint32_t nsteps) {
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t* sLp = reinterpret_cast<uint32_t*>(smem);
-    double* sD = reinterpret_cast<double*>(smem + kSmemLevels * 4);
+    uint32_t* sDone = sLp + kSmemLevels;
+    double* sD = reinterpret_cast<double*>(smem + (kSmemLevels + kWsLevels) * 4);
     for (uint32_t k = ctaPtr[blockIdx.x]; k < ctaPtr[blockIdx.x + 1]; ++k) {
         const MixForest F = b.forests[ctaForests[k]];
         const uint32_t* lp = b.levelPtr + F.level0;
@@ -524,7 +641,10 @@ __global__ void __launch_bounds__(1024, 1) hsForestStepMixed(MixBatch b, const u
             E.PAR = b.par + F.node0;
         }
         __syncthreads();
-        stepForest(b, F, ctaForests[k], E, lp, nsteps);
+        if (elimWarps && F.nLevels <= kWsLevels - 1 && F.nLevels < kSmemLevels && blockDim.x > 32 * elimWarps)
+            stepForestWS(b, F, ctaForests[k], E, lp, sDone, elimWarps, nsteps);
+        else
+            stepForest(b, F, ctaForests[k], E, lp, nsteps);
     }
 }
 
@@ -614,10 +734,10 @@ cudaError_t uploadMixedTypes(const ChanType* ct, int nct, const C2dType* kt, int
 
 cudaError_t launchForestStepMixed(const MixBatch& b, const uint32_t* ctaPtr, const uint32_t* ctaForests,
                                   uint32_t nCtas, uint32_t threadsPerCta, uint32_t smemBytes, uint32_t cap,
-                                  uint32_t nsteps, cudaStream_t st) {
+                                  uint32_t elimWarps, uint32_t nsteps, cudaStream_t st) {
     cudaError_t e = cudaFuncSetAttribute(hsForestStepMixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes);
     if (e != cudaSuccess) return e;
-    hsForestStepMixed<<<nCtas, threadsPerCta, smemBytes, st>>>(b, ctaPtr, ctaForests, cap, nsteps);
+    hsForestStepMixed<<<nCtas, threadsPerCta, smemBytes, st>>>(b, ctaPtr, ctaForests, cap, elimWarps, nsteps);
     return cudaGetLastError();
 }
 

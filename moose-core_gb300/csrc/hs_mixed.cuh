@@ -76,6 +76,7 @@ struct SynType {           // SynChan constants at the clock dt
 constexpr uint32_t kNoParent = 0xFFFF;   // MixBatch::par of a root
 constexpr uint32_t kMaxForestNodes = 0xFFFF;
 constexpr uint32_t kSmemLevels = 1024;      // level offsets kept in shared memory
+constexpr uint32_t kWsLevels = 256;         // per-level counters of the split step
 
 // A forest: nodes [node0, node0 + nNodes), level offsets (forest-local)
 // levelPtr[level0 .. level0 + nLevels], cells forestCells[cell0 ..].
@@ -121,8 +122,9 @@ struct MixBatch {
     // per node (global index)
     const uint32_t* nodeInfo;    // flags, K(Ca) type, gate mask (bits above)
     const uint32_t* ctype4;      // 4 channel type bytes
-    const uint32_t* topo;        // forest-local first child | child count << 16
+    const uint32_t* topo;        // forest-local first child | child count << 16 | level (<= 255) << 24
     const uint16_t* par;         // forest-local parent, kNoParent for a root
+    uint32_t* err;               // set to 1 when a bounded wait gave up
     const uint32_t* injIdx;      // inject entry of a kNodeInject node
     const double *off, *HS2, *CmByDt, *EmByRm;
     double* V;

@@ -1,16 +1,17 @@
 """Autotuner for the batched HSolve: picks the packing and launch shape.
 
 The knobs (``HsBatchTuning``): threads per CTA, CTAs per SM and forest size
-(which set how cells are packed into shared-memory forests), and dt steps per
+(which set how cells are packed into shared-memory forests), the warps that
+eliminate while the others assemble (mixed precision), and dt steps per
 launch.  Every choice computes the same results (bit-identical, tested), so
 the tuner only measures: for each candidate it (re)packs the batch, reinits
 it, runs a few warm-up steps, then times ``steps`` dt steps with CUDA events
 on the batch's stream (``Batch.kernel_time``), and keeps the fastest.
 
 Search: coordinate descent from the defaults -- first the packing (CTAs per
-SM x forest size, each a re-layout), then threads per CTA, then steps per
-launch -- so the number of timed runs grows with the sum, not the product,
-of the candidate lists.  Results are cached per workload signature in a JSON
+SM x forest size, each a re-layout), then threads per CTA, eliminator warps
+and steps per launch -- so the number of timed runs grows with the sum, not
+the product, of the candidate lists.  Results are cached per workload signature in a JSON
 file so that a repeated workload skips the search.
 """
 import hashlib
@@ -24,11 +25,13 @@ from .abi import HS_PREC_FP64
 MIXED_SPACE = {
     "packing": [(1, 0), (1, 6000), (1, 4096), (2, 0)],       # (ctas_per_sm, forest_nodes)
     "threads_per_cta": [1024, 768, 512],
+    "elim_warps": [4, 5, 3],
     "steps_per_launch": [100, 50, 200],
 }
 FP64_SPACE = {
     "packing": [(4, 0), (2, 0), (8, 0)],
     "threads_per_cta": [256, 128],
+    "elim_warps": [0],
     "steps_per_launch": [100, 50, 200],
 }
 
@@ -74,9 +77,9 @@ def coordinate_descent(space, measure, start):
     best = dict(start)
     best_t = measure(best)
     trials = [(dict(best), best_t)]
-    for knob in ("packing", "threads_per_cta", "steps_per_launch"):
-        for v in space[knob]:
-            if best[knob] == v:
+    for knob in ("packing", "threads_per_cta", "elim_warps", "steps_per_launch"):
+        for v in space.get(knob, ()):
+            if best.get(knob) == v:
                 continue
             cand = dict(best)
             cand[knob] = v
@@ -102,7 +105,8 @@ def autotune(batch, dt, steps=200, warmup=50, space=None, cache=None, use_cache=
     def apply(cfg):
         cps, fn = cfg["packing"]
         batch.tune(threads_per_cta=cfg["threads_per_cta"], ctas_per_sm=cps,
-                   steps_per_launch=cfg["steps_per_launch"], forest_nodes=fn)
+                   steps_per_launch=cfg["steps_per_launch"], forest_nodes=fn,
+                   elim_warps=cfg.get("elim_warps") or 0)
         batch.reinit(dt)
 
     def measure(cfg):
@@ -118,17 +122,17 @@ def autotune(batch, dt, steps=200, warmup=50, space=None, cache=None, use_cache=
     if key in table:
         hit = table[key]
         cfg = {"packing": tuple(hit["packing"]), "threads_per_cta": hit["threads_per_cta"],
-               "steps_per_launch": hit["steps_per_launch"]}
+               "elim_warps": hit.get("elim_warps", 0), "steps_per_launch": hit["steps_per_launch"]}
         apply(cfg)
         out = dict(hit)
         out["cached"] = True
         return out
     start = {"packing": space["packing"][0], "threads_per_cta": space["threads_per_cta"][0],
-             "steps_per_launch": space["steps_per_launch"][0]}
+             "elim_warps": space.get("elim_warps", [0])[0], "steps_per_launch": space["steps_per_launch"][0]}
     best, trials = coordinate_descent(space, measure, start)
     apply(best)
     out = {"packing": list(best["packing"]), "threads_per_cta": best["threads_per_cta"],
-           "steps_per_launch": best["steps_per_launch"],
+           "elim_warps": best["elim_warps"], "steps_per_launch": best["steps_per_launch"],
            "ms_per_step": min(t for _, t in trials), "trials": len(trials)}
     if use_cache:
         table[key] = out

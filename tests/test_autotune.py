@@ -22,7 +22,7 @@ def test_coordinate_descent_finds_the_best_along_each_knob():
     start = {"packing": (1, 0), "threads_per_cta": 1024, "steps_per_launch": 100}
     best, trials = autotune.coordinate_descent(space, measure, start)
     assert best == {"packing": (1, 4096), "threads_per_cta": 512, "steps_per_launch": 200}
-    # sum, not product, of the candidate lists
+    # sum, not product, of the candidate lists (no elim_warps list here)
     assert len(trials) == 1 + 2 + 2 + 2 == len(calls)
 
 
@@ -61,7 +61,8 @@ def test_tuned_batch_computes_the_same(tmp_path):
     ref.reinit(dt)
     ref.process(300)
     b = Batch(cells, dt, HS_PREC_MIXED)
-    space = {"packing": [(1, 0), (1, 256)], "threads_per_cta": [1024, 256], "steps_per_launch": [100, 30]}
+    space = {"packing": [(1, 0), (1, 256)], "threads_per_cta": [1024, 256], "elim_warps": [4, 2],
+             "steps_per_launch": [100, 30]}
     got = autotune.autotune(b, dt, steps=60, warmup=10, space=space, cache=str(tmp_path / "c.json"))
     assert got["threads_per_cta"] in (1024, 256) and got["cached"] is False
     again = autotune.autotune(b, dt, space=space, cache=str(tmp_path / "c.json"))
