@@ -506,9 +506,9 @@ constexpr uint32_t kLevelWaitRounds = 1u << 24;
 // first and count the finished nodes of each level in `done` (shared
 // memory).  The eliminators start a level of the forward elimination as soon
 // as its count is complete, so the elimination of the deep levels overlaps
-// the assembly of the shallow ones; then they substitute back.  Meanwhile the
-// assemblers emit the previous step's outputs and advance the next step's
-// SynChans.  Forests of at most 255 levels (the level of a node is kept in
+// the assembly of the shallow ones; meanwhile the assemblers emit the
+// previous step's outputs and advance the next step's SynChans.  Then the
+// whole CTA substitutes back.  Forests of at most 255 levels (the level of a node is kept in
 // the top byte of its topology word).
 __device__ void stepForestWS(const MixBatch& b, const MixForest& F, uint32_t f, const Elim& E, const uint32_t* lp,
                              uint32_t* done, uint32_t elimWarps, uint32_t nsteps) {
@@ -552,17 +552,6 @@ __device__ void stepForestWS(const MixBatch& b, const MixForest& F, uint32_t f, 
                 }
                 groupSync(1, nE);
             }
-            // back substitution
-            for (uint32_t L = 0; L < F.nLevels; ++L) {
-                const uint32_t e = lp[L + 1];
-                for (uint32_t i = lp[L] + tid; i < e; i += nE) {
-                    const uint32_t p = E.PAR[i];
-                    double vm = E.R[i];
-                    if (p != kNoParent) vm = fma(-E.D[i], E.R[p], vm);
-                    E.R[i] = vm;
-                }
-                groupSync(1, nE);
-            }
         } else {
             // assembly, deepest level first (the highest node indices)
             for (uint32_t j = atid; j < F.nNodes; j += nA) {
@@ -595,6 +584,17 @@ __device__ void stepForestWS(const MixBatch& b, const MixForest& F, uint32_t f, 
                 for (uint32_t k = k0 + atid; k < k1; k += nA) synapseStep(b, k, step + 1);
         }
         __syncthreads();
+        // back substitution by the whole CTA
+        for (uint32_t L = 0; L < F.nLevels; ++L) {
+            const uint32_t e = lp[L + 1];
+            for (uint32_t i = lp[L] + tid; i < e; i += nth) {
+                const uint32_t p = E.PAR[i];
+                double vm = E.R[i];
+                if (p != kNoParent) vm = fma(-E.D[i], E.R[p], vm);
+                E.R[i] = vm;
+            }
+            __syncthreads();
+        }
     }
     finishForest(b, F, f, E, step);
 }
