@@ -646,7 +646,11 @@ int buildMixed(HsBatch* b) {
     std::vector<uint16_t> par(nN, (uint16_t)kNoParent);
     std::vector<double> off(nN), HS2(nN), CmByDt(nN), EmByRm(nN);
     std::vector<float> gbarS((size_t)kMaxChan * ld, 0.f);
-    std::vector<double> stateS((size_t)3 * kMaxChan * ld, 0.0);
+    std::vector<float2> stateS((size_t)3 * kMaxChan * ld, make_float2(0.f, 0.f));
+    auto pair = [](double x) {
+        const float hi = (float)x;
+        return make_float2(hi, (float)(x - (double)hi));
+    };
     std::vector<float> poolBasal(nN, 0.f), poolG1(nN, 0.f), poolF2(nN, 0.f), poolCeil(nN, 0.f), poolFloor(nN, 0.f);
     std::vector<float> k2gbar(nN, 0.f), k2x0(nN, 0.f);
     std::vector<uint8_t> synTypeV;
@@ -716,9 +720,9 @@ int buildMixed(HsBatch* b) {
                     types = (types & ~(0xFFu << (8 * j))) | ((uint32_t)ti << (8 * j));
                     gbarS[(size_t)j * ld + g] = (float)(P.Gbar[q] * P.modulation[q]);
                     int s = P.stateOff[q];
-                    if (P.Xpow[q] > 0.0) stateS[(size_t)(3 * j) * ld + g] = P.state0[s++];
-                    if (P.Ypow[q] > 0.0) stateS[(size_t)(3 * j + 1) * ld + g] = P.state0[s++];
-                    if (P.Zpow[q] > 0.0) stateS[(size_t)(3 * j + 2) * ld + g] = P.state0[s++];
+                    if (P.Xpow[q] > 0.0) stateS[(size_t)(3 * j) * ld + g] = pair(P.state0[s++]);
+                    if (P.Ypow[q] > 0.0) stateS[(size_t)(3 * j + 1) * ld + g] = pair(P.state0[s++]);
+                    if (P.Zpow[q] > 0.0) stateS[(size_t)(3 * j + 2) * ld + g] = pair(P.state0[s++]);
                     if (P.Xpow[q] > 0.0) info |= 1u << (kNodeGateShift + 3 * j);
                     if (P.Ypow[q] > 0.0) info |= 1u << (kNodeGateShift + 3 * j + 1);
                     if (P.Zpow[q] > 0.0) info |= 1u << (kNodeGateShift + 3 * j + 2);

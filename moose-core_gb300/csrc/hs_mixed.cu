@@ -80,18 +80,6 @@ __device__ __forceinline__ double widenF(float x) {
     return __hiloint2double((int)hi, (int)lo);
 }
 
-// FP64 to FP32 by truncation with integer operations (for values used only
-// as FP32 inputs: gate states in [0, 1]): exponent rebiased by -896, the top
-// 23 fraction bits kept; magnitudes below the FP32 normal range give zero.
-__device__ __forceinline__ float narrowF(double x) {
-    const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
-    const uint32_t e = (hi >> 20) & 0x7FFu;
-    const uint32_t sign = hi & 0x80000000u;
-    if (e <= 896u) return __uint_as_float(sign);
-    if (e >= 1151u) return __uint_as_float(sign | 0x7F800000u | (e == 0x7FFu && ((hi & 0xFFFFFu) | lo) ? 1u : 0u));
-    return __uint_as_float(sign | ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
-}
-
 // Lerp of the table row pair for column `col` (A at col, B at col + 1).
 __device__ __forceinline__ float2 lookupF(const RowF& r, uint32_t nCol, int col) {
     const float* ap = r.p + col;
@@ -100,18 +88,30 @@ __device__ __forceinline__ float2 lookupF(const RowF& r, uint32_t nCol, int col)
     return make_float2(fmaf(b.x - a.x, r.frac, a.x), fmaf(b.y - a.y, r.frac, a.y));
 }
 
-// New value of a gate with state x (FP64) over one step, from C1, C2 of
-// its table row.  The reference's trapezoidal step (x(2-T) + dt C1)/T with
-// T = 1 + h, h = dt/2 C2 (hsolve/HSolveActive.cpp:272-273) is the same
-// number as x + (dt C1 - 2 h x)/(1 + h); the increment is computed in FP32
-// and accumulated into the FP64 state, so that the small per-step changes
-// of slow gates are not lost to FP32 rounding of the state itself.
-// Instantaneous gates: x = C1/C2.
-__device__ __forceinline__ double gateStep(float2 C, double x, float dt, float hdt, bool inst) {
-    if (inst) return widenF(__fdividef(C.x, C.y));
-    const float xf = narrowF(x);
+// A gate state held as the unevaluated sum hi + lo of two FP32 numbers
+// (|lo| <= ulp(hi)/2), about 48 significant bits.  Adding an FP32 increment
+// uses Knuth's TwoSum (the exact rounding error of hi + d) and Dekker's
+// Fast2Sum to renormalise, all on the FP32 pipe: a plain FP32 state would
+// lose the small per-step increments of slow gates, and an FP64 add issues
+// at 1/64 of the FP32 rate on this GPU, on the pipe the elimination needs.
+__device__ __forceinline__ float2 addPair(float2 x, float d) {
+    const float s = __fadd_rn(x.x, d);
+    const float bv = __fsub_rn(s, x.x);
+    const float err = __fadd_rn(__fsub_rn(x.x, __fsub_rn(s, bv)), __fsub_rn(d, bv));
+    const float lo = __fadd_rn(x.y, err);
+    const float hi = __fadd_rn(s, lo);
+    return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
+}
+
+// New value of a gate with state x over one step, from C1, C2 of its table
+// row.  The reference's trapezoidal step (x(2-T) + dt C1)/T with T = 1 + h,
+// h = dt/2 C2 (hsolve/HSolveActive.cpp:272-273) is the same number as
+// x + (dt C1 - 2 h x)/(1 + h): the increment is computed in FP32 and added
+// to the two-float state.  Instantaneous gates: x = C1/C2.
+__device__ __forceinline__ float2 gateStep(float2 C, float2 x, float dt, float hdt, bool inst) {
+    if (inst) return make_float2(__fdividef(C.x, C.y), 0.f);
     const float h = hdt * C.y;
-    return x + widenF(__fdividef(fmaf(-2.0f * h, xf, dt * C.x), 1.0f + h));
+    return addPair(x, __fdividef(fmaf(-2.0f * h, x.x, dt * C.x), 1.0f + h));
 }
 
 __device__ __forceinline__ void interp2dF(const float* T, const float* geom, uint32_t nx, uint32_t ny,
@@ -207,25 +207,25 @@ __device__ __forceinline__ void assembleNode(const MixBatch& b, uint32_t n, uint
         const uint32_t tj = (types >> (8 * j)) & 0xFF;
         if (tj == kNoType) continue;
         const ChanType& t = c_chanTypes[tj];
-        double* st = b.state + (uint64_t)(3 * j) * ld + n;
+        float2* st = b.state + (uint64_t)(3 * j) * ld + n;
         float frac = 1.f;
         if (t.xp) {
-            const double x = gateStep(lookupF(vr, b.vCol, t.colX), st[0], dt, hdt, t.instant & 1);
+            const float2 x = gateStep(lookupF(vr, b.vCol, t.colX), st[0], dt, hdt, t.instant & 1);
             st[0] = x;
-            frac *= powi(narrowF(x), t.xp, t.xpf);
+            frac *= powi(x.x, t.xp, t.xpf);
         }
         if (t.yp) {
-            const double y = gateStep(lookupF(vr, b.vCol, t.colY), st[ld], dt, hdt, t.instant & 2);
+            const float2 y = gateStep(lookupF(vr, b.vCol, t.colY), st[ld], dt, hdt, t.instant & 2);
             st[ld] = y;
-            frac *= powi(narrowF(y), t.yp, t.ypf);
+            frac *= powi(y.x, t.yp, t.ypf);
         }
         if (t.zp) {
             float2 C;
             if (t.zCa) C = lookupF(rowF(b.caTab, b.caCol, b.caRows, ca, b.caMin, b.caMax, b.caInvDx), b.caCol, t.colZ);
             else C = lookupF(vr, b.vCol, t.colZ);
-            const double z = gateStep(C, st[2 * ld], dt, hdt, t.instant & 4);
+            const float2 z = gateStep(C, st[2 * ld], dt, hdt, t.instant & 4);
             st[2 * ld] = z;
-            frac *= powi(narrowF(z), t.zp, t.zpf);
+            frac *= powi(z.x, t.zp, t.zpf);
         }
         const float gk = gb[j] * frac;
         G += gk;
@@ -669,15 +669,16 @@ __global__ void hsReinitNodesMixed(MixBatch b, uint32_t nNodes, const double* __
         const uint32_t tj = (types >> (8 * j)) & 0xFF;
         if (tj == kNoType) break;
         const ChanType& t = c_chanTypes[tj];
-        double* st = b.state + (uint64_t)(3 * j) * ld + n;
-        if (t.xp) st[0] = gateStep(lookupF(vr, b.vCol, t.colX), 0.0, 0.f, 0.f, true);
-        if (t.yp) st[ld] = gateStep(lookupF(vr, b.vCol, t.colY), 0.0, 0.f, 0.f, true);
+        float2* st = b.state + (uint64_t)(3 * j) * ld + n;
+        const float2 z0 = make_float2(0.f, 0.f);
+        if (t.xp) st[0] = gateStep(lookupF(vr, b.vCol, t.colX), z0, 0.f, 0.f, true);
+        if (t.yp) st[ld] = gateStep(lookupF(vr, b.vCol, t.colY), z0, 0.f, 0.f, true);
         if (t.zp) {
             if (t.zCa)
                 st[2 * ld] = gateStep(lookupF(rowF(b.caTab, b.caCol, b.caRows, ca, b.caMin, b.caMax, b.caInvDx),
-                                              b.caCol, t.colZ), 0.0, 0.f, 0.f, true);
+                                              b.caCol, t.colZ), z0, 0.f, 0.f, true);
             else
-                st[2 * ld] = gateStep(lookupF(vr, b.vCol, t.colZ), 0.0, 0.f, 0.f, true);
+                st[2 * ld] = gateStep(lookupF(vr, b.vCol, t.colZ), z0, 0.f, 0.f, true);
         }
     }
     if (((info >> 8) & 0xFF) != kNoType) b.k2x[n] = k2x0[n];

@@ -25,9 +25,9 @@
 //   at most one Ca pool, one HHChannel2D per compartment; SynChans in CSR.
 //
 // Precision: rate tables, gate increments, channel conductances, K(Ca), Ca
-// pools and synapses are FP32; gate states accumulate the FP32 increments in
-// FP64; Vm, matrix assembly, forward elimination and back substitution are
-// FP64.
+// pools and synapses are FP32; gate states are two-float sums (~48 bits)
+// that accumulate the FP32 increments; Vm, matrix assembly, forward
+// elimination and back substitution are FP64.
 #pragma once
 
 #include <cstdint>
@@ -131,7 +131,7 @@ struct MixBatch {
     double *elimD, *elimR;       // elimination scratch of global forests
     float *caG, *caGE;           // Ca-feeding conductance of the step
     const float* gbar;           // [kMaxChan][ld]  Gbar * modulation
-    double* state;               // [3*kMaxChan][ld] gate states (FP64 accumulators)
+    float2* state;               // [3*kMaxChan][ld] gate states, two-float sums hi + lo
     // pool (one per node)
     float *poolC, *poolCa;
     const float *poolG1, *poolF2, *poolBasal, *poolCeil, *poolFloor;   // poolG1 = 1 - factor1
