@@ -33,8 +33,8 @@
 
 namespace hsg {
 int setLastError(int code, const std::string& msg);
-cudaError_t uploadMixedTypes(const ChanType* ct, int nct, const C2dType* kt, int nkt, const SynType* st,
-                             int nst, cudaStream_t s);
+cudaError_t uploadMixedTypes(const ChanType* ct, const ChanPow* cp, int nct, const C2dType* kt, int nkt,
+                             const SynType* st, int nst, cudaStream_t s);
 cudaError_t launchForestStepMixed(const MixBatch& b, const uint32_t* ctaPtr, const uint32_t* ctaForests,
                                   uint32_t nCtas, uint32_t threadsPerCta, uint32_t smemBytes, uint32_t cap,
                                   uint32_t elimWarps, uint32_t nsteps, cudaStream_t st);
@@ -639,7 +639,11 @@ int buildMixed(HsBatch* b) {
     std::vector<float> g2d, g2dGeom;
     std::vector<uint64_t> g2dOff;
     std::vector<uint32_t> g2dN;
-    std::vector<ChanType> ctypes;
+    struct ChanKey {          // a channel type with its general powers (for dedup)
+        ChanType t;
+        ChanPow p;
+    };
+    std::vector<ChanKey> ctypes;
     std::vector<C2dType> ktypes;
     const uint64_t ld = (nN + 31) / 32 * 32;
     std::vector<uint32_t> nodeInfo(nN), ctype4(nN), topo(nN), injIdx(nN, 0), syn0;
@@ -694,12 +698,13 @@ int buildMixed(HsBatch* b) {
                 if (q1 - q0 > (uint32_t)kMaxChan)
                     return berr(HS_ENOTSUP, "mixed batch: more than 4 HHChannels in a compartment");
                 for (uint32_t q = q0; q < q1; ++q) {
-                    ChanType ty;
-                    std::memset(&ty, 0, sizeof(ty));
+                    ChanKey key;
+                    std::memset(&key, 0, sizeof(key));
+                    ChanType& ty = key.t;
                     ty.ek = (float)P.Ek[q];
-                    ty.xp = powCode(P.Xpow[q], ty.xpf);
-                    ty.yp = powCode(P.Ypow[q], ty.ypf);
-                    ty.zp = powCode(P.Zpow[q], ty.zpf);
+                    ty.xp = powCode(P.Xpow[q], key.p.x);
+                    ty.yp = powCode(P.Ypow[q], key.p.y);
+                    ty.zp = powCode(P.Zpow[q], key.p.z);
                     ty.instant = (int8_t)P.instant[q];
                     ty.colX = (int16_t)(P.colX[q] < 0 ? 0 : P.colX[q]);
                     ty.colY = (int16_t)(P.colY[q] < 0 ? 0 : P.colY[q]);
@@ -714,7 +719,7 @@ int buildMixed(HsBatch* b) {
                             return berr(HS_ENOTSUP, "mixed batch: channel feeds another compartment's pool");
                         ty.caTarget = 1;
                     }
-                    const int ti = typeIndex(ctypes, ty, kMaxChanTypes - 1);
+                    const int ti = typeIndex(ctypes, key, kMaxChanTypes - 1);
                     if (ti < 0) return berr(HS_ENOTSUP, "mixed batch: too many channel types");
                     const uint32_t j = q - q0;
                     types = (types & ~(0xFFu << (8 * j))) | ((uint32_t)ti << (8 * j));
@@ -948,7 +953,13 @@ int buildMixed(HsBatch* b) {
     b->dCtaForests = D.up(ctaForests, st);
     b->nCtas = busy;
     if (D.err != cudaSuccess) return cerr(D.err, "mixed batch upload");
-    cudaError_t e = uploadMixedTypes(ctypes.data(), (int)ctypes.size(), ktypes.data(), (int)ktypes.size(),
+    std::vector<ChanType> ctT;
+    std::vector<ChanPow> ctP;
+    for (const ChanKey& k : ctypes) {
+        ctT.push_back(k.t);
+        ctP.push_back(k.p);
+    }
+    cudaError_t e = uploadMixedTypes(ctT.data(), ctP.data(), (int)ctT.size(), ktypes.data(), (int)ktypes.size(),
                                      nullptr, 0, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cerr(e, "mixed batch types");
@@ -1147,7 +1158,7 @@ int hs_batch_reinit(HsBatch* b, double clock_dt) {
             evStep[e2] = (uint32_t)std::min<uint64_t>(s, 0xffffffffu);
             evAct[e2] = (float)(H.evW[e2] / clock_dt);
         }
-        e = uploadMixedTypes(nullptr, 0, nullptr, 0, types.data(), (int)types.size(), b->st);
+        e = uploadMixedTypes(nullptr, nullptr, 0, nullptr, 0, types.data(), (int)types.size(), b->st);
         if (e == cudaSuccess && !norm.empty())
             e = cudaMemcpyAsync(b->dSynNorm, norm.data(), norm.size() * 4, cudaMemcpyHostToDevice, b->st);
         if (e == cudaSuccess && !evStep.empty())
@@ -1302,7 +1313,18 @@ int hs_batch_set_stop_steps(HsBatch* b, const uint64_t* stop, uint32_t n) {
     static_assert(sizeof(unsigned long long) == sizeof(uint64_t), "64-bit step counts");
     cudaError_t e = cudaMemcpyAsync(b->dStopStep, stop, (size_t)n * 8, cudaMemcpyHostToDevice, b->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
-    return e == cudaSuccess ? HS_OK : cerr(e, "stop steps");
+    if (e != cudaSuccess) return cerr(e, "stop steps");
+    uint32_t any = 0;
+    for (uint32_t c = 0; c < n; ++c) any |= stop[c] != UINT64_MAX;
+    if (any != b->mb.anyStop) {
+        // the flag is a kernel argument: a captured graph must be rebuilt
+        b->mb.anyStop = any;
+        if (b->gexec) {
+            cudaGraphExecDestroy(b->gexec);
+            b->gexec = nullptr;
+        }
+    }
+    return HS_OK;
 }
 
 int hs_batch_read_steps(HsBatch* b, uint64_t* out, uint32_t n) {

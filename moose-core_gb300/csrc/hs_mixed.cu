@@ -25,6 +25,19 @@
 namespace hsg {
 
 __constant__ ChanType c_chanTypes[kMaxChanTypes];
+__constant__ ChanPow c_chanPow[kMaxChanTypes];
+
+// Stop step of a cell (none unless the batch set some).
+__device__ __forceinline__ unsigned long long stopOf(const MixBatch& b, uint32_t cell) {
+    return b.anyStop ? b.stopStep[cell] : ~0ull;
+}
+
+__device__ __forceinline__ ChanType chanType(uint32_t tj) {
+    const uint4 v = *reinterpret_cast<const uint4*>(&c_chanTypes[tj]);
+    ChanType t;
+    *reinterpret_cast<uint4*>(&t) = v;
+    return t;
+}
 __constant__ C2dType c_c2dTypes[kMaxC2dTypes];
 __constant__ SynType c_synTypes[kMaxSynTypes];
 
@@ -206,18 +219,18 @@ __device__ __forceinline__ void assembleNode(const MixBatch& b, uint32_t n, uint
     for (int j = 0; j < kMaxChan; ++j) {
         const uint32_t tj = (types >> (8 * j)) & 0xFF;
         if (tj == kNoType) continue;
-        const ChanType& t = c_chanTypes[tj];
+        const ChanType t = chanType(tj);
         float2* st = b.state + (uint64_t)(3 * j) * ld + n;
         float frac = 1.f;
         if (t.xp) {
             const float2 x = gateStep(lookupF(vr, b.vCol, t.colX), st[0], dt, hdt, t.instant & 1);
             st[0] = x;
-            frac *= powi(x.x, t.xp, t.xpf);
+            frac *= powi(x.x, t.xp, t.xp < 0 ? c_chanPow[tj].x : 0.f);
         }
         if (t.yp) {
             const float2 y = gateStep(lookupF(vr, b.vCol, t.colY), st[ld], dt, hdt, t.instant & 2);
             st[ld] = y;
-            frac *= powi(y.x, t.yp, t.ypf);
+            frac *= powi(y.x, t.yp, t.yp < 0 ? c_chanPow[tj].y : 0.f);
         }
         if (t.zp) {
             float2 C;
@@ -225,7 +238,7 @@ __device__ __forceinline__ void assembleNode(const MixBatch& b, uint32_t n, uint
             else C = lookupF(vr, b.vCol, t.colZ);
             const float2 z = gateStep(C, st[2 * ld], dt, hdt, t.instant & 4);
             st[2 * ld] = z;
-            frac *= powi(z.x, t.zp, t.zpf);
+            frac *= powi(z.x, t.zp, t.zp < 0 ? c_chanPow[tj].z : 0.f);
         }
         const float gk = gb[j] * frac;
         G += gk;
@@ -275,7 +288,7 @@ __device__ __forceinline__ void assembleNode(const MixBatch& b, uint32_t n, uint
 // the assembly of that step adds.  Needs no Vm, so it runs ahead of the
 // assembly (see stepForest).
 __device__ __forceinline__ void synapseStep(const MixBatch& b, uint32_t k, unsigned long long step) {
-    if (step >= b.stopStep[__ldg(b.synCell + k)]) return;
+    if (step >= stopOf(b, __ldg(b.synCell + k))) return;
     const SynType& t = c_synTypes[__ldg(b.synType + k)];
     uint32_t e = b.evCur[k];
     const uint32_t end = __ldg(b.evEnd + k);
@@ -305,7 +318,7 @@ __device__ __forceinline__ void forestStimulus(const MixBatch& b, const MixFores
     for (uint32_t k = threadIdx.x; k < F.nCells; k += blockDim.x) {
         const uint32_t cell = b.forestCells[F.cell0 + k];
         const MixCellRange cr = b.cells[cell];
-        if (!cr.nStim || step >= b.stopStep[cell]) continue;
+        if (!cr.nStim || step >= stopOf(b, cell)) continue;
         uint32_t cur = b.stimCur[cell];
         while (cur < cr.nStim && b.stimStep[cr.stim0 + cur] <= step) {
             b.injVal[cr.inj0 + b.stimEntry[cr.stim0 + cur]] = b.stimValue[cr.stim0 + cur];
@@ -323,7 +336,7 @@ __device__ __forceinline__ void forestOutputs(const MixBatch& b, const MixForest
     const bool sample = ((step + 1) % b.recStride) == 0;
     for (uint32_t k = t0; k < F.nCells; k += nt) {
         const uint32_t cell = b.forestCells[F.cell0 + k];
-        if (step >= b.stopStep[cell]) continue;
+        if (step >= stopOf(b, cell)) continue;
         const MixCellRange cr = b.cells[cell];
         for (uint32_t g = cr.sg0; g < cr.sg0 + cr.nSg; ++g) {
             const double Vs = b.V[b.sgNode[g]];
@@ -391,13 +404,14 @@ __device__ void finishForest(const MixBatch& b, const MixForest& F, uint32_t f, 
         const uint32_t n = F.node0 + i;
         const uint32_t info = __ldg(b.nodeInfo + n);
         if (info & kNodeCenter) continue;
-        if (step - 1 < b.stopStep[__ldg(b.cellOf + n)]) updateNode(b, n, info, E.R[i]);
+        if (step - 1 < stopOf(b, __ldg(b.cellOf + n))) updateNode(b, n, info, E.R[i]);
     }
     __syncthreads();
     forestOutputs(b, F, step - 1, tid, nth);
     for (uint32_t k = tid; k < F.nCells; k += nth) {
         const uint32_t cell = b.forestCells[F.cell0 + k];
-        b.stepCount[cell] = step < b.stopStep[cell] ? step : b.stopStep[cell];
+        const unsigned long long stop = stopOf(b, cell);
+        b.stepCount[cell] = step < stop ? step : stop;
     }
     if (tid == 0) b.forestStep[f] = step;
     __syncthreads();
@@ -429,7 +443,7 @@ __device__ void stepForest(const MixBatch& b, const MixForest& F, uint32_t f, co
             if (tid < b.nPf && i + nth - tid < F.nNodes) prefetchNodes(b, tid, F.node0 + i + nth - tid, nth);
             const uint32_t n = F.node0 + i;
             const uint32_t info = __ldg(b.nodeInfo + n);
-            const unsigned long long stop = b.stopStep[__ldg(b.cellOf + n)];
+            const unsigned long long stop = b.anyStop ? b.stopStep[__ldg(b.cellOf + n)] : ~0ull;
             const bool live = step < stop;                  // this step advances the cell
             const bool pending = s > 0 && step - 1 < stop;  // the previous step's update
             double d = 1.0, r = 0.0;
@@ -562,7 +576,7 @@ __device__ void stepForestWS(const MixBatch& b, const MixForest& F, uint32_t f, 
                 }
                 const uint32_t n = F.node0 + i;
                 const uint32_t info = __ldg(b.nodeInfo + n);
-                const unsigned long long stop = b.stopStep[__ldg(b.cellOf + n)];
+                const unsigned long long stop = b.anyStop ? b.stopStep[__ldg(b.cellOf + n)] : ~0ull;
                 const bool live = step < stop;
                 const bool pending = s > 0 && step - 1 < stop;
                 double d = 1.0, r = 0.0;
@@ -668,7 +682,7 @@ __global__ void hsReinitNodesMixed(MixBatch b, uint32_t nNodes, const double* __
     for (int j = 0; j < kMaxChan; ++j) {
         const uint32_t tj = (types >> (8 * j)) & 0xFF;
         if (tj == kNoType) break;
-        const ChanType& t = c_chanTypes[tj];
+        const ChanType t = chanType(tj);
         float2* st = b.state + (uint64_t)(3 * j) * ld + n;
         const float2 z0 = make_float2(0.f, 0.f);
         if (t.xp) st[0] = gateStep(lookupF(vr, b.vCol, t.colX), z0, 0.f, 0.f, true);
@@ -722,10 +736,12 @@ cudaError_t launchScatterInject(double* const* addr, uint8_t* const* flag, const
     return cudaGetLastError();
 }
 
-cudaError_t uploadMixedTypes(const ChanType* ct, int nct, const C2dType* kt, int nkt, const SynType* st,
-                             int nst, cudaStream_t s) {
+cudaError_t uploadMixedTypes(const ChanType* ct, const ChanPow* cp, int nct, const C2dType* kt, int nkt,
+                             const SynType* st, int nst, cudaStream_t s) {
     cudaError_t e = cudaSuccess;
     if (nct) e = cudaMemcpyToSymbolAsync(c_chanTypes, ct, nct * sizeof(ChanType), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && nct)
+        e = cudaMemcpyToSymbolAsync(c_chanPow, cp, nct * sizeof(ChanPow), 0, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && nkt)
         e = cudaMemcpyToSymbolAsync(c_c2dTypes, kt, nkt * sizeof(C2dType), 0, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && nst)

@@ -49,14 +49,21 @@ constexpr uint32_t kNodeSyn = 1u << 3;       // has SynChans
 // bits 16..27: gate present, bit kNodeGateShift + 3*slot + gate (X, Y, Z)
 constexpr uint32_t kNodeGateShift = 16;
 
-struct ChanType {          // one HHChannel prototype (hsolve/HSolveStruct.h:55-108)
+// One HHChannel prototype (hsolve/HSolveStruct.h:55-108), 16 bytes so that
+// a kernel reads it with one vector load; general (non-integer) powers are
+// in a separate table.
+struct alignas(16) ChanType {
     float ek;
-    int8_t xp, yp, zp;     // powers 1..4, -1 general (powf), 0 absent
+    int8_t xp, yp, zp;     // powers 1..4, -1 general (the type's ChanPow), 0 absent
     int8_t instant;
-    float xpf, ypf, zpf;   // general powers
     int16_t colX, colY, colZ;   // table columns (floats) of A for X/Y/Z
     int8_t zCa;            // 1: Z gate on the Ca table with the node's pool
     int8_t caTarget;       // 1: feeds the node's pool
+};
+static_assert(sizeof(ChanType) == 16, "ChanType is one 16-byte load");
+
+struct ChanPow {           // general powers of a channel type's X, Y, Z
+    float x, y, z, pad;
 };
 
 struct C2dType {           // one HHChannel2D prototype
@@ -116,6 +123,7 @@ struct MixBatch {
     const MixForest* forests;
     unsigned long long* forestStep;      // steps done by each forest
     const unsigned long long* stopStep;  // per cell: no step at or after this one
+    uint32_t anyStop;                    // 0: no cell has a stop step
     const uint32_t* cellOf;              // per node: its cell
     const uint32_t* forestCells;
     const uint32_t* levelPtr;
