@@ -42,6 +42,10 @@ import tempfile
 import threading
 import time
 
+# concurrent kernels of the serving loop's cohorts need more hardware work
+# queues than the default 8 (set before CUDA starts in this process)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "moose-core_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -480,7 +484,7 @@ def main():
     ap.add_argument("--serve-window", type=float, default=0.5, help="s of arrivals at the offered rate")
     ap.add_argument("--serve-rate-low", type=float, default=10.0, help="a second, low arrival rate")
     ap.add_argument("--serve-window-low", type=float, default=8.0)
-    ap.add_argument("--serve-chunk", type=int, default=2000)
+    ap.add_argument("--serve-chunk", type=int, default=4000)
     ap.add_argument("--serve-admit", type=float, default=0.05, help="s between admission rounds")
     ap.add_argument("--serve-budget", type=float, default=150e9)
     args = ap.parse_args()

@@ -369,6 +369,11 @@ int hs_batch_set_stop_steps(HsBatch* b, const uint64_t* stop, uint32_t n);
 int hs_batch_read_steps(HsBatch* b, uint64_t* out, uint32_t n);
 /* Spikes recorded so far by each cell. */
 int hs_batch_read_spike_counts(HsBatch* b, uint32_t* out, uint32_t n);
+/* One round trip for a serving loop: trace samples [first, first+count)
+ * (as hs_batch_read_trace_window), each cell's step count and spike count
+ * (n_cells entries each); any output may be null. */
+int hs_batch_poll(HsBatch* b, uint32_t first, uint32_t count, double* trace, uint64_t* steps,
+                  uint32_t* spike_counts);
 /* Device memory held by the batch, in bytes. */
 int hs_batch_device_bytes(HsBatch* b, uint64_t* out);
 /* Spikes of one cell from its `first`-th on; *n = the cell's total count.

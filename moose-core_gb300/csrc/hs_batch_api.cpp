@@ -33,8 +33,6 @@
 
 namespace hsg {
 int setLastError(int code, const std::string& msg);
-cudaError_t uploadMixedTypes(const ChanType* ct, const ChanPow* cp, int nct, const C2dType* kt, int nkt,
-                             const SynType* st, int nst, cudaStream_t s);
 cudaError_t launchForestStepMixed(const MixBatch& b, const uint32_t* ctaPtr, const uint32_t* ctaForests,
                                   uint32_t nCtas, uint32_t threadsPerCta, uint32_t smemBytes, uint32_t cap,
                                   uint32_t elimWarps, uint32_t nsteps, cudaStream_t st);
@@ -59,14 +57,19 @@ uint64_t fnv(const void* p, size_t n, uint64_t h = 1469598103934665603ull) {
     return h;
 }
 
+// Device buffers allocated and freed in stream order on the batch's stream
+// (cudaMallocAsync / cudaFreeAsync from the device's pool): unlike cudaFree,
+// releasing a batch does not wait for the work of other batches running on
+// the GPU.
 struct DevBuf {
     std::vector<void*> ptrs;
     cudaError_t err = cudaSuccess;
     uint64_t bytes = 0;
+    cudaStream_t st = nullptr;
     template <class T>
     T* alloc(size_t n) {
         void* p = nullptr;
-        if (err == cudaSuccess) err = cudaMalloc(&p, (n ? n : 1) * sizeof(T));
+        if (err == cudaSuccess) err = cudaMallocAsync(&p, (n ? n : 1) * sizeof(T), st);
         if (err == cudaSuccess) {
             ptrs.push_back(p);
             bytes += (n ? n : 1) * sizeof(T);
@@ -87,7 +90,7 @@ struct DevBuf {
         return p;
     }
     void freeAll() {
-        for (void* p : ptrs) cudaFree(p);
+        for (void* p : ptrs) cudaFreeAsync(p, st);
         ptrs.clear();
         bytes = 0;
     }
@@ -136,6 +139,7 @@ struct HsBatch {
     uint32_t *dCtaPtr = nullptr, *dCtaForests = nullptr;
     uint32_t mixCap = 0, mixSmem = 0;
     unsigned long long* dStopStep = nullptr;    // mixed: per-cell stop steps
+    SynType* dSynTypes = nullptr;               // mixed: SynChan constants at the clock dt
     DevBuf buf;              // long-lived allocations
     DevBuf packBuf;          // packing arrays (replaced by retuning)
     // FP64
@@ -315,7 +319,7 @@ int buildFp64(HsBatch* b, const HsCellDesc* cells) {
         layoutCell(b->plans[c], dry, b->dcs[c], b->spikeCap, b->st, &sh[c]);
     }
     b->arena.size = dry.used + 256;
-    e = cudaMalloc(&b->arena.base, b->arena.size);
+    e = cudaMallocAsync(&b->arena.base, b->arena.size, b->st);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->arena.base, 0, b->arena.size, b->st);
     for (uint32_t c = 0; c < nC && e == cudaSuccess; ++c)
         e = layoutCell(b->plans[c], b->arena, b->dcs[c], b->spikeCap, b->st, &sh[c]);
@@ -959,9 +963,13 @@ int buildMixed(HsBatch* b) {
         ctT.push_back(k.t);
         ctP.push_back(k.p);
     }
-    cudaError_t e = uploadMixedTypes(ctT.data(), ctP.data(), (int)ctT.size(), ktypes.data(), (int)ktypes.size(),
-                                     nullptr, 0, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    m.chanTypes = D.up(ctT, st);
+    m.chanPow = D.up(ctP, st);
+    m.c2dTypes = D.up(ktypes, st);
+    b->dSynTypes = D.zeros<SynType>(kMaxSynTypes, st);
+    m.synTypes = b->dSynTypes;
+    if (D.err != cudaSuccess) return cerr(D.err, "mixed batch types");
+    cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cerr(e, "mixed batch types");
     return HS_OK;
 }
@@ -1017,6 +1025,16 @@ int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds, uint32_t n_c
     cudaError_t e = cudaGetDevice(&b->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->nSm, cudaDevAttrMultiProcessorCount, b->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        // keep freed pool memory for reuse instead of returning it at every
+        // synchronisation (batches come and go in a serving loop)
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, b->device) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        b->buf.st = b->packBuf.st = b->recBuf.st = b->injBuf.st = b->st;
+    }
     if (e != cudaSuccess) {
         delete b;
         return cerr(e, "batch stream");
@@ -1063,7 +1081,7 @@ int hs_batch_destroy(HsBatch* b) {
     b->packBuf.freeAll();
     b->recBuf.freeAll();
     b->injBuf.freeAll();
-    if (b->arena.base) cudaFree(b->arena.base);
+    if (b->arena.base) cudaFreeAsync(b->arena.base, b->st);
     if (b->st) cudaStreamDestroy(b->st);
     delete b;
     return HS_OK;
@@ -1158,7 +1176,9 @@ int hs_batch_reinit(HsBatch* b, double clock_dt) {
             evStep[e2] = (uint32_t)std::min<uint64_t>(s, 0xffffffffu);
             evAct[e2] = (float)(H.evW[e2] / clock_dt);
         }
-        e = uploadMixedTypes(nullptr, nullptr, 0, nullptr, 0, types.data(), (int)types.size(), b->st);
+        if (!types.empty())
+            e = cudaMemcpyAsync(b->dSynTypes, types.data(), types.size() * sizeof(SynType), cudaMemcpyHostToDevice,
+                                b->st);
         if (e == cudaSuccess && !norm.empty())
             e = cudaMemcpyAsync(b->dSynNorm, norm.data(), norm.size() * 4, cudaMemcpyHostToDevice, b->st);
         if (e == cudaSuccess && !evStep.empty())
@@ -1343,6 +1363,25 @@ int hs_batch_read_spike_counts(HsBatch* b, uint32_t* out, uint32_t n) {
     cudaError_t e = cudaStreamSynchronize(b->st);
     if (e == cudaSuccess) e = cudaMemcpy(out, b->mb.spikeCount, (size_t)n * 4, cudaMemcpyDeviceToHost);
     return e == cudaSuccess ? HS_OK : cerr(e, "spike counts");
+}
+
+int hs_batch_poll(HsBatch* b, uint32_t first, uint32_t count, double* trace, uint64_t* steps,
+                  uint32_t* spike_counts) {
+    if (!b) return berr(HS_EINVAL, "null batch");
+    if (b->precision != HS_PREC_MIXED) return berr(HS_ENOTSUP, "polling is a mixed-batch feature");
+    cudaError_t e = cudaSuccess;
+    if (count && trace) {
+        if (b->rec.empty()) return berr(HS_ESTATE, "nothing is recorded");
+        if ((uint64_t)first + count > b->recCap) return berr(HS_ECAPACITY, "window beyond the recording capacity");
+        e = cudaMemcpyAsync(trace, b->recBase + (size_t)first * b->rec.size(), (size_t)count * b->rec.size() * 8,
+                            cudaMemcpyDeviceToHost, b->st);
+    }
+    if (e == cudaSuccess && steps)
+        e = cudaMemcpyAsync(steps, b->mb.stepCount, (size_t)b->nCells * 8, cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess && spike_counts)
+        e = cudaMemcpyAsync(spike_counts, b->mb.spikeCount, (size_t)b->nCells * 4, cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    return e == cudaSuccess ? HS_OK : cerr(e, "batch poll");
 }
 
 int hs_batch_device_bytes(HsBatch* b, uint64_t* out) {

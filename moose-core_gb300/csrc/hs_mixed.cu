@@ -24,22 +24,19 @@
 
 namespace hsg {
 
-__constant__ ChanType c_chanTypes[kMaxChanTypes];
-__constant__ ChanPow c_chanPow[kMaxChanTypes];
 
 // Stop step of a cell (none unless the batch set some).
 __device__ __forceinline__ unsigned long long stopOf(const MixBatch& b, uint32_t cell) {
     return b.anyStop ? b.stopStep[cell] : ~0ull;
 }
 
-__device__ __forceinline__ ChanType chanType(uint32_t tj) {
-    const uint4 v = *reinterpret_cast<const uint4*>(&c_chanTypes[tj]);
+// The batch's channel type `tj` (one 16-byte read-only load).
+__device__ __forceinline__ ChanType chanType(const MixBatch& b, uint32_t tj) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(b.chanTypes + tj));
     ChanType t;
     *reinterpret_cast<uint4*>(&t) = v;
     return t;
 }
-__constant__ C2dType c_c2dTypes[kMaxC2dTypes];
-__constant__ SynType c_synTypes[kMaxSynTypes];
 
 // Reciprocal of a positive FP64 pivot: the hardware FP64 reciprocal
 // estimate (rcp.approx.ftz.f64, relative error about 1e-6 measured over
@@ -219,18 +216,18 @@ __device__ __forceinline__ void assembleNode(const MixBatch& b, uint32_t n, uint
     for (int j = 0; j < kMaxChan; ++j) {
         const uint32_t tj = (types >> (8 * j)) & 0xFF;
         if (tj == kNoType) continue;
-        const ChanType t = chanType(tj);
+        const ChanType t = chanType(b, tj);
         float2* st = b.state + (uint64_t)(3 * j) * ld + n;
         float frac = 1.f;
         if (t.xp) {
             const float2 x = gateStep(lookupF(vr, b.vCol, t.colX), st[0], dt, hdt, t.instant & 1);
             st[0] = x;
-            frac *= powi(x.x, t.xp, t.xp < 0 ? c_chanPow[tj].x : 0.f);
+            frac *= powi(x.x, t.xp, t.xp < 0 ? __ldg(&b.chanPow[tj].x) : 0.f);
         }
         if (t.yp) {
             const float2 y = gateStep(lookupF(vr, b.vCol, t.colY), st[ld], dt, hdt, t.instant & 2);
             st[ld] = y;
-            frac *= powi(y.x, t.yp, t.yp < 0 ? c_chanPow[tj].y : 0.f);
+            frac *= powi(y.x, t.yp, t.yp < 0 ? __ldg(&b.chanPow[tj].y) : 0.f);
         }
         if (t.zp) {
             float2 C;
@@ -238,7 +235,7 @@ __device__ __forceinline__ void assembleNode(const MixBatch& b, uint32_t n, uint
             else C = lookupF(vr, b.vCol, t.colZ);
             const float2 z = gateStep(C, st[2 * ld], dt, hdt, t.instant & 4);
             st[2 * ld] = z;
-            frac *= powi(z.x, t.zp, t.zp < 0 ? c_chanPow[tj].z : 0.f);
+            frac *= powi(z.x, t.zp, t.zp < 0 ? __ldg(&b.chanPow[tj].z) : 0.f);
         }
         const float gk = gb[j] * frac;
         G += gk;
@@ -254,7 +251,7 @@ __device__ __forceinline__ void assembleNode(const MixBatch& b, uint32_t n, uint
     }
     // ---- HHChannel2D (K(Ca)) on this step's Vm and Ca
     if (k2 != kNoType) {
-        const C2dType& t = c_c2dTypes[k2];
+        const C2dType& t = b.c2dTypes[k2];
         const float x = t.dep0 == 0 ? v : t.dep0 == 1 ? ca : 0.f;
         const float y = t.dep1 == 0 ? v : t.dep1 == 1 ? ca : 0.f;
         float A, B;
@@ -289,7 +286,7 @@ __device__ __forceinline__ void assembleNode(const MixBatch& b, uint32_t n, uint
 // assembly (see stepForest).
 __device__ __forceinline__ void synapseStep(const MixBatch& b, uint32_t k, unsigned long long step) {
     if (step >= stopOf(b, __ldg(b.synCell + k))) return;
-    const SynType& t = c_synTypes[__ldg(b.synType + k)];
+    const SynType& t = b.synTypes[__ldg(b.synType + k)];
     uint32_t e = b.evCur[k];
     const uint32_t end = __ldg(b.evEnd + k);
     const float sx = b.synX[k], sy = b.synY[k], nm = __ldg(b.synNorm + k);
@@ -682,7 +679,7 @@ __global__ void hsReinitNodesMixed(MixBatch b, uint32_t nNodes, const double* __
     for (int j = 0; j < kMaxChan; ++j) {
         const uint32_t tj = (types >> (8 * j)) & 0xFF;
         if (tj == kNoType) break;
-        const ChanType t = chanType(tj);
+        const ChanType t = chanType(b, tj);
         float2* st = b.state + (uint64_t)(3 * j) * ld + n;
         const float2 z0 = make_float2(0.f, 0.f);
         if (t.xp) st[0] = gateStep(lookupF(vr, b.vCol, t.colX), z0, 0.f, 0.f, true);
@@ -734,19 +731,6 @@ cudaError_t launchScatterInject(double* const* addr, uint8_t* const* flag, const
     if (!n) return cudaSuccess;
     hsScatterInject<<<(n + 255) / 256, 256, 0, st>>>(addr, flag, val, n);
     return cudaGetLastError();
-}
-
-cudaError_t uploadMixedTypes(const ChanType* ct, const ChanPow* cp, int nct, const C2dType* kt, int nkt,
-                             const SynType* st, int nst, cudaStream_t s) {
-    cudaError_t e = cudaSuccess;
-    if (nct) e = cudaMemcpyToSymbolAsync(c_chanTypes, ct, nct * sizeof(ChanType), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess && nct)
-        e = cudaMemcpyToSymbolAsync(c_chanPow, cp, nct * sizeof(ChanPow), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess && nkt)
-        e = cudaMemcpyToSymbolAsync(c_c2dTypes, kt, nkt * sizeof(C2dType), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess && nst)
-        e = cudaMemcpyToSymbolAsync(c_synTypes, st, nst * sizeof(SynType), 0, cudaMemcpyHostToDevice, s);
-    return e;
 }
 
 cudaError_t launchForestStepMixed(const MixBatch& b, const uint32_t* ctaPtr, const uint32_t* ctaForests,

@@ -114,6 +114,11 @@ struct PrefetchArr {
 
 struct MixBatch {
     uint32_t nCells;
+    // prototypes of this batch (read-only device tables)
+    const ChanType* chanTypes;
+    const ChanPow* chanPow;
+    const C2dType* c2dTypes;
+    const SynType* synTypes;     // at the clock dt, written by reinit
     uint64_t ld;                 // slot stride (number of nodes, padded)
     float dtf;
     double dt;

@@ -165,6 +165,18 @@ class Batch:
                                                                 self.n))
         return out
 
+    def poll(self, first, count):
+        """(trace samples [first, first+count), step counts, spike counts) in
+        one device round trip.  Mixed precision only."""
+        ncol = len(self._rec[0]) if self._rec else 0
+        tr = np.empty((count, ncol)) if count else None
+        st = np.empty(self.n, np.uint64)
+        sc = np.empty(self.n, np.uint32)
+        _native.check(_native.load().hs_batch_poll(
+            self._h, int(first), int(count), tr.ctypes.data_as(C.POINTER(C.c_double)) if count else None,
+            st.ctypes.data_as(C.POINTER(C.c_uint64)), sc.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return tr, st, sc
+
     def device_bytes(self):
         v = C.c_uint64()
         _native.check(_native.load().hs_batch_device_bytes(self._h, C.byref(v)))

@@ -26,9 +26,18 @@ only on its own cell): the tests compare each request served in a mix with
 the same request run alone.
 """
 import dataclasses
+import os
 import time
 
 import numpy as np
+
+# Kernels of different streams run concurrently only up to the number of
+# hardware work queues the CUDA context opens (8 unless this variable says
+# otherwise, 32 at most); more running cohorts than queues would share queues
+# and run one after another.  It must be set before CUDA starts in the
+# process: importing this module early (or setting it in the environment)
+# does that.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 from .abi import HS_PREC_MIXED
 from .batch import Batch
@@ -96,6 +105,7 @@ class _Cohort:
         self.spikes = [[] for _ in reqs]
         self.done = np.zeros(n, bool)
         self.bytes = self.batch.device_bytes()
+        self.ctas = self.batch.info()["n_ctas"]
 
     def launch(self, chunk):
         self.batch.process(chunk)
@@ -108,8 +118,9 @@ class _Cohort:
         """Stream the samples and spikes of the last chunk; return the
         indices of requests that completed with it."""
         last = min(self.launched // self.stride, self.cap - 1)
-        if last >= self.next_sample:
-            rows = self.batch.trace_window(self.next_sample, last - self.next_sample + 1)
+        count = last - self.next_sample + 1 if last >= self.next_sample else 0
+        rows, steps, counts = self.batch.poll(self.next_sample, count)
+        if count:
             for i, r in enumerate(self.reqs):
                 if self.done[i]:
                     continue
@@ -117,12 +128,10 @@ class _Cohort:
                 if k_end >= self.next_sample:
                     self.vm[i].append(rows[: k_end - self.next_sample + 1, i].copy())
             self.next_sample = last + 1
-        counts = self.batch.spike_counts()
         for i in np.nonzero(counts > self.spikes_seen)[0]:
             _, t, _ = self.batch.cell_spikes(int(i), int(self.spikes_seen[i]))
             self.spikes[i].append(t)
             self.spikes_seen[i] += len(t)
-        steps = self.batch.steps()
         fresh = [i for i, r in enumerate(self.reqs) if not self.done[i] and steps[i] >= r.n_steps]
         for i in fresh:
             self.done[i] = True
@@ -135,12 +144,17 @@ class _Cohort:
 class Server:
     """The serving loop.  ``budget_bytes`` bounds the device memory of the
     running cohorts; ``chunk`` is the number of dt steps a cohort advances
-    between two polls of its output.  With ``dense`` a cohort is packed into
-    as few CTAs as forests of about ``forest_nodes`` nodes need."""
+    between two polls of its output.  A cohort gets one CTA per request while
+    the GPU's ``sms`` SMs have room; once they are taken (and with ``dense``)
+    it is packed into as few CTAs as forests of about ``forest_nodes`` nodes
+    need.  At most
+    ``max_cohorts`` cohorts run at once (the hardware work queues of the
+    context); requests that arrive meanwhile wait and start together as the
+    next cohort."""
 
-    def __init__(self, dt, budget_bytes=150 * 10**9, chunk=2000, record_stride=40, max_cohort=4096,
-                 admit_interval=0.05, dense=True, forest_nodes=7000, tuning=None, clock=time.perf_counter,
-                 cohort_factory=None):
+    def __init__(self, dt, budget_bytes=150 * 10**9, chunk=4000, record_stride=40, max_cohort=4096,
+                 admit_interval=0.05, dense=True, forest_nodes=7000, max_cohorts=32, sms=152, tuning=None,
+                 clock=time.perf_counter, cohort_factory=None):
         self.dt = dt
         self.budget = budget_bytes
         self.chunk = chunk
@@ -149,6 +163,8 @@ class Server:
         self.admit_interval = admit_interval
         self.dense = dense
         self.forest_nodes = forest_nodes
+        self.max_cohorts = max_cohorts
+        self.sms = sms
         self.tuning = dict(tuning or {})
         self.clock = clock
         self.cohort_factory = cohort_factory or _Cohort
@@ -176,11 +192,17 @@ class Server:
         if not take:
             return None
         tuning = dict(self.tuning)
-        if self.dense and "max_ctas" not in tuning:
-            # as few CTAs as full forests need: one forest per CTA, each SM
-            # well used, the other SMs left to the other cohorts
-            nodes = sum(int(1.3 * r.cell.n_compt) for r in take)
-            tuning["max_ctas"] = max(1, -(-nodes // self.forest_nodes))
+        if "max_ctas" not in tuning:
+            busy = sum(getattr(c, "ctas", 0) for c in self.cohorts)
+            if busy + len(take) <= self.sms or not self.dense:
+                # room on the GPU: one CTA (one SM) per request, each runs
+                # as fast as alone
+                tuning["max_ctas"] = len(take)
+            else:
+                # the SMs are taken: as few CTAs as full forests need, each
+                # SM well used
+                nodes = sum(int(1.3 * r.cell.n_compt) for r in take)
+                tuning["max_ctas"] = max(1, -(-nodes // self.forest_nodes))
         return self.cohort_factory(take, self.dt, self.stride, self.chunk, now, tuning)
 
     def run(self, requests, real_time=True, t0=None):
@@ -195,7 +217,7 @@ class Server:
             while pending and (not real_time or pending[0].arrival <= now):
                 self.waiting.append(pending.pop(0))
             progressed = False
-            if self.waiting and now - last_admit >= self.admit_interval:
+            if self.waiting and now - last_admit >= self.admit_interval and len(self.cohorts) < self.max_cohorts:
                 fresh = self._admit(now)
                 last_admit = now
                 if fresh is not None:

@@ -154,3 +154,29 @@ def test_mixed_edge_cases_against_the_oracle():
             oc.step(250)
             worst = max(worst, float(np.abs(b.vm(i) - oc.vm()).max()))
     assert worst <= 1e-4, "max |dVm| = %g V" % worst
+
+
+def test_concurrent_batches_keep_their_own_prototypes():
+    """Two mixed batches with different channel sets on one GPU: creating
+    and stepping the second does not change what the first computes (each
+    batch carries its own channel, K(Ca) and SynChan tables)."""
+    cells_a = small_population(5, 31, n_syn=4)
+    cells_b = [models.config1_cell(n_cable=40, inject=0.4e-9) for _ in range(3)]
+    ref = Batch(cells_a, DT, HS_PREC_MIXED)
+    ref.reinit(DT)
+    ref.process(400)
+    a = Batch(cells_a, DT, HS_PREC_MIXED)
+    a.reinit(DT)
+    a.process(200)
+    b = Batch(cells_b, DT, HS_PREC_MIXED)
+    b.reinit(DT)
+    b.process(100)
+    a.process(200)
+    b.process(100)
+    for i in range(len(cells_a)):
+        assert np.array_equal(a.vm(i), ref.vm(i)), i
+    solo = Batch(cells_b, DT, HS_PREC_MIXED)
+    solo.reinit(DT)
+    solo.process(200)
+    for i in range(len(cells_b)):
+        assert np.array_equal(b.vm(i), solo.vm(i)), i
