@@ -204,9 +204,9 @@ int repack(HsBatch* b) {
     if (b->precision != HS_PREC_FP64) return HS_OK;
     b->packBuf.freeAll();
     b->packBuf.err = cudaSuccess;
-    const uint32_t teamsPerCta = b->threadsPerCta / 32;
+    const uint32_t warpsPerCta = b->threadsPerCta / 32;
     b->nCtas = std::max<uint32_t>(1, b->nSm * b->ctasPerSm);
-    b->nWarps = b->nCtas * teamsPerCta;
+    b->nWarps = b->nCtas * warpsPerCta;
     std::vector<double> cost(b->nCells);
     for (uint32_t c = 0; c < b->nCells; ++c) {
         const CellPlan& P = b->plans[c];
@@ -223,24 +223,24 @@ int repack(HsBatch* b) {
         Item it = cta.top();
         cta.pop();
         ctaCells[it.second].push_back(c);
-        // a CTA runs its teams concurrently: its load is spread over them
-        cta.push({it.first + cost[c] / teamsPerCta, it.second});
+        // a CTA runs its warps concurrently: its load is spread over them
+        cta.push({it.first + cost[c] / warpsPerCta, it.second});
     }
-    std::vector<std::vector<uint32_t>> teamCells(b->nWarps);
+    std::vector<std::vector<uint32_t>> warpCells(b->nWarps);
     for (uint32_t k = 0; k < b->nCtas; ++k) {
         std::priority_queue<Item, std::vector<Item>, std::greater<Item>> wq;
-        for (uint32_t w = 0; w < teamsPerCta; ++w) wq.push({0.0, k * teamsPerCta + w});
+        for (uint32_t w = 0; w < warpsPerCta; ++w) wq.push({0.0, k * warpsPerCta + w});
         for (uint32_t c : ctaCells[k]) {
             Item it = wq.top();
             wq.pop();
-            teamCells[it.second].push_back(c);
+            warpCells[it.second].push_back(c);
             wq.push({it.first + cost[c], it.second});
         }
     }
     std::vector<uint32_t> ptr(b->nWarps + 1, 0), cells;
     for (uint32_t w = 0; w < b->nWarps; ++w) {
-        ptr[w + 1] = ptr[w] + (uint32_t)teamCells[w].size();
-        cells.insert(cells.end(), teamCells[w].begin(), teamCells[w].end());
+        ptr[w + 1] = ptr[w] + (uint32_t)warpCells[w].size();
+        cells.insert(cells.end(), warpCells[w].begin(), warpCells[w].end());
     }
     b->dWarpPtr = b->packBuf.up(ptr, b->st);
     b->dWarpCells = b->packBuf.up(cells, b->st);
