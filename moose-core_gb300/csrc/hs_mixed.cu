@@ -548,18 +548,37 @@ __device__ void stepForestWS(const MixBatch& b, const MixForest& F, uint32_t f, 
                     __nanosleep(128);
                 }
                 __threadfence_block();
-                for (uint32_t i = b0 + tid; i < e; i += nE) {
-                    const uint32_t t = E.TOPO[i];
+                if (2 * (e - b0) <= nE) {
+                    // a narrow level: two lanes per node, the even one on the
+                    // pivot (D), the odd one on the right-hand side (R), so
+                    // that each child costs one FP64 warp instruction instead
+                    // of two (the FP64 cost is per warp instruction)
+                    const uint32_t i = b0 + (tid >> 1);
+                    const bool rl = tid & 1u;
+                    const bool on = i < e;
+                    const uint32_t t = on ? E.TOPO[i] : 0u;
                     const uint32_t c0 = t & 0xFFFF, c1 = c0 + ((t >> 16) & 0xFF);
-                    double d = E.D[i], r = E.R[i];
-                    for (uint32_t c = c0; c < c1; ++c) {
-                        const double oc = E.OFF[c];
-                        d = fma(-oc, E.D[c], d);
-                        r = fma(-oc, E.R[c], r);
+                    double* const A = rl ? E.R : E.D;
+                    double x = on ? A[i] : 1.0;
+                    for (uint32_t c = c0; c < c1; ++c) x = fma(-E.OFF[c], A[c], x);
+                    const double ivd = rcpPivot(x);
+                    const double iv = __shfl_sync(0xFFFFFFFFu, ivd, (tid & 31u) & ~1u);
+                    const double y = (rl ? x : (on ? E.OFF[i] : 0.0)) * iv;
+                    if (on) A[i] = y;
+                } else {
+                    for (uint32_t i = b0 + tid; i < e; i += nE) {
+                        const uint32_t t = E.TOPO[i];
+                        const uint32_t c0 = t & 0xFFFF, c1 = c0 + ((t >> 16) & 0xFF);
+                        double d = E.D[i], r = E.R[i];
+                        for (uint32_t c = c0; c < c1; ++c) {
+                            const double oc = E.OFF[c];
+                            d = fma(-oc, E.D[c], d);
+                            r = fma(-oc, E.R[c], r);
+                        }
+                        const double iv = rcpPivot(d);
+                        E.R[i] = r * iv;
+                        E.D[i] = E.OFF[i] * iv;
                     }
-                    const double iv = rcpPivot(d);
-                    E.R[i] = r * iv;
-                    E.D[i] = E.OFF[i] * iv;
                 }
                 groupSync(1, nE);
             }
