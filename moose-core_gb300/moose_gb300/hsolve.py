@@ -227,3 +227,12 @@ class HSolve:
 
     def add_gkek(self, compt, gk, ek):
         _native.check(_native.load().hs_add_gkek(self._h, compt, gk, ek))
+
+    def add_conc(self, chan, conc):
+        """The `concen` message of a zombie HHChannel (HSolve::addConc): the
+        external concentration its Ca-dependent gate reads."""
+        _native.check(_native.load().hs_add_conc(self._h, chan, conc))
+
+    def add_ica(self, pool, ica):
+        """The `current` message of a zombie CaConc (HSolve::iCa)."""
+        _native.check(_native.load().hs_add_ica(self._h, pool, ica))

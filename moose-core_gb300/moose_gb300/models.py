@@ -214,16 +214,18 @@ def config1_cell(n_cable=200, inject=0.5e-9, t_on=0.05, t_off=0.45, dt=25e-6):
 def active_cell(parent, d, L, inject=0.5e-9, n_syn=0, syn_rate=5.0, t_end=1.0,
                 rng=None, gca=5.0, gkca=50.0, kca_tables=None, ca_thickness=0.1e-6,
                 syn_weight_median=0.5e-9, syn_weight_sigma=0.5, cadivs=CADIVS,
-                inject_step=0):
+                inject_step=0, passive_props=None):
     """HH Na/K + Ca(HVA) + K(Ca) HHChannel2D + CaConc on every compartment.
 
     The Ca channel feeds the compartment's CaConc (IkOut -> current, HSolve's
     caTarget) and the CaConc feeds the K(Ca) channel's conc1 (concOut).
     Optionally `n_syn` SynChans (tau1 1 ms, tau2 3 ms, Ek 0) at random
     compartments, each driven by a Poisson train at `syn_rate`.
+    `passive_props` = (Ra, Rm, Cm, area) replaces the passive values derived
+    from d and L (e.g. those of a morphology loaded from a file).
     """
     n = len(parent)
-    Ra, Rm, Cm, area = passive(d, L)
+    Ra, Rm, Cm, area = passive(d, L) if passive_props is None else passive_props
     (mA, mB), (hA, hB) = hh_na_tables()
     nA, nB = hh_k_tables()
     (cxA, cxB), (cyA, cyB) = ca_hva_tables()
