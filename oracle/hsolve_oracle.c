@@ -1397,6 +1397,40 @@ int orc_set_field(OrcCell* c, int kind, int field, uint32_t index, double value)
     return HS_EINVAL;
 }
 
+/* Message destinations of the solver, model indices (hsolve/HSolveInterface.cpp).
+ * HSolve::addInject (:213-219): injectVarying += value (the map entry is made
+ * if absent); consumed and zeroed by the next updateMatrix. */
+int orc_add_inject(OrcCell* c, uint32_t compt, double value) {
+    if (compt >= c->d->n_compt || c->hinesOf[compt] == UINT32_MAX) return HS_EINVAL;
+    uint32_t i = c->hinesOf[compt];
+    c->injPresent[i] = 1;
+    c->injectVarying[i] += value;
+    return 0;
+}
+
+/* HSolve::addGkEk (:247-252): externalCurrent[2i] += Gk, [2i+1] += Gk Ek. */
+int orc_add_gkek(OrcCell* c, uint32_t compt, double Gk, double Ek) {
+    if (compt >= c->d->n_compt || c->hinesOf[compt] == UINT32_MAX) return HS_EINVAL;
+    uint32_t i = c->hinesOf[compt];
+    c->externalCurrent[2 * i] += Gk;
+    c->externalCurrent[2 * i + 1] += Gk * Ek;
+    return 0;
+}
+
+/* HSolve::addConc (:254-259): externalCalcium[channel] = conc. */
+int orc_add_conc(OrcCell* c, uint32_t chan, double conc) {
+    if (chan >= c->d->n_chan || c->chanSolverOf[chan] < 0) return HS_EINVAL;
+    c->externalCalcium[c->chanSolverOf[chan]] = conc;
+    return 0;
+}
+
+/* HSolve::iCa (:469-480): caActivation[pool] += iCa. */
+int orc_add_ica(OrcCell* c, uint32_t pool, double ica) {
+    if (pool >= c->d->n_pool || c->poolSolverOf[pool] < 0) return HS_EINVAL;
+    c->caActivation[c->poolSolverOf[pool]] += ica;
+    return 0;
+}
+
 void orc_destroy(OrcCell* c) {
     if (!c) return;
     free(c->compartmentId); free(c->hinesOf); free(c->V); free(c->CmByDt); free(c->EmByRm);

@@ -72,6 +72,12 @@ void orc_table_grid(const OrcCell* c, double* g6);
 /* Field access mirroring HSolveInterface (model indices). */
 int orc_get_field(const OrcCell* c, int kind, int field, uint32_t index, double* out);
 int orc_set_field(OrcCell* c, int kind, int field, uint32_t index, double value);
+/* Message destinations (HSolve::addInject, addGkEk, addConc, iCa), model
+ * indices; 0 or HS_EINVAL. */
+int orc_add_inject(OrcCell* c, uint32_t compt, double value);
+int orc_add_gkek(OrcCell* c, uint32_t compt, double Gk, double Ek);
+int orc_add_conc(OrcCell* c, uint32_t chan, double conc);
+int orc_add_ica(OrcCell* c, uint32_t pool, double ica);
 
 /* Passive known-answer interface (HinesMatrix/HSolvePassive unit tests):
  * tree given directly in Hines order as child lists (CSR). */

@@ -64,6 +64,11 @@ def lib():
         L.orc_get_field.argtypes = [vp, C.c_int, C.c_int, C.c_uint32, pd]
         L.orc_set_field.restype = C.c_int
         L.orc_set_field.argtypes = [vp, C.c_int, C.c_int, C.c_uint32, C.c_double]
+        for f in ("orc_add_inject", "orc_add_conc", "orc_add_ica"):
+            getattr(L, f).restype = C.c_int
+            getattr(L, f).argtypes = [vp, C.c_uint32, C.c_double]
+        L.orc_add_gkek.restype = C.c_int
+        L.orc_add_gkek.argtypes = [vp, C.c_uint32, C.c_double, C.c_double]
         L.orc_passive_create.restype = vp
         L.orc_passive_create.argtypes = [C.c_uint32, pu, pu, pd, pd, pd, pd, pd, C.c_double]
         for f in ("orc_passive_update", "orc_forward", "orc_backward"):
@@ -148,6 +153,23 @@ class OracleCell:
     def set(self, kind, field, index, value):
         if lib().orc_set_field(self.h, kind, field, index, float(value)):
             raise IndexError("oracle set_field failed")
+
+    # message destinations (HSolve::addInject, addGkEk, addConc, iCa)
+    def add_inject(self, compt, value):
+        if lib().orc_add_inject(self.h, int(compt), float(value)):
+            raise IndexError("oracle add_inject failed")
+
+    def add_gkek(self, compt, gk, ek):
+        if lib().orc_add_gkek(self.h, int(compt), float(gk), float(ek)):
+            raise IndexError("oracle add_gkek failed")
+
+    def add_conc(self, chan, conc):
+        if lib().orc_add_conc(self.h, int(chan), float(conc)):
+            raise IndexError("oracle add_conc failed")
+
+    def add_ica(self, pool, ica):
+        if lib().orc_add_ica(self.h, int(pool), float(ica)):
+            raise IndexError("oracle add_ica failed")
 
 
 class OraclePassive:

@@ -21,3 +21,23 @@ def load_model(z, prefix="model_"):
         gates2d.append((float(r[0]), float(r[1]), float(r[2]), float(r[3]), AB[0], AB[1]))
     meta = {k[5:]: z[k] for k in z.files if k.startswith("meta_")}
     return CellModel(seed=int(z[prefix + "seed"]), gates=gates, gates2d=gates2d, meta=meta, **kw)
+
+
+def replay_messages(z, solver, per_step):
+    """Drive `solver` (oracle or GPU drop-in) with the values the reference's
+    StimulusTables sent at each step (inject, external conc, Ca current) and
+    sample Vm/Ca like the reference's Tables."""
+    rec, recp = z["rec"], z["rec_pool"]
+    stride, n = int(z["stride"]), int(z["nsteps"])
+    vm, ca = [solver.vm()[rec]], [solver.ca()[recp]]
+    for k in range(n):
+        solver.add_inject(0, z["sent_inject"][k])
+        for c in z["ext"]:
+            solver.add_conc(int(c), z["sent_conc"][k])
+        solver.add_ica(0, z["sent_ica"][k])
+        per_step(solver)
+        if (k + 1) % stride == 0:
+            vm.append(solver.vm()[rec])
+            ca.append(solver.ca()[recp])
+    return np.array(vm).T, np.array(ca).T
+

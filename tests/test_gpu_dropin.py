@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from loader import load_model
+from loader import load_model, replay_messages
 from moose_gb300 import models
 from moose_gb300.abi import HS_KIND_CHAN, HS_KIND_COMPT, HS_KIND_POOL, FIELDS, CellModel
 from moose_gb300.hsolve import HSolve
@@ -144,3 +144,42 @@ def test_process_in_chunks_equals_one_call():
     for _ in range(30):
         b.process(100)
     assert np.array_equal(a.vm(), b.vm())
+
+
+def test_message_destinations_golden_bit_exact():
+    """addInject, addConc, iCa through the C ABI each step, and SK gates on
+    the compartment's CaConc: bit-exact with the reference HSolve driven by
+    StimulusTables (active_msgs.npz; no libm call on this path)."""
+    z = np.load(os.path.join(GOLDEN, "active_msgs.npz"))
+    m = load_model(z)
+    dt = float(z["dt"])
+    h = HSolve(m, dt=dt)
+    h.target = m.seed
+    assert [getattr(h, k) for k in ("vMin", "vMax", "vDiv", "caMin", "caMax", "caDiv")] == list(z["grid"])
+    h.reinit(dt)
+    vm, ca = replay_messages(z, h, lambda s: s.process(1))
+    assert np.array_equal(vm, z["vm"])
+    assert np.array_equal(ca, z["ca"])
+    assert np.array_equal(h.vm(), z["final_vm"])
+
+
+def test_add_gkek_matches_oracle():
+    """HSolve::addGkEk (external channel currents) on random compartments,
+    every step: bit-exact with the oracle."""
+    z = np.load(os.path.join(GOLDEN, "active_msgs.npz"))
+    m = load_model(z)
+    h = HSolve(m, dt=25e-6)
+    h.target = m.seed
+    h.reinit(25e-6)
+    oc = OracleCell(m, 25e-6)
+    oc.reinit(25e-6)
+    rng = np.random.default_rng(3)
+    for k in range(300):
+        for c in rng.integers(0, m.n_compt, 3):
+            g, e = float(rng.uniform(0, 5e-9)), float(rng.uniform(-0.09, 0.05))
+            h.add_gkek(int(c), g, e)
+            oc.add_gkek(int(c), g, e)
+        h.process(1)
+        oc.step(1)
+    assert np.array_equal(h.vm(), oc.vm())
+    assert np.array_equal(h.ca(), oc.ca())

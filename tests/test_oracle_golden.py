@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from loader import load_model
+from loader import load_model, replay_messages
 from oracle import OracleCell, OraclePassive
 
 H = lambda v: np.array([float.fromhex(x) for x in v])
@@ -86,3 +86,19 @@ def test_table_grid_matches_reference():
     oc = OracleCell(load_model(z), float(z["dt"]))
     g = oc.table_grid()
     assert np.array_equal(g[:3], z["grid"][:3])
+
+
+def test_message_destinations_and_ca_gates_bit_exact():
+    """addInject, addConc (external Ca of an SK gate, V row while it is 0),
+    iCa, and SK gates on the compartment's own CaConc, against the reference
+    HSolve driven by StimulusTables (active_msgs.npz)."""
+    z = np.load(os.path.join(GOLDEN, "active_msgs.npz"))
+    m = load_model(z)
+    dt = float(z["dt"])
+    oc = OracleCell(m, dt)
+    assert np.array_equal(oc.table_grid(), z["grid"])
+    oc.reinit(dt)
+    vm, ca = replay_messages(z, oc, lambda s: s.step(1))
+    assert np.array_equal(vm, z["vm"])
+    assert np.array_equal(ca, z["ca"])
+    assert np.array_equal(oc.vm(), z["final_vm"])
