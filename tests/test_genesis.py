@@ -1,0 +1,98 @@
+"""GENESIS .p loading (moose_gb300.genesis) against what the reference's
+ReadCell builds.
+
+tests/golden/genesis/*.p are seeded synthetic cell files; genesis_golden.npz
+holds, for each, every compartment the reference loadModel made (creation
+order), every channel's Gbar and Ek, CaConc B after zombification, SpikeGen
+thresholds and an HSolve run with a soma inject (written by
+tests/golden/make_golden_genesis.py, which also defines the channel library
+used here).  The bar is bit-for-bit equality.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from moose_gb300 import genesis
+from oracle import OracleCell
+
+sys.path.insert(0, GOLDEN)
+from make_golden_genesis import library  # noqa: E402
+
+Z = np.load(os.path.join(GOLDEN, "genesis_golden.npz"))
+FILES = sorted({k.split("/")[0] for k in Z.files if "/" in k})
+LIB = library(Z)
+
+
+def path(name):
+    return os.path.join(GOLDEN, "genesis", name + ".p")
+
+
+@pytest.mark.parametrize("name", FILES)
+def test_compartments_bit_exact(name):
+    m = genesis.load_p(path(name), LIB)
+    assert m.meta["names"] == list(Z[name + "/names"])
+    assert np.array_equal(m.parent, Z[name + "/parent"])
+    for f in ("Ra", "Rm", "Cm", "Em", "initVm"):
+        assert np.array_equal(getattr(m, f), Z[name + "/" + f]), f
+    assert np.array_equal(m.meta["diameter"], Z[name + "/diameter"])
+    assert np.array_equal(m.meta["length"], Z[name + "/length"])
+    for k, f in enumerate(("x0", "y0", "z0", "x", "y", "z")):
+        assert np.array_equal(m.meta["coords"][:, k], Z[name + "/" + f]), f
+
+
+@pytest.mark.parametrize("name", FILES)
+def test_channels_pools_spikegens(name):
+    rc = genesis.read_cell(path(name), LIB)
+    got = [(i, o[0], o[2]["Gbar"], o[1].Ek) for i, c in enumerate(rc.compts) for o in c.objs
+           if isinstance(o[1], (genesis.HHChannelProto, genesis.HHChannel2DProto))]
+    assert [g[0] for g in got] == list(Z[name + "/chan_compt"])
+    assert [g[1] for g in got] == list(Z[name + "/chan_name"])
+    assert np.array_equal([g[2] for g in got], Z[name + "/chan_Gbar"])
+    assert np.array_equal([g[3] for g in got], Z[name + "/chan_Ek"])
+    m = genesis.load_p(path(name), LIB)
+    assert np.array_equal(m.pool_B, Z[name + "/pool_B"])
+    assert np.array_equal(m.sg_threshold, Z[name + "/sg_threshold"])
+
+
+@pytest.mark.parametrize("name", FILES)
+def test_oracle_on_loaded_cell_matches_reference_hsolve(name):
+    m = genesis.load_p(path(name), LIB)
+    m.inject[0] = float(Z["inject"])
+    dt, stride, n = float(Z["dt"]), int(Z["stride"]), int(Z["nsteps"])
+    rec = Z[name + "/rec"]
+    oc = OracleCell(m, dt)
+    oc.reinit(dt)
+    npool = min(3, len(m.pool_compt))
+    vm, ca = [oc.vm()[rec]], [oc.ca()[:npool]]
+    for _ in range(n // stride):
+        oc.step(stride)
+        vm.append(oc.vm()[rec])
+        ca.append(oc.ca()[:npool])
+    assert np.array_equal(np.array(vm).T, Z[name + "/vm"])
+    if npool:
+        assert np.array_equal(np.array(ca).T, Z[name + "/ca"])
+    assert np.array_equal(oc.spikes()[1], Z[name + "/spikes"])
+    assert np.array_equal(oc.vm(), Z[name + "/final_vm"])
+
+
+def test_unsupported_forms_are_rejected(tmp_path):
+    for body in ("*symmetric\n*start_cell\nsoma none 10 0 0 10\n",
+                 "*compt /library/proto\nsoma none 10 0 0 10\n",
+                 "*start_cell /other/cell\nsoma none 10 0 0 10\n"):
+        p = tmp_path / "x.p"
+        p.write_text(body)
+        with pytest.raises(ValueError):
+            genesis.load_p(str(p), LIB)
+
+
+def test_comment_block_line_starting_with_star_is_a_command(tmp_path):
+    # inside /* */ a line that starts with '*' is still read as a command
+    # (ReadCell::innerRead), so *polar below takes effect
+    p = tmp_path / "c.p"
+    p.write_text("/* block\n*polar\n*/\nsoma none 10 90 90 10\n")
+    rc = genesis.read_cell(str(p), LIB)
+    assert rc.polar == 1
+    assert abs(rc.compts[0].y - 10e-6) < 1e-12
