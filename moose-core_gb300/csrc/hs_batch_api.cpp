@@ -436,19 +436,81 @@ int starTree(const CellPlan& P, StarTree& S) {
 // counters (4 B each) there.
 constexpr uint32_t kForestNodeBytes = 30;
 
+// The rate tables of a mixed batch: one V table and one Ca table for all
+// cells.  Every cell's table must lie on the same grid (min, max, rows, dx);
+// their species (A/B column pairs, createLookupTables) are merged, a species
+// with the same values in several cells stored once.  colMap[c][k] is the
+// union column of column k of cell c's table (k even: the A of a species).
+struct UnionTable {
+    double min = 0, max = 0, dx = 0;
+    uint32_t nPts = 0, nCol = 0;
+    std::vector<double> data;                    // nPts x nCol
+    std::vector<std::vector<int32_t>> colMap;    // per cell
+};
+
+int unionTables(HsBatch* b, bool ca, UnionTable& U) {
+    const uint32_t nC = b->nCells;
+    U = UnionTable();
+    U.colMap.resize(nC);
+    std::vector<std::vector<double>> species;    // column pairs of the union: A rows then B rows
+    std::multimap<uint64_t, uint32_t> byHash;
+    std::map<std::pair<uint64_t, size_t>, std::vector<int32_t>> byTable;   // distinct tables
+    bool have = false;
+    for (uint32_t c = 0; c < nC; ++c) {
+        const Table& T = ca ? b->plans[c].caTable : b->plans[c].vTable;
+        if (T.nCol == 0) continue;
+        if (!have) {
+            U.min = T.min, U.max = T.max, U.dx = T.dx, U.nPts = T.nPts;
+            have = true;
+        } else if (T.min != U.min || T.max != U.max || T.dx != U.dx || T.nPts != U.nPts) {
+            return berr(HS_ENOTSUP, std::string("mixed batch: the cells' ") + (ca ? "Ca" : "V") +
+                                        " rate tables lie on different grids (min, max, divisions)");
+        }
+        const auto key = std::make_pair(fnv(T.data.data(), T.data.size() * 8), T.data.size());
+        auto it = byTable.find(key);
+        if (it == byTable.end()) {
+            std::vector<int32_t> map(T.nCol, -1);
+            for (uint32_t s = 0; s + 1 < T.nCol; s += 2) {
+                std::vector<double> col(2 * (size_t)T.nPts);
+                for (uint32_t r = 0; r < T.nPts; ++r) {
+                    col[r] = T.data[(size_t)r * T.nCol + s];
+                    col[T.nPts + r] = T.data[(size_t)r * T.nCol + s + 1];
+                }
+                const uint64_t h = fnv(col.data(), col.size() * 8);
+                int32_t u = -1;
+                for (auto r = byHash.equal_range(h); r.first != r.second; ++r.first)
+                    if (species[r.first->second] == col) u = (int32_t)r.first->second;
+                if (u < 0) {
+                    u = (int32_t)species.size();
+                    species.push_back(std::move(col));
+                    byHash.emplace(h, (uint32_t)u);
+                }
+                map[s] = 2 * u;
+                map[s + 1] = 2 * u + 1;
+            }
+            it = byTable.emplace(key, std::move(map)).first;
+        }
+        U.colMap[c] = it->second;
+    }
+    U.nCol = 2 * (uint32_t)species.size();
+    U.data.assign((size_t)U.nPts * U.nCol, 0.0);
+    for (size_t u = 0; u < species.size(); ++u)
+        for (uint32_t r = 0; r < U.nPts; ++r) {
+            U.data[(size_t)r * U.nCol + 2 * u] = species[u][r];
+            U.data[(size_t)r * U.nCol + 2 * u + 1] = species[u][U.nPts + r];
+        }
+    return HS_OK;
+}
+
 int buildMixed(HsBatch* b) {
     const uint32_t nC = b->nCells;
     MixHost& H = b->mh;
     H = MixHost();
-    // one shared V table and Ca table for the batch
-    const Table& V0 = b->plans[0].vTable;
-    const Table& C0 = b->plans[0].caTable;
-    for (uint32_t c = 1; c < nC; ++c) {
-        const Table& V = b->plans[c].vTable;
-        const Table& Ca = b->plans[c].caTable;
-        if (V.data != V0.data || V.min != V0.min || V.max != V0.max || Ca.data != C0.data)
-            return berr(HS_ENOTSUP, "mixed batch: all cells must share one rate-table set");
-    }
+    // one V table and one Ca table for the batch: the union of the cells'
+    UnionTable V0, C0;
+    int urc = unionTables(b, false, V0);
+    if (urc == HS_OK) urc = unionTables(b, true, C0);
+    if (urc != HS_OK) return urc;
     // forest capacity from the shared memory of a CTA
     int optin = 0, perSm = 0;
     cudaError_t ce = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
@@ -710,10 +772,23 @@ int buildMixed(HsBatch* b) {
                     ty.yp = powCode(P.Ypow[q], key.p.y);
                     ty.zp = powCode(P.Zpow[q], key.p.z);
                     ty.instant = (int8_t)P.instant[q];
-                    ty.colX = (int16_t)(P.colX[q] < 0 ? 0 : P.colX[q]);
-                    ty.colY = (int16_t)(P.colY[q] < 0 ? 0 : P.colY[q]);
-                    ty.colZ = (int16_t)(P.colZ[q] < 0 ? 0 : P.colZ[q]);
-                    if (P.Zpow[q] > 0.0 && P.zSrc[q] >= 0) {
+                    // columns of the union tables; a Z gate on its pool reads the
+                    // Ca table, any other gate the V table (with the column
+                    // number it has, as HSolveActive::advanceChannels does)
+                    const bool zCaTab = P.Zpow[q] > 0.0 && P.zSrc[q] >= 0;
+                    const std::vector<int32_t>& vm = V0.colMap[ci];
+                    const std::vector<int32_t>& cm = C0.colMap[ci];
+                    auto col = [](const std::vector<int32_t>& m, int32_t k) -> int32_t {
+                        return k < 0 ? 0 : (size_t)k < m.size() ? m[k] : -1;
+                    };
+                    const int32_t cx = col(vm, P.colX[q]), cy = col(vm, P.colY[q]);
+                    const int32_t cz = col(zCaTab ? cm : vm, P.colZ[q]);
+                    if (cx < 0 || cy < 0 || cz < 0 || cx > 0x7FFF || cy > 0x7FFF || cz > 0x7FFF)
+                        return berr(HS_ENOTSUP, "mixed batch: a gate column outside its rate table");
+                    ty.colX = (int16_t)cx;
+                    ty.colY = (int16_t)cy;
+                    ty.colZ = (int16_t)cz;
+                    if (zCaTab) {
                         if (P.zSrc[q] != (int32_t)pb0 || pe0 == pb0)
                             return berr(HS_ENOTSUP, "mixed batch: Ca-dependent gate reads another compartment's pool");
                         ty.zCa = 1;

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from moose_gb300 import genesis
+from moose_gb300 import genesis, models
 from moose_gb300.abi import HS_PREC_MIXED
 from moose_gb300.batch import Batch
 from moose_gb300.hsolve import HSolve
@@ -69,15 +69,27 @@ def test_dropin_matches_reference_hsolve(name):
     assert len(h.spikes()[1]) == len(Z[name + "/spikes"])
 
 
-@pytest.mark.parametrize("group", [("relative_cartesian",) * 3, ("absolute_polar", "spherical_soma")])
-def test_mixed_batch_within_tolerance(group):
-    """One mixed batch per channel set (a batch shares one rate-table set):
-    the full-channel cell at three injects; the two HH-only cells."""
+def _run(cells, n=4000):
+    b = Batch(cells, 25e-6, HS_PREC_MIXED, steps_per_launch=100)
+    b.reinit(25e-6)
+    b.process(n)
+    return b
+
+
+def test_mixed_batch_of_different_channel_sets():
+    """Cells with different channel libraries in one mixed batch (their rate
+    tables merged into one): each within 0.1 mV / 0.05 ms of the oracle, and
+    bit-identical to the same cell in a batch of its own channel set."""
     cells = []
-    for k, name in enumerate(group):
+    for k, name in enumerate(("relative_cartesian", "relative_cartesian", "absolute_polar", "spherical_soma")):
         m = genesis.load_p(path(name), LIB)
         m.inject[0] = float(Z["inject"]) * (1.0 + 0.5 * k)
         cells.append(m)
+    kA, kB = models.kca_2d_tables(vdivs=300, cadivs=300)
+    rng = np.random.default_rng(5)
+    parent, d, L = models.branched_morphology(rng, 150, 0.5, 4)
+    cells.append(models.active_cell(parent, d, L, inject=0.6e-9, kca_tables=(kA, kB), t_end=0.1))
+    cells.append(models.config1_cell(n_cable=60, inject=0.4e-9))
     b = Batch(cells, 25e-6, HS_PREC_MIXED, steps_per_launch=100)
     b.reinit(25e-6)
     oracles = []
@@ -99,3 +111,19 @@ def test_mixed_batch_within_tolerance(group):
         assert len(got) == len(ref), "cell %d spike count %d vs %d" % (i, len(got), len(ref))
         if len(ref):
             assert np.abs(got - ref).max() <= 5e-5
+    alone = _run(cells[:2])
+    hh = _run(cells[2:4])
+    for i in range(2):
+        assert np.array_equal(alone.vm(i), b.vm(i))
+        assert np.array_equal(hh.vm(i), b.vm(2 + i))
+
+
+def test_mixed_batch_rejects_different_voltage_grids():
+    a = models.config1_cell(n_cable=10)
+    c = models.config1_cell(n_cable=10)
+    (mA, mB), (hA, hB) = models.hh_na_tables(vdivs=1000)
+    nA, nB = models.hh_k_tables(vdivs=1000)
+    c.gates = [(models.VMIN, models.VMAX, mA, mB), (models.VMIN, models.VMAX, hA, hB),
+               (models.VMIN, models.VMAX, nA, nB)]
+    with pytest.raises(Exception, match="different grids"):
+        Batch([a, c], 25e-6, HS_PREC_MIXED)
