@@ -344,6 +344,16 @@ int hs_batch_read_trace_window(HsBatch* b, uint32_t first, uint32_t count,
 int hs_batch_inject_targets(HsBatch* b, const uint32_t* cell, const uint32_t* compt,
                             uint32_t n);
 int hs_batch_set_inject(HsBatch* b, const double* values, uint32_t n);
+/* The modulation field of channels of a batch between process() calls, as
+ * a chem->elec Adaptor (signeur/Adaptor.cpp) sets it each step: kind
+ * HS_KIND_CHAN = HHChannel k of cells[k] (HSolve::setHHmodulation,
+ * hsolve/HSolveInterface.cpp:445-451: a value <= 0 keeps the old one),
+ * HS_KIND_CHAN2D / HS_KIND_SYNCHAN = that HHChannel2D / SynChan
+ * (ChanCommon::vSetModulation, biophysics/ChanCommon.cpp:46-49).  Indices
+ * are the cell description's; the values apply from the next step and
+ * persist across reinit and repacking.  Returns after the writes are done. */
+int hs_batch_set_modulation(HsBatch* b, int kind, const uint32_t* cells, const uint32_t* index,
+                            const double* values, uint32_t n);
 /* The inject of compartment compt[k] of cell cell[k] becomes values[k], for
  * k < n, without allocating any memory: the writes go through a fixed
  * host staging array and a fixed device scratch array of 32768 entries

@@ -40,6 +40,7 @@ cudaError_t launchBatchReinitMixed(const MixBatch& b, uint32_t nNodes, const dou
                                    const uint32_t* evStart, cudaStream_t st);
 cudaError_t launchScatterInject(double* const* addr, uint8_t* const* flag, const double* val, uint32_t n,
                                 cudaStream_t st);
+cudaError_t launchScatterValues(const ValueWrite* w, uint32_t n, cudaStream_t st);
 }  // namespace hsg
 
 using namespace hsg;
@@ -101,6 +102,9 @@ struct MixHost {
     std::vector<MixCellRange> cells;
     std::vector<std::vector<int64_t>> nodeOf;     // per cell: model compartment -> global node
     std::vector<std::vector<int64_t>> poolOf;     // per cell: model pool -> global pool
+    std::vector<std::vector<int64_t>> chanSlot;   // per cell: model HHChannel -> node * kMaxChan + slot
+    std::vector<std::vector<int64_t>> c2dNode;    // per cell: model HHChannel2D -> node
+    std::vector<std::vector<int64_t>> synGlobal;  // per cell: model SynChan -> global SynChan
     std::vector<double> initVm;                   // per node
     std::vector<float> c2dX0;
     std::vector<uint32_t> evStart;                // per SynChan (global)
@@ -638,6 +642,9 @@ int buildMixed(HsBatch* b) {
     // 4. per-cell lists: inject entries, stimulus, SpikeGens; model maps
     H.cells.resize(nC);
     H.nodeOf.resize(nC);
+    H.chanSlot.resize(nC);
+    H.c2dNode.resize(nC);
+    H.synGlobal.resize(nC);
     H.poolOf.resize(nC);
     b->injEntryOf.clear();
     std::vector<double> injVal, stimValue;
@@ -652,6 +659,9 @@ int buildMixed(HsBatch* b) {
         MixCellRange& R = H.cells[ci];
         std::memset(&R, 0, sizeof(R));
         H.nodeOf[ci].assign(P.hinesOf.size(), -1);
+        H.chanSlot[ci].assign(P.chanSolverOf.size(), -1);
+        H.c2dNode[ci].assign(P.K2, -1);
+        H.synGlobal[ci].assign(P.S, -1);
         for (size_t m = 0; m < P.hinesOf.size(); ++m)
             if (P.hinesOf[m] >= 0) H.nodeOf[ci][m] = posOf[ci][P.hinesOf[m]];
         H.poolOf[ci].assign(P.poolSolverOf.size(), -1);
@@ -803,6 +813,7 @@ int buildMixed(HsBatch* b) {
                     const uint32_t j = q - q0;
                     types = (types & ~(0xFFu << (8 * j))) | ((uint32_t)ti << (8 * j));
                     gbarS[(size_t)j * ld + g] = (float)(P.Gbar[q] * P.modulation[q]);
+                    H.chanSlot[ci][P.chanModel[q]] = (int64_t)g * kMaxChan + j;
                     int s = P.stateOff[q];
                     if (P.Xpow[q] > 0.0) stateS[(size_t)(3 * j) * ld + g] = pair(P.state0[s++]);
                     if (P.Ypow[q] > 0.0) stateS[(size_t)(3 * j + 1) * ld + g] = pair(P.state0[s++]);
@@ -850,6 +861,7 @@ int buildMixed(HsBatch* b) {
                     if (ti < 0) return berr(HS_ENOTSUP, "mixed batch: too many HHChannel2D types");
                     info = (info & ~(0xFFu << 8)) | ((uint32_t)ti << 8);
                     k2gbar[g] = (float)(P.c2dGbar[kk] * P.c2dMod[kk]);
+                    H.c2dNode[ci][kk] = g;
                     k2x0[g] = (float)P.c2dX0[kk];
                 }
                 if (synPtr[ci][t + 1] > synPtr[ci][t]) info |= kNodeSyn;
@@ -863,6 +875,7 @@ int buildMixed(HsBatch* b) {
                         H.synTypeKey.push_back(key);
                     }
                     synTypeV.push_back((uint8_t)ti);
+                    H.synGlobal[ci][kk2] = (int64_t)H.synGbar.size();
                     H.synGbar.push_back(P.synGbar[kk2]);
                     H.synTau1.push_back(P.synTau1[kk2]);
                     H.synTau2.push_back(P.synTau2[kk2]);
@@ -1768,3 +1781,76 @@ int hs_batch_read_spikes(HsBatch* b, uint32_t* cell, uint32_t* gen, double* time
 }
 
 }  // extern "C"
+
+// The modulation field of HHChannels, HHChannel2Ds or SynChans of a batch,
+// between process() calls: the zombie HHChannel's setModulation
+// (HSolve::setHHmodulation, hsolve/HSolveInterface.cpp:445-451: values <= 0
+// keep the old one) and the external channels' own field
+// (ChanCommon::vSetModulation, biophysics/ChanCommon.cpp:46-49), as an
+// Adaptor (signeur/Adaptor.cpp) writes it from a chemical model each step.
+int hs_batch_set_modulation(HsBatch* b, int kind, const uint32_t* cell, const uint32_t* index, const double* value,
+                            uint32_t n) {
+    if (!b || (n && (!cell || !index || !value))) return berr(HS_EINVAL, "null argument");
+    if (kind != HS_KIND_CHAN && kind != HS_KIND_CHAN2D && kind != HS_KIND_SYNCHAN)
+        return berr(HS_EINVAL, "modulation: kind must be HS_KIND_CHAN, HS_KIND_CHAN2D or HS_KIND_SYNCHAN");
+    const bool mixed = b->precision != HS_PREC_FP64;
+    std::vector<ValueWrite> w;
+    w.reserve(n);
+    for (uint32_t k = 0; k < n; ++k) {
+        if (cell[k] >= b->nCells) return berr(HS_EINVAL, "modulation: cell out of range");
+        CellPlan& P = b->plans[cell[k]];
+        const uint32_t c = cell[k], m = index[k];
+        const double v = value[k];
+        if (kind == HS_KIND_CHAN) {
+            if (m >= P.chanSolverOf.size() || P.chanSolverOf[m] < 0)
+                return berr(HS_EINVAL, "modulation: HHChannel not in the cell");
+            if (!(v > 0.0)) continue;
+            const uint32_t q = (uint32_t)P.chanSolverOf[m];
+            P.modulation[q] = v;
+            if (!mixed) {
+                w.push_back({b->dcs[c].mod + q, v, 0, 0});
+            } else {
+                const int64_t sl = b->mh.chanSlot[c][m];
+                if (sl < 0) return berr(HS_EINVAL, "modulation: HHChannel without a slot");
+                float* gb = const_cast<float*>(b->mb.gbar) + (size_t)(sl % kMaxChan) * b->mb.ld + sl / kMaxChan;
+                w.push_back({gb, P.Gbar[q] * v, 1, 0});
+            }
+        } else if (kind == HS_KIND_CHAN2D) {
+            if (m >= P.K2) return berr(HS_EINVAL, "modulation: HHChannel2D not in the cell");
+            P.c2dMod[m] = v;
+            if (!mixed) {
+                w.push_back({b->dcs[c].c2dMod + m, v, 0, 0});
+            } else {
+                const int64_t g = b->mh.c2dNode[c][m];
+                if (g < 0) return berr(HS_EINVAL, "modulation: HHChannel2D without a node");
+                w.push_back({const_cast<float*>(b->mb.k2gbar) + g, P.c2dGbar[m] * v, 1, 0});
+            }
+        } else {
+            if (m >= P.S) return berr(HS_EINVAL, "modulation: SynChan not in the cell");
+            P.synMod[m] = v;
+            if (!mixed) {
+                w.push_back({b->dcs[c].synMod + m, v, 0, 0});
+            } else {
+                const int64_t s = b->mh.synGlobal[c][m];
+                if (s < 0) return berr(HS_EINVAL, "modulation: SynChan not in the layout");
+                b->mh.synMod[s] = v;
+                if (b->reinited) {          // norm (at the clock dt) x modulation, as reinit sets it
+                    double xc1, xc2, yc1, yc2, nm;
+                    synchanConstants(b->mh.synTau1[s], b->mh.synTau2[s], b->mh.synGbar[s], b->clockDt, &xc1,
+                                     &xc2, &yc1, &yc2, &nm);
+                    w.push_back({const_cast<float*>(b->mb.synNorm) + s, nm * v, 1, 0});
+                }
+            }
+        }
+    }
+    if (w.empty()) return HS_OK;
+    ValueWrite* d = nullptr;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&d), w.size() * sizeof(ValueWrite), b->st);
+    if (e != cudaSuccess) return cerr(e, "modulation");
+    e = cudaMemcpyAsync(d, w.data(), w.size() * sizeof(ValueWrite), cudaMemcpyHostToDevice, b->st);
+    if (e == cudaSuccess) e = launchScatterValues(d, (uint32_t)w.size(), b->st);
+    cudaError_t f = cudaFreeAsync(d, b->st);
+    if (e == cudaSuccess) e = f;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);     // w is released on return
+    return e == cudaSuccess ? HS_OK : cerr(e, "modulation");
+}

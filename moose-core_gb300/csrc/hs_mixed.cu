@@ -745,6 +745,20 @@ __global__ void hsScatterInject(double* const* __restrict__ addr, uint8_t* const
     if (flag[i]) *flag[i] = 1;
 }
 
+__global__ void hsScatterValues(const ValueWrite* __restrict__ w, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const ValueWrite x = w[i];
+    if (x.f32) *static_cast<float*>(x.addr) = (float)x.value;
+    else *static_cast<double*>(x.addr) = x.value;
+}
+
+cudaError_t launchScatterValues(const ValueWrite* w, uint32_t n, cudaStream_t st) {
+    if (!n) return cudaSuccess;
+    hsScatterValues<<<(n + 255) / 256, 256, 0, st>>>(w, n);
+    return cudaGetLastError();
+}
+
 cudaError_t launchScatterInject(double* const* addr, uint8_t* const* flag, const double* val, uint32_t n,
                                 cudaStream_t st) {
     if (!n) return cudaSuccess;

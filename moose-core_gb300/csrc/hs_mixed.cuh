@@ -112,6 +112,15 @@ struct PrefetchArr {
     uint32_t n;
 };
 
+// One value written into device memory by hsScatterValues: the float
+// (f32 = 1) or double (f32 = 0) at `addr`.
+struct ValueWrite {
+    void* addr;
+    double value;
+    uint32_t f32;
+    uint32_t pad;
+};
+
 struct MixBatch {
     uint32_t nCells;
     // prototypes of this batch (read-only device tables)

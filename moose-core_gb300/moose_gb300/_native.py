@@ -67,6 +67,7 @@ def load(build_if_missing=True):
         "hs_batch_read_trace_window": (i32, [vp, u32, u32, vp]),
         "hs_batch_inject_targets": (i32, [vp, pu, pu, u32]),
         "hs_batch_set_inject": (i32, [vp, vp, u32]),
+        "hs_batch_set_modulation": (i32, [vp, i32, pu, pu, pd, u32]),
         "hs_batch_read_spikes": (i32, [vp, pu, pu, pd, u32, pu]),
         "hs_batch_info": (i32, [vp, C.POINTER(u64), pu, pu, pu]),
         "hs_batch_stream": (i32, [vp, C.POINTER(vp)]),

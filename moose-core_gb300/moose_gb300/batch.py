@@ -122,6 +122,18 @@ class Batch:
         ptr = values.data_ptr() if hasattr(values, "data_ptr") else values.ctypes.data
         _native.check(_native.load().hs_batch_set_inject(self._h, C.c_void_p(ptr), len(self._inj[0])))
 
+    def set_modulation(self, kind, cells, index, values):
+        """modulation of (cells[k], channel index[k]) = values[k]; kind is
+        HS_KIND_CHAN (HHChannel; values <= 0 are ignored, as
+        HSolve::setHHmodulation does), HS_KIND_CHAN2D or HS_KIND_SYNCHAN."""
+        c = np.ascontiguousarray(cells, np.uint32)
+        i = np.ascontiguousarray(index, np.uint32)
+        v = np.ascontiguousarray(values, np.float64)
+        pu = C.POINTER(C.c_uint32)
+        _native.check(_native.load().hs_batch_set_modulation(self._h, int(kind), c.ctypes.data_as(pu),
+                                                             i.ctypes.data_as(pu),
+                                                             v.ctypes.data_as(C.POINTER(C.c_double)), len(v)))
+
     def set_inject_at(self, cells, compts, values):
         """inject of (cells[k], compts[k]) = values[k], without allocating
         (hs_batch_set_inject_at; at most 32768 writes per call)."""

@@ -111,6 +111,7 @@ struct OrcCell {
 
     /* tick-4 external objects */
     double* c2dX; double* c2dVm; double* c2dConc1; double* c2dConc2; double* c2dGk;
+    double* c2dMod; double* synMod;     /* modulation fields (ChanCommon), writable */
     double* synX; double* synY; double* synAct; double* synGk;
     double* synXc1; double* synXc2; double* synYc1; double* synYc2; double* synNorm;
     double* synDt;
@@ -895,6 +896,10 @@ OrcCell* orc_create(const HsCellDesc* d, uint32_t seed, double dt, char* err, ui
     c->c2dConc1 = (double*)xcalloc(d->n_chan2d + 1, sizeof(double));
     c->c2dConc2 = (double*)xcalloc(d->n_chan2d + 1, sizeof(double));
     c->c2dGk = (double*)xcalloc(d->n_chan2d + 1, sizeof(double));
+    c->c2dMod = (double*)xcalloc(d->n_chan2d + 1, sizeof(double));
+    for (uint32_t k = 0; k < d->n_chan2d; k++) c->c2dMod[k] = d->c2d_modulation[k];
+    c->synMod = (double*)xcalloc(d->n_syn + 1, sizeof(double));
+    for (uint32_t k = 0; k < d->n_syn; k++) c->synMod[k] = d->syn_modulation[k];
     for (uint32_t k = 0; k < d->n_chan2d; k++) {
         if (c->hinesOf[d->c2d_compt[k]] == UINT32_MAX) FAIL("HHChannel2D compartment not in the tree");
         if (d->c2d_xgate[k] < 0 || d->c2d_xgate[k] >= (int32_t)d->n_gate2d) FAIL("HHChannel2D gate index out of range");
@@ -1198,7 +1203,7 @@ void orc_step(OrcCell* c, uint32_t nsteps) {
                 else c->c2dX[k] = c->c2dX[k] + A * dt;
                 g_ *= takePower(c->c2dX[k], d->c2d_Xpower[k]);
             }
-            c->c2dGk[k] = g_ * d->c2d_modulation[k];
+            c->c2dGk[k] = g_ * c->c2dMod[k];
             uint32_t h = c->hinesOf[d->c2d_compt[k]];
             c->externalCurrent[2 * h] += c->c2dGk[k];
             c->externalCurrent[2 * h + 1] += c->c2dGk[k] * d->c2d_Ek[k];
@@ -1208,7 +1213,7 @@ void orc_step(OrcCell* c, uint32_t nsteps) {
             c->synX[k] = c->synAct[k] * c->synXc1[k] + c->synX[k] * c->synXc2[k];
             c->synY[k] = c->synX[k] * c->synYc1[k] + c->synY[k] * c->synYc2[k];
             c->synAct[k] = 0.0;
-            c->synGk[k] = c->synY[k] * c->synNorm[k] * d->syn_modulation[k];
+            c->synGk[k] = c->synY[k] * c->synNorm[k] * c->synMod[k];
             uint32_t h = c->hinesOf[d->syn_compt[k]];
             c->externalCurrent[2 * h] += c->synGk[k];
             c->externalCurrent[2 * h + 1] += c->synGk[k] * d->syn_Ek[k];
@@ -1382,6 +1387,18 @@ int orc_set_field(OrcCell* c, int kind, int field, uint32_t index, double value)
         }
         return HS_EINVAL;
     }
+    /* HHChannel2D and SynChan stay outside the solver: their own modulation
+     * field, set as given (ChanCommon::vSetModulation, biophysics/ChanCommon.cpp:46-49) */
+    if (kind == HS_KIND_CHAN2D) {
+        if (index >= c->d->n_chan2d) return HS_EINVAL;
+        if (field == HS_F_MODULATION) { c->c2dMod[index] = value; return 0; }
+        return HS_EINVAL;
+    }
+    if (kind == HS_KIND_SYNCHAN) {
+        if (index >= c->d->n_syn) return HS_EINVAL;
+        if (field == HS_F_MODULATION) { c->synMod[index] = value; return 0; }
+        return HS_EINVAL;
+    }
     if (kind == HS_KIND_POOL) {
         if (index >= c->d->n_pool || c->poolSolverOf[index] < 0) return HS_EINVAL;
         uint32_t p = (uint32_t)c->poolSolverOf[index];
@@ -1447,6 +1464,7 @@ void orc_destroy(OrcCell* c) {
     free(c->poolModel); free(c->poolSolverOf);
     free(c->vTable.table); free(c->caTable.table);
     free(c->c2dX); free(c->c2dVm); free(c->c2dConc1); free(c->c2dConc2); free(c->c2dGk);
+    free(c->c2dMod); free(c->synMod);
     free(c->synX); free(c->synY); free(c->synAct); free(c->synGk);
     free(c->synXc1); free(c->synXc2); free(c->synYc1); free(c->synYc2); free(c->synNorm); free(c->synDt);
     free(c->evOff); free(c->evTime); free(c->evW); free(c->evPtr);

@@ -9,7 +9,8 @@ import numpy as np
 import pytest
 
 from moose_gb300 import models
-from moose_gb300.abi import HS_PREC_FP64, HS_PREC_MIXED
+from moose_gb300.abi import (FIELDS, HS_KIND_CHAN, HS_KIND_CHAN2D, HS_KIND_SYNCHAN, HS_PREC_FP64,
+                              HS_PREC_MIXED)
 from moose_gb300.batch import Batch
 from moose_gb300.hsolve import HSolve
 from oracle import OracleCell
@@ -180,3 +181,46 @@ def test_concurrent_batches_keep_their_own_prototypes():
     solo.process(200)
     for i in range(len(cells_b)):
         assert np.array_equal(b.vm(i), solo.vm(i)), i
+
+
+def test_modulation_writes():
+    """hs_batch_set_modulation (an Adaptor driving channel modulation) on
+    HHChannels (one write of 0, which setHHmodulation ignores), HHChannel2Ds
+    and SynChans part way through a run: the FP64 batch bit-exact with the
+    drop-in given the same field writes, the mixed batch within 0.1 mV of
+    the oracle given them."""
+    cells = small_population(6, 9, n_syn=6, t_end=0.1)
+    writes = []
+    for c, m in enumerate(cells):
+        writes += [(HS_KIND_CHAN, c, 0, 1.3), (HS_KIND_CHAN, c, 4, 0.0), (HS_KIND_CHAN, c, 7, 0.6),
+                   (HS_KIND_CHAN2D, c, 2, 0.5), (HS_KIND_SYNCHAN, c, 1, 2.0)]
+    fmod = FIELDS["modulation"]
+
+    def apply_batch(b):
+        for kind in (HS_KIND_CHAN, HS_KIND_CHAN2D, HS_KIND_SYNCHAN):
+            w = [x for x in writes if x[0] == kind]
+            b.set_modulation(kind, [x[1] for x in w], [x[2] for x in w], [x[3] for x in w])
+
+    fb = Batch(cells, DT, HS_PREC_FP64)
+    mb = Batch(cells, DT, HS_PREC_MIXED)
+    for b in (fb, mb):
+        b.reinit(DT)
+        b.process(300)
+        apply_batch(b)
+        b.process(700)
+    for c, m in enumerate(cells):
+        h = HSolve(m, dt=DT)
+        h.target = m.seed
+        h.reinit(DT)
+        h.process(300)
+        oc = OracleCell(m, DT)
+        oc.reinit(DT)
+        oc.step(300)
+        for kind, cc, i, v in writes:
+            if cc == c:
+                h._set(kind, fmod, i, v)
+                oc.set(kind, fmod, i, v)
+        h.process(700)
+        oc.step(700)
+        assert np.array_equal(fb.vm(c), h.vm()), c
+        assert np.abs(mb.vm(c) - oc.vm()).max() <= 1e-4, c
