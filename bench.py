@@ -17,6 +17,8 @@ The JSON line carries:
              reads back the somatic Vm trace of the chunk;
   fp64_dropin the plain FP64 drop-in (one HSolve instance per cell, one CTA
              each) on a sample of the same cells, and the ratio to `value`;
+  single_cell the FP64 drop-in on the single-cell case (soma + 200-compartment
+             HH cable, 0.5 s), next to the same cell on one host core;
   fp64_batch the FP64 batch (one warp per cell, the drop-in's arithmetic,
              bit-identical results) on all cells of the workload;
   accuracy   max |dVm| and spike-time shift of the mixed batch against the
@@ -424,6 +426,26 @@ def run_ours(args, rank, world, cpu_pool):
                              % (len(sub), args.acc_steps)}
             f.close()
             mx.close()
+        # the single-cell drop-in case: soma + 200-compartment HH cable, 0.5 s
+        single = None
+        n1 = 20000
+        if not args.skip_single:
+            m1 = models.config1_cell()
+            h = HSolve(m1, dt=DT)
+            h.target = m1.seed
+            h.reinit(DT)
+            h.process(200)
+            h.sync()
+            h.reinit(DT)
+            t0 = time.perf_counter()
+            h.process(n1)
+            h.sync()
+            g_s = time.perf_counter() - t0
+            h.close()
+            single = {"workload": "single cell: soma + 200-compartment HH cable (Na m3h, K n4), 20,000 dt steps "
+                                  "of 25 us (0.5 s), FP64 drop-in through hs_process", "wall_s": g_s,
+                      "value": m1.n_compt * n1 / g_s, "unit": "compartment-steps/s",
+                      "us_per_step": g_s / n1 * 1e6}
         cpu = None
         if cpu_pool is not None:
             tcpu = cpu_pool.step(args.cpu_chunk)
@@ -432,6 +454,18 @@ def run_ours(args, rank, world, cpu_pool):
             cpu = {"value": cv, "unit": "compartment-steps/s", "cores": cpu_pool.workers, "kind": "port",
                    "sample": "%d compartments of the workload's cells x %d dt steps in %d processes"
                              % (cpu_pool.ncomp, 2 * args.cpu_chunk, cpu_pool.workers)}
+            if single is not None:
+                # the same single cell on one host core (the CPU HSolve restatement)
+                from oracle import OracleCell
+                m1 = models.config1_cell()
+                oc = OracleCell(m1, DT)
+                oc.reinit(DT)
+                t0 = time.perf_counter()
+                oc.step(n1)
+                c_s = time.perf_counter() - t0
+                cpu["single_cell"] = {"wall_s": c_s, "value": m1.n_compt * n1 / c_s, "cores": 1,
+                                      "sample": "the single-cell workload, all 20,000 dt steps"}
+                single["gpu_over_cpu_1core"] = c_s / single["wall_s"]
         launches = args.steps * math.ceil(args.chunk / spl)
         out = {"metric": "compartment-steps/s", "value": value, "unit": "compartment-steps/s",
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -447,7 +481,7 @@ def run_ours(args, rank, world, cpu_pool):
                        "h2d_bytes_per_step": args.cells * 8,
                        "d2h_bytes_per_step": (args.chunk // stride) * args.cells * 8},
                "roofline": roof, "cpu_baseline": cpu, "fp64_dropin": dropin, "fp64_batch": fp64b,
-               "accuracy": acc,
+               "accuracy": acc, "single_cell": single,
                "clocks": clk, "gpu_launches": launches}
         if not args.skip_serving:
             out["serving"] = run_serving(args)
@@ -477,6 +511,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-serving", action="store_true")
     ap.add_argument("--skip-fp64-batch", action="store_true")
+    ap.add_argument("--skip-single", action="store_true", help="skip the single-cell drop-in case")
     ap.add_argument("--fp64-batch-steps", type=int, default=100)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--serving-only", action="store_true", help="print only the serving measurement")
