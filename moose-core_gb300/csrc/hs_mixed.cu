@@ -642,6 +642,20 @@ __global__ void __launch_bounds__(1024, 1) hsForestStepMixed(MixBatch b, const u
     double* sD = reinterpret_cast<double*>(smem + (kSmemLevels + kWsLevels) * 4);
     for (uint32_t k = ctaPtr[blockIdx.x]; k < ctaPtr[blockIdx.x + 1]; ++k) {
         const MixForest F = b.forests[ctaForests[k]];
+        if (b.anyStop) {
+            // a forest whose cells have all reached their stop step is only
+            // counted on: stepping it would change nothing (stopped cells keep
+            // their state, outputs and step counts), and skipping it lets the
+            // CTA return and free its SM for other batches
+            const unsigned long long done = b.forestStep[ctaForests[k]];
+            int live = 0;
+            for (uint32_t c = threadIdx.x; c < F.nCells; c += blockDim.x)
+                live |= done < b.stopStep[b.forestCells[F.cell0 + c]];
+            if (!__syncthreads_or(live)) {
+                if (threadIdx.x == 0) b.forestStep[ctaForests[k]] = done + nsteps;
+                continue;
+            }
+        }
         const uint32_t* lp = b.levelPtr + F.level0;
         if (F.nLevels < kSmemLevels) {
             for (uint32_t i = threadIdx.x; i <= F.nLevels; i += blockDim.x) sLp[i] = lp[i];
