@@ -150,11 +150,14 @@ class Server:
     need.  At most
     ``max_cohorts`` cohorts run at once (the hardware work queues of the
     context); requests that arrive meanwhile wait and start together as the
-    next cohort."""
+    next cohort.  An admission round makes one cohort per duration class
+    (``duration_classes``: dt-step boundaries): the requests that share a
+    cohort, and so its forests, then end at about the same time, and the
+    kernel skips a forest whose cells have all stopped, which frees its SM."""
 
     def __init__(self, dt, budget_bytes=150 * 10**9, chunk=4000, record_stride=40, max_cohort=4096,
                  admit_interval=0.05, dense=True, forest_nodes=7000, max_cohorts=32, sms=152, tuning=None,
-                 clock=time.perf_counter, cohort_factory=None):
+                 clock=time.perf_counter, cohort_factory=None, duration_classes=(16000, 40000)):
         self.dt = dt
         self.budget = budget_bytes
         self.chunk = chunk
@@ -168,6 +171,7 @@ class Server:
         self.tuning = dict(tuning or {})
         self.clock = clock
         self.cohort_factory = cohort_factory or _Cohort
+        self.duration_classes = tuple(sorted(duration_classes or ()))
         self.cohorts = []
         self.waiting = []
         self.results = []
@@ -177,17 +181,29 @@ class Server:
     def used_bytes(self):
         return sum(c.bytes for c in self.cohorts)
 
+    def _class(self, r):
+        return sum(r.n_steps >= b for b in self.duration_classes)
+
     def _admit(self, now):
+        """A cohort of waiting requests of the first waiting request's
+        duration class, in arrival order, within the memory budget."""
         take, est = [], 0
         used = self.used_bytes()
-        while self.waiting and len(take) < self.max_cohort:
-            r = self.waiting[0]
+        if not self.waiting:
+            return None
+        cls = self._class(self.waiting[0])
+        k = 0
+        while k < len(self.waiting) and len(take) < self.max_cohort:
+            r = self.waiting[k]
+            if self._class(r) != cls:
+                k += 1
+                continue
             e = estimate_bytes(r.cell, r.n_steps, self.stride)
             if not take:
                 e += cohort_overhead(r.cell)
             if used + est + e > self.budget:
                 break
-            take.append(self.waiting.pop(0))
+            take.append(self.waiting.pop(k))
             est += e
         if not take:
             return None
@@ -218,9 +234,14 @@ class Server:
                 self.waiting.append(pending.pop(0))
             progressed = False
             if self.waiting and now - last_admit >= self.admit_interval and len(self.cohorts) < self.max_cohorts:
-                fresh = self._admit(now)
                 last_admit = now
-                if fresh is not None:
+                # one cohort per duration class present
+                for _ in range(len(self.duration_classes) + 1):
+                    if not self.waiting or len(self.cohorts) >= self.max_cohorts:
+                        break
+                    fresh = self._admit(now)
+                    if fresh is None:
+                        break
                     fresh.launch(self.chunk)
                     self.cohorts.append(fresh)
                     progressed = True

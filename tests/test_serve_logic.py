@@ -95,3 +95,17 @@ def test_summary_percentiles():
     assert abs(s["p50_latency_s"] - 50.5) < 1e-9
     assert s["p99_latency_s"] > 99.0
     assert s["compartment_steps_per_s"] == 100 * 100 * 1000 / 10.0
+
+
+def test_a_round_makes_one_cohort_per_duration_class():
+    FakeCohort.created = []
+    steps = [4000, 20000, 60000, 5000, 30000, 70000, 12000]
+    reqs = [serve.Request(i, _Cell(200), n, arrival=0.0) for i, n in enumerate(steps)]
+    srv = make_server(chunk=4000, record_stride=40, duration_classes=(16000, 40000))
+    res = srv.run(reqs, real_time=False)
+    assert sorted(r.rid for r in res) == list(range(len(steps)))
+    classes = [{srv._class(r) for r in c.reqs} for c in FakeCohort.created]
+    assert all(len(c) == 1 for c in classes)
+    assert len(FakeCohort.created) == 3
+    # all three were admitted in the first round
+    assert len({c.admitted for c in FakeCohort.created}) == 1
