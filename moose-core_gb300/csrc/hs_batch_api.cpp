@@ -143,6 +143,8 @@ struct HsBatch {
     uint32_t *dCtaPtr = nullptr, *dCtaForests = nullptr;
     uint32_t mixCap = 0, mixSmem = 0;
     unsigned long long* dStopStep = nullptr;    // mixed: per-cell stop steps
+    unsigned long long* dForestStop = nullptr;  // mixed: per-forest largest stop step
+    std::vector<uint32_t> forestCellPtr, forestCellIdx;   // mixed: cells of each forest (host)
     SynType* dSynTypes = nullptr;               // mixed: SynChan constants at the clock dt
     DevBuf buf;              // long-lived allocations
     DevBuf packBuf;          // packing arrays (replaced by retuning)
@@ -917,6 +919,11 @@ int buildMixed(HsBatch* b) {
         m.cellOf = D.up(cellOf, st);
         b->dStopStep = D.up(std::vector<unsigned long long>(nC, ~0ull), st);
         m.stopStep = b->dStopStep;
+        b->dForestStop = D.up(std::vector<unsigned long long>(fdev.size(), ~0ull), st);
+        m.forestStop = b->dForestStop;
+        b->forestCellPtr.assign(fdev.size() + 1, 0);
+        for (size_t fi = 0; fi < fdev.size(); ++fi) b->forestCellPtr[fi + 1] = fdev[fi].cell0 + fdev[fi].nCells;
+        b->forestCellIdx = forestCells;
     }
     m.forestCells = D.up(forestCells, st);
     m.levelPtr = D.up(levelPtr, st);
@@ -1419,7 +1426,16 @@ int hs_batch_set_stop_steps(HsBatch* b, const uint64_t* stop, uint32_t n) {
     if (b->precision != HS_PREC_MIXED) return berr(HS_ENOTSUP, "stop steps are a mixed-batch feature");
     if (n != b->nCells) return berr(HS_EINVAL, "n must equal the number of cells");
     static_assert(sizeof(unsigned long long) == sizeof(uint64_t), "64-bit step counts");
+    // per forest, the largest stop step of its cells: the kernel skips a
+    // forest whose step count has reached it
+    const size_t nF = b->forestCellPtr.empty() ? 0 : b->forestCellPtr.size() - 1;
+    std::vector<unsigned long long> fstop(nF, 0);
+    for (size_t f = 0; f < nF; ++f)
+        for (uint32_t k = b->forestCellPtr[f]; k < b->forestCellPtr[f + 1]; ++k)
+            fstop[f] = std::max<unsigned long long>(fstop[f], stop[b->forestCellIdx[k]]);
     cudaError_t e = cudaMemcpyAsync(b->dStopStep, stop, (size_t)n * 8, cudaMemcpyHostToDevice, b->st);
+    if (e == cudaSuccess && nF)
+        e = cudaMemcpyAsync(b->dForestStop, fstop.data(), nF * 8, cudaMemcpyHostToDevice, b->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
     if (e != cudaSuccess) return cerr(e, "stop steps");
     uint32_t any = 0;

@@ -633,6 +633,10 @@ __device__ void stepForestWS(const MixBatch& b, const MixForest& F, uint32_t f, 
 // Dynamic shared memory: kSmemLevels level offsets, then for shared forests
 // the elimination arrays of `cap` nodes: D, R, OFF (8 B each), TOPO (4 B),
 // PAR (2 B).
+// kStops: the batch has stop steps (b.anyStop); the batches without (the
+// throughput case) get an instantiation without the forest check, whose
+// registers are allocated as if it did not exist.
+template <bool kStops>
 __global__ void __launch_bounds__(1024, 1) hsForestStepMixed(MixBatch b, const uint32_t* __restrict__ ctaPtr,
                                                              const uint32_t* __restrict__ ctaForests, uint32_t cap,
                                                              uint32_t elimWarps, uint32_t nsteps) {
@@ -642,19 +646,14 @@ __global__ void __launch_bounds__(1024, 1) hsForestStepMixed(MixBatch b, const u
     double* sD = reinterpret_cast<double*>(smem + (kSmemLevels + kWsLevels) * 4);
     for (uint32_t k = ctaPtr[blockIdx.x]; k < ctaPtr[blockIdx.x + 1]; ++k) {
         const MixForest F = b.forests[ctaForests[k]];
-        if (b.anyStop) {
-            // a forest whose cells have all reached their stop step is only
-            // counted on: stepping it would change nothing (stopped cells keep
-            // their state, outputs and step counts), and skipping it lets the
-            // CTA return and free its SM for other batches
-            const unsigned long long done = b.forestStep[ctaForests[k]];
-            int live = 0;
-            for (uint32_t c = threadIdx.x; c < F.nCells; c += blockDim.x)
-                live |= done < b.stopStep[b.forestCells[F.cell0 + c]];
-            if (!__syncthreads_or(live)) {
-                if (threadIdx.x == 0) b.forestStep[ctaForests[k]] = done + nsteps;
-                continue;
-            }
+        if (kStops && b.forestStep[ctaForests[k]] >= b.forestStop[ctaForests[k]]) {
+            // every cell of the forest has reached its stop step: stepping it
+            // would change nothing (stopped cells keep their state, outputs
+            // and step counts), so its steps are only counted and the CTA
+            // can return and free its SM for other batches
+            __syncthreads();
+            if (threadIdx.x == 0) b.forestStep[ctaForests[k]] += nsteps;
+            continue;
         }
         const uint32_t* lp = b.levelPtr + F.level0;
         if (F.nLevels < kSmemLevels) {
@@ -783,9 +782,10 @@ cudaError_t launchScatterInject(double* const* addr, uint8_t* const* flag, const
 cudaError_t launchForestStepMixed(const MixBatch& b, const uint32_t* ctaPtr, const uint32_t* ctaForests,
                                   uint32_t nCtas, uint32_t threadsPerCta, uint32_t smemBytes, uint32_t cap,
                                   uint32_t elimWarps, uint32_t nsteps, cudaStream_t st) {
-    cudaError_t e = cudaFuncSetAttribute(hsForestStepMixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes);
+    auto kern = b.anyStop ? hsForestStepMixed<true> : hsForestStepMixed<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes);
     if (e != cudaSuccess) return e;
-    hsForestStepMixed<<<nCtas, threadsPerCta, smemBytes, st>>>(b, ctaPtr, ctaForests, cap, elimWarps, nsteps);
+    kern<<<nCtas, threadsPerCta, smemBytes, st>>>(b, ctaPtr, ctaForests, cap, elimWarps, nsteps);
     return cudaGetLastError();
 }
 

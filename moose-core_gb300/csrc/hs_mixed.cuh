@@ -137,6 +137,7 @@ struct MixBatch {
     const MixForest* forests;
     unsigned long long* forestStep;      // steps done by each forest
     const unsigned long long* stopStep;  // per cell: no step at or after this one
+    const unsigned long long* forestStop;   // per forest: the largest stop step of its cells
     uint32_t anyStop;                    // 0: no cell has a stop step
     const uint32_t* cellOf;              // per node: its cell
     const uint32_t* forestCells;
