@@ -684,8 +684,15 @@ __global__ void __launch_bounds__(1024, 1) hsForestStepMixed(MixBatch b, const u
             E.PAR = b.par + F.node0;
         }
         __syncthreads();
-        if (elimWarps && F.nLevels <= kWsLevels - 1 && F.nLevels < kSmemLevels && blockDim.x > 32 * elimWarps)
-            stepForestWS(b, F, ctaForests[k], E, lp, sDone, elimWarps, nsteps);
+        // a forest eliminated in global memory (a cell too large for shared
+        // memory, as serving requests can be) has wide levels of slow loads:
+        // twice the eliminator warps (measured on a 10,000-compartment cell:
+        // 184 -> 159 us per step).  Only in the instantiation for batches
+        // with stop steps, so that the throughput kernel's registers stay
+        // as they are.
+        const uint32_t ew = kStops && !F.shared ? min(2 * elimWarps, 16u) : elimWarps;
+        if (ew && F.nLevels <= kWsLevels - 1 && F.nLevels < kSmemLevels && blockDim.x > 32 * ew)
+            stepForestWS(b, F, ctaForests[k], E, lp, sDone, ew, nsteps);
         else
             stepForest(b, F, ctaForests[k], E, lp, nsteps);
     }
