@@ -272,6 +272,21 @@ int hs_add_gkek(HsSolver* s, uint32_t compt, double Gk, double Ek);
 int hs_add_conc(HsSolver* s, uint32_t chan, double conc);
 int hs_add_ica(HsSolver* s, uint32_t pool, double ica);
 
+/* Synaptic events at run time: event e is queued in the SimpleSynHandler of
+ * SynChan `syn[e]` with delivery time time[e] and weight weight[e]
+ * (`SimpleSynHandler::addSpike`, `synapse/SimpleSynHandler.cpp:86-90`; the
+ * caller adds the synapse delay, as `Synapse::addSpike` does at
+ * `synapse/Synapse.cpp:104-113`).  An event is delivered at the first step
+ * whose clock time is >= its time, as weight/dt into the SynChan's
+ * activation (`SimpleSynHandler::vProcess`, lines 98-113), including events
+ * whose time has already passed.  Events with equal times on one SynChan
+ * are summed in the order they were pushed, after the description's.
+ * reinit drops every queued runtime event (`SimpleSynHandler::vReinit`).
+ * Times must not be NaN.  The events reach the device at the next
+ * hs_process. */
+int hs_push_events(HsSolver* s, const uint32_t* syn, const double* time,
+                   const double* weight, uint32_t n);
+
 /* Bulk reads in model order (n = n_compt / n_pool). */
 int hs_read_vm(HsSolver* s, double* out, uint32_t n);
 int hs_read_ca(HsSolver* s, double* out, uint32_t n);

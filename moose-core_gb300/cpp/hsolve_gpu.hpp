@@ -6,7 +6,8 @@
 // the solver fields dt, caAdvance, vDiv/vMin/vMax, caDiv/caMin/caMax;
 // setup from a seed compartment (HSolve::setPath -> setup); reinit and
 // process; the zombie fields of compartments, HHChannels and CaConcs; and
-// the message destinations addInject, addGkEk, addConc and iCa.  A MOOSE
+// the message destinations addInject, addGkEk, addConc, iCa and the
+// synaptic events of SimpleSynHandler::addSpike.  A MOOSE
 // build keeps its HSolve Cinfo and forwards to this class (or to the C ABI
 // directly); other C++ hosts use it as the solver object.
 //
@@ -185,6 +186,12 @@ public:
     void addGkEk(uint32_t c, double Gk, double Ek) { check(hs_add_gkek(handle(), c, Gk, Ek)); }
     void addConc(uint32_t k, double conc) { check(hs_add_conc(handle(), k, conc)); }
     void iCa(uint32_t p, double ica) { check(hs_add_ica(handle(), p, ica)); }
+    // SimpleSynHandler::addSpike for SynChan k's handler (time includes the
+    // synapse delay, as Synapse::addSpike adds it); delivered from the next
+    // process() on, dropped by reinit()
+    void addSpike(uint32_t k, double time, double weight) {
+        check(hs_push_events(handle(), &k, &time, &weight, 1));
+    }
 
     // ---- bulk reads in model order (a Table per compartment would need
     // a device read per field access)

@@ -7,6 +7,7 @@
 // stores Ra; modulation ignores non-positive values).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -51,7 +52,126 @@ struct HsSolver {
     uint32_t* recCompt = nullptr;
     double* recBuf = nullptr;
     std::vector<uint32_t> recHost;
+    // Runtime synaptic events (hs_push_events).  Until the first push the
+    // kernel reads the description's events in the arena; after it, a
+    // solver-owned copy holding the undelivered events of every SynChan,
+    // merged in time order.  hostPtr/hostTime/hostW mirror that copy.
+    std::vector<uint32_t> pendSyn;
+    std::vector<double> pendTime, pendW;
+    bool evOwned = false;
+    std::vector<uint32_t> hostPtr;    // S+1 bounds, then S cursors (= the bounds)
+    std::vector<double> hostTime, hostW;
+    uint32_t* ownIdx = nullptr;       // device: evPtr (S+1), evCur (S)
+    double* ownEv = nullptr;          // device: time (ownCap), weight (ownCap)
+    size_t ownCap = 0;
+    const uint32_t* descPtr = nullptr;
+    uint32_t* descCur = nullptr;
+    const double *descTime = nullptr, *descW = nullptr;
 };
+
+namespace {
+
+// Hands the pushed events to the device before a process call.  Per SynChan
+// the new queue is the events not yet delivered (from the device cursor on)
+// merged with the pushed ones in time order, queued events first on equal
+// times and pushed ones in push order: the order in which
+// SimpleSynHandler::vProcess pops its heap for distinct times.  Delivered
+// events are dropped.  The step kernel is unchanged: it walks the new arrays
+// exactly as it walks the description's.
+int flushEvents(HsSolver* s) {
+    if (s->pendSyn.empty()) return HS_OK;
+    const uint32_t S = s->P.S;
+    std::vector<uint32_t> cur(S);
+    cudaError_t e = cudaStreamSynchronize(s->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(cur.data(), s->dc.evCur, S * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cudaErr(e, "push events");
+    const std::vector<uint32_t>& ptr = s->evOwned ? s->hostPtr : s->P.evPtr;
+    const std::vector<double>& tq = s->evOwned ? s->hostTime : s->P.evTime;
+    const std::vector<double>& wq = s->evOwned ? s->hostW : s->P.evW;
+    const size_t n = s->pendSyn.size();
+    size_t total = n;
+    for (uint32_t k = 0; k < S; ++k) {
+        cur[k] = std::min(std::max(cur[k], ptr[k]), ptr[k + 1]);
+        total += ptr[k + 1] - cur[k];
+    }
+    if (total > 0xffffffffull) return setErr(HS_ENOMEM, "too many queued synaptic events");
+    std::vector<uint32_t> ord(n);
+    for (size_t i = 0; i < n; ++i) ord[i] = (uint32_t)i;
+    std::stable_sort(ord.begin(), ord.end(), [s](uint32_t a, uint32_t b) {
+        if (s->pendSyn[a] != s->pendSyn[b]) return s->pendSyn[a] < s->pendSyn[b];
+        return s->pendTime[a] < s->pendTime[b];
+    });
+    std::vector<uint32_t> nptr(2 * (size_t)S + 1);
+    std::vector<double> nt, nw;
+    nt.reserve(total);
+    nw.reserve(total);
+    size_t p = 0;
+    for (uint32_t k = 0; k < S; ++k) {
+        nptr[k] = (uint32_t)nt.size();
+        uint32_t a = cur[k], aEnd = ptr[k + 1];
+        size_t pe = p;
+        while (pe < n && s->pendSyn[ord[pe]] == k) ++pe;
+        while (a < aEnd || p < pe) {
+            if (p == pe || (a < aEnd && tq[a] <= s->pendTime[ord[p]])) {
+                nt.push_back(tq[a]);
+                nw.push_back(wq[a]);
+                ++a;
+            } else {
+                nt.push_back(s->pendTime[ord[p]]);
+                nw.push_back(s->pendW[ord[p]]);
+                ++p;
+            }
+        }
+    }
+    nptr[S] = (uint32_t)nt.size();
+    for (uint32_t k = 0; k < S; ++k) nptr[S + 1 + k] = nptr[k];   // cursors at the start
+    const size_t m = nt.size();
+    if (!s->ownIdx) {
+        e = cudaMalloc(&s->ownIdx, nptr.size() * sizeof(uint32_t));
+        if (e != cudaSuccess) {
+            s->ownIdx = nullptr;
+            return cudaErr(e, "push events");
+        }
+    }
+    // a grown buffer replaces the old one only once it holds the new queue,
+    // so that a failed allocation or copy leaves the solver's queue as it was
+    double* ev = s->ownEv;
+    size_t cap = s->ownCap;
+    if (m > cap) {
+        cap = std::max(m, 2 * cap);
+        e = cudaMalloc(&ev, 2 * cap * sizeof(double));
+        if (e != cudaSuccess) return cudaErr(e, "push events");
+    }
+    e = cudaMemcpyAsync(s->ownIdx, nptr.data(), nptr.size() * sizeof(uint32_t),
+                        cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ev, nt.data(), m * sizeof(double), cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ev + cap, nw.data(), m * sizeof(double), cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) {
+        if (ev != s->ownEv) cudaFree(ev);
+        return cudaErr(e, "push events");
+    }
+    if (ev != s->ownEv && s->ownEv) cudaFree(s->ownEv);
+    s->ownEv = ev;
+    s->ownCap = cap;
+    s->hostPtr.swap(nptr);
+    s->hostTime.swap(nt);
+    s->hostW.swap(nw);
+    s->dc.evPtr = s->ownIdx;
+    s->dc.evCur = s->ownIdx + S + 1;
+    s->dc.evTime = s->ownEv;
+    s->dc.evW = s->ownEv + s->ownCap;
+    s->evOwned = true;
+    s->pendSyn.clear();
+    s->pendTime.clear();
+    s->pendW.clear();
+    return HS_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -109,6 +229,10 @@ int hs_create(const HsCellDesc* cell, uint32_t seed, double dt, int precision, H
     if (e == cudaSuccess) e = cudaMemsetAsync(s->arena.base, 0, s->arena.size, s->st);
     if (e == cudaSuccess) e = layoutCell(s->P, s->arena, s->dc, spikeCap, s->st);
     s->dcDev = s->arena.take<DevCell>(1);
+    s->descPtr = s->dc.evPtr;
+    s->descCur = s->dc.evCur;
+    s->descTime = s->dc.evTime;
+    s->descW = s->dc.evW;
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
     if (e != cudaSuccess) {
         int rc = cudaErr(e, "device setup");
@@ -131,6 +255,8 @@ int hs_destroy(HsSolver* s) {
     if (s->arena.base) cudaFree(s->arena.base);
     if (s->recCompt) cudaFree(s->recCompt);
     if (s->recBuf) cudaFree(s->recBuf);
+    if (s->ownIdx) cudaFree(s->ownIdx);
+    if (s->ownEv) cudaFree(s->ownEv);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
     return HS_OK;
@@ -142,6 +268,18 @@ int hs_reinit(HsSolver* s, double clock_dt) {
     s->dt_ = clock_dt;            // HSolve::reinit: dt_ = p->dt
     s->clockDt = clock_dt;
     s->dc.dt = clock_dt;
+    // SimpleSynHandler::vReinit empties the queue; the description's events
+    // are queued again (the reinit kernel rewinds their cursors).
+    s->pendSyn.clear();
+    s->pendTime.clear();
+    s->pendW.clear();
+    if (s->evOwned) {
+        s->dc.evPtr = s->descPtr;
+        s->dc.evCur = s->descCur;
+        s->dc.evTime = s->descTime;
+        s->dc.evW = s->descW;
+        s->evOwned = false;
+    }
     std::vector<double> sc(5 * (size_t)s->P.S + 1);
     synConsts(s->P, clock_dt, sc.data());
     cudaError_t e = cudaMemcpyAsync((void*)s->dc.synConst, sc.data(), 5 * (size_t)s->P.S * 8,
@@ -160,6 +298,8 @@ int hs_process(HsSolver* s, uint32_t nsteps) {
     if (!s) return setErr(HS_EINVAL, "null solver");
     if (!s->reinited) return setErr(HS_ESTATE, "reinit before process");
     if (nsteps == 0) return HS_OK;
+    int rc = flushEvents(s);
+    if (rc) return rc;
     cudaError_t e = launchStepFp64(s->dc, nsteps, s->st);
     if (e != cudaSuccess) return cudaErr(e, "process");
     return HS_OK;
@@ -481,6 +621,21 @@ int hs_add_ica(HsSolver* s, uint32_t pool, double ica) {
     double cur;
     if ((rc = readDev(s, s->dc.iCa + p, &cur))) return rc;
     return writeDev(s, s->dc.iCa + p, cur + ica);
+}
+
+int hs_push_events(HsSolver* s, const uint32_t* syn, const double* time, const double* weight,
+                   uint32_t n) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    if (n == 0) return HS_OK;
+    if (!syn || !time || !weight) return setErr(HS_EINVAL, "null argument");
+    for (uint32_t i = 0; i < n; ++i) {
+        if (syn[i] >= s->P.S) return setErr(HS_EINVAL, "event SynChan index out of range");
+        if (std::isnan(time[i])) return setErr(HS_EINVAL, "event time is NaN");
+    }
+    s->pendSyn.insert(s->pendSyn.end(), syn, syn + n);
+    s->pendTime.insert(s->pendTime.end(), time, time + n);
+    s->pendW.insert(s->pendW.end(), weight, weight + n);
+    return HS_OK;
 }
 
 int hs_read_vm(HsSolver* s, double* out, uint32_t n) {

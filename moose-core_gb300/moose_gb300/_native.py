@@ -48,6 +48,7 @@ def load(build_if_missing=True):
         "hs_add_gkek": (i32, [vp, u32, d, d]),
         "hs_add_conc": (i32, [vp, u32, d]),
         "hs_add_ica": (i32, [vp, u32, d]),
+        "hs_push_events": (i32, [vp, pu, pd, pd, u32]),
         "hs_read_vm": (i32, [vp, pd, u32]),
         "hs_read_ca": (i32, [vp, pd, u32]),
         "hs_record": (i32, [vp, pu, u32, u32, u32]),

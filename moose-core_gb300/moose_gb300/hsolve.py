@@ -59,6 +59,11 @@ class HHChannel2D(_Zombie):
 class SynChan(_Zombie):
     _kind = HS_KIND_SYNCHAN
 
+    def add_spike(self, time, weight=1.0, delay=0.0):
+        """`Synapse::addSpike` on a synapse of this SynChan's handler: the
+        event is queued for time + delay with the synapse's weight."""
+        self._s.push_events([self._i], [float(time) + float(delay)], [weight])
+
 
 class HSolve:
     """One HSolve instance on the GPU (FP64, reference operation order)."""
@@ -236,3 +241,17 @@ class HSolve:
     def add_ica(self, pool, ica):
         """The `current` message of a zombie CaConc (HSolve::iCa)."""
         _native.check(_native.load().hs_add_ica(self._h, pool, ica))
+
+    def push_events(self, syn, time, weight):
+        """Queue synaptic events at run time (SimpleSynHandler::addSpike):
+        event e reaches SynChan syn[e] at time[e] (spike time + synapse
+        delay) with weight[e]; delivered by the next process()."""
+        syn = np.ascontiguousarray(np.atleast_1d(syn), dtype=np.uint32)
+        time = np.ascontiguousarray(np.atleast_1d(time), dtype=np.float64)
+        weight = np.ascontiguousarray(np.atleast_1d(weight), dtype=np.float64)
+        if not (len(syn) == len(time) == len(weight)):
+            raise ValueError("syn, time and weight differ in length")
+        _native.check(_native.load().hs_push_events(
+            self._h, syn.ctypes.data_as(C.POINTER(C.c_uint32)),
+            time.ctypes.data_as(C.POINTER(C.c_double)),
+            weight.ctypes.data_as(C.POINTER(C.c_double)), len(syn)))

@@ -117,6 +117,11 @@ struct OrcCell {
     double* synDt;
     /* events per synchan, sorted by (time, input order) */
     uint32_t* evOff; double* evTime; double* evW; uint32_t* evPtr;
+    /* events queued at run time (SimpleSynHandler::addSpike after reinit):
+       per synchan a dvec pair sorted by (time, push order), consumed from
+       rtHead; tick 1 pops the two queues in time order, description first
+       on equal times */
+    dvec* rtTime; dvec* rtW; uint32_t* rtHead;
     /* spikegens */
     double* sgLast; int* sgFired; uint32_t* sgComptHines; uint32_t nSg;
     ivec spikeGen; dvec spikeTime;
@@ -919,6 +924,9 @@ OrcCell* orc_create(const HsCellDesc* d, uint32_t seed, double dt, char* err, ui
     c->evPtr = (uint32_t*)xcalloc(ns + 1, sizeof(uint32_t));
     c->evTime = (double*)xcalloc(d->n_event + 1, sizeof(double));
     c->evW = (double*)xcalloc(d->n_event + 1, sizeof(double));
+    c->rtTime = (dvec*)xcalloc(ns + 1, sizeof(dvec));
+    c->rtW = (dvec*)xcalloc(ns + 1, sizeof(dvec));
+    c->rtHead = (uint32_t*)xcalloc(ns + 1, sizeof(uint32_t));
     for (uint32_t e = 0; e < d->n_event; e++) {
         if (d->ev_syn[e] >= ns) FAIL("event synchan index out of range");
         c->evOff[d->ev_syn[e] + 1]++;
@@ -1010,6 +1018,7 @@ void orc_reinit(OrcCell* c, double clock_dt) {
         double dt = clock_dt;
         double tau1 = d->syn_tau1[k], tau2 = d->syn_tau2[k];
         c->evPtr[k] = c->evOff[k];
+        c->rtTime[k].n = 0; c->rtW[k].n = 0; c->rtHead[k] = 0;
         c->synDt[k] = dt;
         c->synAct[k] = 0.0; c->synGk[k] = 0.0; c->synX[k] = 0.0; c->synY[k] = 0.0;
         c->synXc1[k] = tau1 * (1.0 - exp(-dt / tau1));
@@ -1178,9 +1187,19 @@ void orc_step(OrcCell* c, uint32_t nsteps) {
         /* tick 1: SimpleSynHandler -> SynChan::activation */
         for (uint32_t k = 0; k < d->n_syn; k++) {
             double activation = 0.0;
-            while (c->evPtr[k] < c->evOff[k + 1] && c->evTime[c->evPtr[k]] <= currTime) {
-                activation += c->evW[c->evPtr[k]] / dt;
-                c->evPtr[k]++;
+            const dvec* rt = &c->rtTime[k];
+            for (;;) {
+                int desc = c->evPtr[k] < c->evOff[k + 1] && c->evTime[c->evPtr[k]] <= currTime;
+                int run = c->rtHead[k] < rt->n && rt->v[c->rtHead[k]] <= currTime;
+                if (desc && (!run || c->evTime[c->evPtr[k]] <= rt->v[c->rtHead[k]])) {
+                    activation += c->evW[c->evPtr[k]] / dt;
+                    c->evPtr[k]++;
+                } else if (run) {
+                    activation += c->rtW[k].v[c->rtHead[k]] / dt;
+                    c->rtHead[k]++;
+                } else {
+                    break;
+                }
             }
             if (activation != 0.0) c->synAct[k] += activation;
         }
@@ -1448,6 +1467,24 @@ int orc_add_ica(OrcCell* c, uint32_t pool, double ica) {
     return 0;
 }
 
+/* SimpleSynHandler::addSpike (synapse/SimpleSynHandler.cpp:86-90): the event
+   joins the synchan's queue behind every queued event with time <= its own
+   (the caller has added the synapse delay, synapse/Synapse.cpp:104-113). */
+int orc_push_event(OrcCell* c, uint32_t syn, double time, double weight) {
+    if (!c->d || syn >= c->d->n_syn || time != time) return HS_EINVAL;
+    dvec* t = &c->rtTime[syn];
+    dvec* w = &c->rtW[syn];
+    if (c->rtHead[syn] == t->n) { t->n = 0; w->n = 0; c->rtHead[syn] = 0; }
+    dpush(t, time);
+    dpush(w, weight);
+    size_t pos = t->n - 1;
+    while (pos > c->rtHead[syn] && t->v[pos - 1] > time) {
+        t->v[pos] = t->v[pos - 1]; w->v[pos] = w->v[pos - 1]; pos--;
+    }
+    t->v[pos] = time; w->v[pos] = weight;
+    return 0;
+}
+
 void orc_destroy(OrcCell* c) {
     if (!c) return;
     free(c->compartmentId); free(c->hinesOf); free(c->V); free(c->CmByDt); free(c->EmByRm);
@@ -1468,6 +1505,9 @@ void orc_destroy(OrcCell* c) {
     free(c->synX); free(c->synY); free(c->synAct); free(c->synGk);
     free(c->synXc1); free(c->synXc2); free(c->synYc1); free(c->synYc2); free(c->synNorm); free(c->synDt);
     free(c->evOff); free(c->evTime); free(c->evW); free(c->evPtr);
+    if (c->rtTime)
+        for (uint32_t k = 0; k < c->d->n_syn; k++) { free(c->rtTime[k].v); free(c->rtW[k].v); }
+    free(c->rtTime); free(c->rtW); free(c->rtHead);
     free(c->sgLast); free(c->sgFired); free(c->sgComptHines);
     free(c->spikeGen.v); free(c->spikeTime.v);
     free(c);

@@ -78,6 +78,10 @@ int orc_add_inject(OrcCell* c, uint32_t compt, double value);
 int orc_add_gkek(OrcCell* c, uint32_t compt, double Gk, double Ek);
 int orc_add_conc(OrcCell* c, uint32_t chan, double conc);
 int orc_add_ica(OrcCell* c, uint32_t pool, double ica);
+/* Synaptic event queued at run time (SimpleSynHandler::addSpike): delivered
+ * at the first step whose clock time is >= time, as weight/dt; dropped by
+ * reinit.  0, or HS_EINVAL for a bad index or a NaN time. */
+int orc_push_event(OrcCell* c, uint32_t syn, double time, double weight);
 
 /* Passive known-answer interface (HinesMatrix/HSolvePassive unit tests):
  * tree given directly in Hines order as child lists (CSR). */

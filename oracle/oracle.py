@@ -67,6 +67,8 @@ def lib():
         for f in ("orc_add_inject", "orc_add_conc", "orc_add_ica"):
             getattr(L, f).restype = C.c_int
             getattr(L, f).argtypes = [vp, C.c_uint32, C.c_double]
+        L.orc_push_event.restype = C.c_int
+        L.orc_push_event.argtypes = [vp, C.c_uint32, C.c_double, C.c_double]
         L.orc_add_gkek.restype = C.c_int
         L.orc_add_gkek.argtypes = [vp, C.c_uint32, C.c_double, C.c_double]
         L.orc_passive_create.restype = vp
@@ -170,6 +172,12 @@ class OracleCell:
     def add_ica(self, pool, ica):
         if lib().orc_add_ica(self.h, int(pool), float(ica)):
             raise IndexError("oracle add_ica failed")
+
+    def push_events(self, syn, time, weight):
+        """SimpleSynHandler::addSpike for each (syn, time, weight), in order."""
+        for k, t, w in zip(np.atleast_1d(syn), np.atleast_1d(time), np.atleast_1d(weight)):
+            if lib().orc_push_event(self.h, int(k), float(t), float(w)):
+                raise IndexError("oracle push_events failed")
 
 
 class OraclePassive:

@@ -67,5 +67,11 @@ extern "C" int hsolve_cpp_errors(const HsCellDesc* d) {
     } catch (const moose_gb300::Error& e) {
         if (e.code() != HS_EINVAL) return 7;
     }
+    try {
+        h.addSpike(0, 1e-3, 1e-9);                // no solver: rejected like a field access
+        return 8;
+    } catch (const moose_gb300::Error& e) {
+        if (e.code() != HS_EINVAL) return 9;
+    }
     return 0;
 }

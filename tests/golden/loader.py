@@ -41,3 +41,29 @@ def replay_messages(z, solver, per_step):
             ca.append(solver.ca()[recp])
     return np.array(vm).T, np.array(ca).T
 
+
+
+def push_pre_reinit(z, solver):
+    """The events active_events.npz pushed before reinit (synapse 1 of each
+    SynChan, delay added as Synapse::addSpike adds it); reinit drops them."""
+    k = z["pre_syn"]
+    solver.push_events(k, z["pre_time"] + z["syn_delay"][k, 1], z["syn_weight"][k, 1])
+
+
+def replay_events(z, solver, advance):
+    """Drive `solver` (oracle or GPU drop-in, after reinit) through
+    active_events.npz: `advance(solver, n)` steps it, and once `push_step`
+    steps have run the events of that chunk are pushed with time = spike
+    time + synapse delay and the synapse's weight.  Returns the Vm samples
+    of the reference's Tables (every `stride` steps, sample 0 at reinit)."""
+    w, dl = z["syn_weight"], z["syn_delay"]
+    ps, pk, pj, pt = z["push_step"], z["push_syn"], z["push_synapse"], z["push_time"]
+    rec, stride, n = z["rec"], int(z["stride"]), int(z["nsteps"])
+    vm = [solver.vm()[rec]]
+    for cur in range(0, n, stride):
+        sel = ps == cur
+        if sel.any():
+            solver.push_events(pk[sel], pt[sel] + dl[pk[sel], pj[sel]], w[pk[sel], pj[sel]])
+        advance(solver, stride)
+        vm.append(solver.vm()[rec])
+    return np.array(vm).T

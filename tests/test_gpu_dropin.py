@@ -12,8 +12,8 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from loader import load_model, replay_messages
-from moose_gb300 import models
+from loader import load_model, push_pre_reinit, replay_events, replay_messages
+from moose_gb300 import _native, models
 from moose_gb300.abi import HS_KIND_CHAN, HS_KIND_COMPT, HS_KIND_POOL, FIELDS, CellModel
 from moose_gb300.hsolve import HSolve
 from oracle import OracleCell
@@ -183,3 +183,97 @@ def test_add_gkek_matches_oracle():
         oc.step(1)
     assert np.array_equal(h.vm(), oc.vm())
     assert np.array_equal(h.ca(), oc.ca())
+
+
+def test_runtime_events_golden():
+    """hs_push_events between process calls (SimpleSynHandler::addSpike via
+    Synapse::addSpike): bit-exact with the oracle on this host, and with the
+    reference HSolve (active_events.npz) to 1e-12 -- the SynChan constants
+    come from the host libm's exp, which may differ by an ulp between the
+    machine that wrote the golden and this one.  Same spike times."""
+    z = np.load(os.path.join(GOLDEN, "active_events.npz"))
+    m = load_model(z)
+    dt = float(z["dt"])
+    h = HSolve(m, dt=dt)
+    h.target = m.seed
+    push_pre_reinit(z, h)
+    h.reinit(dt)
+    vm = replay_events(z, h, lambda s, n: s.process(n))
+    oc = OracleCell(m, dt)
+    push_pre_reinit(z, oc)
+    oc.reinit(dt)
+    ovm = replay_events(z, oc, lambda s, n: s.step(n))
+    assert np.array_equal(vm, ovm)
+    assert np.array_equal(h.vm(), oc.vm())
+    assert np.array_equal(h.spikes()[1], oc.spikes()[1])
+    ref = z["vm"]
+    assert np.all(np.abs(vm - ref) <= 1e-12 * np.maximum(np.abs(ref), 1e-3))
+    assert len(h.spikes()[1]) == len(z["spikes"])
+
+
+def test_runtime_events_reinit_ties_and_growth():
+    """Pushes of growing size (the device queue is reallocated several
+    times), ties on one SynChan with different weights (summed in push
+    order), events at -inf/+inf, a SynChan view's add_spike with a delay,
+    and a reinit in the middle that drops the queued runtime events and
+    queues the description's again: bit-exact with the oracle throughout."""
+    z = np.load(os.path.join(GOLDEN, "active_events.npz"))
+    m = load_model(z)
+    dt = 25e-6
+    ns = len(m.syn_compt)
+    h = HSolve(m, dt=dt)
+    h.target = m.seed
+    h.reinit(dt)
+    oc = OracleCell(m, dt)
+    oc.reinit(dt)
+    rng = np.random.default_rng(5)
+    step = 0
+    for rnd in range(2):
+        for chunk in range(8):
+            n = 40 * 4 ** min(chunk, 4)
+            k = rng.integers(0, ns, n)
+            t = dt * step + rng.uniform(-2e-3, 6e-3, n)
+            w = rng.uniform(0.1e-9, 1e-9, n)
+            t[: n // 8] = dt * (step + 3) + 0.5 * dt          # ties with different weights
+            k[: n // 8] = chunk % ns
+            h.push_events(k, t, w)
+            oc.push_events(k, t, w)
+            if chunk == 2:
+                inf = [-np.inf, np.inf]
+                h.push_events([1, 2], inf, [1e-9, 1e-9])
+                oc.push_events([1, 2], inf, [1e-9, 1e-9])
+                h.synchan(3).add_spike(dt * step, 0.7e-9, delay=1.1e-3)
+                oc.push_events([3], [dt * step + 1.1e-3], [0.7e-9])
+            h.process(100)
+            oc.step(100)
+            step += 100
+            assert np.array_equal(h.vm(), oc.vm())
+        h.push_events([0, 1], [dt * (step + 5)] * 2, [5e-9, 5e-9])    # dropped by the reinit
+        oc.push_events([0, 1], [dt * (step + 5)] * 2, [5e-9, 5e-9])
+        h.reinit(dt)
+        oc.reinit(dt)
+        step = 0
+    h.process(200)
+    oc.step(200)
+    assert np.array_equal(h.vm(), oc.vm())
+    assert np.array_equal(h.spikes()[1], oc.spikes()[1])
+
+
+def test_push_events_rejects_bad_input():
+    z = np.load(os.path.join(GOLDEN, "active_events.npz"))
+    m = load_model(z)
+    h = HSolve(m, dt=25e-6)
+    h.target = m.seed
+    h.reinit(25e-6)
+    with pytest.raises(_native.HsError):
+        h.push_events([len(m.syn_compt)], [1e-3], [1e-9])
+    with pytest.raises(_native.HsError):
+        h.push_events([0, 1], [1e-3, float("nan")], [1e-9, 1e-9])
+    h.push_events([], [], [])
+    # the rejected calls queued nothing: the run equals one without pushes
+    ref = HSolve(m, dt=25e-6)
+    ref.target = m.seed
+    ref.reinit(25e-6)
+    h.process(300)
+    ref.process(300)
+    assert np.array_equal(h.vm(), ref.vm())

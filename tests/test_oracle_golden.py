@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from loader import load_model, replay_messages
+from loader import load_model, push_pre_reinit, replay_events, replay_messages
 from oracle import OracleCell, OraclePassive
 
 H = lambda v: np.array([float.fromhex(x) for x in v])
@@ -102,3 +102,64 @@ def test_message_destinations_and_ca_gates_bit_exact():
     assert np.array_equal(vm, z["vm"])
     assert np.array_equal(ca, z["ca"])
     assert np.array_equal(oc.vm(), z["final_vm"])
+
+
+def test_runtime_events_bit_exact():
+    """Synaptic events pushed between process calls (SimpleSynHandler::addSpike
+    via Synapse::addSpike with its delay): late events, events on a step's
+    clock time, two synapses of one handler, events pushed before reinit
+    (dropped), against the reference HSolve (active_events.npz)."""
+    z = np.load(os.path.join(GOLDEN, "active_events.npz"))
+    m = load_model(z)
+    dt = float(z["dt"])
+    oc = OracleCell(m, dt)
+    push_pre_reinit(z, oc)
+    oc.reinit(dt)
+    vm = replay_events(z, oc, lambda s, n: s.step(n))
+    assert np.array_equal(vm, z["vm"])
+    assert np.array_equal(oc.vm(), z["final_vm"])
+    assert np.array_equal(oc.spikes()[1], z["spikes"])
+
+
+def test_runtime_events_change_the_trace():
+    """The pushed events matter: without them the trace differs from the
+    golden (so the bit-exact match above is not vacuous)."""
+    z = np.load(os.path.join(GOLDEN, "active_events.npz"))
+    m = load_model(z)
+    dt = float(z["dt"])
+    oc = OracleCell(m, dt)
+    oc.reinit(dt)
+    oc.step(int(z["nsteps"]))
+    assert not np.array_equal(oc.vm(), z["final_vm"])
+
+
+def test_oracle_push_event_rejects_bad_input():
+    z = np.load(os.path.join(GOLDEN, "active_events.npz"))
+    oc = OracleCell(load_model(z), float(z["dt"]))
+    with pytest.raises(IndexError):
+        oc.push_events([len(z["model_syn_compt"])], [0.0], [1e-9])
+    with pytest.raises(IndexError):
+        oc.push_events([0], [float("nan")], [1e-9])
+
+
+def test_runtime_events_golden_pins_reinit_drop_and_clock_time():
+    """Two mistakes planted in how the oracle is driven both break the match:
+    keeping the events pushed before reinit, and events on a step's clock
+    time arriving one ulp later (one step late).  So the golden pins
+    SimpleSynHandler::vReinit's drop and the `time <= currTime` test."""
+    z = np.load(os.path.join(GOLDEN, "active_events.npz"))
+    m = load_model(z)
+    dt = float(z["dt"])
+    oc = OracleCell(m, dt)
+    oc.reinit(dt)
+    push_pre_reinit(z, oc)
+    assert not np.array_equal(replay_events(z, oc, lambda s, n: s.step(n)), z["vm"])
+    zz = dict(z)
+    pt = zz["push_time"].copy()
+    on_clock = pt == dt * np.round(pt / dt)
+    assert on_clock.sum() >= 50
+    pt[on_clock] = np.nextafter(pt[on_clock], np.inf)
+    zz["push_time"] = pt
+    oc = OracleCell(m, dt)
+    oc.reinit(dt)
+    assert not np.array_equal(replay_events(zz, oc, lambda s, n: s.step(n)), z["vm"])
