@@ -441,11 +441,23 @@ def run_ours(args, rank, world, cpu_pool):
             h.process(n1)
             h.sync()
             g_s = time.perf_counter() - t0
+            # zombie field access between steps, as a script reading every
+            # compartment's Vm after each step does: one step, then all reads
+            comps = [h.compartment(i) for i in range(m1.n_compt)]
+            t0 = time.perf_counter()
+            for _ in range(20):
+                h.process(1)
+                for c in comps:
+                    c.Vm
+            f_s = time.perf_counter() - t0
             h.close()
             single = {"workload": "single cell: soma + 200-compartment HH cable (Na m3h, K n4), 20,000 dt steps "
                                   "of 25 us (0.5 s), FP64 drop-in through hs_process", "wall_s": g_s,
                       "value": m1.n_compt * n1 / g_s, "unit": "compartment-steps/s",
-                      "us_per_step": g_s / n1 * 1e6}
+                      "us_per_step": g_s / n1 * 1e6,
+                      "step_and_read_all_vm_us": f_s / 20 * 1e6,
+                      "field_access": "one dt step then Vm of all %d compartments through hs_get_field, "
+                                      "from Python" % m1.n_compt}
         cpu = None
         if cpu_pool is not None:
             tcpu = cpu_pool.step(args.cpu_chunk)

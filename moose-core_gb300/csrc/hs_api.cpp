@@ -10,8 +10,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <new>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/moose_gb300.h"
@@ -67,9 +69,95 @@ struct HsSolver {
     const uint32_t* descPtr = nullptr;
     uint32_t* descCur = nullptr;
     const double *descTime = nullptr, *descW = nullptr;
+    // Field access mirror (see readDev/writeDev): host copies of arena
+    // pages, valid while their epoch is the solver's; the epoch moves on
+    // whenever device work may have changed the arena.  Writes wait in
+    // `writes` (last one per address) until flushWrites scatters them.
+    uint64_t epoch = 1;
+    std::unordered_map<size_t, std::pair<uint64_t, std::vector<uint8_t>>> pages;
+    std::map<uintptr_t, FieldWrite> writes;
+    std::vector<FieldWrite> writeList;
+    FieldWrite* dWrites = nullptr;
+    size_t dWritesCap = 0;
 };
 
 namespace {
+
+// ---- field access between process calls ------------------------------------
+// The zombie get/set calls (hsolve/HSolveInterface.cpp) arrive one field at a
+// time, typically many between two steps (a script reading every
+// compartment's Vm, Tables polling, message destinations read-modify-writing
+// their targets).  They are served from a host mirror of the solver's arena
+// in pages of kPage bytes: a page is copied from the device on its first read
+// after the device last ran; a write updates the mirror and is queued; the
+// queue is applied by one scatter kernel before the next launch, before any
+// page is copied again and before any direct device read.  So a burst of
+// field reads costs one device round trip per page touched, and writes cost
+// none until the next step.
+constexpr size_t kPage = 64 * 1024;
+
+// Applies the queued writes on the solver's stream (no wait: the launch or
+// copy that needs them is queued behind the scatter).
+int flushWrites(HsSolver* s) {
+    if (s->writes.empty()) return HS_OK;
+    s->writeList.clear();
+    for (const auto& kv : s->writes) s->writeList.push_back(kv.second);
+    const size_t n = s->writeList.size();
+    if (n > s->dWritesCap) {
+        // cudaFree waits for the device, so no scatter still reads the old list
+        if (s->dWrites) cudaFree(s->dWrites);
+        s->dWrites = nullptr;
+        s->dWritesCap = 0;
+        const size_t cap = std::max<size_t>(n, 256);
+        cudaError_t e = cudaMalloc(&s->dWrites, cap * sizeof(FieldWrite));
+        if (e != cudaSuccess) {
+            s->dWrites = nullptr;
+            return cudaErr(e, "field write");
+        }
+        s->dWritesCap = cap;
+    }
+    // the pageable source is staged by the copy call itself
+    cudaError_t e = cudaMemcpyAsync(s->dWrites, s->writeList.data(), n * sizeof(FieldWrite),
+                                    cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess) e = launchScatterFields(s->dWrites, (uint32_t)n, s->st);
+    if (e != cudaSuccess) return cudaErr(e, "field write");
+    s->writes.clear();
+    return HS_OK;
+}
+
+// Device work changed (or may have changed) the arena: every mirrored page
+// is stale.
+void arenaMoved(HsSolver* s) { ++s->epoch; }
+
+// The arena page holding [a, a + n), or -1 when the range is not inside one
+// page of the arena.
+int64_t pageOf(const HsSolver* s, const void* p, size_t n) {
+    const uintptr_t a = (uintptr_t)p, base = (uintptr_t)s->arena.base;
+    if (!s->arena.base || a < base || a + n > base + s->arena.size) return -1;
+    const size_t off = a - base;
+    if (off / kPage != (off + n - 1) / kPage) return -1;
+    return (int64_t)(off / kPage);
+}
+
+// The current host copy of arena page `idx`.
+int mirrorPage(HsSolver* s, size_t idx, uint8_t** out) {
+    auto& pg = s->pages[idx];
+    if (pg.first != s->epoch) {
+        int rc = flushWrites(s);
+        if (rc) return rc;
+        const size_t off = idx * kPage, n = std::min(kPage, s->arena.size - off);
+        pg.second.resize(n);
+        cudaError_t e = cudaMemcpyAsync(pg.second.data(), s->arena.base + off, n, cudaMemcpyDeviceToHost, s->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        if (e != cudaSuccess) {
+            pg.first = 0;
+            return cudaErr(e, "field read");
+        }
+        pg.first = s->epoch;
+    }
+    *out = pg.second.data();
+    return HS_OK;
+}
 
 // Hands the pushed events to the device before a process call.  Per SynChan
 // the new queue is the events not yet delivered (from the device cursor on)
@@ -257,6 +345,7 @@ int hs_destroy(HsSolver* s) {
     if (s->recBuf) cudaFree(s->recBuf);
     if (s->ownIdx) cudaFree(s->ownIdx);
     if (s->ownEv) cudaFree(s->ownEv);
+    if (s->dWrites) cudaFree(s->dWrites);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
     return HS_OK;
@@ -282,6 +371,9 @@ int hs_reinit(HsSolver* s, double clock_dt) {
     }
     std::vector<double> sc(5 * (size_t)s->P.S + 1);
     synConsts(s->P, clock_dt, sc.data());
+    int rc = flushWrites(s);
+    if (rc) return rc;
+    arenaMoved(s);
     cudaError_t e = cudaMemcpyAsync((void*)s->dc.synConst, sc.data(), 5 * (size_t)s->P.S * 8,
                                     cudaMemcpyHostToDevice, s->st);
     if (e == cudaSuccess)
@@ -299,7 +391,9 @@ int hs_process(HsSolver* s, uint32_t nsteps) {
     if (!s->reinited) return setErr(HS_ESTATE, "reinit before process");
     if (nsteps == 0) return HS_OK;
     int rc = flushEvents(s);
+    if (!rc) rc = flushWrites(s);
     if (rc) return rc;
+    arenaMoved(s);
     cudaError_t e = launchStepFp64(s->dc, nsteps, s->st);
     if (e != cudaSuccess) return cudaErr(e, "process");
     return HS_OK;
@@ -307,6 +401,7 @@ int hs_process(HsSolver* s, uint32_t nsteps) {
 
 int hs_sync(HsSolver* s) {
     if (!s) return setErr(HS_EINVAL, "null solver");
+    if (int rc = flushWrites(s)) return rc;
     cudaError_t e = cudaStreamSynchronize(s->st);
     if (e != cudaSuccess) return cudaErr(e, "sync");
     return HS_OK;
@@ -339,6 +434,7 @@ int hs_get_table_grid(HsSolver* s, double* vmin, double* vmax, int* vdiv, double
 
 int hs_get_nsteps(HsSolver* s, uint64_t* out) {
     if (!s || !out) return setErr(HS_EINVAL, "null argument");
+    if (int rc = flushWrites(s)) return rc;
     DevCtl ctl;
     cudaError_t e = cudaMemcpyAsync(&ctl, s->dc.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, s->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
@@ -351,17 +447,43 @@ int hs_get_nsteps(HsSolver* s, uint64_t* out) {
 
 namespace {
 
+// One field value through the mirror (every field lives in the arena).
 template <class T>
 int readDev(HsSolver* s, const T* p, T* out) {
-    cudaError_t e = cudaMemcpyAsync(out, p, sizeof(T), cudaMemcpyDeviceToHost, s->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
-    return e == cudaSuccess ? HS_OK : cudaErr(e, "field read");
+    const int64_t idx = pageOf(s, p, sizeof(T));
+    if (idx < 0) {
+        int rc = flushWrites(s);
+        if (rc) return rc;
+        cudaError_t e = cudaMemcpyAsync(out, p, sizeof(T), cudaMemcpyDeviceToHost, s->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        return e == cudaSuccess ? HS_OK : cudaErr(e, "field read");
+    }
+    uint8_t* pg;
+    int rc = mirrorPage(s, (size_t)idx, &pg);
+    if (rc) return rc;
+    std::memcpy(out, pg + ((const uint8_t*)p - (const uint8_t*)s->arena.base - (size_t)idx * kPage), sizeof(T));
+    return HS_OK;
 }
 template <class T>
 int writeDev(HsSolver* s, T* p, T v) {
-    cudaError_t e = cudaMemcpyAsync(p, &v, sizeof(T), cudaMemcpyHostToDevice, s->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
-    return e == cudaSuccess ? HS_OK : cudaErr(e, "field write");
+    static_assert(sizeof(T) == 1 || sizeof(T) == 4 || sizeof(T) == 8, "field write size");
+    const int64_t idx = pageOf(s, p, sizeof(T));
+    if (idx < 0 || ((uintptr_t)p % sizeof(T)) != 0) {
+        int rc = flushWrites(s);
+        if (rc) return rc;
+        cudaError_t e = cudaMemcpyAsync(p, &v, sizeof(T), cudaMemcpyHostToDevice, s->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        arenaMoved(s);
+        return e == cudaSuccess ? HS_OK : cudaErr(e, "field write");
+    }
+    FieldWrite w{p, 0ull, (uint32_t)sizeof(T), 0u};
+    std::memcpy(&w.bits, &v, sizeof(T));
+    s->writes[(uintptr_t)p] = w;
+    auto it = s->pages.find((size_t)idx);
+    if (it != s->pages.end() && it->second.first == s->epoch)
+        std::memcpy(it->second.second.data() + ((uint8_t*)p - (uint8_t*)s->arena.base - (size_t)idx * kPage), &v,
+                    sizeof(T));
+    return HS_OK;
 }
 
 int comptIndex(HsSolver* s, uint32_t m, uint32_t* h) {
@@ -641,6 +763,7 @@ int hs_push_events(HsSolver* s, const uint32_t* syn, const double* time, const d
 int hs_read_vm(HsSolver* s, double* out, uint32_t n) {
     if (!s || !out) return setErr(HS_EINVAL, "null argument");
     if (n != s->P.hinesOf.size()) return setErr(HS_EINVAL, "n must equal the model's compartment count");
+    if (int rc = flushWrites(s)) return rc;
     std::vector<double> v(s->P.N);
     cudaError_t e = cudaMemcpyAsync(v.data(), s->dc.V, v.size() * 8, cudaMemcpyDeviceToHost, s->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
@@ -652,6 +775,7 @@ int hs_read_vm(HsSolver* s, double* out, uint32_t n) {
 int hs_read_ca(HsSolver* s, double* out, uint32_t n) {
     if (!s || !out) return setErr(HS_EINVAL, "null argument");
     if (n != s->P.poolSolverOf.size()) return setErr(HS_EINVAL, "n must equal the model's pool count");
+    if (int rc = flushWrites(s)) return rc;
     std::vector<double> v(s->P.P + 1);
     cudaError_t e = cudaMemcpyAsync(v.data(), s->dc.ca, s->P.P * 8, cudaMemcpyDeviceToHost, s->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
@@ -692,6 +816,7 @@ int hs_record(HsSolver* s, const uint32_t* compts, uint32_t n, uint32_t stride, 
 
 int hs_read_trace(HsSolver* s, double* out, uint32_t capacity, uint32_t* n_samples) {
     if (!s || !n_samples) return setErr(HS_EINVAL, "null argument");
+    if (int rc = flushWrites(s)) return rc;
     DevCtl ctl;
     cudaError_t e = cudaMemcpyAsync(&ctl, s->dc.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, s->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
@@ -708,6 +833,7 @@ int hs_read_trace(HsSolver* s, double* out, uint32_t capacity, uint32_t* n_sampl
 
 int hs_read_spikes(HsSolver* s, uint32_t* gen, double* time, uint32_t capacity, uint32_t* n) {
     if (!s || !n) return setErr(HS_EINVAL, "null argument");
+    if (int rc = flushWrites(s)) return rc;
     DevCtl ctl;
     cudaError_t e = cudaMemcpyAsync(&ctl, s->dc.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, s->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);

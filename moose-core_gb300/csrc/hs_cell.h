@@ -45,6 +45,9 @@ cudaError_t layoutCell(const CellPlan& P, Arena& a, DevCell& dc, uint32_t spikeC
 void synConsts(const CellPlan& P, double dt, double* out);
 
 cudaError_t launchStepFp64(const DevCell& c, uint32_t nsteps, cudaStream_t st);
+// The queued field writes of a drop-in solver, one thread each (distinct
+// addresses).
+cudaError_t launchScatterFields(const FieldWrite* w, uint32_t n, cudaStream_t st);
 // HSolveActive::reinit + tick-1/4 object reinit of `nCells` cells, on device.
 cudaError_t launchReinitFp64(const DevCell* cells, uint32_t nCells, cudaStream_t st);
 cudaError_t launchBatchStepFp64(const DevCell* cells, const uint32_t* warpCellPtr,

@@ -90,6 +90,15 @@ struct DevCell {
     DevCtl* ctl;
 };
 
+// One queued field write of the drop-in: `size` (1, 4 or 8) bytes of `bits`
+// to `addr`, an address inside the solver's arena aligned to `size`.
+struct FieldWrite {
+    void* addr;
+    unsigned long long bits;
+    uint32_t size;
+    uint32_t pad;
+};
+
 // ---------------------------------------------------------------------------
 // FP64 helpers, reference order
 

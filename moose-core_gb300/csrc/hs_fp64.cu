@@ -374,6 +374,21 @@ __global__ void hsReinitFp64(const DevCell* __restrict__ cells, uint32_t nCells)
     }
 }
 
+__global__ void hsScatterFields(const FieldWrite* __restrict__ w, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const FieldWrite x = w[i];
+    if (x.size == 8) *static_cast<unsigned long long*>(x.addr) = x.bits;
+    else if (x.size == 4) *static_cast<uint32_t*>(x.addr) = (uint32_t)x.bits;
+    else *static_cast<uint8_t*>(x.addr) = (uint8_t)x.bits;
+}
+
+cudaError_t launchScatterFields(const FieldWrite* w, uint32_t n, cudaStream_t st) {
+    if (!n) return cudaSuccess;
+    hsScatterFields<<<(n + 255) / 256, 256, 0, st>>>(w, n);
+    return cudaGetLastError();
+}
+
 cudaError_t launchStepFp64(const DevCell& c, uint32_t nsteps, cudaStream_t st) {
     hsStepFp64<<<1, 256, 0, st>>>(c, nsteps);
     return cudaGetLastError();

@@ -277,3 +277,73 @@ def test_push_events_rejects_bad_input():
     h.process(300)
     ref.process(300)
     assert np.array_equal(h.vm(), ref.vm())
+
+
+def test_field_access_between_steps_matches_oracle():
+    """Zombie field reads and writes between process calls (served by the
+    solver's host mirror of its device arena, writes queued until the next
+    launch): reads after a step see the step's values; a read right after a
+    write sees the write, also through the bulk read; the last of two writes
+    to one field wins; message destinations accumulate within a step;
+    CaConc setCa/setCaBasal read-modify-write; every value equal to the
+    oracle's, and the run stays bit-exact with it."""
+    z = np.load(os.path.join(GOLDEN, "active_msgs.npz"))
+    m = load_model(z)
+    dt = 25e-6
+    h = HSolve(m, dt=dt)
+    h.target = m.seed
+    h.reinit(dt)
+    oc = OracleCell(m, dt)
+    oc.reinit(dt)
+    n, nch, npool = m.n_compt, len(m.chan_compt), len(m.pool_compt)
+    rng = np.random.default_rng(9)
+    C, CH, PL = HS_KIND_COMPT, HS_KIND_CHAN, HS_KIND_POOL
+
+    def same(kind, f, i):
+        a, b = h._get(kind, FIELDS[f], i), oc.get(kind, FIELDS[f], i)
+        assert a == b, (kind, f, i, a, b)
+        return a
+
+    def put(kind, f, i, v):
+        h._set(kind, FIELDS[f], i, v)
+        oc.set(kind, FIELDS[f], i, v)
+
+    for rnd in range(6):
+        h.process(37)
+        oc.step(37)
+        for i in range(n):
+            same(C, "Vm", i)
+        for i in range(0, n, 5):
+            same(C, "Im", i)
+        for q in range(0, nch, 7):
+            for f in ("Gk", "Ik", "X", "Y"):
+                same(CH, f, q)
+        for p in range(0, npool, 3):
+            same(PL, "Ca", p)
+        i = int(rng.integers(0, n))
+        v = float(rng.uniform(-0.07, -0.05))
+        put(C, "Vm", i, -0.03)
+        put(C, "Vm", i, v)
+        assert same(C, "Vm", i) == v
+        assert h.vm()[i] == v
+        q = int(rng.integers(0, nch))
+        put(CH, "Gbar", q, float(rng.uniform(1e-9, 3e-8)))
+        same(CH, "Gbar", q)
+        p = int(rng.integers(0, npool))
+        put(PL, "Ca", p, float(rng.uniform(6e-5, 2e-4)))
+        same(PL, "Ca", p)
+        put(PL, "CaBasal", p, float(rng.uniform(4e-5, 6e-5)))
+        same(PL, "Ca", p)
+        put(C, "inject", 0, float(rng.uniform(0.1e-9, 0.5e-9)))
+        same(C, "inject", 0)
+        for val in (1e-10, 2.5e-10):
+            h.add_inject(0, val)
+            oc.add_inject(0, val)
+        h.add_ica(0, 1e-12)
+        oc.add_ica(0, 1e-12)
+        h.add_ica(0, 2e-12)
+        oc.add_ica(0, 2e-12)
+    h.process(50)
+    oc.step(50)
+    assert np.array_equal(h.vm(), oc.vm())
+    assert np.array_equal(h.ca(), oc.ca())
