@@ -261,6 +261,10 @@ int hs_get_nsteps(HsSolver* s, uint64_t* out);
 #define HS_F_TAU      34   /* write-only pair with B: set both via hs_set_tau_b */
 #define HS_F_B        35
 
+/* Between process calls, reads are served from a host mirror of the
+ * solver's device memory (refreshed page by page after each process), and
+ * writes are queued and applied before the next process, reinit or bulk
+ * read; a read always sees the writes made before it. */
 int hs_get_field(HsSolver* s, int kind, int field, uint32_t index, double* out);
 int hs_set_field(HsSolver* s, int kind, int field, uint32_t index, double value);
 int hs_set_tau_b(HsSolver* s, uint32_t pool, double tau, double B);
