@@ -142,9 +142,22 @@ __device__ __forceinline__ void eliminateWarp(const DevCell& c, uint32_t lane) {
     double* M = c.M;
     for (uint32_t l = 0; l < c.fLevels; ++l) {
         for (uint32_t k = c.fLevelPtr[l] + lane; k < c.fLevelPtr[l + 1]; k += 32) {
+            // t -= l / pivot * a.  A row's consecutive updates by one pivot
+            // (its diagonal and right-hand side: the reference computes
+            // HS[4i+1] / HS[4i] for both) share the quotient: it is computed
+            // once, the same IEEE division of the same operands, which takes
+            // one FP64 division off each level of the dependency chain.
+            int32_t ql = -1, qp = -1;
+            double q = 0.0;
             for (uint32_t o = c.fOpPtr[k]; o < c.fOpPtr[k + 1]; ++o) {
                 int4 op = c.fOps[o];
-                M[op.x] -= M[op.y] / M[op.w] * M[op.z];
+                if (op.y != ql || op.w != qp) {
+                    q = M[op.y] / M[op.w];
+                    ql = op.y;
+                    qp = op.w;
+                }
+                M[op.x] -= q * M[op.z];
+                if (op.x == ql || op.x == qp) ql = -1;   // an operand changed
             }
         }
         __syncwarp();
