@@ -69,6 +69,10 @@ cudaError_t layoutCell(const CellPlan& P, Arena& a, DevCell& c, uint32_t spikeCa
     c.bRows = u.put(P.bRows);
     c.bTermPtr = u.put(P.bTermPtr);
     c.bTerms = reinterpret_cast<const int2*>(u.put(P.bTerms));
+    c.fRun = u.put(P.fRun);
+    c.fRunRow = u.put(P.fRunRow);
+    c.bRun = u.put(P.bRun);
+    c.bRunRow = u.put(P.bRunRow);
     c.Gbar = u.put(P.Gbar);
     c.Ek = u.put(P.Ek);
     c.Xpow = u.put(P.Xpow);

@@ -41,6 +41,7 @@ struct DevCell {
     const int4* fOps;
     const uint32_t *bLevelPtr, *bRows, *bTermPtr;
     const int2* bTerms;
+    const uint32_t *fRun, *fRunRow, *bRun, *bRunRow;   // cable runs per level
     // channels
     double *Gbar, *Ek, *Xpow, *Ypow, *Zpow, *mod, *Gk, *state, *extCa;
     int32_t* instant;

@@ -138,9 +138,64 @@ __device__ __forceinline__ void comptStep(const DevCell& c, uint32_t ic) {
 }
 
 // ---- elimination (one warp) -------------------------------------------------
+// A level costs the eliminating warp ~150 instructions of index loads and
+// loop control around its few FP64 operations, all on one dependency chain.
+// A run of cable rows (one row per level, see CellPlan::fRun/bRun) is walked
+// by lane 0 alone with the pivot's values carried in registers, the row
+// indices computed (row r: diagonal M[r], right-hand side M[N + r],
+// off-diagonal to r + 1 at M[2N + H + r]) and the next row's operands loaded
+// ahead; the operations and their order are those of the general loop.
+__device__ __forceinline__ void forwardCableRun(const DevCell& c, uint32_t r, uint32_t run) {
+    double* M = c.M;
+    const uint32_t N = c.N, offBase = 2 * N + c.H;
+    double d = M[r - 1], rhs = M[N + r - 1];
+    double off = M[offBase + r - 1], dNext = M[r], rNext = M[N + r];
+    for (uint32_t i = 0; i < run; ++i, ++r) {
+        const double o = off, dr = dNext, rr = rNext;
+        if (i + 1 < run) {
+            off = M[offBase + r];
+            dNext = M[r + 1];
+            rNext = M[N + r + 1];
+        }
+        const double q = o / d;
+        d = dr - q * o;
+        rhs = rr - q * rhs;
+        M[r] = d;
+        M[N + r] = rhs;
+    }
+}
+
+__device__ __forceinline__ void backwardCableRun(const DevCell& c, uint32_t i, uint32_t run) {
+    const double* M = c.M;
+    const uint32_t N = c.N, offBase = 2 * N + c.H;
+    double vNext = c.VMid[i + 1];
+    double rhs = M[N + i], off = M[offBase + i], diag = M[i], vOld = c.V[i];
+    for (uint32_t j = 0; j < run; ++j, --i) {
+        const double r = rhs, o = off, dg = diag, vo = vOld;
+        if (j + 1 < run) {
+            rhs = M[N + i - 1];
+            off = M[offBase + i - 1];
+            diag = M[i - 1];
+            vOld = c.V[i - 1];
+        }
+        double v = r;
+        v -= o * vNext;
+        v /= dg;
+        c.VMid[i] = v;
+        c.V[i] = 2 * v - vo;
+        vNext = v;
+    }
+}
+
 __device__ __forceinline__ void eliminateWarp(const DevCell& c, uint32_t lane) {
     double* M = c.M;
     for (uint32_t l = 0; l < c.fLevels; ++l) {
+        if (const uint32_t run = c.fRun[l]) {
+            if (lane == 0) forwardCableRun(c, c.fRunRow[l], run);
+            __syncwarp();
+            l += run - 1;
+            continue;
+        }
         for (uint32_t k = c.fLevelPtr[l] + lane; k < c.fLevelPtr[l + 1]; k += 32) {
             // t -= l / pivot * a.  A row's consecutive updates by one pivot
             // (its diagonal and right-hand side: the reference computes
@@ -164,6 +219,12 @@ __device__ __forceinline__ void eliminateWarp(const DevCell& c, uint32_t lane) {
     }
     const uint32_t N = c.N;
     for (uint32_t l = 0; l < c.bLevels; ++l) {
+        if (const uint32_t run = c.bRun[l]) {
+            if (lane == 0) backwardCableRun(c, c.bRunRow[l], run);
+            __syncwarp();
+            l += run - 1;
+            continue;
+        }
         for (uint32_t k = c.bLevelPtr[l] + lane; k < c.bLevelPtr[l + 1]; k += 32) {
             uint32_t i = c.bRows[k];
             double v = M[N + i];
@@ -283,7 +344,7 @@ __device__ void stepCell(const DevCell& c, uint32_t nsteps, uint32_t tid, uint32
     }
 }
 
-__global__ void __launch_bounds__(256) hsStepFp64(DevCell c, uint32_t nsteps) {
+__global__ void __launch_bounds__(256, 1) hsStepFp64(DevCell c, uint32_t nsteps) {
     stepCell<false>(c, nsteps, threadIdx.x, blockDim.x);
 }
 

@@ -414,6 +414,52 @@ bool buildPlan(const HsCellDesc& d, uint32_t seed, double dt, CellPlan& P, std::
         P.bTermPtr[k + 1] = P.bTermPtr[k] + (uint32_t)rowTerms[r].size();
         for (const BwdTerm& t : rowTerms[r]) P.bTerms.push_back(t);
     }
+    // Cable runs of the two sweeps (a cable row eliminated by its
+    // predecessor: the two chainOps updates and nothing else; substituted
+    // from its successor: the one OFF term).
+    {
+        const int32_t offBase = (int32_t)(2 * N + H);
+        const uint32_t LF = (uint32_t)P.fLevelPtr.size() - 1, LB = (uint32_t)P.bLevelPtr.size() - 1;
+        auto fCable = [&](uint32_t l, uint32_t& row) {
+            if (P.fLevelPtr[l + 1] - P.fLevelPtr[l] != 1) return false;
+            const uint32_t k = P.fLevelPtr[l];
+            row = P.fRows[k];
+            if (row == 0 || P.fOpPtr[k + 1] - P.fOpPtr[k] != 2) return false;
+            const FwdOp& a = P.fOps[P.fOpPtr[k]];
+            const FwdOp& b = P.fOps[P.fOpPtr[k] + 1];
+            const int32_t p = (int32_t)row - 1, off = offBase + p;
+            return a.t == (int32_t)row && a.l == off && a.a == off && a.p == p &&
+                   b.t == (int32_t)(N + row) && b.l == off && b.a == (int32_t)N + p && b.p == p;
+        };
+        auto bCable = [&](uint32_t l, uint32_t& row) {
+            if (P.bLevelPtr[l + 1] - P.bLevelPtr[l] != 1) return false;
+            const uint32_t k = P.bLevelPtr[l];
+            row = P.bRows[k];
+            if (row + 1 >= N || P.bTermPtr[k + 1] - P.bTermPtr[k] != 1) return false;
+            const BwdTerm& t = P.bTerms[P.bTermPtr[k]];
+            return t.coef == offBase + (int32_t)row && t.src == (int32_t)row + 1;
+        };
+        P.fRun.assign(LF, 0);
+        P.fRunRow.assign(LF, 0);
+        for (uint32_t l = 0, r0 = 0, r = 0; l < LF;) {
+            if (!fCable(l, r0)) { ++l; continue; }
+            uint32_t len = 1;
+            while (l + len < LF && fCable(l + len, r) && r == r0 + len) ++len;
+            P.fRun[l] = len;
+            P.fRunRow[l] = r0;
+            l += len;
+        }
+        P.bRun.assign(LB, 0);
+        P.bRunRow.assign(LB, 0);
+        for (uint32_t l = 0, i0 = 0, i = 0; l < LB;) {
+            if (!bCable(l, i0)) { ++l; continue; }
+            uint32_t len = 1;
+            while (l + len < LB && bCable(l + len, i) && i + len == i0) ++len;
+            P.bRun[l] = len;
+            P.bRunRow[l] = i0;
+            l += len;
+        }
+    }
 
     // readHHChannels (hsolve/HSolveActiveSetup.cpp:162-235)
     std::vector<std::vector<uint32_t>> chansOf(d.n_compt);

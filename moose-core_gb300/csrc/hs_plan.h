@@ -68,6 +68,12 @@ struct CellPlan {
     std::vector<FwdOp> fOps;
     std::vector<uint32_t> bLevelPtr, bRows, bTermPtr;
     std::vector<BwdTerm> bTerms;
+    // Cable runs: at the first level of a run of consecutive one-row levels
+    // whose rows are plain cable rows (forward: rows r0, r0+1, ... each
+    // updated only by the previous row; backward: rows i0, i0-1, ... each
+    // with the single term on the next row), the run's length and first
+    // row; 0 elsewhere.  Per level.
+    std::vector<uint32_t> fRun, fRunRow, bRun, bRunRow;
     uint32_t maxLevelWidthF = 0, maxLevelWidthB = 0;
     // channels (solver order)
     uint32_t C = 0, G = 0;
