@@ -18,6 +18,7 @@
 
 #include "../../include/moose_gb300.h"
 #include "hs_cell.h"
+#include "hs_events.h"
 #include "hs_plan.h"
 
 using namespace hsg;
@@ -159,13 +160,10 @@ int mirrorPage(HsSolver* s, size_t idx, uint8_t** out) {
     return HS_OK;
 }
 
-// Hands the pushed events to the device before a process call.  Per SynChan
-// the new queue is the events not yet delivered (from the device cursor on)
-// merged with the pushed ones in time order, queued events first on equal
-// times and pushed ones in push order: the order in which
-// SimpleSynHandler::vProcess pops its heap for distinct times.  Delivered
-// events are dropped.  The step kernel is unchanged: it walks the new arrays
-// exactly as it walks the description's.
+// Hands the pushed events to the device before a process call: the queue
+// is rebuilt on the host (mergeEventQueue, hs_events.h) from the device
+// cursors and uploaded to solver-owned arrays.  The step kernel is
+// unchanged: it walks them exactly as it walks the description's events.
 int flushEvents(HsSolver* s) {
     if (s->pendSyn.empty()) return HS_OK;
     const uint32_t S = s->P.S;
@@ -174,46 +172,12 @@ int flushEvents(HsSolver* s) {
     if (e == cudaSuccess)
         e = cudaMemcpy(cur.data(), s->dc.evCur, S * sizeof(uint32_t), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cudaErr(e, "push events");
-    const std::vector<uint32_t>& ptr = s->evOwned ? s->hostPtr : s->P.evPtr;
-    const std::vector<double>& tq = s->evOwned ? s->hostTime : s->P.evTime;
-    const std::vector<double>& wq = s->evOwned ? s->hostW : s->P.evW;
-    const size_t n = s->pendSyn.size();
-    size_t total = n;
-    for (uint32_t k = 0; k < S; ++k) {
-        cur[k] = std::min(std::max(cur[k], ptr[k]), ptr[k + 1]);
-        total += ptr[k + 1] - cur[k];
-    }
-    if (total > 0xffffffffull) return setErr(HS_ENOMEM, "too many queued synaptic events");
-    std::vector<uint32_t> ord(n);
-    for (size_t i = 0; i < n; ++i) ord[i] = (uint32_t)i;
-    std::stable_sort(ord.begin(), ord.end(), [s](uint32_t a, uint32_t b) {
-        if (s->pendSyn[a] != s->pendSyn[b]) return s->pendSyn[a] < s->pendSyn[b];
-        return s->pendTime[a] < s->pendTime[b];
-    });
-    std::vector<uint32_t> nptr(2 * (size_t)S + 1);
+    std::vector<uint32_t> nptr;
     std::vector<double> nt, nw;
-    nt.reserve(total);
-    nw.reserve(total);
-    size_t p = 0;
-    for (uint32_t k = 0; k < S; ++k) {
-        nptr[k] = (uint32_t)nt.size();
-        uint32_t a = cur[k], aEnd = ptr[k + 1];
-        size_t pe = p;
-        while (pe < n && s->pendSyn[ord[pe]] == k) ++pe;
-        while (a < aEnd || p < pe) {
-            if (p == pe || (a < aEnd && tq[a] <= s->pendTime[ord[p]])) {
-                nt.push_back(tq[a]);
-                nw.push_back(wq[a]);
-                ++a;
-            } else {
-                nt.push_back(s->pendTime[ord[p]]);
-                nw.push_back(s->pendW[ord[p]]);
-                ++p;
-            }
-        }
-    }
-    nptr[S] = (uint32_t)nt.size();
-    for (uint32_t k = 0; k < S; ++k) nptr[S + 1 + k] = nptr[k];   // cursors at the start
+    if (!mergeEventQueue(S, s->evOwned ? s->hostPtr : s->P.evPtr, s->evOwned ? s->hostTime : s->P.evTime,
+                         s->evOwned ? s->hostW : s->P.evW, cur, s->pendSyn, s->pendTime, s->pendW, nptr, nt,
+                         nw))
+        return setErr(HS_ENOMEM, "too many queued synaptic events");
     const size_t m = nt.size();
     if (!s->ownIdx) {
         e = cudaMalloc(&s->ownIdx, nptr.size() * sizeof(uint32_t));
