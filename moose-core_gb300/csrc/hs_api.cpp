@@ -105,8 +105,12 @@ int flushWrites(HsSolver* s) {
     for (const auto& kv : s->writes) s->writeList.push_back(kv.second);
     const size_t n = s->writeList.size();
     if (n > s->dWritesCap) {
-        // cudaFree waits for the device, so no scatter still reads the old list
-        if (s->dWrites) cudaFree(s->dWrites);
+        // no scatter may still read the old list when it is freed
+        if (s->dWrites) {
+            cudaError_t e = cudaStreamSynchronize(s->st);
+            if (e != cudaSuccess) return cudaErr(e, "field write");
+            cudaFree(s->dWrites);
+        }
         s->dWrites = nullptr;
         s->dWritesCap = 0;
         const size_t cap = std::max<size_t>(n, 256);
