@@ -16,6 +16,11 @@ reference: the tests read only the files written here.
    floats (exact bits).
 2. ``active_*.npz`` -- traces of full models stepped by the reference
    ``moose`` Python module with an HSolve (see ``active_models()``).
+
+The other fixtures have their own scripts beside this one, run the same way
+after the reference build: ``make_golden_msgs.py`` (message destinations),
+``make_golden_events.py`` (synaptic events pushed at run time),
+``make_golden_swc.py`` and ``make_golden_genesis.py`` (the loaders).
 """
 import json
 import os
