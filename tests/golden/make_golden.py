@@ -20,6 +20,7 @@ reference: the tests read only the files written here.
 The other fixtures have their own scripts beside this one, run the same way
 after the reference build: ``make_golden_msgs.py`` (message destinations),
 ``make_golden_events.py`` (synaptic events pushed at run time),
+``make_golden_rdes.py`` (the reference's rdesigneur known-answer tests),
 ``make_golden_swc.py`` and ``make_golden_genesis.py`` (the loaders).
 """
 import json

@@ -347,3 +347,35 @@ def test_field_access_between_steps_matches_oracle():
     oc.step(50)
     assert np.array_equal(h.vm(), oc.vm())
     assert np.array_equal(h.ca(), oc.ca())
+
+
+@pytest.mark.parametrize("name", ["rdes_squid_axon", "rdes_current_pulse"])
+def test_rdesigneur_known_answers(name):
+    """The reference's rdesigneur KATs (test_32 squid axon, test_20 current
+    pulse) through the C ABI: the soma trace recorded on the device equals
+    the reference HSolve's bit for bit and passes the test's own check."""
+    from test_oracle_golden import check_rdes_kat
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    m = load_model(z)
+    dt = float(z["dt"])
+    h = HSolve(m, dt=dt)
+    h.target = m.seed
+    n, stride = int(z["nsteps"]), int(z["stride"])
+    h.record([0], stride, n // stride + 1)
+    h.reinit(dt)
+    h.process(n)
+    vm = h.trace()[0]
+    assert np.array_equal(vm, z["vm"])
+    check_rdes_kat(z, vm)
+
+
+def test_rdesigneur_minimal_model_fields():
+    """tests/rdesigneur/test_1_minimalModel.py through the C ABI: the zombie
+    fields right after setup equal the reference HSolve's readback exactly."""
+    z = np.load(os.path.join(GOLDEN, "rdes_minimal.npz"))
+    m = load_model(z)
+    h = HSolve(m, dt=float(z["dt"]))
+    h.target = m.seed
+    got = np.array([getattr(h.compartment(0), str(k)) for k in z["kat_fields"]])
+    assert np.array_equal(got, z["ref_values"])
+    assert np.allclose(got, z["kat_values"], rtol=1e-12, atol=0.0)

@@ -163,3 +163,52 @@ def test_runtime_events_golden_pins_reinit_drop_and_clock_time():
     oc = OracleCell(m, dt)
     oc.reinit(dt)
     assert not np.array_equal(replay_events(zz, oc, lambda s, n: s.step(n)), z["vm"])
+
+
+def _soma_trace(solver, z, advance):
+    stride, n = int(z["stride"]), int(z["nsteps"])
+    vm = [solver.vm()[0]]
+    for _ in range(n // stride):
+        advance(solver, stride)
+        vm.append(solver.vm()[0])
+    return np.array(vm)
+
+
+def check_rdes_kat(z, vm):
+    """The reference test's own assertion on the soma trace."""
+    if "kat_samples" in z.files:     # tests/rdesigneur/test_32_squid_axon_propgn.py
+        assert np.allclose(vm[::int(z["kat_every"])], z["kat_samples"])
+    else:                            # tests/rdesigneur/test_20_currentPulse.py
+        hist, edges = np.histogram(vm)
+        assert np.allclose(vm.mean(), z["kat_mean"]) and np.allclose(vm.std(), z["kat_std"])
+        assert np.allclose(hist, z["kat_hist"]) and np.allclose(edges, z["kat_edges"])
+
+
+@pytest.mark.parametrize("name", ["rdes_squid_axon", "rdes_current_pulse"])
+def test_rdesigneur_known_answers(name):
+    """The reference's rdesigneur KATs (test_32 squid axon: 201
+    compartments, Na/K gates on different voltage grids merged by the
+    solver; test_20 passive soma under a current pulse), assembled and run
+    by the reference HSolve (make_golden_rdes.py): the oracle's soma trace
+    equals the reference's bit for bit and passes the test's own check."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    m = load_model(z)
+    dt = float(z["dt"])
+    oc = OracleCell(m, dt)
+    oc.reinit(dt)
+    vm = _soma_trace(oc, z, lambda s, n: s.step(n))
+    assert np.array_equal(vm, z["vm"])
+    check_rdes_kat(z, vm)
+
+
+def test_rdesigneur_minimal_model_fields():
+    """tests/rdesigneur/test_1_minimalModel.py: the passive soma's zombie
+    fields right after setup (Cm, Em, Im, Ra, Rm, Vm, initVm, inject) equal
+    the reference HSolve's readback exactly and the doctest's printed
+    values to their printed precision."""
+    from moose_gb300.abi import FIELDS, HS_KIND_COMPT
+    z = np.load(os.path.join(GOLDEN, "rdes_minimal.npz"))
+    oc = OracleCell(load_model(z), float(z["dt"]))
+    got = np.array([oc.get(HS_KIND_COMPT, FIELDS[str(k)], 0) for k in z["kat_fields"]])
+    assert np.array_equal(got, z["ref_values"])
+    assert np.allclose(got, z["kat_values"], rtol=1e-12, atol=0.0)
