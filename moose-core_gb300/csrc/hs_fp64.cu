@@ -187,16 +187,27 @@ __device__ __forceinline__ void backwardCableRun(const DevCell& c, uint32_t i, u
     }
 }
 
-__device__ __forceinline__ void eliminateWarp(const DevCell& c, uint32_t lane) {
+template <bool WARP>
+__device__ __forceinline__ void levelSync() {
+    if (WARP) __syncwarp();
+    else __syncthreads();
+}
+
+// Forward elimination and back substitution by a group of `nth` threads:
+// one warp per cell in the FP64 batch, the whole CTA in the drop-in (the
+// rows of a level are independent, so a wide level of a branched cell is
+// shared by all warps instead of walked by one; a barrier per level).
+template <bool WARP>
+__device__ __forceinline__ void eliminate(const DevCell& c, uint32_t tid, uint32_t nth) {
     double* M = c.M;
     for (uint32_t l = 0; l < c.fLevels; ++l) {
         if (const uint32_t run = c.fRun[l]) {
-            if (lane == 0) forwardCableRun(c, c.fRunRow[l], run);
-            __syncwarp();
+            if (tid == 0) forwardCableRun(c, c.fRunRow[l], run);
+            levelSync<WARP>();
             l += run - 1;
             continue;
         }
-        for (uint32_t k = c.fLevelPtr[l] + lane; k < c.fLevelPtr[l + 1]; k += 32) {
+        for (uint32_t k = c.fLevelPtr[l] + tid; k < c.fLevelPtr[l + 1]; k += nth) {
             // t -= l / pivot * a.  A row's consecutive updates by one pivot
             // (its diagonal and right-hand side: the reference computes
             // HS[4i+1] / HS[4i] for both) share the quotient: it is computed
@@ -215,17 +226,17 @@ __device__ __forceinline__ void eliminateWarp(const DevCell& c, uint32_t lane) {
                 if (op.x == ql || op.x == qp) ql = -1;   // an operand changed
             }
         }
-        __syncwarp();
+        levelSync<WARP>();
     }
     const uint32_t N = c.N;
     for (uint32_t l = 0; l < c.bLevels; ++l) {
         if (const uint32_t run = c.bRun[l]) {
-            if (lane == 0) backwardCableRun(c, c.bRunRow[l], run);
-            __syncwarp();
+            if (tid == 0) backwardCableRun(c, c.bRunRow[l], run);
+            levelSync<WARP>();
             l += run - 1;
             continue;
         }
-        for (uint32_t k = c.bLevelPtr[l] + lane; k < c.bLevelPtr[l + 1]; k += 32) {
+        for (uint32_t k = c.bLevelPtr[l] + tid; k < c.bLevelPtr[l + 1]; k += nth) {
             uint32_t i = c.bRows[k];
             double v = M[N + i];
             for (uint32_t t = c.bTermPtr[k]; t < c.bTermPtr[k + 1]; ++t) {
@@ -236,7 +247,7 @@ __device__ __forceinline__ void eliminateWarp(const DevCell& c, uint32_t lane) {
             c.VMid[i] = v;
             c.V[i] = 2 * v - c.V[i];
         }
-        __syncwarp();
+        levelSync<WARP>();
     }
 }
 
@@ -293,7 +304,7 @@ __device__ void stepCell(const DevCell& c, uint32_t nsteps, uint32_t tid, uint32
         for (uint32_t h = tid; h < c.H; h += nth) c.M[2 * c.N + h] = c.HJ0[h];
         for (uint32_t ic = tid; ic < c.N; ic += nth) comptStep(c, ic);
         groupSync<WARP>();
-        if (WARP || tid < 32) eliminateWarp(c, tid & 31);
+        eliminate<WARP>(c, tid, nth);
         groupSync<WARP>();
         for (uint32_t p = tid; p < c.P; p += nth) poolStep(c, p);
         groupSync<WARP>();
