@@ -7,7 +7,8 @@
 //   tick 6   HSolveActive::step (hsolve/HSolveActive.cpp:45-66):
 //            advanceChannels + calculateChannelCurrents + updateMatrix
 //            (one thread per compartment), forward elimination and back
-//            substitution (warp 0, level by level over the pull programs),
+//            substitution (level by level over the pull programs, the rows
+//            of a level shared by the CTA; cable runs by one thread),
 //            advanceCalcium (one thread per pool), SpikeGens, trace record.
 // Compiled with --fmad=false: every operation is the reference's IEEE
 // operation in the reference's order, so Vm/Ca are bit-identical to the CPU
@@ -137,7 +138,7 @@ __device__ __forceinline__ void comptStep(const DevCell& c, uint32_t ic) {
     c.M[N + ic] = rhs;
 }
 
-// ---- elimination (one warp) -------------------------------------------------
+// ---- elimination -------------------------------------------------------------
 // A level costs the eliminating warp ~150 instructions of index loads and
 // loop control around its few FP64 operations, all on one dependency chain.
 // A run of cable rows (one row per level, see CellPlan::fRun/bRun) is walked
