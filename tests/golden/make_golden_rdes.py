@@ -5,7 +5,9 @@
 201-compartment squid axon), ``tests/rdesigneur/test_20_currentPulse.py``
 (mean, std and histogram of a passive soma's Vm under a current pulse) and
 ``tests/rdesigneur/test_1_minimalModel.py`` (the zombie fields of that soma
-right after setup, a doctest), in the reference source tree, run their
+right after setup, a doctest) and ``tests/rdesigneur/test_41_ballAndStick.py``
+(a soma and a 10-segment dendrite with per-region Na/K densities; its 61
+soma samples at 3 decimals), in the reference source tree, run their
 models under HSolve and compare with values written in the test files.  Here the same models are assembled with
 the REFERENCE ``moose`` module the way ``rdesigneur.buildModel`` assembles
 them (``python/rdesigneur/rdesigneur.py:232-256``): the cell prototype in
@@ -66,6 +68,17 @@ def test_file_constants(name):
             except (ValueError, TypeError, SyntaxError):
                 pass
     return out
+
+
+def rdesigneur_call(name, func):
+    """The literal keyword arguments of the rd.rdesigneur(...) call inside a
+    test function (cellProto, chanDistrib, stimList, ...)."""
+    tree = ast.parse(open(os.path.join(REF_TESTS, name)).read())
+    fn = next(n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name == func)
+    for node in ast.walk(fn):
+        if isinstance(node, ast.Call) and getattr(node.func, "attr", None) == "rdesigneur":
+            return {k.arg: ast.literal_eval(k.value) for k in node.keywords}
+    raise ValueError("no rdesigneur call in %s.%s" % (name, func))
 
 
 def protos():
@@ -228,6 +241,23 @@ def squid_axon(moose, c):
     return axon
 
 
+def ball_and_stick(moose, name, soma_dia, soma_len, dend_dia, dend_len, nseg):
+    """rdesigneur's ballAndStick cell prototype (rdesigneur.py:505-521): a
+    soma and a dendrite of `nseg` equal segments, rdesigneurProtos.buildCompt
+    defaults for RM, RA, CM, Em and initVm."""
+    P = protos()
+    cell = moose.Neuron("/library/" + name)
+    prev = P.buildCompt(cell, "soma", dia=soma_dia, dx=soma_len)
+    dx = dend_len / nseg
+    x = prev.x
+    for i in range(nseg):
+        compt = P.buildCompt(cell, "dend" + str(i), x=x, dx=dx, dia=dend_dia)
+        moose.connect(prev, "axial", compt, "raxial")
+        prev = compt
+        x += dx
+    return cell
+
+
 def make():
     import moose
     # test_32: squid axon propagation, 0.04 s
@@ -263,6 +293,27 @@ def make():
                         stride=int(round(PLOT_DT / ELEC_DT)), vm=vm, kat_mean=mean, kat_std=std,
                         kat_hist=hist, kat_edges=edges, **save_model(m))
     print("current pulse: %d compartments, %d samples, stim steps %s" % (m.n_compt, len(vm), list(m.stim_step)))
+    # test_41: ball and stick, Na/K densities per region, 0.06 s.  Its own
+    # check averages over every Table, the 3-D viewer's included, which
+    # cannot be built here; the test file's 61 soma samples (3 decimals,
+    # every 1 ms) are checked to their printed precision instead.
+    kw = rdesigneur_call("test_41_ballAndStick.py", "test_ball_and_stick")
+    proto = kw["cellProto"][0]
+    assert proto[0] == "ballAndStick"
+    expected41 = test_file_constants("test_41_ballAndStick.py")["expected"]
+    elec, soma, tab = assemble(moose, lambda: ball_and_stick(moose, *proto[1:]),
+                               [("make_HH_Na", "Na"), ("make_HH_K", "K")], kw["chanDistrib"],
+                               kw["stimList"][0][4])
+    vm0 = setup_vm(moose, elec)
+    nsteps = int(round(0.06 / ELEC_DT))
+    vm, inj = run_stepwise(moose, soma, tab, nsteps)
+    assert np.allclose(vm[::10], expected41, rtol=0.0, atol=5e-4 + 1e-12), "test_41 soma samples"
+    m = extract(moose, elec, soma, inj, vm0)
+    np.savez_compressed(os.path.join(HERE, "rdes_ball_and_stick.npz"), dt=ELEC_DT, nsteps=nsteps,
+                        stride=int(round(PLOT_DT / ELEC_DT)), vm=vm, kat_samples=expected41, kat_every=10,
+                        kat_atol=5e-4, **save_model(m))
+    print("ball and stick: %d compartments, %d channels, stim steps %s" %
+          (m.n_compt, len(m.chan_compt), list(m.stim_step)))
     # test_1: the passive soma's zombie fields right after setup (the
     # doctest of test_simple prints them with moose.showfield)
     kat = doctest_fields("test_1_minimalModel.py", "test_simple")
