@@ -7,7 +7,9 @@
 ``tests/rdesigneur/test_1_minimalModel.py`` (the zombie fields of that soma
 right after setup, a doctest) and ``tests/rdesigneur/test_41_ballAndStick.py``
 (a soma and a 10-segment dendrite with per-region Na/K densities; its 61
-soma samples at 3 decimals), in the reference source tree, run their
+soma samples at 3 decimals) and ``tests/rdesigneur/test_51_periodic_syn_input.py``
+(mean and std of a soma driven by a glu SynChan at 50 Hz), in the
+reference source tree, run their
 models under HSolve and compare with values written in the test files.  Here the same models are assembled with
 the REFERENCE ``moose`` module the way ``rdesigneur.buildModel`` assembles
 them (``python/rdesigneur/rdesigneur.py:232-256``): the cell prototype in
@@ -79,6 +81,16 @@ def rdesigneur_call(name, func):
         if isinstance(node, ast.Call) and getattr(node.func, "attr", None) == "rdesigneur":
             return {k.arg: ast.literal_eval(k.value) for k in node.keywords}
     raise ValueError("no rdesigneur call in %s.%s" % (name, func))
+
+
+def test_file_function_array(name, func, var):
+    """The literal np.array assigned to `var` inside a test function."""
+    tree = ast.parse(open(os.path.join(REF_TESTS, name)).read())
+    fn = next(n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name == func)
+    for node in ast.walk(fn):
+        if isinstance(node, ast.Assign) and any(getattr(t, "id", None) == var for t in node.targets):
+            return _literal(node.value)
+    raise ValueError("no %s in %s.%s" % (var, name, func))
 
 
 def protos():
@@ -164,7 +176,7 @@ def run_stepwise(moose, soma, tab, nsteps):
     return np.array(tab.vector), np.array(injects)
 
 
-def extract(moose, elec, soma, inject_seq, vm0):
+def extract(moose, elec, soma, inject_seq, vm0, events=None):
     """The solver's cell as a CellModel: compartments in depth-first order
     from the soma along `axial` messages (children in message order),
     channels per compartment in `channel` message order, gate tables read
@@ -193,10 +205,13 @@ def extract(moose, elec, soma, inject_seq, vm0):
             gates.append((g.min, g.max, np.array(g.tableA), np.array(g.tableB)))
         return gate_index[key]
 
-    ch_rows = []
+    ch_rows, syn_rows = [], []
     for i, c in enumerate(order):
         for e in c.neighbors["channel"]:
             ch = moose.element(e)
+            if ch.className == "SynChan":
+                syn_rows.append((i, ch.Gbar, ch.Ek, ch.tau1, ch.tau2, ch.modulation))
+                continue
             ch_rows.append(dict(compt=i, Gbar=ch.Gbar, Ek=ch.Ek, Xp=ch.Xpower, Yp=ch.Ypower, Zp=ch.Zpower,
                                 xg=gate(ch, "gateX") if ch.Xpower > 0 else -1,
                                 yg=gate(ch, "gateY") if ch.Ypower > 0 else -1,
@@ -217,6 +232,14 @@ def extract(moose, elec, soma, inject_seq, vm0):
         chan_ca_depend=np.full(nch, -1, np.int32),
         stim_compt=np.zeros(len(steps), np.uint32), stim_step=np.array(steps, np.uint32),
         stim_value=np.array([inject_seq[k] for k in steps]), seed=0)
+    if syn_rows:
+        sc = lambda j, dt: np.array([r[j] for r in syn_rows], dtype=dt)
+        m.syn_compt, m.syn_Gbar, m.syn_Ek = sc(0, np.uint32), sc(1, float), sc(2, float)
+        m.syn_tau1, m.syn_tau2, m.syn_modulation = sc(3, float), sc(4, float), sc(5, float)
+        ev_syn, ev_time, ev_weight = events
+        m.ev_syn = np.asarray(ev_syn, np.uint32)
+        m.ev_time = np.asarray(ev_time, float)
+        m.ev_weight = np.asarray(ev_weight, float)
     return m
 
 
@@ -314,6 +337,47 @@ def make():
                         kat_atol=5e-4, **save_model(m))
     print("ball and stick: %d compartments, %d channels, stim steps %s" %
           (m.n_compt, len(m.chan_compt), list(m.stim_step)))
+    # test_51: a glu SynChan on a soma driven at 50 Hz by a periodic
+    # RandSpike (rdesigneur._buildSynInputOnCompt with doPeriodic), 0.3 s.
+    # The spike times the RandSpike sends to Synapse::addSpike are recorded
+    # by a Table on its spikeOut and become the cell's queued events (the
+    # synapse's weight, no delay): RandSpike and SimpleSynHandler share
+    # tick 1 and the spike reaches the handler in the step it is sent.
+    kw = rdesigneur_call("test_51_periodic_syn_input.py", "test_periodic_syninput")
+    proto, stim = kw["cellProto"][0], kw["stimList"][0]
+    assert proto[0] == "somaProto" and stim[3] == "periodicsyn"
+
+    def soma_proto():
+        cell = moose.Neuron("/library/" + proto[1])   # rdesigneur._buildElecSoma
+        P.buildCompt(cell, "soma", dia=proto[2], dx=proto[3])
+        return cell
+
+    elec, soma, tab = assemble(moose, soma_proto, [(kw["chanProto"][0][0][:-2], kw["chanProto"][0][1])],
+                               kw["chanDistrib"], None)
+    syn_path = soma.path + "/" + stim[2] + "/sh/synapse[0]"
+    rs = P.make_synInput(name="synInput", parent=syn_path)
+    rs.doPeriodic = True
+    moose.element(syn_path).weight = float(stim[1])
+    moose.connect(rs, "spikeOut", syn_path, "addSpike")
+    moose.Neutral("/model/stims")
+    func = moose.Function("/model/stims/stim0")
+    func.expr = stim[4]
+    func.doEvalAtReinit = 1
+    moose.connect(func, "valueOut", rs, "setRate")
+    spk = moose.Table("/model/graphs/spikes")
+    moose.connect(rs, "spikeOut", spk, "input")
+    vm0 = setup_vm(moose, elec)
+    nsteps = int(round(0.3 / ELEC_DT))
+    vm, inj = run_stepwise(moose, soma, tab, nsteps)
+    mean, std = test_file_function_array("test_51_periodic_syn_input.py", "test_periodic_syninput", "expected")
+    assert np.allclose([mean, std], [vm.mean(), vm.std()], rtol=1e-3), "test_51 mean/std"
+    times = np.array(spk.vector)
+    w = moose.element(syn_path).weight
+    m = extract(moose, elec, soma, inj, vm0, events=(np.zeros(len(times)), times, np.full(len(times), w)))
+    np.savez_compressed(os.path.join(HERE, "rdes_periodic_syn.npz"), dt=ELEC_DT, nsteps=nsteps,
+                        stride=int(round(PLOT_DT / ELEC_DT)), vm=vm, kat_mean=mean, kat_std=std, kat_rtol=1e-3,
+                        **save_model(m))
+    print("periodic syn: %d SynChan, %d events" % (len(m.syn_compt), len(m.ev_time)))
     # test_1: the passive soma's zombie fields right after setup (the
     # doctest of test_simple prints them with moose.showfield)
     kat = doctest_fields("test_1_minimalModel.py", "test_simple")

@@ -180,18 +180,22 @@ def check_rdes_kat(z, vm):
         assert np.allclose(vm[::int(z["kat_every"])], z["kat_samples"], rtol=0.0, atol=float(z["kat_atol"]) + 1e-12)
     elif "kat_samples" in z.files:   # tests/rdesigneur/test_32_squid_axon_propgn.py
         assert np.allclose(vm[::int(z["kat_every"])], z["kat_samples"])
+    elif "kat_rtol" in z.files:      # tests/rdesigneur/test_51_periodic_syn_input.py
+        assert np.allclose([z["kat_mean"], z["kat_std"]], [vm.mean(), vm.std()], rtol=float(z["kat_rtol"]))
     else:                            # tests/rdesigneur/test_20_currentPulse.py
         hist, edges = np.histogram(vm)
         assert np.allclose(vm.mean(), z["kat_mean"]) and np.allclose(vm.std(), z["kat_std"])
         assert np.allclose(hist, z["kat_hist"]) and np.allclose(edges, z["kat_edges"])
 
 
-@pytest.mark.parametrize("name", ["rdes_squid_axon", "rdes_current_pulse", "rdes_ball_and_stick"])
+@pytest.mark.parametrize("name", ["rdes_squid_axon", "rdes_current_pulse", "rdes_ball_and_stick",
+                                  "rdes_periodic_syn"])
 def test_rdesigneur_known_answers(name):
     """The reference's rdesigneur KATs (test_32 squid axon: 201
     compartments, Na/K gates on different voltage grids merged by the
     solver; test_20 passive soma under a current pulse; test_41 ball and
-    stick with per-region channel densities), assembled and run
+    stick with per-region channel densities; test_51 a SynChan driven at
+    50 Hz through Synapse::addSpike), assembled and run
     by the reference HSolve (make_golden_rdes.py): the oracle's soma trace
     equals the reference's bit for bit and passes the test's own check."""
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
