@@ -349,10 +349,12 @@ def test_field_access_between_steps_matches_oracle():
     assert np.array_equal(h.ca(), oc.ca())
 
 
-@pytest.mark.parametrize("name", ["rdes_squid_axon", "rdes_current_pulse", "rdes_ball_and_stick"])
+@pytest.mark.parametrize("name", ["rdes_squid_axon", "rdes_current_pulse", "rdes_ball_and_stick",
+                                  "rdes_periodic_syn"])
 def test_rdesigneur_known_answers(name):
     """The reference's rdesigneur KATs (test_32 squid axon, test_20 current
-    pulse, test_41 ball and stick) through the C ABI: the soma trace recorded on the device equals
+    pulse, test_41 ball and stick, test_51 periodic synaptic input) through
+    the C ABI: the soma trace recorded on the device equals
     the reference HSolve's bit for bit and passes the test's own check."""
     from test_oracle_golden import check_rdes_kat
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
