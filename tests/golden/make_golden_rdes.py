@@ -8,7 +8,9 @@
 right after setup, a doctest) and ``tests/rdesigneur/test_41_ballAndStick.py``
 (a soma and a 10-segment dendrite with per-region Na/K densities; its 61
 soma samples at 3 decimals) and ``tests/rdesigneur/test_51_periodic_syn_input.py``
-(mean and std of a soma driven by a glu SynChan at 50 Hz), in the
+(mean and std of a soma driven by a glu SynChan at 50 Hz) and
+``tests/rdesigneur/test_30_squid_currentPulse.py`` (an HH squid soma under a
+current pulse: the doctest's first and last samples, mean and std), in the
 reference source tree, run their
 models under HSolve and compare with values written in the test files.  Here the same models are assembled with
 the REFERENCE ``moose`` module the way ``rdesigneur.buildModel`` assembles
@@ -91,6 +93,28 @@ def test_file_function_array(name, func, var):
         if isinstance(node, ast.Assign) and any(getattr(t, "id", None) == var for t in node.targets):
             return _literal(node.value)
     raise ValueError("no %s in %s.%s" % (var, name, func))
+
+
+def doctest_array_ends(name, func):
+    """The first and last values of the array a test function's doctest
+    prints with numpy's summarising ellipsis."""
+    tree = ast.parse(open(os.path.join(REF_TESTS, name)).read())
+    doc = next(ast.get_docstring(n) for n in tree.body if isinstance(n, ast.FunctionDef) and n.name == func)
+    body = doc[doc.index("array([") + 7:doc.index("])")]
+    head, tail = body.split("...")
+    num = lambda part: [float(x) for x in part.replace("\n", " ").split(",") if x.strip()]
+    return np.array(num(head)), np.array(num(tail))
+
+
+def allclose_literal(name, func):
+    """The literal list given first to np.allclose inside a test function."""
+    tree = ast.parse(open(os.path.join(REF_TESTS, name)).read())
+    fn = next(n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name == func)
+    for node in ast.walk(fn):
+        if isinstance(node, ast.Call) and getattr(node.func, "attr", None) == "allclose" and \
+                isinstance(node.args[0], ast.List):
+            return np.array(ast.literal_eval(node.args[0]))
+    raise ValueError("no np.allclose literal in %s.%s" % (name, func))
 
 
 def protos():
@@ -378,6 +402,28 @@ def make():
                         stride=int(round(PLOT_DT / ELEC_DT)), vm=vm, kat_mean=mean, kat_std=std, kat_rtol=1e-3,
                         **save_model(m))
     print("periodic syn: %d SynChan, %d events" % (len(m.syn_compt), len(m.ev_time)))
+    # test_30: HH squid soma (Na/K on the passive soma), current pulse,
+    # 0.3 s; its doctest prints the Table's first and last three samples to
+    # 8 decimals, and the file gives the trace's mean and std.
+    kw = rdesigneur_call("test_30_squid_currentPulse.py", "test_current_pulse_squid")
+    assert "cellProto" not in kw
+    elec, soma, tab = assemble(moose, lambda: P.makePassiveHHsoma(name="cell"),
+                               [("make_HH_Na", "Na"), ("make_HH_K", "K")], kw["chanDistrib"],
+                               kw["stimList"][0][4])
+    vm0 = setup_vm(moose, elec)
+    nsteps = int(round(0.3 / ELEC_DT))
+    vm, inj = run_stepwise(moose, soma, tab, nsteps)
+    head, tail = doctest_array_ends("test_30_squid_currentPulse.py", "test_current_pulse_squid")
+    mean_std = allclose_literal("test_30_squid_currentPulse.py", "test_current_pulse_squid")
+    assert np.allclose(vm[:len(head)], head, rtol=0.0, atol=5e-9 + 1e-15), "test_30 first samples"
+    assert np.allclose(vm[-len(tail):], tail, rtol=0.0, atol=5e-9 + 1e-15), "test_30 last samples"
+    assert np.allclose(mean_std, [vm.mean(), vm.std()]), "test_30 mean/std"
+    m = extract(moose, elec, soma, inj, vm0)
+    np.savez_compressed(os.path.join(HERE, "rdes_squid_pulse.npz"), dt=ELEC_DT, nsteps=nsteps,
+                        stride=int(round(PLOT_DT / ELEC_DT)), vm=vm, kat_head=head, kat_tail=tail,
+                        kat_mean=mean_std[0], kat_std=mean_std[1], **save_model(m))
+    print("squid pulse: %d compartments, %d channels, stim steps %s" %
+          (m.n_compt, len(m.chan_compt), list(m.stim_step)))
     # test_1: the passive soma's zombie fields right after setup (the
     # doctest of test_simple prints them with moose.showfield)
     kat = doctest_fields("test_1_minimalModel.py", "test_simple")

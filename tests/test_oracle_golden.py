@@ -180,6 +180,11 @@ def check_rdes_kat(z, vm):
         assert np.allclose(vm[::int(z["kat_every"])], z["kat_samples"], rtol=0.0, atol=float(z["kat_atol"]) + 1e-12)
     elif "kat_samples" in z.files:   # tests/rdesigneur/test_32_squid_axon_propgn.py
         assert np.allclose(vm[::int(z["kat_every"])], z["kat_samples"])
+    elif "kat_head" in z.files:      # tests/rdesigneur/test_30_squid_currentPulse.py (8 decimals)
+        h, t = z["kat_head"], z["kat_tail"]
+        assert np.allclose(vm[:len(h)], h, rtol=0.0, atol=5e-9 + 1e-15)
+        assert np.allclose(vm[-len(t):], t, rtol=0.0, atol=5e-9 + 1e-15)
+        assert np.allclose([z["kat_mean"], z["kat_std"]], [vm.mean(), vm.std()])
     elif "kat_rtol" in z.files:      # tests/rdesigneur/test_51_periodic_syn_input.py
         assert np.allclose([z["kat_mean"], z["kat_std"]], [vm.mean(), vm.std()], rtol=float(z["kat_rtol"]))
     else:                            # tests/rdesigneur/test_20_currentPulse.py
@@ -189,13 +194,14 @@ def check_rdes_kat(z, vm):
 
 
 @pytest.mark.parametrize("name", ["rdes_squid_axon", "rdes_current_pulse", "rdes_ball_and_stick",
-                                  "rdes_periodic_syn"])
+                                  "rdes_periodic_syn", "rdes_squid_pulse"])
 def test_rdesigneur_known_answers(name):
     """The reference's rdesigneur KATs (test_32 squid axon: 201
     compartments, Na/K gates on different voltage grids merged by the
     solver; test_20 passive soma under a current pulse; test_41 ball and
     stick with per-region channel densities; test_51 a SynChan driven at
-    50 Hz through Synapse::addSpike), assembled and run
+    50 Hz through Synapse::addSpike; test_30 an HH squid soma under a
+    current pulse), assembled and run
     by the reference HSolve (make_golden_rdes.py): the oracle's soma trace
     equals the reference's bit for bit and passes the test's own check."""
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
