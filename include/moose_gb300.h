@@ -382,7 +382,11 @@ int hs_batch_set_modulation(HsBatch* b, int kind, const uint32_t* cells, const u
  * a device looks up the scratch address and should come before any stream
  * capture on it; calls share the storage, are serialised by a lock and
  * return after the writes are done.  Same targets and rules as
- * hs_batch_inject_targets + hs_batch_set_inject.  No counterpart in the
+ * hs_batch_inject_targets + hs_batch_set_inject.  Name each (cell, compt)
+ * pair at most once per call: a pair named twice gets one of its values,
+ * which one is not defined.  The scratch address is looked up once per
+ * device and kept, which assumes the device's primary context is not reset
+ * (cudaDeviceReset) while the library is loaded.  No counterpart in the
  * reference. */
 int hs_batch_set_inject_at(HsBatch* b, const uint32_t* cell, const uint32_t* compt,
                            const double* values, uint32_t n);

@@ -755,24 +755,45 @@ int hs_read_ca(HsSolver* s, double* out, uint32_t n) {
 int hs_record(HsSolver* s, const uint32_t* compts, uint32_t n, uint32_t stride, uint32_t capacity) {
     if (!s) return setErr(HS_EINVAL, "null solver");
     if (n && (!compts || stride == 0 || capacity == 0)) return setErr(HS_EINVAL, "bad recording request");
-    cudaStreamSynchronize(s->st);
-    if (s->recCompt) cudaFree(s->recCompt);
-    if (s->recBuf) cudaFree(s->recBuf);
-    s->recCompt = nullptr;
-    s->recBuf = nullptr;
-    s->recHost.clear();
+    // Every target is checked before the old recording is released, so a
+    // rejected request leaves the previous recording in place.
+    std::vector<uint32_t> rows;
+    rows.reserve(n);
     for (uint32_t r = 0; r < n; ++r) {
         uint32_t h;
         int rc = comptIndex(s, compts[r], &h);
         if (rc) return rc;
-        s->recHost.push_back(h);
+        rows.push_back(h);
     }
+    cudaStreamSynchronize(s->st);
+    // From here on the step kernel sees no recording until the new one is
+    // complete, so it never writes into a released buffer.
     s->dc.nRec = 0;
-    if (!n) return HS_OK;
-    cudaError_t e = cudaMalloc(&s->recCompt, n * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&s->recBuf, (size_t)n * capacity * sizeof(double));
-    if (e == cudaSuccess) e = cudaMemcpy(s->recCompt, s->recHost.data(), n * 4, cudaMemcpyHostToDevice);
+    s->dc.recCompt = nullptr;
+    s->dc.recBuf = nullptr;
+    if (s->recCompt) cudaFree(s->recCompt);
+    if (s->recBuf) cudaFree(s->recBuf);
+    s->recCompt = nullptr;
+    s->recBuf = nullptr;
+    s->recHost = std::move(rows);
+    // The sample count restarts with the new buffer (reinit sets it again).
+    cudaError_t e = cudaMemsetAsync(&s->dc.ctl->nSamples, 0, sizeof(uint32_t), s->st);
     if (e != cudaSuccess) return cudaErr(e, "record");
+    if (!n) return HS_OK;
+    e = cudaMalloc(&s->recCompt, n * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&s->recBuf, (size_t)n * capacity * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->recBuf, 0, (size_t)n * capacity * sizeof(double), s->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->recCompt, s->recHost.data(), n * 4, cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) {
+        if (s->recCompt) cudaFree(s->recCompt);
+        if (s->recBuf) cudaFree(s->recBuf);
+        s->recCompt = nullptr;
+        s->recBuf = nullptr;
+        s->recHost.clear();
+        return cudaErr(e, "record");
+    }
     s->dc.nRec = n;
     s->dc.recLd = n;
     s->dc.recStride = stride;

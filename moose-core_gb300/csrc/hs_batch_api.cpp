@@ -1580,15 +1580,8 @@ int hs_batch_record(HsBatch* b, const uint32_t* cell, const uint32_t* compt, uin
                     uint32_t capacity) {
     if (!b) return berr(HS_EINVAL, "null batch");
     if (n && (!cell || !compt || stride == 0 || capacity == 0)) return berr(HS_EINVAL, "bad recording request");
-    cudaStreamSynchronize(b->st);
-    if (b->gexec) {
-        cudaGraphExecDestroy(b->gexec);
-        b->gexec = nullptr;
-    }
-    b->recBuf.freeAll();
-    b->recBuf.err = cudaSuccess;
-    b->rec.clear();
-    // group by cell, keep the request order within a cell
+    // Every target is checked before the old recording is released, so a
+    // rejected request leaves the previous recording in place.
     std::vector<std::vector<uint32_t>> per(b->nCells);
     for (uint32_t r = 0; r < n; ++r) {
         if (cell[r] >= b->nCells) return berr(HS_EINVAL, "recorded cell out of range");
@@ -1597,22 +1590,68 @@ int hs_batch_record(HsBatch* b, const uint32_t* cell, const uint32_t* compt, uin
             return berr(HS_EINVAL, "recorded compartment not in the cell");
         per[cell[r]].push_back(compt[r]);
     }
+    cudaStreamSynchronize(b->st);
+    if (b->gexec) {
+        cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
+    }
+    b->recBuf.freeAll();
+    b->recBuf.err = cudaSuccess;
+    b->rec.clear();
+    b->recBase = nullptr;
+    // No recording until the new one is in place: the kernels never see the
+    // freed buffers, even if an allocation below fails.
+    for (DevCell& d : b->dcs) {
+        d.nRec = 0;
+        d.recCompt = nullptr;
+        d.recBuf = nullptr;
+    }
+    for (MixCellRange& R : b->mh.cells) R.rec0 = R.nRec = 0;
+    b->mb.recNode = nullptr;
+    b->mb.recBuf = nullptr;
+    b->mb.recLd = 0;
+    auto cleared = [&](cudaError_t e0) -> int {
+        cudaError_t e = cudaSuccess;
+        if (b->precision == HS_PREC_FP64) {
+            int rc = uploadDcs(b);
+            if (rc) return rc;
+        } else if (!b->mh.cells.empty()) {
+            e = cudaMemcpyAsync((void*)b->mb.cells, b->mh.cells.data(),
+                                b->mh.cells.size() * sizeof(MixCellRange), cudaMemcpyHostToDevice, b->st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+        }
+        if (e0 != cudaSuccess) return cerr(e0, "batch record");
+        return e == cudaSuccess ? HS_OK : cerr(e, "batch record");
+    };
+    if (!n) return cleared(cudaSuccess);
     b->recCap = capacity;
     b->recStride = stride;
-    double* buf = n ? b->recBuf.zeros<double>((size_t)n * capacity, b->st) : nullptr;
-    b->recBase = buf;
+    double* buf = b->recBuf.zeros<double>((size_t)n * capacity, b->st);
+    if (b->recBuf.err != cudaSuccess) {
+        cudaError_t e = b->recBuf.err;
+        b->recBuf.freeAll();
+        b->recBuf.err = cudaSuccess;
+        return cleared(e);
+    }
     uint32_t col = 0;
     if (b->precision == HS_PREC_FP64) {
         std::vector<uint32_t> hidx;
         std::vector<uint32_t> starts(b->nCells);
+        std::vector<std::pair<uint32_t, uint32_t>> rec;
         for (uint32_t c = 0; c < b->nCells; ++c) {
             starts[c] = (uint32_t)hidx.size();
             for (uint32_t m : per[c]) {
                 hidx.push_back((uint32_t)b->plans[c].hinesOf[m]);
-                b->rec.push_back({c, m});
+                rec.push_back({c, m});
             }
         }
         uint32_t* didx = b->recBuf.up(hidx, b->st);
+        if (b->recBuf.err != cudaSuccess) {
+            cudaError_t e = b->recBuf.err;
+            b->recBuf.freeAll();
+            b->recBuf.err = cudaSuccess;
+            return cleared(e);
+        }
         for (uint32_t c = 0; c < b->nCells; ++c) {
             DevCell& d = b->dcs[c];
             d.nRec = (uint32_t)per[c].size();
@@ -1622,29 +1661,39 @@ int hs_batch_record(HsBatch* b, const uint32_t* cell, const uint32_t* compt, uin
             d.recCompt = didx + starts[c];
             d.recBuf = buf + starts[c];
         }
-        if (b->recBuf.err != cudaSuccess) return cerr(b->recBuf.err, "batch record");
+        b->rec = std::move(rec);
+        b->recBase = buf;
         return uploadDcs(b);
     }
     std::vector<uint32_t> nodes;
+    std::vector<std::pair<uint32_t, uint32_t>> rec;
     for (uint32_t c = 0; c < b->nCells; ++c) {
         MixCellRange& R = b->mh.cells[c];
         R.rec0 = col;
         R.nRec = (uint32_t)per[c].size();
         for (uint32_t m : per[c]) {
             nodes.push_back((uint32_t)b->mh.nodeOf[c][m]);
-            b->rec.push_back({c, m});
+            rec.push_back({c, m});
         }
         col += R.nRec;
     }
-    b->mb.recNode = b->recBuf.up(nodes, b->st);
+    uint32_t* dnodes = b->recBuf.up(nodes, b->st);
+    if (b->recBuf.err != cudaSuccess) {
+        cudaError_t e = b->recBuf.err;
+        b->recBuf.freeAll();
+        b->recBuf.err = cudaSuccess;
+        for (MixCellRange& R : b->mh.cells) R.rec0 = R.nRec = 0;
+        return cleared(e);
+    }
+    b->mb.recNode = dnodes;
     b->mb.recBuf = buf;
     b->mb.recLd = n;
     b->mb.recCap = capacity;
     b->mb.recStride = stride;
-    cudaError_t e = b->recBuf.err;
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync((void*)b->mb.cells, b->mh.cells.data(), b->mh.cells.size() * sizeof(MixCellRange),
-                            cudaMemcpyHostToDevice, b->st);
+    b->rec = std::move(rec);
+    b->recBase = buf;
+    cudaError_t e = cudaMemcpyAsync((void*)b->mb.cells, b->mh.cells.data(), b->mh.cells.size() * sizeof(MixCellRange),
+                                    cudaMemcpyHostToDevice, b->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
     return e == cudaSuccess ? HS_OK : cerr(e, "batch record");
 }

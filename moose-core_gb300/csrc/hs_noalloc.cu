@@ -16,8 +16,13 @@
 //     device current, by cudaGetSymbolAddress on the first call that uses the
 //     device; that first call should therefore come before any stream
 //     capture is begun on the device;
+//     the address is kept for the life of the library, so the device's
+//     primary context must not be reset (cudaDeviceReset) in between;
 //   * nothing in the scratch has to start at zero: a call writes the n
-//     entries it uses before its kernel reads them.
+//     entries it uses before its kernel reads them;
+//   * the n writes of one call are applied by n independent threads, so a
+//     (cell, compartment) pair named twice in one call ends with one of its
+//     two values, which one is not defined.
 // The storage is shared by every batch of the process: calls are serialised
 // by a lock and each returns only after its kernel has finished reading the
 // scratch, so calls that overlap in time (from several host threads) wait

@@ -84,10 +84,10 @@ class Batch:
     def record(self, cells, compts, stride, capacity):
         c = np.ascontiguousarray(cells, np.uint32)
         m = np.ascontiguousarray(compts, np.uint32)
-        self._rec = (c, m, int(capacity))
         pu = C.POINTER(C.c_uint32)
         _native.check(_native.load().hs_batch_record(self._h, c.ctypes.data_as(pu), m.ctypes.data_as(pu), len(c),
                                                      int(stride), int(capacity)))
+        self._rec = (c, m, int(capacity))
 
     def trace(self):
         """Samples x recorded columns, columns grouped by cell in cell order."""

@@ -205,9 +205,9 @@ class HSolve:
 
     def record(self, compts, stride, capacity):
         a = np.ascontiguousarray(compts, np.uint32)
-        self._rec = (a, int(capacity))
         _native.check(_native.load().hs_record(self._h, a.ctypes.data_as(C.POINTER(C.c_uint32)), len(a),
                                                int(stride), int(capacity)))
+        self._rec = (a, int(capacity))
 
     def trace(self):
         a, cap = self._rec

@@ -224,3 +224,24 @@ def test_modulation_writes():
         oc.step(700)
         assert np.array_equal(fb.vm(c), h.vm()), c
         assert np.abs(mb.vm(c) - oc.vm()).max() <= 1e-4, c
+
+
+@pytest.mark.parametrize("prec", [HS_PREC_FP64, HS_PREC_MIXED])
+def test_failed_record_keeps_previous_recording(prec):
+    """A rejected hs_batch_record leaves the previous recording in place and
+    the batch keeps stepping into live buffers."""
+    from moose_gb300._native import HsError
+    cells = small_population(4, 8)
+    b = Batch(cells, DT, prec)
+    b.record([0, 2], [0, 3], 10, 31)
+    b.reinit(DT)
+    b.process(100)
+    with pytest.raises(HsError):
+        b.record([0, 9], [0, 0], 10, 31)
+    with pytest.raises(HsError):
+        b.record([0, 1], [0, 100_000], 10, 31)
+    b.process(200)
+    tr, cols = b.trace()
+    assert tr.shape == (31, 2)
+    assert np.array_equal(tr[-1], [b.vm(c)[m] for c, m in cols])
+    b.close()

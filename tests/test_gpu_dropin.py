@@ -350,10 +350,11 @@ def test_field_access_between_steps_matches_oracle():
 
 
 @pytest.mark.parametrize("name", ["rdes_squid_axon", "rdes_current_pulse", "rdes_ball_and_stick",
-                                  "rdes_periodic_syn"])
+                                  "rdes_periodic_syn", "rdes_squid_pulse"])
 def test_rdesigneur_known_answers(name):
     """The reference's rdesigneur KATs (test_32 squid axon, test_20 current
-    pulse, test_41 ball and stick, test_51 periodic synaptic input) through
+    pulse, test_41 ball and stick, test_51 periodic synaptic input, test_30
+    squid current pulse) through
     the C ABI: the soma trace recorded on the device equals
     the reference HSolve's bit for bit and passes the test's own check."""
     from test_oracle_golden import check_rdes_kat
@@ -381,3 +382,32 @@ def test_rdesigneur_minimal_model_fields():
     got = np.array([getattr(h.compartment(0), str(k)) for k in z["kat_fields"]])
     assert np.array_equal(got, z["ref_values"])
     assert np.allclose(got, z["kat_values"], rtol=1e-12, atol=0.0)
+
+
+def test_failed_record_keeps_previous_recording():
+    """A rejected hs_record (a compartment outside the cell) leaves the
+    recording made before it in place: the next process() writes the
+    trace into live buffers and the trace equals the oracle's."""
+    from moose_gb300._native import HsError
+    dt = 25e-6
+    m = models.config1_cell(n_cable=30, t_on=0.0, t_off=0.01)
+    h = HSolve(m, dt=dt)
+    h.target = 0
+    h.record([0, 7], 10, 41)
+    h.reinit(dt)
+    with pytest.raises(HsError):
+        h.record([0, 10_000], 10, 41)
+    h.process(400)
+    oc = OracleCell(m, dt)
+    oc.reinit(dt)
+    want = [oc.vm()[[0, 7]]]
+    for _ in range(40):
+        oc.step(10)
+        want.append(oc.vm()[[0, 7]])
+    assert np.array_equal(h.trace(), np.array(want).T)
+    # a new recording after process() starts its own sample count
+    h.record([3], 5, 4)
+    h.process(20)
+    oc.step(20)
+    tr = h.trace()
+    assert tr.shape == (1, 4) and tr[0, -1] == oc.vm()[3]
