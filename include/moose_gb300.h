@@ -331,6 +331,13 @@ typedef struct HsBatchTuning {
     uint32_t elim_warps;        /* mixed: warps of a CTA that eliminate while the
                                    others assemble (default 4; 0 keeps the
                                    current value, 0xFFFFFFFF turns the split off) */
+    uint32_t wait_rounds;       /* mixed: most sleep rounds (~128 ns each) an
+                                   eliminator waits for one level's assembly
+                                   before it gives up; after that the launch
+                                   waits no more, finishes its steps and
+                                   hs_batch_sync returns HS_ETIMEOUT until the
+                                   next reinit (default 2^24, about 2 s; 0 keeps
+                                   the current value) */
 } HsBatchTuning;
 
 int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds,

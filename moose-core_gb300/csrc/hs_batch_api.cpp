@@ -136,6 +136,7 @@ struct HsBatch {
     uint32_t forestNodes = 0;    // mixed: forest size limit (0: shared-memory capacity)
     uint32_t maxCtas = 0;        // mixed: CTA limit of the packing (0: one wave)
     uint32_t elimWarps = 4;      // mixed: eliminator warps of the split step (0: no split)
+    uint32_t waitRounds = 1u << 24;   // mixed: sleep rounds of one bounded wait (~128 ns each)
     bool useGraph = true;
     uint32_t nWarps = 0, nCtas = 0;
     uint32_t *dWarpPtr = nullptr, *dWarpCells = nullptr;
@@ -195,6 +196,7 @@ cudaError_t launchStep(HsBatch* b, uint32_t k) {
     if (b->precision == HS_PREC_FP64)
         return launchBatchStepFp64(b->dDcs, b->dWarpPtr, b->dWarpCells, b->nWarps, k, b->threadsPerCta, b->st);
     const uint32_t ew = b->elimWarps && b->threadsPerCta > 32 * b->elimWarps ? b->elimWarps : 0;
+    b->mb.waitRounds = b->waitRounds;
     return launchForestStepMixed(b->mb, b->dCtaPtr, b->dCtaForests, b->nCtas, b->threadsPerCta, b->mixSmem,
                                  b->mixCap, ew, k, b->st);
 }
@@ -1145,6 +1147,7 @@ int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds, uint32_t n_c
         b->forestNodes = tuning->forest_nodes;
         b->maxCtas = tuning->max_ctas;
         if (tuning->elim_warps) b->elimWarps = tuning->elim_warps == 0xFFFFFFFFu ? 0 : tuning->elim_warps;
+        if (tuning->wait_rounds) b->waitRounds = tuning->wait_rounds;
         b->useGraph = tuning->use_graph != 0;
     }
     const uint32_t maxTpc = precision == HS_PREC_FP64 ? 256 : 1024;
@@ -1199,6 +1202,7 @@ int hs_batch_tune(HsBatch* b, const HsBatchTuning* t) {
     b->forestNodes = t->forest_nodes;
     b->maxCtas = t->max_ctas;
     if (t->elim_warps) b->elimWarps = t->elim_warps == 0xFFFFFFFFu ? 0 : t->elim_warps;
+    if (t->wait_rounds) b->waitRounds = t->wait_rounds;
     if (t->steps_per_launch) b->stepsPerLaunch = t->steps_per_launch;
     b->useGraph = t->use_graph != 0;
     if (relayout) {
@@ -1284,6 +1288,8 @@ int hs_batch_reinit(HsBatch* b, double clock_dt) {
         b->mb.dt = clock_dt;
         b->mb.dtf = (float)clock_dt;
         b->mb.caAdvance = b->caAdvance;
+        // a timed-out wait invalidated the old state; the new one is valid
+        if (e == cudaSuccess) e = cudaMemsetAsync(b->mb.err, 0, sizeof(uint32_t), b->st);
         if (e == cudaSuccess)
             e = launchBatchReinitMixed(b->mb, (uint32_t)H.nNodes, b->dMixInitVm, b->dMixC2dX0, b->dEvStart, b->st);
     }
@@ -1382,7 +1388,8 @@ int hs_batch_sync(HsBatch* b) {
         uint32_t flag = 0;
         e = cudaMemcpy(&flag, b->mb.err, 4, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return cerr(e, "batch sync");
-        if (flag) return berr(HS_ETIMEOUT, "a bounded wait of the split step gave up; results are invalid");
+        if (flag)
+            return berr(HS_ETIMEOUT, "a bounded wait of the split step gave up; results are invalid until reinit");
     }
     return HS_OK;
 }
@@ -1799,48 +1806,57 @@ int hs_batch_read_spikes(HsBatch* b, uint32_t* cell, uint32_t* gen, double* time
     if (!b || !n) return berr(HS_EINVAL, "null argument");
     cudaError_t e = cudaStreamSynchronize(b->st);
     if (e != cudaSuccess) return cerr(e, "batch spikes");
-    uint32_t total = 0, k = 0;
-    bool overflow = false;
+    // counts of every cell in one copy
+    const uint32_t nC = b->nCells;
+    DevBuf tmp;
+    tmp.st = b->st;
+    std::vector<uint32_t> cnt(nC);
+    const uint32_t cap = b->spikeCap;
     if (b->precision == HS_PREC_FP64) {
-        for (uint32_t c = 0; c < b->nCells; ++c) {
-            DevCtl ctl;
-            e = cudaMemcpy(&ctl, b->dcs[c].ctl, sizeof(ctl), cudaMemcpyDeviceToHost);
-            if (e != cudaSuccess) return cerr(e, "batch spikes");
-            uint32_t m = std::min(ctl.nSpikes, b->dcs[c].spikeCap);
-            overflow |= ctl.nSpikes > m;
-            total += ctl.nSpikes;
-            if (!m || k >= capacity) continue;
-            std::vector<uint32_t> g(m);
-            std::vector<double> t(m);
-            cudaMemcpy(g.data(), b->dcs[c].spikeGen, m * 4, cudaMemcpyDeviceToHost);
-            cudaMemcpy(t.data(), b->dcs[c].spikeTime, m * 8, cudaMemcpyDeviceToHost);
-            for (uint32_t i = 0; i < m && k < capacity; ++i, ++k) {
-                if (cell) cell[k] = c;
-                if (gen) gen[k] = g[i];
-                if (time) time[k] = t[i];
-            }
-        }
+        uint32_t* dcnt = tmp.alloc<uint32_t>(nC);
+        e = tmp.err;
+        if (e == cudaSuccess) e = launchSpikeCountsFp64(b->dDcs, nC, dcnt, b->st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(cnt.data(), dcnt, (size_t)nC * 4, cudaMemcpyDeviceToHost, b->st);
     } else {
-        std::vector<uint32_t> cnt(b->nCells);
-        e = cudaMemcpy(cnt.data(), b->mb.spikeCount, b->nCells * 4, cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) return cerr(e, "batch spikes");
-        for (uint32_t c = 0; c < b->nCells; ++c) {
-            uint32_t m = std::min(cnt[c], b->spikeCap);
-            overflow |= cnt[c] > m;
-            total += cnt[c];
-            if (!m || k >= capacity) continue;
-            std::vector<uint32_t> g(m);
-            std::vector<float> t(m);
-            cudaMemcpy(g.data(), b->mb.spikeGen + (size_t)c * b->spikeCap, m * 4, cudaMemcpyDeviceToHost);
-            cudaMemcpy(t.data(), b->mb.spikeTime + (size_t)c * b->spikeCap, m * 4, cudaMemcpyDeviceToHost);
-            for (uint32_t i = 0; i < m && k < capacity; ++i, ++k) {
-                if (cell) cell[k] = c;
-                if (gen) gen[k] = g[i];
-                if (time) time[k] = t[i];
-            }
-        }
+        e = cudaMemcpyAsync(cnt.data(), b->mb.spikeCount, (size_t)nC * 4, cudaMemcpyDeviceToHost, b->st);
     }
-    *n = total;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    if (e != cudaSuccess) {
+        tmp.freeAll();
+        return cerr(e, "batch spikes");
+    }
+    // the stored spikes of the cells that fit in `capacity`, gathered on the
+    // device into one list and read with one copy per array
+    std::vector<uint32_t> off(nC + 1, 0);
+    uint64_t total = 0;
+    bool overflow = false;
+    for (uint32_t c = 0; c < nC; ++c) {
+        const uint32_t m = std::min(cnt[c], cap);
+        overflow |= cnt[c] > m;
+        total += cnt[c];
+        off[c + 1] = off[c] + m;
+    }
+    const uint32_t stored = off[nC];
+    const uint32_t k = std::min(stored, capacity);
+    if (k && (cell || gen || time)) {
+        const uint32_t* doff = tmp.up(off, b->st);
+        uint32_t* dgen = tmp.alloc<uint32_t>(stored);
+        double* dtime = tmp.alloc<double>(stored);
+        e = tmp.err;
+        if (e == cudaSuccess)
+            e = launchGatherSpikes(b->precision == HS_PREC_FP64 ? b->dDcs : nullptr, b->mb.spikeGen,
+                                   b->mb.spikeTime, cap, nC, doff, dgen, dtime, b->st);
+        if (e == cudaSuccess && gen) e = cudaMemcpyAsync(gen, dgen, (size_t)k * 4, cudaMemcpyDeviceToHost, b->st);
+        if (e == cudaSuccess && time) e = cudaMemcpyAsync(time, dtime, (size_t)k * 8, cudaMemcpyDeviceToHost, b->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+        if (e == cudaSuccess && cell)
+            for (uint32_t c = 0; c < nC && off[c] < k; ++c)
+                for (uint32_t i = off[c]; i < off[c + 1] && i < k; ++i) cell[i] = c;
+    }
+    tmp.freeAll();
+    if (e != cudaSuccess) return cerr(e, "batch spikes");
+    *n = (uint32_t)std::min<uint64_t>(total, 0xFFFFFFFFu);
     if (overflow) return berr(HS_ECAPACITY, "a cell's spike buffer overflowed");
     return HS_OK;
 }

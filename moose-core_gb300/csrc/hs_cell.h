@@ -50,6 +50,13 @@ cudaError_t launchStepFp64(const DevCell& c, uint32_t nsteps, cudaStream_t st);
 cudaError_t launchScatterFields(const FieldWrite* w, uint32_t n, cudaStream_t st);
 // HSolveActive::reinit + tick-1/4 object reinit of `nCells` cells, on device.
 cudaError_t launchReinitFp64(const DevCell* cells, uint32_t nCells, cudaStream_t st);
+// Spike read-back of a batch: per-cell counts (FP64 batch), then the stored
+// spikes of every cell gathered at off[c] .. off[c+1] (FP64: from `cells`;
+// mixed: `cells` null, from the [cell][cap] arrays srcGen/srcTime).
+cudaError_t launchSpikeCountsFp64(const DevCell* cells, uint32_t nCells, uint32_t* counts, cudaStream_t st);
+cudaError_t launchGatherSpikes(const DevCell* cells, const uint32_t* srcGen, const float* srcTime, uint32_t cap,
+                               uint32_t nCells, const uint32_t* off, uint32_t* gen, double* time,
+                               cudaStream_t st);
 cudaError_t launchBatchStepFp64(const DevCell* cells, const uint32_t* warpCellPtr,
                                 const uint32_t* warpCells, uint32_t nWarps, uint32_t nsteps,
                                 uint32_t threadsPerCta, cudaStream_t st);

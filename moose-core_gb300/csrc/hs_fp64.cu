@@ -469,6 +469,55 @@ __global__ void hsScatterFields(const FieldWrite* __restrict__ w, uint32_t n) {
     else *static_cast<uint8_t*>(x.addr) = (uint8_t)x.bits;
 }
 
+// Spike read-back of a batch: each cell's spike count, then every cell's
+// stored spikes gathered into one list (cell c at off[c] .. off[c+1]), so
+// that the host reads all cells with one copy per array.
+__global__ void hsSpikeCountsFp64(const DevCell* __restrict__ cells, uint32_t nCells, uint32_t* __restrict__ counts) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < nCells) counts[c] = cells[c].ctl->nSpikes;
+}
+
+__global__ void hsGatherSpikesFp64(const DevCell* __restrict__ cells, uint32_t nCells,
+                                   const uint32_t* __restrict__ off, uint32_t* __restrict__ gen,
+                                   double* __restrict__ time) {
+    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (c >= nCells) return;
+    const uint32_t o = off[c], m = off[c + 1] - o;
+    const DevCell& d = cells[c];
+    for (uint32_t i = lane; i < m; i += 32) {
+        gen[o + i] = d.spikeGen[i];
+        time[o + i] = d.spikeTime[i];
+    }
+}
+
+__global__ void hsGatherSpikesMixed(const uint32_t* __restrict__ srcGen, const float* __restrict__ srcTime,
+                                    uint32_t cap, uint32_t nCells, const uint32_t* __restrict__ off,
+                                    uint32_t* __restrict__ gen, double* __restrict__ time) {
+    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (c >= nCells) return;
+    const uint32_t o = off[c], m = off[c + 1] - o;
+    for (uint32_t i = lane; i < m; i += 32) {
+        gen[o + i] = srcGen[(size_t)c * cap + i];
+        time[o + i] = (double)srcTime[(size_t)c * cap + i];
+    }
+}
+
+cudaError_t launchSpikeCountsFp64(const DevCell* cells, uint32_t nCells, uint32_t* counts, cudaStream_t st) {
+    if (!nCells) return cudaSuccess;
+    hsSpikeCountsFp64<<<(nCells + 255) / 256, 256, 0, st>>>(cells, nCells, counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launchGatherSpikes(const DevCell* cells, const uint32_t* srcGen, const float* srcTime, uint32_t cap,
+                               uint32_t nCells, const uint32_t* off, uint32_t* gen, double* time,
+                               cudaStream_t st) {
+    if (!nCells) return cudaSuccess;
+    const uint32_t blocks = (nCells * 32 + 255) / 256;
+    if (cells) hsGatherSpikesFp64<<<blocks, 256, 0, st>>>(cells, nCells, off, gen, time);
+    else hsGatherSpikesMixed<<<blocks, 256, 0, st>>>(srcGen, srcTime, cap, nCells, off, gen, time);
+    return cudaGetLastError();
+}
+
 cudaError_t launchScatterFields(const FieldWrite* w, uint32_t n, cudaStream_t st) {
     if (!n) return cudaSuccess;
     hsScatterFields<<<(n + 255) / 256, 256, 0, st>>>(w, n);

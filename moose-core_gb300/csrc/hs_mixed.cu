@@ -507,10 +507,27 @@ __device__ __forceinline__ void groupSync(uint32_t id, uint32_t count) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 
-// Spin limit of an eliminator warp waiting for a level's assembly (each
-// round sleeps ~128 ns): far longer than any assembly, short enough that a
-// lost update ends the kernel with an error instead of a hang.
-constexpr uint32_t kLevelWaitRounds = 1u << 24;
+// Bounded wait of an eliminator for a level's assembly: at most
+// b.waitRounds rounds of ~128 ns (default 2^24, far longer than any
+// assembly), so that a lost update ends the kernel with an error instead of
+// a hang.  A thread that gave up once, or that sees the batch's error flag
+// set by another CTA, waits no more in this launch: the launch then ends
+// after at most one bounded wait per eliminator thread, and its results are
+// marked invalid (hs_batch_sync returns HS_ETIMEOUT).
+__device__ __forceinline__ bool waitLevel(const MixBatch& b, const uint32_t* done, uint32_t need, bool& gaveUp) {
+    if (gaveUp) return false;
+    uint32_t rounds = 0;
+    while (*(volatile const uint32_t*)done < need) {
+        ++rounds;
+        if (rounds > b.waitRounds || ((rounds & 1023u) == 0 && *(volatile const uint32_t*)b.err)) {
+            atomicExch(b.err, 1u);
+            gaveUp = true;
+            return false;
+        }
+        __nanosleep(128);
+    }
+    return true;
+}
 
 // The same steps as stepForest with the CTA split into two groups.  The
 // first `elimWarps` warps eliminate; the others assemble nodes deepest level
@@ -531,6 +548,7 @@ __device__ void stepForestWS(const MixBatch& b, const MixForest& F, uint32_t f, 
     unsigned long long step = b.forestStep[f];
     const uint32_t k0 = __ldg(b.syn0 + F.node0), k1 = __ldg(b.syn0 + F.node0 + F.nNodes);
     for (uint32_t k = k0 + tid; k < k1; k += nth) synapseStep(b, k, step);
+    bool gaveUp = false;
     for (uint32_t s = 0; s < nsteps; ++s, ++step) {
         for (uint32_t L = tid; L < F.nLevels; L += nth) done[L] = 0;
         forestStimulus(b, F, step);
@@ -539,14 +557,7 @@ __device__ void stepForestWS(const MixBatch& b, const MixForest& F, uint32_t f, 
             // forward elimination, each level once the assemblers finished it
             for (int L = (int)F.nLevels - 1; L >= 0; --L) {
                 const uint32_t b0 = lp[L], e = lp[L + 1];
-                uint32_t rounds = 0;
-                while (*(volatile uint32_t*)&done[L] < e - b0) {
-                    if (++rounds > kLevelWaitRounds) {
-                        atomicExch(b.err, 1u);
-                        break;
-                    }
-                    __nanosleep(128);
-                }
+                waitLevel(b, &done[L], e - b0, gaveUp);
                 __threadfence_block();
                 if (2 * (e - b0) <= nE) {
                     // a narrow level: two lanes per node, the even one on the

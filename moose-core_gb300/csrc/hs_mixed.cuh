@@ -148,6 +148,7 @@ struct MixBatch {
     const uint32_t* topo;        // forest-local first child | child count << 16 | level (<= 255) << 24
     const uint16_t* par;         // forest-local parent, kNoParent for a root
     uint32_t* err;               // set to 1 when a bounded wait gave up
+    uint32_t waitRounds;         // sleep rounds of one bounded wait
     const uint32_t* injIdx;      // inject entry of a kNodeInject node
     const double *off, *HS2, *CmByDt, *EmByRm;
     double* V;

@@ -31,16 +31,23 @@ import time
 
 import numpy as np
 
-# Kernels of different streams run concurrently only up to the number of
-# hardware work queues the CUDA context opens (8 unless this variable says
-# otherwise, 32 at most); more running cohorts than queues would share queues
-# and run one after another.  It must be set before CUDA starts in the
-# process: importing this module early (or setting it in the environment)
-# does that.
-os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
-
 from .abi import HS_PREC_MIXED
 from .batch import Batch
+
+
+def configure_work_queues(n=32):
+    """Ask CUDA for `n` hardware work queues (CUDA_DEVICE_MAX_CONNECTIONS,
+    at most 32; 8 by default).  Kernels of different streams run at the same
+    time only up to that number, so with more running cohorts than queues
+    the cohorts share queues and run one after another.
+
+    Precondition: call it before CUDA starts in the process (before the
+    first call into the library or torch.cuda); afterwards the context
+    keeps the number it opened with.  An existing setting in the
+    environment is kept.  Returns the value in effect for a context created
+    from now on."""
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", str(int(n)))
+    return int(os.environ["CUDA_DEVICE_MAX_CONNECTIONS"])
 
 
 @dataclasses.dataclass
@@ -153,7 +160,11 @@ class Server:
     next cohort.  An admission round makes one cohort per duration class
     (``duration_classes``: dt-step boundaries): the requests that share a
     cohort, and so its forests, then end at about the same time, and the
-    kernel skips a forest whose cells have all stopped, which frees its SM."""
+    kernel skips a forest whose cells have all stopped, which frees its SM.
+
+    Cohorts overlap on the GPU only as far as the context's hardware work
+    queues allow: call ``configure_work_queues(max_cohorts)`` before CUDA
+    starts in the process."""
 
     def __init__(self, dt, budget_bytes=150 * 10**9, chunk=4000, record_stride=40, max_cohort=4096,
                  admit_interval=0.05, dense=True, forest_nodes=7000, max_cohorts=32, sms=152, tuning=None,

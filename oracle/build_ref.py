@@ -35,7 +35,20 @@ import sysconfig
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
+# The one place that names where the reference sources lie: MOOSE_REF_SRC,
+# else the checkout this recipe was written against.  Every other script
+# that reads reference files takes the path from here (source_dir()).
 SRC = os.environ.get("MOOSE_REF_SRC", "/root/reference")
+
+
+def source_dir(required=True):
+    """The reference source tree, or None (required=False) / SystemExit
+    with a message (required=True) when it is not there."""
+    if os.path.isdir(SRC):
+        return SRC
+    if required:
+        raise SystemExit("reference sources not found at %s (set MOOSE_REF_SRC)" % SRC)
+    return None
 
 # Sub-libraries linked whole into _moose (reference meson.build, `sublibs`).
 SUBDIRS = [

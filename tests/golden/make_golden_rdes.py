@@ -41,7 +41,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF_TESTS = "/root/reference/tests/rdesigneur"
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+from build_ref import source_dir  # noqa: E402
+REF_TESTS = os.path.join(source_dir(), "tests", "rdesigneur")
 sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.join(REPO, "oracle", "_ref"))
 sys.path.insert(0, os.path.join(REPO, "moose-core_gb300"))

@@ -245,3 +245,33 @@ def test_failed_record_keeps_previous_recording(prec):
     assert tr.shape == (31, 2)
     assert np.array_equal(tr[-1], [b.vm(c)[m] for c, m in cols])
     b.close()
+
+
+def test_bounded_wait_gives_up_with_etimeout():
+    """The split step's eliminator waits are bounded: with a limit of one
+    sleep round (~128 ns, shorter than the assembly of any level) every
+    eliminator gives up at its first wait, the launch still ends, and
+    hs_batch_sync reports HS_ETIMEOUT; nothing faults.  reinit clears the
+    flag, and a fresh batch of the same cells steps correctly afterwards."""
+    from moose_gb300._native import HsError
+    from moose_gb300.abi import HS_ETIMEOUT
+    cells = small_population(6, 12, lo=100, hi=300)
+    b = Batch(cells, DT, HS_PREC_MIXED, wait_rounds=1, steps_per_launch=20)
+    b.reinit(DT)
+    b.process(100)
+    with pytest.raises(HsError) as ei:
+        b.sync()
+    assert ei.value.code == HS_ETIMEOUT
+    b.reinit(DT)
+    b.sync()                       # the flag is cleared by reinit
+    b.close()
+    good = Batch(cells, DT, HS_PREC_MIXED, steps_per_launch=20)
+    good.reinit(DT)
+    good.process(200)
+    good.sync()
+    for i, m in enumerate(cells):
+        o = OracleCell(m, DT)
+        o.reinit(DT)
+        o.step(200)
+        assert np.abs(good.vm(i) - o.vm()).max() <= 1e-4
+    good.close()

@@ -12,6 +12,11 @@ from moose_gb300 import serve
 
 pytestmark = pytest.mark.gpu
 
+# cohorts of the serving loop overlap on the GPU only with enough hardware
+# work queues; pytest imports every test module before the first test starts
+# CUDA, so this takes effect for the whole run
+serve.configure_work_queues(32)
+
 DT = 25e-6
 
 
