@@ -21,8 +21,12 @@ The JSON line carries:
              HH cable, 0.5 s), next to the same cell on one host core;
   fp64_batch the FP64 batch (one warp per cell, the drop-in's arithmetic,
              bit-identical results) on all cells of the workload;
-  accuracy   max |dVm| and spike-time shift of the mixed batch against the
-             FP64 path (bit-identical to the reference HSolve) on a subset;
+  accuracy   max |dVm| (soma every dt step, every compartment every 1,000
+             steps) and spike-time shift of the mixed batch against the FP64
+             batch (bit-identical to the reference HSolve) on 256 of the
+             cells for the full 1 s (--accuracy-full: all 4,096 cells);
+  config2    the 256-cell workload as written: every cell its own FP64
+             drop-in HSolve, beside the CPU restatement on the same cells;
   roofline   the stepping kernel against the measured HBM copy bandwidth;
   cpu_baseline the CPU restatement of HSolve (the oracle) on the host cores;
   config.autotuned  the packing and launch shape the autotuner picked.
@@ -60,13 +64,13 @@ SEED = 1
 # ---------------------------------------------------------------------------
 # CPU side: the oracle (CPU restatement of HSolve), one process per core
 
-def _cpu_worker(conn, cell_ids, n_cells, t_end):
+def _cpu_worker(conn, cell_ids, n_cells, t_end, config=CONFIG):
     import numpy as np  # noqa: F401
     from moose_gb300 import models
     from oracle import OracleCell
-    sizes, _, _ = models.population_sizes(CONFIG, SEED, n_cells)
+    sizes, _, _ = models.population_sizes(config, SEED, n_cells)
     kca = models.kca_2d_tables()
-    cells = [models.make_cell(CONFIG, SEED, i, t_end=t_end, kca_tables=kca, sizes=sizes) for i in cell_ids]
+    cells = [models.make_cell(config, SEED, i, t_end=t_end, kca_tables=kca, sizes=sizes) for i in cell_ids]
     oc = []
     for m in cells:
         o = OracleCell(m, DT)
@@ -87,9 +91,9 @@ def _cpu_worker(conn, cell_ids, n_cells, t_end):
 class CpuPool:
     """Cells of the workload split over `workers` processes (LPT on size)."""
 
-    def __init__(self, cell_ids, n_cells, workers, t_end):
+    def __init__(self, cell_ids, n_cells, workers, t_end, config=CONFIG):
         from moose_gb300 import models
-        sizes, _, _ = models.population_sizes(CONFIG, SEED, n_cells)
+        sizes, _, _ = models.population_sizes(config, SEED, n_cells)
         groups = [[] for _ in range(workers)]
         load = [0] * workers
         for i in sorted(cell_ids, key=lambda k: -sizes[k]):
@@ -102,7 +106,7 @@ class CpuPool:
             if not g:
                 continue
             a, b = ctx.Pipe()
-            p = ctx.Process(target=_cpu_worker, args=(b, g, n_cells, t_end), daemon=True)
+            p = ctx.Process(target=_cpu_worker, args=(b, g, n_cells, t_end, config), daemon=True)
             p.start()
             self.conns.append(a)
             self.procs.append(p)
@@ -257,6 +261,126 @@ def run_serving(args):
     return out
 
 
+def compare_mixed_fp64(cells, nsteps, chunk):
+    """Accuracy of the mixed-precision batch against the FP64 batch (every
+    cell bit-identical to the FP64 drop-in, itself bit-identical to the
+    reference HSolve where no libm call differs): both batches step the same
+    cells side by side (their own streams); the soma Vm of every cell is
+    compared at every dt step, every compartment's Vm at the end of every
+    chunk of `chunk` steps, and the spike trains at the end."""
+    import numpy as np
+    from moose_gb300.abi import HS_PREC_FP64, HS_PREC_MIXED
+    from moose_gb300.batch import Batch
+    n = len(cells)
+    f = Batch(cells, DT, HS_PREC_FP64)
+    mx = Batch(cells, DT, HS_PREC_MIXED)
+    somas = np.zeros(n, np.uint32)
+    for bb in (f, mx):
+        bb.record(np.arange(n), somas, 1, nsteps + 1)
+        bb.reinit(DT)
+    worst_soma = worst_all = 0.0
+    worst_cell = -1
+    done = 0
+    t0 = time.perf_counter()
+    wf = np.empty((chunk + 1, n))
+    wm = np.empty((chunk + 1, n))
+    while done < nsteps:
+        k = min(chunk, nsteps - done)
+        f.process(k)
+        mx.process(k)
+        f.sync()
+        mx.sync()
+        f.trace_window(done, k + 1, wf[:k + 1])
+        mx.trace_window(done, k + 1, wm[:k + 1])
+        d = np.abs(wf[:k + 1] - wm[:k + 1]).max(axis=0)
+        if d.max() > worst_soma:
+            worst_soma, worst_cell = float(d.max()), int(d.argmax())
+        worst_all = max(worst_all, float(np.abs(f.read_all("Vm") - mx.read_all("Vm")).max()))
+        done += k
+    wall = time.perf_counter() - t0
+    cf, _, sf = f.spikes()
+    cm, _, sm = mx.spikes()
+    shift, counts_equal, unequal = 0.0, True, 0
+    for i in range(n):
+        a, b = np.sort(sf[cf == i]), np.sort(sm[cm == i])
+        if len(a) != len(b):
+            counts_equal = False
+            unequal += 1
+        elif len(a):
+            shift = max(shift, float(np.abs(a - b).max()))
+    f.close()
+    mx.close()
+    ncomp = sum(m.n_compt for m in cells)
+    return {"max_abs_dVm_V": max(worst_soma, worst_all), "max_abs_dVm_soma_every_step_V": worst_soma,
+            "max_abs_dVm_all_compartments_chunk_ends_V": worst_all, "worst_soma_cell": worst_cell,
+            "max_spike_shift_s": shift, "spike_counts_equal": counts_equal, "cells_with_unequal_counts": unequal,
+            "spikes": int(len(sf)), "cells": n, "compartments": ncomp, "dt_steps": nsteps,
+            "chunk_dt_steps": chunk, "bounds": {"dVm_V": 1e-4, "spike_shift_s": 5e-5},
+            "within_bounds": bool(max(worst_soma, worst_all) <= 1e-4 and shift <= 5e-5 and counts_equal),
+            "wall_s": wall,
+            "compared": "mixed batch vs FP64 batch: soma Vm every dt step, every compartment's Vm at every "
+                        "chunk end, spike times and counts of every cell"}
+
+
+def run_accuracy_full(args):
+    """The whole synaptic workload (every cell, the full 1 s) through
+    compare_mixed_fp64; prints one JSON line."""
+    import torch
+    from moose_gb300 import models
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    kca = models.kca_2d_tables()
+    sizes, _, _ = models.population_sizes(CONFIG, SEED, args.cells)
+    t_end = args.acc_steps * DT + 0.01
+    cells = [models.make_cell(CONFIG, SEED, i, t_end=t_end, kca_tables=kca, sizes=sizes) for i in range(args.cells)]
+    out = compare_mixed_fp64(cells, args.acc_steps, args.chunk)
+    out["workload"] = "hsolve_4096cells_mixed_syn200" if args.cells == 4096 else "%d cells" % args.cells
+    return out
+
+
+def run_config2(args, cpu_pool):
+    """The 256-cell workload as written: every cell its own FP64 drop-in
+    HSolve (one CTA, its own stream; all cells queued before any waits),
+    --config2-steps dt steps, wall-clocked; beside the CPU HSolve restatement
+    on the same cells on the host cores."""
+    from moose_gb300 import models
+    from moose_gb300.hsolve import HSolve
+    n_cells = 256
+    sizes, _, _ = models.population_sizes(2, SEED, n_cells)
+    kca = models.kca_2d_tables()
+    t_end = (args.config2_steps + 50) * DT
+    cells = [models.make_cell(2, SEED, i, t_end=t_end, kca_tables=kca, sizes=sizes) for i in range(n_cells)]
+    hs = []
+    for m in cells:
+        h = HSolve(m, dt=DT)
+        h.target = m.seed
+        h.reinit(DT)
+        hs.append(h)
+    for h in hs:
+        h.process(20)
+    for h in hs:
+        h.sync()
+    t0 = time.perf_counter()
+    for h in hs:
+        h.process(args.config2_steps)
+    for h in hs:
+        h.sync()
+    wall = time.perf_counter() - t0
+    for h in hs:
+        h.close()
+    ncomp = int(sum(m.n_compt for m in cells))
+    out = {"workload": "256 cells, binary branching, 100..1,000 compartments, HH + Ca(HVA) + K(Ca) HHChannel2D + "
+                       "CaConc, each its own FP64 drop-in HSolve", "cells": n_cells, "compartments": ncomp,
+           "dt_steps": args.config2_steps, "wall_s": wall, "value": ncomp * args.config2_steps / wall,
+           "unit": "compartment-steps/s"}
+    if cpu_pool is not None:
+        tcpu = cpu_pool.step(args.config2_cpu_steps)
+        cv = cpu_pool.ncomp * args.config2_cpu_steps / tcpu
+        out["cpu_baseline"] = {"value": cv, "unit": "compartment-steps/s", "cores": cpu_pool.workers,
+                               "kind": "port", "sample": "all 256 cells x %d dt steps" % args.config2_cpu_steps}
+        out["gpu_over_cpu"] = out["value"] / cv
+    return out
+
+
 def run_ours(args, rank, world, cpu_pool):
     import numpy as np
     import torch
@@ -398,34 +522,13 @@ def run_ours(args, rank, world, cpu_pool):
         acc = None
         if not args.skip_accuracy:
             ids = list(range(0, args.cells, max(1, args.cells // args.acc_cells)))[: args.acc_cells]
-            sub = [cells[i] for i in ids]
-            f = Batch(sub, DT, HS_PREC_FP64)
-            mx = Batch(sub, DT, HS_PREC_MIXED)
-            ssub = np.zeros(len(sub), np.uint32)
-            for bb in (f, mx):
-                bb.record(np.arange(len(sub)), ssub, 1, args.acc_steps + 1)
-                bb.reinit(DT)
-                bb.process(args.acc_steps)
-                bb.sync()
-            tf, tm = f.trace()[0], mx.trace()[0]
-            dv = float(np.abs(tf - tm).max())
-            dall = max(float(np.abs(f.vm(i) - mx.vm(i)).max()) for i in range(len(sub)))
-            cf, _, sf = f.spikes()
-            cm, _, sm = mx.spikes()
-            shift, counts_equal = 0.0, True
-            for i in range(len(sub)):
-                a, bsp = np.sort(sf[cf == i]), np.sort(sm[cm == i])
-                if len(a) != len(bsp):
-                    counts_equal = False
-                elif len(a):
-                    shift = max(shift, float(np.abs(a - bsp).max()))
-            acc = {"max_abs_dVm_V": max(dv, dall), "max_spike_shift_s": shift,
-                   "spike_counts_equal": counts_equal, "spikes": int(len(sf)),
-                   "sample": "%d cells, %d dt steps, soma every step + all compartments at the end, "
-                             "mixed batch vs FP64 batch (bit-identical to the reference HSolve)"
-                             % (len(sub), args.acc_steps)}
-            f.close()
-            mx.close()
+            t_acc = args.acc_steps * DT + 0.01      # synaptic trains and stimulus cover the whole run
+            acc_cells = [models.make_cell(CONFIG, SEED, i, t_end=t_acc, kca_tables=kca, sizes=sizes) for i in ids]
+            acc = compare_mixed_fp64(acc_cells, args.acc_steps, args.acc_chunk)
+            del acc_cells
+            acc["sample"] = ("%d of %d cells (every %d-th), %d dt steps (%.2f s)"
+                             % (len(ids), args.cells, max(1, args.cells // args.acc_cells), args.acc_steps,
+                                args.acc_steps * DT))
         # the single-cell drop-in case: soma + 200-compartment HH cable, 0.5 s
         single = None
         n1 = 20000
@@ -478,6 +581,9 @@ def run_ours(args, rank, world, cpu_pool):
                 cpu["single_cell"] = {"wall_s": c_s, "value": m1.n_compt * n1 / c_s, "cores": 1,
                                       "sample": "the single-cell workload, all 20,000 dt steps"}
                 single["gpu_over_cpu_1core"] = c_s / single["wall_s"]
+        cfg2 = None
+        if not args.skip_config2:
+            cfg2 = run_config2(args, args.config2_pool)
         launches = args.steps * math.ceil(args.chunk / spl)
         out = {"metric": "compartment-steps/s", "value": value, "unit": "compartment-steps/s",
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -493,7 +599,7 @@ def run_ours(args, rank, world, cpu_pool):
                        "h2d_bytes_per_step": args.cells * 8,
                        "d2h_bytes_per_step": (args.chunk // stride) * args.cells * 8},
                "roofline": roof, "cpu_baseline": cpu, "fp64_dropin": dropin, "fp64_batch": fp64b,
-               "accuracy": acc, "single_cell": single,
+               "accuracy": acc, "single_cell": single, "config2": cfg2,
                "clocks": clk, "gpu_launches": launches}
         if not args.skip_serving:
             out["serving"] = run_serving(args)
@@ -512,12 +618,18 @@ def main():
     ap.add_argument("--steps-per-launch", type=int, default=0)
     ap.add_argument("--dropin-cells", type=int, default=128)
     ap.add_argument("--dropin-steps", type=int, default=200)
-    ap.add_argument("--acc-cells", type=int, default=32)
-    ap.add_argument("--acc-steps", type=int, default=4000)
+    ap.add_argument("--acc-cells", type=int, default=256)
+    ap.add_argument("--acc-steps", type=int, default=40000)
+    ap.add_argument("--acc-chunk", type=int, default=1000, help="dt steps between full-state comparisons")
+    ap.add_argument("--accuracy-full", action="store_true",
+                    help="only the accuracy comparison, on every cell of the workload for --acc-steps")
+    ap.add_argument("--config2-steps", type=int, default=2000)
+    ap.add_argument("--config2-cpu-steps", type=int, default=200)
+    ap.add_argument("--skip-config2", action="store_true")
     ap.add_argument("--cpu-cells", type=int, default=128)
     ap.add_argument("--cpu-chunk", type=int, default=400)
     ap.add_argument("--ref-cells", type=int, default=128)
-    ap.add_argument("--ref-chunk", type=int, default=100)
+    ap.add_argument("--ref-chunk", type=int, default=200)
     ap.add_argument("--skip-dropin", action="store_true")
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
@@ -542,6 +654,9 @@ def main():
         if out is not None:
             print(json.dumps(out))
         return 0
+    if args.accuracy_full:
+        print(json.dumps({"accuracy_full": run_accuracy_full(args)}))
+        return 0
     if args.serving_only:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
@@ -552,12 +667,18 @@ def main():
     if rank == 0 and not args.skip_cpu:
         ids = list(range(0, args.cells, max(1, args.cells // args.cpu_cells)))[: args.cpu_cells]
         cpu_pool = CpuPool(ids, args.cells, os.cpu_count() or 1, (2 * args.cpu_chunk + 2) * DT)
+    args.config2_pool = None
+    if rank == 0 and not args.skip_cpu and not args.skip_config2:
+        args.config2_pool = CpuPool(list(range(256)), 256, os.cpu_count() or 1,
+                                    (args.config2_cpu_steps + 2) * DT, config=2)
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
     out = run_ours(args, rank, world, cpu_pool)
     if cpu_pool is not None:
         cpu_pool.close()
+    if args.config2_pool is not None:
+        args.config2_pool.close()
     if out is not None:
         print(json.dumps(out))
     if world > 1:

@@ -355,6 +355,13 @@ int hs_batch_idle(HsBatch* b, int* idle);
 /* Vm of every compartment of cell `cell` in model order. */
 int hs_batch_read_vm(HsBatch* b, uint32_t cell, double* out, uint32_t n);
 int hs_batch_read_ca(HsBatch* b, uint32_t cell, double* out, uint32_t n);
+/* Vm (field HS_F_VM) or Ca (HS_F_CA) of every compartment (pool) of every
+ * cell, cell after cell, each cell in model order: n = the batch's total
+ * compartment (pool) count.  One gather on the device and one copy,
+ * whatever the number of cells: the chunk-boundary form of the solver's
+ * outgoing VmOut/concOut values (`HSolveActive::sendValues`,
+ * hsolve/HSolveActive.cpp:342-385) for a whole population. */
+int hs_batch_read_all(HsBatch* b, int field, double* out, uint64_t n);
 int hs_batch_record(HsBatch* b, const uint32_t* cell, const uint32_t* compt,
                     uint32_t n, uint32_t stride, uint32_t capacity_samples);
 int hs_batch_read_trace(HsBatch* b, double* out, uint32_t capacity,

@@ -170,6 +170,13 @@ struct HsBatch {
     DevBuf recBuf;
     double* recBase = nullptr;
     uint32_t recCap = 0, recStride = 1;
+    // bulk reads of every cell (hs_batch_read_all): gather lists built on
+    // first use, dropped with the layout
+    DevBuf gatherBuf;
+    const void** dGatherVm = nullptr;
+    const void** dGatherCa = nullptr;
+    double* dGatherOut = nullptr;
+    uint64_t nAllCompt = 0, nAllPool = 0;
     // spikes
     uint32_t spikeCap = 1024;
     // inject targets
@@ -1179,6 +1186,7 @@ int hs_batch_destroy(HsBatch* b) {
     b->packBuf.freeAll();
     b->recBuf.freeAll();
     b->injBuf.freeAll();
+    b->gatherBuf.freeAll();
     if (b->arena.base) cudaFreeAsync(b->arena.base, b->st);
     if (b->st) cudaStreamDestroy(b->st);
     delete b;
@@ -1221,6 +1229,10 @@ int hs_batch_tune(HsBatch* b, const HsBatchTuning* t) {
         b->injBuf.freeAll();
         b->injBuf.err = cudaSuccess;
         b->nInjTargets = 0;
+        b->gatherBuf.freeAll();
+        b->gatherBuf.err = cudaSuccess;
+        b->dGatherVm = b->dGatherCa = nullptr;
+        b->dGatherOut = nullptr;
         b->reinited = false;
         int rc = buildMixed(b);
         if (rc != HS_OK) return rc;
@@ -1572,15 +1584,74 @@ int hs_batch_read_ca(HsBatch* b, uint32_t cell, double* out, uint32_t n) {
         if (e != cudaSuccess) return cerr(e, "batch read ca");
         for (uint32_t m = 0; m < n; ++m) out[m] = P.poolSolverOf[m] < 0 ? NAN : v[P.poolSolverOf[m]];
     } else {
-        for (uint32_t m = 0; m < n; ++m) {
-            int64_t g = b->mh.poolOf[cell][m];
-            float x = NAN;
-            if (g >= 0) e = cudaMemcpy(&x, b->mb.poolCa + g, 4, cudaMemcpyDeviceToHost);
-            if (e != cudaSuccess) return cerr(e, "batch read ca");
-            out[m] = g < 0 ? NAN : x;
-        }
+        // the cell's pools are node-indexed inside one forest: one copy
+        const std::vector<int64_t>& po = b->mh.poolOf[cell];
+        int64_t lo = INT64_MAX, hi = -1;
+        for (int64_t g : po)
+            if (g >= 0) {
+                lo = std::min(lo, g);
+                hi = std::max(hi, g);
+            }
+        std::vector<float> v(hi >= lo ? (size_t)(hi - lo + 1) : 0);
+        if (!v.empty()) e = cudaMemcpy(v.data(), b->mb.poolCa + lo, v.size() * 4, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cerr(e, "batch read ca");
+        for (uint32_t m = 0; m < n; ++m) out[m] = po[m] < 0 ? NAN : (double)v[po[m] - lo];
     }
     return HS_OK;
+}
+
+int hs_batch_read_all(HsBatch* b, int field, double* out, uint64_t n) {
+    if (!b || (!out && n)) return berr(HS_EINVAL, "null argument");
+    if (field != HS_F_VM && field != HS_F_CA) return berr(HS_EINVAL, "field must be HS_F_VM or HS_F_CA");
+    const bool vm = field == HS_F_VM;
+    if (!b->nAllCompt && !b->nAllPool)
+        for (const CellPlan& P : b->plans) {
+            b->nAllCompt += P.hinesOf.size();
+            b->nAllPool += P.poolSolverOf.size();
+        }
+    const uint64_t total = vm ? b->nAllCompt : b->nAllPool;
+    if (n != total) return berr(HS_EINVAL, "n must equal the batch's total compartment (pool) count");
+    if (!n) return HS_OK;
+    const void**& list = vm ? b->dGatherVm : b->dGatherCa;
+    b->gatherBuf.st = b->st;
+    if (!list) {
+        // device address of every value, cell after cell in model order
+        std::vector<const void*> src;
+        src.reserve(total);
+        for (uint32_t c = 0; c < b->nCells; ++c) {
+            const CellPlan& P = b->plans[c];
+            if (vm) {
+                for (size_t m = 0; m < P.hinesOf.size(); ++m) {
+                    if (b->precision == HS_PREC_FP64)
+                        src.push_back(P.hinesOf[m] < 0 ? nullptr : b->dcs[c].V + P.hinesOf[m]);
+                    else
+                        src.push_back(b->mh.nodeOf[c][m] < 0 ? nullptr : b->mb.V + b->mh.nodeOf[c][m]);
+                }
+            } else {
+                for (size_t m = 0; m < P.poolSolverOf.size(); ++m) {
+                    if (b->precision == HS_PREC_FP64)
+                        src.push_back(P.poolSolverOf[m] < 0 ? nullptr : b->dcs[c].ca + P.poolSolverOf[m]);
+                    else
+                        src.push_back(b->mh.poolOf[c][m] < 0 ? nullptr : b->mb.poolCa + b->mh.poolOf[c][m]);
+                }
+            }
+        }
+        list = b->gatherBuf.up(src, b->st);
+        if (!b->dGatherOut) b->dGatherOut = b->gatherBuf.alloc<double>(std::max(b->nAllCompt, b->nAllPool));
+        if (b->gatherBuf.err != cudaSuccess) {
+            cudaError_t e = b->gatherBuf.err;
+            b->gatherBuf.freeAll();
+            b->gatherBuf.err = cudaSuccess;
+            b->dGatherVm = b->dGatherCa = nullptr;
+            b->dGatherOut = nullptr;
+            return cerr(e, "read all");
+        }
+    }
+    const uint32_t f32 = (!vm && b->precision == HS_PREC_MIXED) ? 1u : 0u;
+    cudaError_t e = launchGatherValues(list, f32, n, b->dGatherOut, b->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, b->dGatherOut, n * 8, cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    return e == cudaSuccess ? HS_OK : cerr(e, "read all");
 }
 
 int hs_batch_record(HsBatch* b, const uint32_t* cell, const uint32_t* compt, uint32_t n, uint32_t stride,

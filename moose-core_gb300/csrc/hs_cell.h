@@ -53,6 +53,9 @@ cudaError_t launchReinitFp64(const DevCell* cells, uint32_t nCells, cudaStream_t
 // Spike read-back of a batch: per-cell counts (FP64 batch), then the stored
 // spikes of every cell gathered at off[c] .. off[c+1] (FP64: from `cells`;
 // mixed: `cells` null, from the [cell][cap] arrays srcGen/srcTime).
+// out[k] = *src[k] for a gather list of n device addresses (doubles, or
+// floats when f32); NaN where src[k] is null.
+cudaError_t launchGatherValues(const void* const* src, uint32_t f32, uint64_t n, double* out, cudaStream_t st);
 cudaError_t launchSpikeCountsFp64(const DevCell* cells, uint32_t nCells, uint32_t* counts, cudaStream_t st);
 cudaError_t launchGatherSpikes(const DevCell* cells, const uint32_t* srcGen, const float* srcTime, uint32_t cap,
                                uint32_t nCells, const uint32_t* off, uint32_t* gen, double* time,

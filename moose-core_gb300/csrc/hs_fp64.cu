@@ -502,6 +502,23 @@ __global__ void hsGatherSpikesMixed(const uint32_t* __restrict__ srcGen, const f
     }
 }
 
+// One value per entry of a gather list: out[k] = *src[k] (a double, or a
+// float when f32), NaN for a null entry.
+__global__ void hsGatherValues(const void* const* __restrict__ src, uint32_t f32, uint64_t n,
+                               double* __restrict__ out) {
+    const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const void* p = src[k];
+    out[k] = !p ? __longlong_as_double(0x7FF8000000000000ll)
+                : f32 ? (double)*static_cast<const float*>(p) : *static_cast<const double*>(p);
+}
+
+cudaError_t launchGatherValues(const void* const* src, uint32_t f32, uint64_t n, double* out, cudaStream_t st) {
+    if (!n) return cudaSuccess;
+    hsGatherValues<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, f32, n, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launchSpikeCountsFp64(const DevCell* cells, uint32_t nCells, uint32_t* counts, cudaStream_t st) {
     if (!nCells) return cudaSuccess;
     hsSpikeCountsFp64<<<(nCells + 255) / 256, 256, 0, st>>>(cells, nCells, counts);

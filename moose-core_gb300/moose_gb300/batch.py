@@ -82,6 +82,19 @@ class Batch:
                                                           out.ctypes.data_as(C.POINTER(C.c_double)), len(out)))
         return out
 
+    def read_all(self, field="Vm", out=None):
+        """Vm (or Ca, field="Ca") of every compartment (pool) of every cell,
+        cell after cell in model order, with one device gather and one copy."""
+        from .abi import FIELDS
+        if field not in ("Vm", "Ca"):
+            raise ValueError("field must be 'Vm' or 'Ca'")
+        fid = FIELDS[field]
+        n = sum(m.n_compt for m in self.cells) if field == "Vm" else sum(len(m.pool_compt) for m in self.cells)
+        if out is None:
+            out = np.empty(n)
+        _native.check(_native.load().hs_batch_read_all(self._h, fid, out.ctypes.data_as(C.POINTER(C.c_double)), n))
+        return out
+
     def record(self, cells, compts, stride, capacity):
         c = np.ascontiguousarray(cells, np.uint32)
         m = np.ascontiguousarray(compts, np.uint32)
