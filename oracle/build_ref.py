@@ -14,6 +14,12 @@ Differences from the reference's meson recipe, and why:
   * ``-ffp-contract=off``: keep ``a*b+c`` as two rounded operations, so the
     reference's FP64 arithmetic is the plain IEEE sequence the oracle and the
     GPU drop-in restate.
+  * the MOOSE-side binding of the GPU solver
+    (``moose-core_gb300/cpp/moose_hsolve_bridge.cpp``: an HSolve's setup
+    vectors -> ``HsCellDesc``) is compiled against these sources and linked
+    into the extension, as a maintainer adding the drop-in to MOOSE would;
+    it only adds exported functions (``hsb_*``) and changes no behaviour,
+    and the tests call it on HSolves built by the reference's own pymoose.
   * unit tests: a second object set compiled with ``-DDO_UNIT_TESTS`` is not
     needed; the passive-solver known-answer harness (``ref_passive_harness.cpp``)
     links the reference's own HinesMatrix/HSolvePassive objects directly.
@@ -35,6 +41,8 @@ import sysconfig
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
+REPO = os.path.dirname(HERE)
+BRIDGE = os.path.join(REPO, "moose-core_gb300", "cpp", "moose_hsolve_bridge.cpp")
 # The one place that names where the reference sources lie: MOOSE_REF_SRC,
 # else the checkout this recipe was written against.  Every other script
 # that reads reference files takes the path from here (source_dir()).
@@ -128,6 +136,11 @@ def main():
     pym_obj, err = compile_one("pybind11/pymoose.cpp", inc)
     if err:
         errors.append((pym_obj, err))
+    bridge_obj = os.path.join(OUT, "obj", "moose_hsolve_bridge.o")
+    r = subprocess.run(["g++"] + CXXFLAGS + inc + ["-I" + os.path.join(REPO, "include"), "-c", BRIDGE,
+                        "-o", bridge_obj], capture_output=True, text=True)
+    if r.returncode != 0:
+        errors.append((bridge_obj, r.stderr[-4000:]))
     if errors:
         for obj, err in errors:
             print("FAILED", obj, "\n", err, file=sys.stderr)
@@ -142,7 +155,7 @@ def main():
     shutil.copytree(os.path.join(SRC, "python", "moose"), pkg)
     ext = os.path.join(pkg, "_moose" + sysconfig.get_config_var("EXT_SUFFIX"))
     subprocess.check_call(
-        ["g++", "-shared", "-o", ext, pym_obj, "-Wl,--whole-archive", lib,
+        ["g++", "-shared", "-o", ext, pym_obj, bridge_obj, "-Wl,--whole-archive", lib,
          "-Wl,--no-whole-archive", "-lpthread"])
     rd = os.path.join(OUT, "rdesigneur")
     if os.path.isdir(rd):

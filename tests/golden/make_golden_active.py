@@ -46,6 +46,13 @@ def save_model(m, prefix="model_"):
     return out
 
 
+def synapse(sh, j):
+    """Synapse j of a SimpleSynHandler (by path: indexing the handler's
+    `synapse` field does not convert in every pymoose build)."""
+    import moose
+    return moose.element("%s/synapse[%d]" % (sh.path, j))
+
+
 def build_moose(m, dt, cell="/cell"):
     import moose
     for p in ("/cell", "/library"):
@@ -161,11 +168,11 @@ def build_moose(m, dt, cell="/cell"):
         sc.modulation = m.syn_modulation[k]
         sh = moose.SimpleSynHandler(sc.path + "/sh")
         sh.numSynapses = 1
-        sh.synapse[0].delay = 0.0
+        synapse(sh, 0).delay = 0.0
         w = np.unique(m.ev_weight[m.ev_syn == k])
         if len(w) > 1:
             raise ValueError("one synapse per SynChan: its events share one weight")
-        sh.synapse[0].weight = float(w[0]) if len(w) else 1.0
+        synapse(sh, 0).weight = float(w[0]) if len(w) else 1.0
         moose.connect(sh, "activationOut", sc, "activation")
         moose.connect(sc, "channel", comp[m.syn_compt[k]], "channel")
         handlers.append(sh)
@@ -209,7 +216,7 @@ def run_moose(m, dt, nsteps, rec_compts, rec_pools=(), stride=1, ca_advance=1,
     moose.reinit()
     # events are queued after reinit (SimpleSynHandler::vReinit clears them)
     for e in range(len(m.ev_syn)):
-        handlers[m.ev_syn[e]].synapse[0].addSpike(float(m.ev_time[e]))
+        synapse(handlers[m.ev_syn[e]], 0).addSpike(float(m.ev_time[e]))
     cur = 0
     sched = list(zip(m.stim_step.tolist(), m.stim_compt.tolist(), m.stim_value.tolist()))
     for step, c, v in sched + [(nsteps, None, None)]:

@@ -34,7 +34,7 @@ sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.join(REPO, "oracle", "_ref"))
 sys.path.insert(0, os.path.join(REPO, "moose-core_gb300"))
 
-from make_golden_active import build_moose, save_model  # noqa: E402
+from make_golden_active import build_moose, save_model, synapse  # noqa: E402
 from moose_gb300 import models  # noqa: E402
 
 DT, NSTEPS, STRIDE, CHUNK = 25e-6, 4000, 4, 200
@@ -96,8 +96,8 @@ def make():
     for k, sh in enumerate(handlers):
         sh.numSynapses = 2
         for j in range(2):
-            sh.synapse[j].weight = float(w[k, j])
-            sh.synapse[j].delay = float(dl[k, j])
+            synapse(sh, j).weight = float(w[k, j])
+            synapse(sh, j).delay = float(dl[k, j])
     for t in range(8):
         moose.setClock(t, DT)
     moose.setClock(8, DT * STRIDE)
@@ -113,10 +113,10 @@ def make():
     h.dt = DT
     h.target = comp[m.seed].path
     for k, t in zip(pre_syn, pre_time):
-        handlers[int(k)].synapse[1].addSpike(float(t))
+        synapse(handlers[int(k)], 1).addSpike(float(t))
     moose.reinit()
     for e in range(len(m.ev_syn)):
-        handlers[int(m.ev_syn[e])].synapse[0].addSpike(float(m.ev_time[e]))
+        synapse(handlers[int(m.ev_syn[e])], 0).addSpike(float(m.ev_time[e]))
     stops = sorted(set(m.stim_step.tolist()) | set(p_step.tolist()) | {NSTEPS})
     cur = 0
     for step in stops:
@@ -126,7 +126,7 @@ def make():
         for i in np.nonzero(m.stim_step == step)[0]:
             comp[int(m.stim_compt[i])].inject = float(m.stim_value[i])
         for i in np.nonzero(p_step == step)[0]:
-            handlers[int(p_syn[i])].synapse[int(p_sy[i])].addSpike(float(p_time[i]))
+            synapse(handlers[int(p_syn[i])], int(p_sy[i])).addSpike(float(p_time[i]))
     vm = np.array([t.vector for t in tabs])
     out = dict(dt=DT, nsteps=NSTEPS, stride=STRIDE, chunk=CHUNK, rec=np.array(rec), vm=vm,
                final_vm=np.array([c.Vm for c in comp]), spikes=np.array(spk.vector),
