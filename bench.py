@@ -221,7 +221,7 @@ def run_reference(args, rank, world):
                     "d2h_bytes_per_step": 0}}
 
 
-def run_serving(args):
+def run_serving(args, capacity=None):
     """The serving loop on Poisson arrivals of the serving workload (cells of
     100..10,000 compartments, 0.1..2 s, step current or 50..500 synapses),
     150 GB budget: once at the offered rate over a bounded window (the loop is
@@ -235,8 +235,18 @@ def run_serving(args):
            "budget_bytes": args.serve_budget, "chunk_dt_steps": args.serve_chunk,
            "admit_interval_s": args.serve_admit}
     rid = 0
-    for name, rate, window in (("offered", args.serve_rate, args.serve_window),
-                               ("low_rate", args.serve_rate_low, args.serve_window_low)):
+    runs = [("offered", args.serve_rate, args.serve_window),
+            ("low_rate", args.serve_rate_low, args.serve_window_low)]
+    if capacity:
+        # the rate the loop sustains: a fraction of its capacity, the batch's
+        # compartment-steps/s over the mean work of a serving request
+        mean_work = float(np.mean([a * b for a, b in (models.serving_request_work(SEED, 10**6 + k, DT)
+                                                      for k in range(4000))]))
+        rate = round(args.serve_load * capacity / mean_work, 1)
+        out["capacity_requests_per_s"] = capacity / mean_work
+        out["mean_request_compartment_steps"] = mean_work
+        runs.append(("sustained", rate, args.serve_window_sustained))
+    for name, rate, window in runs:
         rng = np.random.default_rng([SEED, 77, int(rate)])
         t, arrivals = 0.0, []
         while True:
@@ -602,7 +612,7 @@ def run_ours(args, rank, world, cpu_pool):
                "accuracy": acc, "single_cell": single, "config2": cfg2,
                "clocks": clk, "gpu_launches": launches}
         if not args.skip_serving:
-            out["serving"] = run_serving(args)
+            out["serving"] = run_serving(args, capacity=value / world)
     b.close()
     return out
 
@@ -643,6 +653,9 @@ def main():
     ap.add_argument("--serve-window", type=float, default=0.5, help="s of arrivals at the offered rate")
     ap.add_argument("--serve-rate-low", type=float, default=10.0, help="a second, low arrival rate")
     ap.add_argument("--serve-window-low", type=float, default=8.0)
+    ap.add_argument("--serve-load", type=float, default=0.6,
+                    help="sustained run: offered load as a fraction of the batch's capacity")
+    ap.add_argument("--serve-window-sustained", type=float, default=6.0)
     ap.add_argument("--serve-chunk", type=int, default=4000)
     ap.add_argument("--serve-admit", type=float, default=0.05, help="s between admission rounds")
     ap.add_argument("--serve-budget", type=float, default=150e9)

@@ -350,6 +350,15 @@ def population(config, seed=1, n_cells=None, t_end=1.0, kca_tables=None):
             for i in range(len(sizes))]
 
 
+def serving_request_work(seed, i, dt=25e-6):
+    """(compartments, dt steps) of request i of the serving workload, from the
+    same draws as serving_request without building the cell."""
+    rng = np.random.default_rng([seed, 5, i])
+    n = int(loguniform_int(rng, 100, 10000, 1)[0])
+    duration = float(rng.uniform(0.1, 2.0))
+    return n, int(round(duration / dt))
+
+
 def serving_request(seed, i, dt=25e-6, kca_tables=None):
     """Request i of the serving workload: (cell, dt steps to simulate).
 

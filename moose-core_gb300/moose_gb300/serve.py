@@ -294,4 +294,14 @@ def summarize(results, wall_s, offered_rate=None):
            "compartment_steps_per_s": work / wall_s if wall_s > 0 else None}
     if offered_rate is not None:
         out["offered_rate_per_s"] = offered_rate
+    if len(results) >= 8:
+        # queueing delay (admission minus arrival) by arrival order: a queue
+        # that stays bounded keeps the last quarter's delay near the first's
+        rs = sorted(results, key=lambda r: r.arrival)
+        wait = np.array([r.admitted - r.arrival for r in rs])
+        q = len(wait) // 4
+        out["p50_queue_wait_s"] = float(np.percentile(wait, 50))
+        out["p99_queue_wait_s"] = float(np.percentile(wait, 99))
+        out["queue_wait_first_quarter_s"] = float(wait[:q].mean())
+        out["queue_wait_last_quarter_s"] = float(wait[-q:].mean())
     return out
