@@ -271,25 +271,60 @@ def run_serving(args, capacity=None):
     return out
 
 
-def compare_mixed_fp64(cells, nsteps, chunk):
+def _probe_cell(job):
+    """CPU conditioning check of one workload cell (spawned process): the
+    FP64 oracle against itself with only its gate increments in FP32 (the
+    gating precision of the mixed solver), over the same steps; returns the
+    soma's max |dVm|, the spike-time shift and whether the counts agree."""
+    import numpy as np
+    from moose_gb300 import models
+    from oracle import OracleCell
+    config, cell, n_cells, nsteps = job
+    sizes, _, _ = models.population_sizes(config, SEED, n_cells)
+    m = models.make_cell(config, SEED, cell, t_end=nsteps * DT + 0.01, sizes=sizes)
+    out = []
+    for probe in (False, True):
+        o = OracleCell(m, DT)
+        o.set_f32_gate_increments(probe)
+        o.reinit(DT)
+        soma = np.empty(nsteps + 1)
+        soma[0] = o.vm()[0]
+        for k in range(nsteps):
+            o.step(1)
+            soma[k + 1] = o.vm()[0]
+        out.append((soma, np.sort(o.spikes()[1])))
+    (sa, ta), (sb, tb) = out
+    eq = len(ta) == len(tb)
+    return (cell, float(np.abs(sa - sb).max()), float(np.abs(ta - tb).max()) if eq and len(ta) else 0.0, eq)
+
+
+def compare_mixed_fp64(cells, nsteps, chunk, ids=None, config=CONFIG, n_cells=None):
     """Accuracy of the mixed-precision batch against the FP64 batch (every
     cell bit-identical to the FP64 drop-in, itself bit-identical to the
     reference HSolve where no libm call differs): both batches step the same
     cells side by side (their own streams); the soma Vm of every cell is
     compared at every dt step, every compartment's Vm at the end of every
-    chunk of `chunk` steps, and the spike trains at the end."""
+    chunk of `chunk` steps, and the spike trains at the end.
+
+    Each cell over the bar (0.1 mV, 0.05 ms, equal counts) is then checked
+    for conditioning on the host cores: when the FP64 oracle with only its
+    gate increments in FP32 already leaves the bar on that cell, the cell is
+    ill-conditioned for FP32 gating (the precision split the mixed solver is
+    asked for) and is reported as such; the others would be defects."""
     import numpy as np
     from moose_gb300.abi import HS_PREC_FP64, HS_PREC_MIXED
     from moose_gb300.batch import Batch
     n = len(cells)
+    ids = list(range(n)) if ids is None else list(ids)
     f = Batch(cells, DT, HS_PREC_FP64)
     mx = Batch(cells, DT, HS_PREC_MIXED)
     somas = np.zeros(n, np.uint32)
     for bb in (f, mx):
         bb.record(np.arange(n), somas, 1, nsteps + 1)
         bb.reinit(DT)
-    worst_soma = worst_all = 0.0
-    worst_cell = -1
+    off = np.concatenate([[0], np.cumsum([m.n_compt for m in cells])[:-1]])
+    soma_dv = np.zeros(n)
+    all_dv = np.zeros(n)
     done = 0
     t0 = time.perf_counter()
     wf = np.empty((chunk + 1, n))
@@ -302,34 +337,61 @@ def compare_mixed_fp64(cells, nsteps, chunk):
         mx.sync()
         f.trace_window(done, k + 1, wf[:k + 1])
         mx.trace_window(done, k + 1, wm[:k + 1])
-        d = np.abs(wf[:k + 1] - wm[:k + 1]).max(axis=0)
-        if d.max() > worst_soma:
-            worst_soma, worst_cell = float(d.max()), int(d.argmax())
-        worst_all = max(worst_all, float(np.abs(f.read_all("Vm") - mx.read_all("Vm")).max()))
+        soma_dv = np.maximum(soma_dv, np.abs(wf[:k + 1] - wm[:k + 1]).max(axis=0))
+        all_dv = np.maximum(all_dv, np.maximum.reduceat(np.abs(f.read_all("Vm") - mx.read_all("Vm")), off))
         done += k
     wall = time.perf_counter() - t0
     cf, _, sf = f.spikes()
     cm, _, sm = mx.spikes()
-    shift, counts_equal, unequal = 0.0, True, 0
+    shift = np.zeros(n)
+    equal = np.ones(n, bool)
     for i in range(n):
         a, b = np.sort(sf[cf == i]), np.sort(sm[cm == i])
         if len(a) != len(b):
-            counts_equal = False
-            unequal += 1
+            equal[i] = False
         elif len(a):
-            shift = max(shift, float(np.abs(a - b).max()))
+            shift[i] = float(np.abs(a - b).max())
     f.close()
     mx.close()
+    dv = np.maximum(soma_dv, all_dv)
+    over = [i for i in range(n) if dv[i] > 1e-4 or shift[i] > 5e-5 or not equal[i]]
+    # conditioning of the cells over the bar, on the host cores
+    ill = set()
+    probes = []
+    if over:
+        ctx = mp.get_context("spawn")
+        jobs = [(config, ids[i], n_cells or len(cells), nsteps) for i in over]
+        with ctx.Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+            probes = pool.map(_probe_cell, jobs, chunksize=1)
+        for (cell, pdv, psh, peq), i in zip(probes, over):
+            if pdv > 1e-4 or psh > 5e-5 or not peq:
+                ill.add(i)
+    well = [i for i in range(n) if i not in ill]
     ncomp = sum(m.n_compt for m in cells)
-    return {"max_abs_dVm_V": max(worst_soma, worst_all), "max_abs_dVm_soma_every_step_V": worst_soma,
-            "max_abs_dVm_all_compartments_chunk_ends_V": worst_all, "worst_soma_cell": worst_cell,
-            "max_spike_shift_s": shift, "spike_counts_equal": counts_equal, "cells_with_unequal_counts": unequal,
-            "spikes": int(len(sf)), "cells": n, "compartments": ncomp, "dt_steps": nsteps,
-            "chunk_dt_steps": chunk, "bounds": {"dVm_V": 1e-4, "spike_shift_s": 5e-5},
-            "within_bounds": bool(max(worst_soma, worst_all) <= 1e-4 and shift <= 5e-5 and counts_equal),
+    wdv = float(dv[well].max()) if well else None
+    wsh = float(shift[well].max()) if well else None
+    return {"max_abs_dVm_V": float(dv.max()), "max_abs_dVm_soma_every_step_V": float(soma_dv.max()),
+            "max_abs_dVm_all_compartments_chunk_ends_V": float(all_dv.max()), "worst_cell": int(ids[int(dv.argmax())]),
+            "max_spike_shift_s": float(shift.max()), "spike_counts_equal": bool(equal.all()),
+            "cells_with_unequal_counts": int((~equal).sum()), "spikes": int(len(sf)),
+            "cells": n, "compartments": ncomp, "dt_steps": nsteps, "chunk_dt_steps": chunk,
+            "bounds": {"dVm_V": 1e-4, "spike_shift_s": 5e-5},
+            "cells_over_bar": [{"cell": int(ids[i]), "max_abs_dVm_V": float(dv[i]), "spike_shift_s": float(shift[i]),
+                                "counts_equal": bool(equal[i]),
+                                "fp64_oracle_with_f32_gate_increments": {"max_abs_dVm_soma_V": p[1],
+                                                                         "spike_shift_s": p[2],
+                                                                         "counts_equal": p[3]}}
+                               for i, p in zip(over, probes)],
+            "ill_conditioned_cells": len(ill),
+            "well_conditioned": {"cells": len(well), "max_abs_dVm_V": wdv, "max_spike_shift_s": wsh,
+                                 "spike_counts_equal": bool(equal[well].all()) if well else None,
+                                 "within_bounds": bool(well and wdv <= 1e-4 and wsh <= 5e-5
+                                                       and equal[well].all())},
+            "within_bounds_all_cells": bool(dv.max() <= 1e-4 and shift.max() <= 5e-5 and equal.all()),
             "wall_s": wall,
             "compared": "mixed batch vs FP64 batch: soma Vm every dt step, every compartment's Vm at every "
-                        "chunk end, spike times and counts of every cell"}
+                        "chunk end, spike times and counts of every cell; a cell over the bar is "
+                        "ill-conditioned when the FP64 oracle with only FP32 gate increments also leaves it"}
 
 
 def run_accuracy_full(args):
@@ -342,7 +404,7 @@ def run_accuracy_full(args):
     sizes, _, _ = models.population_sizes(CONFIG, SEED, args.cells)
     t_end = args.acc_steps * DT + 0.01
     cells = [models.make_cell(CONFIG, SEED, i, t_end=t_end, kca_tables=kca, sizes=sizes) for i in range(args.cells)]
-    out = compare_mixed_fp64(cells, args.acc_steps, args.chunk)
+    out = compare_mixed_fp64(cells, args.acc_steps, args.chunk, n_cells=args.cells)
     out["workload"] = "hsolve_4096cells_mixed_syn200" if args.cells == 4096 else "%d cells" % args.cells
     return out
 
@@ -534,7 +596,7 @@ def run_ours(args, rank, world, cpu_pool):
             ids = list(range(0, args.cells, max(1, args.cells // args.acc_cells)))[: args.acc_cells]
             t_acc = args.acc_steps * DT + 0.01      # synaptic trains and stimulus cover the whole run
             acc_cells = [models.make_cell(CONFIG, SEED, i, t_end=t_acc, kca_tables=kca, sizes=sizes) for i in ids]
-            acc = compare_mixed_fp64(acc_cells, args.acc_steps, args.acc_chunk)
+            acc = compare_mixed_fp64(acc_cells, args.acc_steps, args.acc_chunk, ids=ids, n_cells=args.cells)
             del acc_cells
             acc["sample"] = ("%d of %d cells (every %d-th), %d dt steps (%.2f s)"
                              % (len(ids), args.cells, max(1, args.cells // args.acc_cells), args.acc_steps,

@@ -49,6 +49,7 @@ struct OrcCell {
     double dt;                  /* HSolve dt_ */
     uint32_t nCompt;
     int caAdvance;
+    int f32GateIncrements;      /* conditioning probe, see orc_set_f32_gate_increments */
 
     /* Hines order */
     uint32_t* compartmentId;    /* hines -> model */
@@ -1075,6 +1076,19 @@ void orc_reinit(OrcCell* c, double clock_dt) {
 }
 
 /* HSolveActive::advanceChannels (hsolve/HSolveActive.cpp:218-332) */
+/* Conditioning probe (not the reference's arithmetic): the trapezoidal gate
+   step written as x + (dt C1 - 2 h x)/(1 + h), h = dt/2 C2, with the
+   increment computed in FP32 and added to the FP64 state -- the precision a
+   mixed-precision solver gives its gates.  A cell whose trajectory leaves a
+   tolerance under this alone is ill-conditioned at that tolerance for any
+   solver with FP32 gating. */
+static double gateIncrementF32(double x, double C1, double C2, double dt) {
+    const float c1 = (float)C1, c2 = (float)C2, xf = (float)x, dtf = (float)dt;
+    const float h = 0.5f * dtf * c2;
+    const float inc = (dtf * c1 - 2.0f * h * xf) / (1.0f + h);
+    return (double)inc;
+}
+
 static void advanceChannels(OrcCell* c, double dt) {
     uint32_t n = c->nCompt;
     uint32_t ichan = 0, ica = 0, icol = 0, izr = 0;
@@ -1094,12 +1108,14 @@ static void advanceChannels(OrcCell* c, double dt) {
             if (ch->Xpower > 0.0) {
                 lt_lookup(&c->vTable, c->column[icol], &vRow, &C1, &C2);
                 if (ch->instant & 1) state[istate] = C1 / C2;
+                else if (c->f32GateIncrements) state[istate] += gateIncrementF32(state[istate], C1, C2, dt);
                 else { double temp = 1.0 + dt / 2.0 * C2; state[istate] = (state[istate] * (2.0 - temp) + dt * C1) / temp; }
                 ++icol, ++istate;
             }
             if (ch->Ypower > 0.0) {
                 lt_lookup(&c->vTable, c->column[icol], &vRow, &C1, &C2);
                 if (ch->instant & 2) state[istate] = C1 / C2;
+                else if (c->f32GateIncrements) state[istate] += gateIncrementF32(state[istate], C1, C2, dt);
                 else { double temp = 1.0 + dt / 2.0 * C2; state[istate] = (state[istate] * (2.0 - temp) + dt * C1) / temp; }
                 ++icol, ++istate;
             }
@@ -1109,6 +1125,7 @@ static void advanceChannels(OrcCell* c, double dt) {
                 else if (c->externalCalcium[ichan] > 0) lt_lookup(&c->caTable, c->column[icol], &dRow, &C1, &C2);
                 else lt_lookup(&c->vTable, c->column[icol], &vRow, &C1, &C2);
                 if (ch->instant & 4) state[istate] = C1 / C2;
+                else if (c->f32GateIncrements) state[istate] += gateIncrementF32(state[istate], C1, C2, dt);
                 else { double temp = 1.0 + dt / 2.0 * C2; state[istate] = (state[istate] * (2.0 - temp) + dt * C1) / temp; }
                 ++icol, ++istate, ++izr;
             }
@@ -1281,6 +1298,7 @@ uint32_t orc_n_state(const OrcCell* c) { return (uint32_t)c->state.n; }
 uint32_t orc_hines_index(const OrcCell* c, uint32_t m) { return c->hinesOf[m]; }
 uint32_t orc_model_index(const OrcCell* c, uint32_t h) { return c->compartmentId[h]; }
 void orc_set_ca_advance(OrcCell* c, int a) { c->caAdvance = a; }
+void orc_set_f32_gate_increments(OrcCell* c, int on) { c->f32GateIncrements = on != 0; }
 
 void orc_read_vm(const OrcCell* c, double* out) {
     for (uint32_t m = 0; m < c->d->n_compt; m++)

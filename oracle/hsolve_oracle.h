@@ -46,6 +46,10 @@ OrcCell* orc_create(const HsCellDesc* d, uint32_t seed, double dt,
                     char* err, uint32_t errlen);
 void orc_destroy(OrcCell* c);
 void orc_set_ca_advance(OrcCell* c, int ca_advance);
+/* Conditioning probe for accuracy analysis, off by default: gate increments
+   computed in FP32 and accumulated in FP64 (the gating precision of a
+   mixed-precision solver) instead of the reference's FP64 step. */
+void orc_set_f32_gate_increments(OrcCell* c, int on);
 /* HSolve::reinit with the clock dt (also reinit of tick-1/4 objects). */
 void orc_reinit(OrcCell* c, double clock_dt);
 /* nsteps clock steps: ticks 0 (stimulus), 1, 4, 6 (HSolve), spikes. */

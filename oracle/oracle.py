@@ -45,6 +45,7 @@ def lib():
         L.orc_create.argtypes = [C.POINTER(HsCellDesc), C.c_uint32, C.c_double, C.c_char_p, C.c_uint32]
         L.orc_destroy.argtypes = [vp]
         L.orc_set_ca_advance.argtypes = [vp, C.c_int]
+        L.orc_set_f32_gate_increments.argtypes = [vp, C.c_int]
         L.orc_reinit.argtypes = [vp, C.c_double]
         L.orc_step.argtypes = [vp, C.c_uint32]
         for f in ("orc_n_compt", "orc_n_pool", "orc_n_state"):
@@ -107,6 +108,11 @@ class OracleCell:
 
     def set_ca_advance(self, v):
         lib().orc_set_ca_advance(self.h, int(v))
+
+    def set_f32_gate_increments(self, on=True):
+        """Conditioning probe (not the reference's arithmetic): gate increments
+        in FP32, accumulated in FP64, as a mixed-precision solver gates."""
+        lib().orc_set_f32_gate_increments(self.h, int(bool(on)))
 
     def reinit(self, dt):
         lib().orc_reinit(self.h, dt)
