@@ -311,8 +311,10 @@ int hs_read_spikes(HsSolver* s, uint32_t* gen, double* time, uint32_t capacity,
 typedef struct HsBatch HsBatch;
 
 /* Launch shape of the batched kernel (0 keeps the current value).
- * FP64: one warp steps one cell; cells are packed over ctas_per_sm x
- * SM-count CTAs.  Mixed: one CTA steps a forest of cells at a time; a forest
+ * FP64: one wave of ctas_per_sm x SM-count CTAs (fewer per SM if the
+ * kernel's registers do not fit that many); a warp steps its cells one after
+ * the other, and the cells too large to share a warp's load with others are
+ * stepped by a whole CTA each.  Mixed: one CTA steps a forest of cells at a time; a forest
  * holds its elimination arrays in the CTA's shared memory (30 B per node),
  * so ctas_per_sm and forest_nodes set the forest size.  Changing either (or
  * max_ctas) on a mixed batch renumbers its nodes: its state, recording and
@@ -320,7 +322,7 @@ typedef struct HsBatch HsBatch;
 typedef struct HsBatchTuning {
     uint32_t threads_per_cta;   /* multiple of 32; FP64 <= 256 (default 256),
                                    mixed <= 1024 (default 1024) */
-    uint32_t ctas_per_sm;       /* CTAs per SM (default 4 FP64, 1 mixed) */
+    uint32_t ctas_per_sm;       /* CTAs per SM (default 2 FP64, 1 mixed) */
     uint32_t steps_per_launch;  /* dt steps per kernel launch (default 100) */
     uint32_t use_graph;         /* capture a process() call as a CUDA graph */
     uint32_t forest_nodes;      /* mixed: most nodes per shared-memory forest

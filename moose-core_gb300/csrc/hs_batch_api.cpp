@@ -132,7 +132,7 @@ struct HsBatch {
     std::vector<CellPlan> plans;
     uint64_t nCompt = 0;
     // packing / tuning
-    uint32_t threadsPerCta = 256, ctasPerSm = 4, stepsPerLaunch = 100;
+    uint32_t threadsPerCta = 256, ctasPerSm = 2, stepsPerLaunch = 100;
     uint32_t forestNodes = 0;    // mixed: forest size limit (0: shared-memory capacity)
     uint32_t maxCtas = 0;        // mixed: CTA limit of the packing (0: one wave)
     uint32_t elimWarps = 4;      // mixed: eliminator warps of the split step (0: no split)
@@ -140,6 +140,8 @@ struct HsBatch {
     bool useGraph = true;
     uint32_t nWarps = 0, nCtas = 0;
     uint32_t *dWarpPtr = nullptr, *dWarpCells = nullptr;
+    uint32_t *dCtaCellPtr = nullptr, *dCtaCells = nullptr;   // FP64: cells stepped by a whole CTA
+    uint32_t nCtaWhole = 0;
     // mixed: forests per CTA, shared-memory forest capacity
     uint32_t *dCtaPtr = nullptr, *dCtaForests = nullptr;
     uint32_t mixCap = 0, mixSmem = 0;
@@ -201,16 +203,22 @@ namespace {
 
 cudaError_t launchStep(HsBatch* b, uint32_t k) {
     if (b->precision == HS_PREC_FP64)
-        return launchBatchStepFp64(b->dDcs, b->dWarpPtr, b->dWarpCells, b->nWarps, k, b->threadsPerCta, b->st);
+        return launchBatchStepFp64(b->dDcs, b->dWarpPtr, b->dWarpCells, b->nWarps, b->dCtaCellPtr, b->dCtaCells, k,
+                                   b->threadsPerCta, b->st);
     const uint32_t ew = b->elimWarps && b->threadsPerCta > 32 * b->elimWarps ? b->elimWarps : 0;
     b->mb.waitRounds = b->waitRounds;
     return launchForestStepMixed(b->mb, b->dCtaPtr, b->dCtaForests, b->nCtas, b->threadsPerCta, b->mixSmem,
                                  b->mixCap, ew, k, b->st);
 }
 
-// Longest-processing-time packing of the FP64 batch: cells to the CTAs of one
-// wave, then to the warps inside each CTA.  (The mixed batch packs its
-// forests when its layout is built.)
+// Packing of the FP64 batch into one wave of CTAs (as many per SM as the
+// kernel's registers allow, at most ctas_per_sm).  A warp steps its cells
+// one after the other, so a cell costing more than the balanced load of one
+// warp would bound the step by itself: such cells are stepped by a whole
+// CTA instead (its warps share each compartment loop and each elimination
+// level, as in the drop-in), packed longest first over enough CTAs to carry
+// their load; the other cells are packed longest first over the remaining
+// CTAs and then over their warps.
 int repack(HsBatch* b) {
     if (b->gexec) {
         cudaGraphExecDestroy(b->gexec);
@@ -220,21 +228,50 @@ int repack(HsBatch* b) {
     b->packBuf.freeAll();
     b->packBuf.err = cudaSuccess;
     const uint32_t warpsPerCta = b->threadsPerCta / 32;
-    b->nCtas = std::max<uint32_t>(1, b->nSm * b->ctasPerSm);
+    const int fit = fp64BatchCtasPerSm(b->threadsPerCta);
+    const uint32_t cps = std::max<uint32_t>(1, fit > 0 ? std::min<uint32_t>(b->ctasPerSm, (uint32_t)fit) : b->ctasPerSm);
+    b->nCtas = std::max<uint32_t>(1, b->nSm * cps);
     b->nWarps = b->nCtas * warpsPerCta;
     std::vector<double> cost(b->nCells);
+    double total = 0;
     for (uint32_t c = 0; c < b->nCells; ++c) {
         const CellPlan& P = b->plans[c];
         cost[c] = P.N + 0.3 * P.C + 0.5 * P.S + 2.0 * (P.fLevelPtr.size() + P.bLevelPtr.size());
+        total += cost[c];
     }
     std::vector<uint32_t> order(b->nCells);
     for (uint32_t c = 0; c < b->nCells; ++c) order[c] = c;
     std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return cost[x] > cost[y]; });
+    // a whole CTA steps a cell at a fraction of its warps' combined rate
+    // (a barrier per elimination level, levels narrower than the CTA); this
+    // estimate of the fraction only sizes the CTAs given to the largest cells
+    constexpr double kCtaEfficiency = 0.6;
+    const double perWarp = total / b->nWarps;
+    std::vector<uint32_t> big, small;
+    for (uint32_t c : order) (warpsPerCta > 1 && cost[c] > perWarp ? big : small).push_back(c);
+    double bigLoad = 0;
+    for (uint32_t c : big) bigLoad += cost[c] / (warpsPerCta * kCtaEfficiency);
+    uint32_t mCta = 0;
+    if (!big.empty()) {
+        mCta = (uint32_t)std::ceil(bigLoad / std::max(perWarp, 1e-9));
+        mCta = std::max<uint32_t>(1, std::min<uint32_t>(mCta, small.empty() ? b->nCtas : b->nCtas - 1));
+    }
     using Item = std::pair<double, uint32_t>;
+    std::vector<std::vector<uint32_t>> ctaWhole(b->nCtas);
+    {
+        std::priority_queue<Item, std::vector<Item>, std::greater<Item>> q;
+        for (uint32_t k = 0; k < mCta; ++k) q.push({0.0, k});
+        for (uint32_t c : big) {
+            Item it = q.top();
+            q.pop();
+            ctaWhole[it.second].push_back(c);
+            q.push({it.first + cost[c] / (warpsPerCta * kCtaEfficiency), it.second});
+        }
+    }
     std::priority_queue<Item, std::vector<Item>, std::greater<Item>> cta;
-    for (uint32_t k = 0; k < b->nCtas; ++k) cta.push({0.0, k});
+    for (uint32_t k = mCta; k < b->nCtas; ++k) cta.push({0.0, k});
     std::vector<std::vector<uint32_t>> ctaCells(b->nCtas);
-    for (uint32_t c : order) {
+    for (uint32_t c : small) {
         Item it = cta.top();
         cta.pop();
         ctaCells[it.second].push_back(c);
@@ -257,8 +294,16 @@ int repack(HsBatch* b) {
         ptr[w + 1] = ptr[w] + (uint32_t)warpCells[w].size();
         cells.insert(cells.end(), warpCells[w].begin(), warpCells[w].end());
     }
+    std::vector<uint32_t> cptr(b->nCtas + 1, 0), ccells;
+    for (uint32_t k = 0; k < b->nCtas; ++k) {
+        cptr[k + 1] = cptr[k] + (uint32_t)ctaWhole[k].size();
+        ccells.insert(ccells.end(), ctaWhole[k].begin(), ctaWhole[k].end());
+    }
     b->dWarpPtr = b->packBuf.up(ptr, b->st);
     b->dWarpCells = b->packBuf.up(cells, b->st);
+    b->dCtaCellPtr = b->packBuf.up(cptr, b->st);
+    b->dCtaCells = b->packBuf.up(ccells, b->st);
+    b->nCtaWhole = mCta;
     if (b->packBuf.err == cudaSuccess) b->packBuf.err = cudaStreamSynchronize(b->st);
     if (b->packBuf.err != cudaSuccess) return cerr(b->packBuf.err, "batch packing");
     return HS_OK;

@@ -61,7 +61,10 @@ cudaError_t launchGatherSpikes(const DevCell* cells, const uint32_t* srcGen, con
                                uint32_t nCells, const uint32_t* off, uint32_t* gen, double* time,
                                cudaStream_t st);
 cudaError_t launchBatchStepFp64(const DevCell* cells, const uint32_t* warpCellPtr,
-                                const uint32_t* warpCells, uint32_t nWarps, uint32_t nsteps,
-                                uint32_t threadsPerCta, cudaStream_t st);
+                                const uint32_t* warpCells, uint32_t nWarps, const uint32_t* ctaCellPtr,
+                                const uint32_t* ctaCells, uint32_t nsteps, uint32_t threadsPerCta,
+                                cudaStream_t st);
+// CTAs of the FP64 batch kernel that fit on one SM at once (0 if unknown).
+int fp64BatchCtasPerSm(uint32_t threadsPerCta);
 
 }  // namespace hsg

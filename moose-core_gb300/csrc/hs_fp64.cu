@@ -360,11 +360,22 @@ __global__ void __launch_bounds__(256, 1) hsStepFp64(DevCell c, uint32_t nsteps)
     stepCell<false>(c, nsteps, threadIdx.x, blockDim.x);
 }
 
-// Batched FP64: one warp per cell, cells listed per warp (packed by size).
+// Batched FP64.  A CTA either steps its cells one after the other with all
+// its threads, as the drop-in steps one cell (ctaCellPtr gives it a
+// non-empty list: the largest cells, whose chains would otherwise bound the
+// step), or runs one warp per cell on the cells listed per warp.  Both
+// forms do the drop-in's arithmetic in its order: results are bit-identical
+// whichever form steps a cell.
 __global__ void __launch_bounds__(256) hsBatchStepFp64(const DevCell* __restrict__ cells,
                                                        const uint32_t* __restrict__ warpCellPtr,
                                                        const uint32_t* __restrict__ warpCells,
-                                                       uint32_t nWarps, uint32_t nsteps) {
+                                                       uint32_t nWarps, const uint32_t* __restrict__ ctaCellPtr,
+                                                       const uint32_t* __restrict__ ctaCells, uint32_t nsteps) {
+    const uint32_t c0 = ctaCellPtr[blockIdx.x], c1 = ctaCellPtr[blockIdx.x + 1];
+    if (c0 < c1) {      // uniform over the CTA
+        for (uint32_t k = c0; k < c1; ++k) stepCell<false>(cells[ctaCells[k]], nsteps, threadIdx.x, blockDim.x);
+        return;
+    }
     uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     uint32_t lane = threadIdx.x & 31;
     if (w >= nWarps) return;
@@ -547,11 +558,20 @@ cudaError_t launchStepFp64(const DevCell& c, uint32_t nsteps, cudaStream_t st) {
 }
 
 cudaError_t launchBatchStepFp64(const DevCell* cells, const uint32_t* warpCellPtr,
-                                const uint32_t* warpCells, uint32_t nWarps, uint32_t nsteps,
-                                uint32_t threadsPerCta, cudaStream_t st) {
+                                const uint32_t* warpCells, uint32_t nWarps, const uint32_t* ctaCellPtr,
+                                const uint32_t* ctaCells, uint32_t nsteps, uint32_t threadsPerCta,
+                                cudaStream_t st) {
     uint32_t blocks = (nWarps * 32 + threadsPerCta - 1) / threadsPerCta;
-    hsBatchStepFp64<<<blocks, threadsPerCta, 0, st>>>(cells, warpCellPtr, warpCells, nWarps, nsteps);
+    hsBatchStepFp64<<<blocks, threadsPerCta, 0, st>>>(cells, warpCellPtr, warpCells, nWarps, ctaCellPtr, ctaCells,
+                                                      nsteps);
     return cudaGetLastError();
+}
+
+int fp64BatchCtasPerSm(uint32_t threadsPerCta) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, hsBatchStepFp64, (int)threadsPerCta, 0) != cudaSuccess)
+        return 0;
+    return n;
 }
 
 cudaError_t launchReinitFp64(const DevCell* cells, uint32_t nCells, cudaStream_t st) {

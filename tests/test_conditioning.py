@@ -4,11 +4,11 @@ ill-conditioned cell from a solver defect when the mixed batch leaves the
 0.1 mV / 0.05 ms bar over the synaptic workload's full second.
 
 Off by default (the golden tests run with it off and stay bit-exact).  Cell
-2528 of the 4,096-cell synaptic workload is ill-conditioned: the probe alone
-moves its soma by tens of mV and changes its spike count over 1 s, while a
-1e-13 relative kick to its Vm stays below a microvolt (the amplification is
-large but finite, not a floating-point artefact of the oracle).  Cell 158 is
-well conditioned: the probe moves it by microvolts.  CPU only."""
+861 of the 4,096-cell synaptic workload (136 compartments) is
+ill-conditioned: over 1 s the probe alone moves its soma by about 2 mV
+(20 times the 0.1 mV bar; the larger cell 2528 moves by tens of mV and
+changes its spike count).  Cell 158 is well conditioned: the probe moves it
+by microvolts.  CPU only."""
 import numpy as np
 
 from moose_gb300 import models
@@ -35,10 +35,10 @@ def _cell(i):
 
 
 def test_probe_separates_ill_from_well_conditioned_cells():
-    ill = _cell(2528)
+    ill = _cell(861)
     a, ta = _soma(ill, False)
     b, tb = _soma(ill, True)
-    assert np.abs(a - b).max() > 1e-2 or len(ta) != len(tb)
+    assert np.abs(a - b).max() > 1e-3 or len(ta) != len(tb)
     well = _cell(158)
     c, tc = _soma(well, False)
     d, td = _soma(well, True)
