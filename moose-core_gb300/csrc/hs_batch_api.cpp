@@ -244,18 +244,39 @@ int repack(HsBatch* b) {
     std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return cost[x] > cost[y]; });
     // a whole CTA steps a cell at a fraction of its warps' combined rate
     // (a barrier per elimination level, levels narrower than the CTA); this
-    // estimate of the fraction only sizes the CTAs given to the largest cells
+    // estimate of the fraction only decides which cells get whole CTAs
     constexpr double kCtaEfficiency = 0.6;
-    const double perWarp = total / b->nWarps;
-    std::vector<uint32_t> big, small;
-    for (uint32_t c : order) (warpsPerCta > 1 && cost[c] > perWarp ? big : small).push_back(c);
-    double bigLoad = 0;
-    for (uint32_t c : big) bigLoad += cost[c] / (warpsPerCta * kCtaEfficiency);
-    uint32_t mCta = 0;
-    if (!big.empty()) {
-        mCta = (uint32_t)std::ceil(bigLoad / std::max(perWarp, 1e-9));
-        mCta = std::max<uint32_t>(1, std::min<uint32_t>(mCta, small.empty() ? b->nCtas : b->nCtas - 1));
-    }
+    const double ctaRate = warpsPerCta > 1 ? warpsPerCta * kCtaEfficiency : 1.0;
+    // the k costliest cells on m whole CTAs, the rest over the warps of the
+    // other CTAs: estimated step time, the larger of the two groups' (each
+    // bounded below by its largest cell and by its load spread evenly)
+    const uint32_t nC = b->nCells;
+    std::vector<double> prefix(nC + 1, 0.0);
+    for (uint32_t i = 0; i < nC; ++i) prefix[i + 1] = prefix[i] + cost[order[i]];
+    uint32_t bestK = 0, bestM = 0;
+    double bestT = std::max(nC ? cost[order[0]] : 0.0, total / b->nWarps);
+    if (warpsPerCta > 1 && b->nCtas > 1)
+        for (uint32_t k = 1; k <= nC; ++k) {
+            const double sb = prefix[k], ss = total - sb;
+            const double bigMax = cost[order[0]] / ctaRate, smallMax = k < nC ? cost[order[k]] : 0.0;
+            // m balancing sb / (m ctaRate) against ss / ((nCtas - m) warpsPerCta)
+            const double mf = k < nC ? b->nCtas * sb / ctaRate / (sb / ctaRate + ss / warpsPerCta) : b->nCtas;
+            for (int dm = 0; dm <= 1; ++dm) {
+                uint32_t m = (uint32_t)std::floor(mf) + dm;
+                m = std::max<uint32_t>(1, std::min<uint32_t>(m, k < nC ? b->nCtas - 1 : b->nCtas));
+                m = std::min<uint32_t>(m, k);
+                const double tb = std::max(bigMax, sb / (m * ctaRate));
+                const double ts = k < nC ? std::max(smallMax, ss / ((double)(b->nCtas - m) * warpsPerCta)) : 0.0;
+                const double t = std::max(tb, ts);
+                if (t < bestT) {
+                    bestT = t;
+                    bestK = k;
+                    bestM = m;
+                }
+            }
+        }
+    std::vector<uint32_t> big(order.begin(), order.begin() + bestK), small(order.begin() + bestK, order.end());
+    const uint32_t mCta = bestM;
     using Item = std::pair<double, uint32_t>;
     std::vector<std::vector<uint32_t>> ctaWhole(b->nCtas);
     {
@@ -265,7 +286,7 @@ int repack(HsBatch* b) {
             Item it = q.top();
             q.pop();
             ctaWhole[it.second].push_back(c);
-            q.push({it.first + cost[c] / (warpsPerCta * kCtaEfficiency), it.second});
+            q.push({it.first + cost[c] / ctaRate, it.second});
         }
     }
     std::priority_queue<Item, std::vector<Item>, std::greater<Item>> cta;
