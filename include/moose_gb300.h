@@ -320,9 +320,9 @@ typedef struct HsBatch HsBatch;
  * max_ctas) on a mixed batch renumbers its nodes: its state, recording and
  * inject targets start over and hs_batch_reinit must follow. */
 typedef struct HsBatchTuning {
-    uint32_t threads_per_cta;   /* multiple of 32; FP64 <= 256 (default 256),
+    uint32_t threads_per_cta;   /* multiple of 32; FP64 <= 256 (default 128),
                                    mixed <= 1024 (default 1024) */
-    uint32_t ctas_per_sm;       /* CTAs per SM (default 2 FP64, 1 mixed) */
+    uint32_t ctas_per_sm;       /* CTAs per SM (default 4 FP64, 1 mixed) */
     uint32_t steps_per_launch;  /* dt steps per kernel launch (default 100) */
     uint32_t use_graph;         /* capture a process() call as a CUDA graph */
     uint32_t forest_nodes;      /* mixed: most nodes per shared-memory forest

@@ -132,7 +132,9 @@ struct HsBatch {
     std::vector<CellPlan> plans;
     uint64_t nCompt = 0;
     // packing / tuning
-    uint32_t threadsPerCta = 256, ctasPerSm = 2, stepsPerLaunch = 100;
+    // FP64 default: 4 CTAs of 128 threads per SM, the launch shape measured
+    // fastest on the 4,096-cell workload (bit-identical in every shape)
+    uint32_t threadsPerCta = 128, ctasPerSm = 4, stepsPerLaunch = 100;
     uint32_t forestNodes = 0;    // mixed: forest size limit (0: shared-memory capacity)
     uint32_t maxCtas = 0;        // mixed: CTA limit of the packing (0: one wave)
     uint32_t elimWarps = 4;      // mixed: eliminator warps of the split step (0: no split)

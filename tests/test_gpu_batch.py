@@ -275,3 +275,25 @@ def test_bounded_wait_gives_up_with_etimeout():
         o.step(200)
         assert np.abs(good.vm(i) - o.vm()).max() <= 1e-4
     good.close()
+
+
+def test_fp64_batch_whole_cta_and_warp_cells_bit_exact():
+    """The FP64 batch steps its largest cells with a whole CTA each and the
+    rest one warp per cell (the packing chooses by cost): a mix of two
+    3,000-compartment cells and small ones is bit-identical to per-cell
+    drop-ins whichever form stepped each cell."""
+    small = small_population(10, 21, n_syn=4, lo=20, hi=200)
+    big = small_population(2, 22, n_syn=4, lo=3000, hi=3001)
+    cells = big[:1] + small + big[1:]
+    b = Batch(cells, DT, HS_PREC_FP64, steps_per_launch=60)
+    b.reinit(DT)
+    b.process(300)
+    for i, m in enumerate(cells):
+        h = HSolve(m, dt=DT)
+        h.target = m.seed
+        h.reinit(DT)
+        h.process(300)
+        assert np.array_equal(b.vm(i), h.vm()), "cell %d" % i
+        assert np.array_equal(b.ca(i), h.ca()), "cell %d" % i
+        h.close()
+    b.close()
