@@ -183,7 +183,43 @@ typedef struct HsCellDesc {
     const uint32_t* stim_compt;
     const uint32_t* stim_step;
     const double* stim_value;
+
+    /* External calcium on tick 1, before the solver's tick 6: DifShells
+     * (`biophysics/DifShell.cpp`), DifBuffers (`biophysics/DifBuffer.cpp`)
+     * and MMPumps (`biophysics/MMPump.cpp`), listed in their tick-1 process
+     * order, with HS_DIF_NPAR parameters each in `difpar` (layouts below).
+     * Their messages, each (kind, src, dst) in creation order: a source's
+     * sends reach its targets in that order, so the accumulations round as
+     * in the reference.  The solver sends each HHChannel's Ik = (Ek - Vm) Gk
+     * after its step (`HSolveActive::sendValues`,
+     * `hsolve/HSolveActive.cpp:354-385`) to the shells its IkOut reaches,
+     * and a shell's concentration reaches an HHChannel's `concen` as
+     * `HSolve::addConc` does (`hsolve/HSolveInterface.cpp:254-259`). */
+    uint32_t n_dif;
+    const int32_t* dif_kind;       /* HS_DIF_* */
+    const double* difpar;          /* n_dif x HS_DIF_NPAR */
+    uint32_t n_dmsg;
+    const int32_t* dmsg_kind;      /* HS_DMSG_* */
+    const uint32_t* dmsg_src;      /* object (HHChannel for HS_DMSG_IK) */
+    const uint32_t* dmsg_dst;      /* object (HHChannel for HS_DMSG_CONC_CHAN) */
 } HsCellDesc;
+
+/* tick-1 object kinds and their parameters (difpar, HS_DIF_NPAR per object) */
+#define HS_DIF_SHELL   0   /* Ceq, D, valence, leak, shapeMode, length, diameter,
+                              thickness, volume, outerArea, innerArea (the last
+                              three used with shapeMode 3 only)            */
+#define HS_DIF_BUFFER  1   /* bTot, kf, kb, D, shapeMode, length, diameter,
+                              thickness, volume, outerArea, innerArea      */
+#define HS_DIF_PUMP    2   /* Vmax, Kd                                     */
+#define HS_DIF_NPAR   12
+/* message kinds */
+#define HS_DMSG_OUTER      0  /* outerDifSourceOut -> fluxFromOut (shell or buffer) */
+#define HS_DMSG_INNER      1  /* innerDifSourceOut -> fluxFromIn                   */
+#define HS_DMSG_CONC_CHAN  2  /* shell concentrationOut -> HHChannel concen         */
+#define HS_DMSG_CONC_BUF   3  /* shell concentrationOut -> buffer concentration     */
+#define HS_DMSG_REACTION   4  /* buffer reactionOut -> shell reaction               */
+#define HS_DMSG_PUMP       5  /* pump PumpOut -> shell mmPump                        */
+#define HS_DMSG_IK         6  /* HHChannel IkOut (sent by the solver) -> shell influx */
 
 /* ------------------------------------------------------------------ */
 /* Library */

@@ -83,8 +83,12 @@ struct HsCellDescStore {
     std::vector<uint32_t> sg_compt;
     std::vector<double> sg_threshold, sg_refractT;
     std::vector<int32_t> sg_edge;
+    std::vector<int32_t> dif_kind;
+    std::vector<double> difpar;
+    std::vector<int32_t> dmsg_kind;
+    std::vector<uint32_t> dmsg_src, dmsg_dst;
     // the MOOSE objects behind each index, for the caller's Id -> index maps
-    std::vector<Id> comptId, chanId, poolId, chan2dId, synId, spikeGenId;
+    std::vector<Id> comptId, chanId, poolId, chan2dId, synId, spikeGenId, difId;
     uint32_t seed = 0;
     HsCellDesc desc{};
 };
@@ -381,6 +385,105 @@ int fillCellDesc(const HSolve& hs, HsCellDescStore& out, std::string& err) {
         out.sg_refractT.push_back(Field<double>::get(o, "refractT"));
         out.sg_edge.push_back(Field<bool>::get(o, "edgeTriggered") ? 1 : 0);
     }
+    // ---- external calcium on tick 1: the DifShells the channels' IkOut
+    // reaches or whose concentrationOut reaches a channel's concen, and every
+    // DifShell, DifBuffer and MMPump connected to those through their
+    // diffusion, concentration, reaction and pump messages
+    {
+        auto cls = [](const Id& x) { return x.element()->cinfo()->name(); };
+        std::vector<Id> seen;
+        std::vector<Id> todo;
+        auto visit = [&](const Id& x) {
+            const string c = cls(x);
+            if ((c == "DifShell" || c == "DifBuffer" || c == "MMPump") &&
+                std::find(seen.begin(), seen.end(), x) == seen.end()) {
+                seen.push_back(x);
+                todo.push_back(x);
+            }
+        };
+        for (const Id& ch : out.chanId) {
+            vector<Id> t;
+            HSolveUtils::targets(ch, "IkOut", t, "DifShell");
+            HSolveUtils::targets(ch, "concen", t, "DifShell");
+            for (const Id& x : t) visit(x);
+        }
+        const char* links[] = {"innerDifSourceOut", "outerDifSourceOut", "concentrationOut", "reactionOut",
+                               "PumpOut", "fluxFromOut", "fluxFromIn", "reaction", "mmPump", "concentration"};
+        while (!todo.empty()) {
+            const Id x = todo.back();
+            todo.pop_back();
+            for (const char* f : links) {
+                vector<Id> t;
+                HSolveUtils::targets(x, f, t);
+                for (const Id& y : t) visit(y);
+            }
+        }
+        // tick-1 process order: the order the objects were created in
+        std::sort(seen.begin(), seen.end(), [](const Id& a, const Id& b) { return a.value() < b.value(); });
+        out.difId = seen;
+        std::map<Id, uint32_t> difIndex;
+        for (uint32_t k = 0; k < seen.size(); ++k) difIndex[seen[k]] = k;
+        std::map<Id, uint32_t> chanIndex;
+        for (uint32_t k = 0; k < out.chanId.size(); ++k) chanIndex[out.chanId[k]] = k;
+        for (uint32_t k = 0; k < seen.size(); ++k) {
+            const Id& x = seen[k];
+            const string c = cls(x);
+            double p[HS_DIF_NPAR] = {0};
+            if (c == "DifShell") {
+                out.dif_kind.push_back(HS_DIF_SHELL);
+                const char* f[] = {"Ceq", "D", "valence", "leak"};
+                for (int i = 0; i < 4; ++i) p[i] = Field<double>::get(x, f[i]);
+                p[4] = Field<unsigned int>::get(x, "shapeMode");
+                const char* g[] = {"length", "diameter", "thickness", "volume", "outerArea", "innerArea"};
+                for (int i = 0; i < 6; ++i) p[5 + i] = Field<double>::get(x, g[i]);
+            } else if (c == "DifBuffer") {
+                out.dif_kind.push_back(HS_DIF_BUFFER);
+                const char* f[] = {"bTot", "kf", "kb", "D"};
+                for (int i = 0; i < 4; ++i) p[i] = Field<double>::get(x, f[i]);
+                p[4] = Field<unsigned int>::get(x, "shapeMode");
+                const char* g[] = {"length", "diameter", "thickness", "volume", "outerArea", "innerArea", "activation"};
+                for (int i = 0; i < 7; ++i) p[5 + i] = Field<double>::get(x, g[i]);
+            } else {
+                out.dif_kind.push_back(HS_DIF_PUMP);
+                p[0] = Field<double>::get(x, "Vmax");
+                p[1] = Field<double>::get(x, "Kd");
+            }
+            out.difpar.insert(out.difpar.end(), p, p + HS_DIF_NPAR);
+        }
+        auto emit = [&](int kind, uint32_t src, uint32_t dst) {
+            out.dmsg_kind.push_back(kind);
+            out.dmsg_src.push_back(src);
+            out.dmsg_dst.push_back(dst);
+        };
+        // each object's sends, in message order per source finfo
+        for (uint32_t k = 0; k < seen.size(); ++k) {
+            const Id& x = seen[k];
+            const struct { const char* finfo; int kind; } srcs[] = {
+                {"innerDifSourceOut", HS_DMSG_INNER}, {"outerDifSourceOut", HS_DMSG_OUTER},
+                {"concentrationOut", HS_DMSG_CONC_CHAN}, {"reactionOut", HS_DMSG_REACTION},
+                {"PumpOut", HS_DMSG_PUMP}};
+            for (const auto& s : srcs) {
+                vector<Id> t;
+                HSolveUtils::targets(x, s.finfo, t);
+                for (const Id& y : t) {
+                    auto di = difIndex.find(y);
+                    auto ci = chanIndex.find(y);
+                    if (s.kind == HS_DMSG_CONC_CHAN) {
+                        if (ci != chanIndex.end()) emit(HS_DMSG_CONC_CHAN, k, ci->second);
+                        else if (di != difIndex.end() && cls(y) == "DifBuffer") emit(HS_DMSG_CONC_BUF, k, di->second);
+                    } else if (di != difIndex.end()) {
+                        emit(s.kind, k, di->second);
+                    }
+                }
+            }
+        }
+        // the solver's IkOut sends, channel order
+        for (uint32_t q = 0; q < out.chanId.size(); ++q) {
+            vector<Id> t;
+            HSolveUtils::targets(out.chanId[q], "IkOut", t, "DifShell");
+            for (const Id& y : t) emit(HS_DMSG_IK, q, difIndex[y]);
+        }
+    }
     // ---- the description
     HsCellDesc& d = out.desc;
     d.n_compt = N;
@@ -452,6 +555,13 @@ int fillCellDesc(const HSolve& hs, HsCellDescStore& out, std::string& err) {
     d.sg_refractT = ptr(out.sg_refractT);
     d.sg_edge = ptr(out.sg_edge);
     d.n_stim = 0;
+    d.n_dif = (uint32_t)out.dif_kind.size();
+    d.dif_kind = ptr(out.dif_kind);
+    d.difpar = ptr(out.difpar);
+    d.n_dmsg = (uint32_t)out.dmsg_kind.size();
+    d.dmsg_kind = ptr(out.dmsg_kind);
+    d.dmsg_src = ptr(out.dmsg_src);
+    d.dmsg_dst = ptr(out.dmsg_dst);
     return 0;
 }
 
@@ -492,14 +602,16 @@ extern "C" __attribute__((visibility("default"))) void hsb_free_cell_desc(const 
 
 extern "C" __attribute__((visibility("default"))) const char* hsb_last_error(void) { return g_err.c_str(); }
 
-// kind: 0 compartment, 1 HHChannel, 2 pool, 3 HHChannel2D, 4 SynChan, 5 SpikeGen
+// kind: 0 compartment, 1 HHChannel, 2 pool, 3 HHChannel2D, 4 SynChan, 5 SpikeGen,
+// 6 tick-1 external calcium object
 extern "C" __attribute__((visibility("default"))) int hsb_object_path(const HsCellDesc* d, int kind,
                                                                       uint32_t index, char* buf, uint32_t cap) {
     auto it = g_stores.find(d);
     if (it == g_stores.end()) return -1;
     const moose_gb300_bridge::HsCellDescStore& st = *it->second;
-    const std::vector<Id>* v[] = {&st.comptId, &st.chanId, &st.poolId, &st.chan2dId, &st.synId, &st.spikeGenId};
-    if (kind < 0 || kind > 5 || index >= v[kind]->size() || !buf || cap == 0) return -1;
+    const std::vector<Id>* v[] = {&st.comptId, &st.chanId, &st.poolId, &st.chan2dId, &st.synId, &st.spikeGenId,
+                                  &st.difId};
+    if (kind < 0 || kind > 6 || index >= v[kind]->size() || !buf || cap == 0) return -1;
     const std::string p = (*v[kind])[index].path();
     const size_t n = std::min<size_t>(p.size(), cap - 1);
     p.copy(buf, n);

@@ -62,7 +62,15 @@ _DESC_FIELDS = [
     ("n_spikegen", C.c_uint32), ("sg_compt", _pu), ("sg_threshold", _pd),
     ("sg_refractT", _pd), ("sg_edge", _pi),
     ("n_stim", C.c_uint32), ("stim_compt", _pu), ("stim_step", _pu), ("stim_value", _pd),
+    ("n_dif", C.c_uint32), ("dif_kind", _pi), ("difpar", _pd),
+    ("n_dmsg", C.c_uint32), ("dmsg_kind", _pi), ("dmsg_src", _pu), ("dmsg_dst", _pu),
 ]
+
+# tick-1 external calcium objects (include/moose_gb300.h HS_DIF_*, HS_DMSG_*)
+HS_DIF_SHELL, HS_DIF_BUFFER, HS_DIF_PUMP = 0, 1, 2
+HS_DIF_NPAR = 12
+(HS_DMSG_OUTER, HS_DMSG_INNER, HS_DMSG_CONC_CHAN, HS_DMSG_CONC_BUF, HS_DMSG_REACTION, HS_DMSG_PUMP,
+ HS_DMSG_IK) = range(7)
 
 
 class HsCellDesc(C.Structure):
@@ -99,11 +107,14 @@ _ARRAYS = {
     "ev_syn": _U32, "ev_time": _F64, "ev_weight": _F64,
     "sg_compt": _U32, "sg_threshold": _F64, "sg_refractT": _F64, "sg_edge": _I32,
     "stim_compt": _U32, "stim_step": _U32, "stim_value": _F64,
+    "dif_kind": _I32, "difpar": _F64,
+    "dmsg_kind": _I32, "dmsg_src": _U32, "dmsg_dst": _U32,
 }
 _COUNTS = {
     "n_compt": "parent", "n_leak": "leak_compt", "n_chan": "chan_compt",
     "n_pool": "pool_compt", "n_chan2d": "c2d_compt", "n_syn": "syn_compt",
     "n_event": "ev_syn", "n_spikegen": "sg_compt", "n_stim": "stim_compt",
+    "n_dif": "dif_kind", "n_dmsg": "dmsg_kind",
 }
 
 
@@ -150,6 +161,9 @@ class CellModel:
                 if len(getattr(self, name)) != n:
                     raise ValueError("array %s has length %d, expected %d"
                                      % (name, len(getattr(self, name)), n))
+        if len(self.difpar) != HS_DIF_NPAR * len(self.dif_kind):
+            raise ValueError("difpar has length %d, expected %d" % (len(self.difpar),
+                                                                    HS_DIF_NPAR * len(self.dif_kind)))
 
     def desc(self):
         """Build an ``HsCellDesc`` pointing into this model's arrays."""

@@ -44,6 +44,18 @@ typedef struct { double c, CaBasal, factor1, factor2, ceiling, floor_; } CaConcS
 
 typedef struct { uint32_t index, rank; } Junction;
 
+/* External calcium objects on tick 1 (DifShell, DifBuffer, MMPump) and their
+   messages, CSR by (source object, message kind) in description order. */
+#define DIF_NK 6            /* object-sourced message kinds HS_DMSG_OUTER .. HS_DMSG_PUMP */
+typedef struct {
+    uint32_t n;
+    double *C, *prevC, *dC, *Cm;                   /* DifShell C_, prevC_, dCbyDt_, Cmultiplier_ */
+    double *bFree, *bBound, *prevFree, *Af, *Bf, *act;   /* DifBuffer */
+    double *vol, *outerA, *innerA;                 /* geometry (calculateVolumeArea at reinit) */
+    uint32_t *off, *dst;                           /* n*DIF_NK+1 */
+    uint32_t *ikOff, *ikDst;                       /* by model HHChannel */
+} DifObjs;
+
 struct OrcCell {
     const HsCellDesc* d;        /* NULL for passive-only cells */
     double dt;                  /* HSolve dt_ */
@@ -128,6 +140,8 @@ struct OrcCell {
     ivec spikeGen; dvec spikeTime;
     /* stimulus */
     uint32_t stimPtr;
+    /* tick-1 external calcium */
+    DifObjs dif;
 
     double clockDt;
     uint64_t nSteps;
@@ -652,6 +666,236 @@ static int cmp_i64(const void* a, const void* b) {
     return x < y ? -1 : x > y;
 }
 
+/* ------------------------------------------------------------------ */
+/* External calcium on tick 1: DifShell (biophysics/DifShell.cpp), DifBuffer
+   (biophysics/DifBuffer.cpp), MMPump (biophysics/MMPump.cpp).  Each object
+   processes in tick order and its sends reach their targets at once, so a
+   target processed later in the same tick sees this step's value. */
+static const double DIF_F = 96485.3415;        /* DifShell::F */
+static const double DIF_EPSILON = 1.0e-10;     /* DifShell::EPSILON, DifBuffer::EPSILON */
+static const double DIF_PI = 3.14159265358979323846;   /* M_PI of the reference's <cmath> */
+#define DP(k, i) (c->d->difpar[(size_t)(k) * HS_DIF_NPAR + (i)])
+
+static const char* dif_setup(OrcCell* c) {
+    const HsCellDesc* d = c->d;
+    DifObjs* o = &c->dif;
+    uint32_t n = d->n_dif;
+    o->n = n;
+    if (!n && !d->n_dmsg) return NULL;
+    if (n && (!d->dif_kind || !d->difpar)) return "tick-1 objects without kinds or parameters";
+    for (uint32_t k = 0; k < n; k++)
+        if (d->dif_kind[k] < HS_DIF_SHELL || d->dif_kind[k] > HS_DIF_PUMP) return "unknown tick-1 object kind";
+    double** arrs[] = {&o->C, &o->prevC, &o->dC, &o->Cm, &o->bFree, &o->bBound, &o->prevFree, &o->Af, &o->Bf,
+                       &o->act, &o->vol, &o->outerA, &o->innerA};
+    for (size_t a = 0; a < sizeof(arrs) / sizeof(arrs[0]); a++) *arrs[a] = (double*)xcalloc(n, sizeof(double));
+    for (uint32_t k = 0; k < n; k++) if (d->dif_kind[k] == HS_DIF_BUFFER) o->act[k] = DP(k, 11);
+    o->off = (uint32_t*)xcalloc((size_t)n * DIF_NK + 1, sizeof(uint32_t));
+    o->ikOff = (uint32_t*)xcalloc((size_t)d->n_chan + 1, sizeof(uint32_t));
+    for (uint32_t m = 0; m < d->n_dmsg; m++) {
+        int kind = d->dmsg_kind[m];
+        uint32_t s = d->dmsg_src[m], t = d->dmsg_dst[m];
+        if (kind == HS_DMSG_IK) {
+            if (s >= d->n_chan || c->chanSolverOf[s] < 0) return "IkOut from a channel the solver does not hold";
+            if (t >= n || d->dif_kind[t] != HS_DIF_SHELL) return "IkOut to an object that is not a DifShell";
+            o->ikOff[s + 1]++;
+            continue;
+        }
+        if (kind < HS_DMSG_OUTER || kind > HS_DMSG_PUMP || s >= n) return "bad tick-1 message";
+        int sk = d->dif_kind[s];
+        int ok;
+        switch (kind) {
+        case HS_DMSG_OUTER: case HS_DMSG_INNER:
+            ok = sk != HS_DIF_PUMP && t < n && d->dif_kind[t] != HS_DIF_PUMP; break;
+        case HS_DMSG_CONC_CHAN:
+            ok = sk == HS_DIF_SHELL && t < d->n_chan && c->chanSolverOf[t] >= 0; break;
+        case HS_DMSG_CONC_BUF:
+            ok = sk == HS_DIF_SHELL && t < n && d->dif_kind[t] == HS_DIF_BUFFER; break;
+        case HS_DMSG_REACTION:
+            ok = sk == HS_DIF_BUFFER && t < n && d->dif_kind[t] == HS_DIF_SHELL; break;
+        default:  /* HS_DMSG_PUMP */
+            ok = sk == HS_DIF_PUMP && t < n && d->dif_kind[t] == HS_DIF_SHELL; break;
+        }
+        if (!ok) return "tick-1 message between objects of the wrong kinds";
+        o->off[(size_t)s * DIF_NK + kind + 1]++;
+    }
+    for (size_t i = 0; i < (size_t)n * DIF_NK; i++) o->off[i + 1] += o->off[i];
+    for (uint32_t k = 0; k < d->n_chan; k++) o->ikOff[k + 1] += o->ikOff[k];
+    o->dst = (uint32_t*)xcalloc(o->off[(size_t)n * DIF_NK] + 1, sizeof(uint32_t));
+    o->ikDst = (uint32_t*)xcalloc(o->ikOff[d->n_chan] + 1, sizeof(uint32_t));
+    uint32_t* fill = (uint32_t*)xcalloc((size_t)n * DIF_NK + d->n_chan + 1, sizeof(uint32_t));
+    for (uint32_t m = 0; m < d->n_dmsg; m++) {
+        uint32_t s = d->dmsg_src[m];
+        if (d->dmsg_kind[m] == HS_DMSG_IK) {
+            o->ikDst[o->ikOff[s] + fill[(size_t)n * DIF_NK + s]++] = d->dmsg_dst[m];
+        } else {
+            size_t slot = (size_t)s * DIF_NK + d->dmsg_kind[m];
+            o->dst[o->off[slot] + fill[slot]++] = d->dmsg_dst[m];
+        }
+    }
+    free(fill);
+    return NULL;
+}
+
+/* DifShell::calculateVolumeArea and the same in DifBuffer::vReinit */
+static void dif_geometry(OrcCell* c, uint32_t k) {
+    DifObjs* o = &c->dif;
+    int shape = (int)DP(k, 4);
+    double length = DP(k, 5), diameter = DP(k, 6), thickness = DP(k, 7);
+    double rOut = diameter / 2.;
+    double rIn = rOut - thickness;
+    if (rIn < 0) rIn = 0.;
+    if (shape == 0) {
+        if (length == 0.0) {
+            o->vol[k] = 4. / 3. * DIF_PI * (rOut * rOut * rOut - rIn * rIn * rIn);
+            o->outerA[k] = 4 * DIF_PI * rOut * rOut;
+            o->innerA[k] = 4 * DIF_PI * rIn * rIn;
+        } else {
+            o->vol[k] = (DIF_PI * length) * (rOut * rOut - rIn * rIn);
+            o->outerA[k] = 2 * DIF_PI * rOut * length;
+            o->innerA[k] = 2 * DIF_PI * rIn * length;
+        }
+    } else if (shape == 1) {
+        o->vol[k] = DIF_PI * diameter * diameter * thickness / 4.0;
+        o->outerA[k] = DIF_PI * diameter * diameter / 4.0;
+        o->innerA[k] = o->outerA[k];
+    } else {    /* 3: user defined */
+        o->vol[k] = DP(k, 8);
+        o->outerA[k] = DP(k, 9);
+        o->innerA[k] = DP(k, 10);
+    }
+}
+
+/* DifShell::integrate, DifBuffer::integrate */
+static double dif_integrate(double state, double dt, double A, double B) {
+    if (B > DIF_EPSILON) {
+        double x = exp(-B * dt);
+        return state * x + (A / B) * (1 - x);
+    }
+    return state + A * dt;
+}
+
+/* inner/outerDifSourceOut of object s: fluxFromIn/Out of each target */
+static void dif_send_flux(OrcCell* c, uint32_t s, int kind, double value, double thickness) {
+    DifObjs* o = &c->dif;
+    size_t slot = (size_t)s * DIF_NK + kind;
+    for (uint32_t i = o->off[slot]; i < o->off[slot + 1]; i++) {
+        uint32_t t = o->dst[i];
+        double D = c->d->dif_kind[t] == HS_DIF_SHELL ? DP(t, 1) : DP(t, 3);
+        double area = kind == HS_DMSG_OUTER ? o->outerA[t] : o->innerA[t];
+        double tt = DP(t, 7);
+        if (c->d->dif_kind[t] == HS_DIF_SHELL) {
+            /* vFluxFromOut / vFluxFromIn */
+            double diff = 2. * D / o->vol[t] * area / (thickness + tt);
+            o->dC[t] += diff * value;
+            o->Cm[t] += diff;
+        } else {
+            double dif = 2 * D / o->vol[t] * area / (tt + thickness);
+            o->Af[t] += dif * value;
+            o->Bf[t] += dif;
+        }
+    }
+}
+
+/* concentrationOut of shell s: HHChannel concen (HSolve::addConc) and
+   DifBuffer concentration (vBuffer: activation) */
+static void dif_send_conc(OrcCell* c, uint32_t s, double C) {
+    DifObjs* o = &c->dif;
+    size_t slot = (size_t)s * DIF_NK + HS_DMSG_CONC_CHAN;
+    for (uint32_t i = o->off[slot]; i < o->off[slot + 1]; i++)
+        c->externalCalcium[c->chanSolverOf[o->dst[i]]] = C;
+    slot = (size_t)s * DIF_NK + HS_DMSG_CONC_BUF;
+    for (uint32_t i = o->off[slot]; i < o->off[slot + 1]; i++) o->act[o->dst[i]] = C;
+}
+
+/* every object's reinit, tick order (DifShell::vReinit, DifBuffer::vReinit;
+   MMPump::reinit does nothing) */
+static void dif_reinit(OrcCell* c) {
+    DifObjs* o = &c->dif;
+    for (uint32_t k = 0; k < o->n; k++) {
+        int kind = c->d->dif_kind[k];
+        if (kind == HS_DIF_SHELL) {
+            o->dC[k] = DP(k, 3);
+            o->Cm[k] = 0;
+            dif_geometry(c, k);
+            o->C[k] = DP(k, 0);
+            o->prevC[k] = DP(k, 0);
+            dif_send_conc(c, k, o->C[k]);
+            dif_send_flux(c, k, HS_DMSG_INNER, o->prevC[k], DP(k, 7));
+            dif_send_flux(c, k, HS_DMSG_OUTER, o->prevC[k], DP(k, 7));
+        } else if (kind == HS_DIF_BUFFER) {
+            o->Af[k] = 0;
+            o->Bf[k] = 0;
+            dif_geometry(c, k);
+            double bTot = DP(k, 0), kf = DP(k, 1), kb = DP(k, 2);
+            o->bFree[k] = bTot / (1 + o->act[k] * kf / kb);
+            o->prevFree[k] = o->bFree[k];
+            o->bBound[k] = bTot - o->bFree[k];
+            dif_send_flux(c, k, HS_DMSG_INNER, o->prevFree[k], DP(k, 7));
+            dif_send_flux(c, k, HS_DMSG_OUTER, o->prevFree[k], DP(k, 7));
+        }
+    }
+}
+
+/* every object's process, tick order (DifShell::vProcess,
+   DifBuffer::vProcess, MMPump::process) */
+static void dif_process(OrcCell* c, double dt) {
+    DifObjs* o = &c->dif;
+    for (uint32_t k = 0; k < o->n; k++) {
+        int kind = c->d->dif_kind[k];
+        if (kind == HS_DIF_SHELL) {
+            o->C[k] = dif_integrate(o->C[k], dt, o->dC[k], o->Cm[k]);
+            o->dC[k] = DP(k, 3);
+            o->Cm[k] = 0;
+            o->prevC[k] = o->C[k];
+            dif_send_flux(c, k, HS_DMSG_INNER, o->prevC[k], DP(k, 7));
+            dif_send_flux(c, k, HS_DMSG_OUTER, o->prevC[k], DP(k, 7));
+            dif_send_conc(c, k, o->C[k]);
+        } else if (kind == HS_DIF_BUFFER) {
+            double bTot = DP(k, 0), kf = DP(k, 1), kb = DP(k, 2);
+            o->Af[k] += kb * o->bBound[k];
+            o->Bf[k] += kf * o->act[k];
+            o->bFree[k] = dif_integrate(o->bFree[k], dt, o->Af[k], o->Bf[k]);
+            o->bBound[k] = bTot - o->bFree[k];
+            o->prevFree[k] = o->bFree[k];
+            dif_send_flux(c, k, HS_DMSG_INNER, o->prevFree[k], DP(k, 7));
+            dif_send_flux(c, k, HS_DMSG_OUTER, o->prevFree[k], DP(k, 7));
+            /* reactionOut -> DifShell::vBuffer */
+            size_t slot = (size_t)k * DIF_NK + HS_DMSG_REACTION;
+            for (uint32_t i = o->off[slot]; i < o->off[slot + 1]; i++) {
+                uint32_t t = o->dst[i];
+                o->dC[t] += kb * o->bBound[k];
+                o->Cm[t] += kf * o->bFree[k];
+            }
+            o->Af[k] = 0;
+            o->Bf[k] = 0;
+        } else {
+            /* PumpOut -> DifShell::vMMPump */
+            double vMax = DP(k, 0), Kd = DP(k, 1);
+            size_t slot = (size_t)k * DIF_NK + HS_DMSG_PUMP;
+            for (uint32_t i = o->off[slot]; i < o->off[slot + 1]; i++) {
+                uint32_t t = o->dst[i];
+                o->Cm[t] += (vMax / o->vol[t]) / (o->C[t] + Kd);
+            }
+        }
+    }
+}
+
+/* HSolveActive::sendValues, IkOut (hsolve/HSolveActive.cpp:367-376):
+   (Ek - Vm) Gk of each channel, channel order, to DifShell::vInflux */
+static void dif_send_ik(OrcCell* c) {
+    DifObjs* o = &c->dif;
+    if (!o->ikOff) return;
+    for (uint32_t q = 0; q < c->nChan; q++) {
+        uint32_t k = c->chanModel[q];
+        if (o->ikOff[k] == o->ikOff[k + 1]) continue;
+        double I = (c->Ek[q] - c->V[c->chan2compt[q]]) * c->Gk[q];
+        for (uint32_t i = o->ikOff[k]; i < o->ikOff[k + 1]; i++) {
+            uint32_t t = o->ikDst[i];
+            o->dC[t] += I / (DIF_F * DP(t, 2) * o->vol[t]);
+        }
+    }
+}
+
 OrcCell* orc_create(const HsCellDesc* d, uint32_t seed, double dt, char* err, uint32_t errlen) {
 #define FAIL(msg) do { if (err && errlen) snprintf(err, errlen, "%s", msg); orc_destroy(c); return NULL; } while (0)
     OrcCell* c = (OrcCell*)xcalloc(1, sizeof(OrcCell));
@@ -950,6 +1194,10 @@ OrcCell* orc_create(const HsCellDesc* d, uint32_t seed, double dt, char* err, ui
         if (d->stim_compt[k] >= d->n_compt || c->hinesOf[d->stim_compt[k]] == UINT32_MAX) FAIL("stimulus compartment not in the tree");
         if (k && d->stim_step[k] < d->stim_step[k - 1]) FAIL("stimulus schedule not sorted by step");
     }
+    {
+        const char* e = dif_setup(c);
+        if (e) FAIL(e);
+    }
     return c;
 #undef FAIL
 }
@@ -1041,6 +1289,9 @@ void orc_reinit(OrcCell* c, double clock_dt) {
     for (uint32_t ic = 0; ic < n; ++ic) c->V[ic] = c->initVm[ic];
     for (uint32_t p = 0; p < c->nPool; p++) c->caActivation[p] = 0.0;
     for (uint32_t p = 0; p < c->nPool; p++) { c->caConc[p].c = 0.0; c->ca[p] = c->caConc[p].CaBasal; }
+    /* tick 1 reinits before the solver's tick 6: the shells' concentrations
+       reach the channels' external calcium the gates start from */
+    dif_reinit(c);
     /* reinitChannels */
     uint32_t ichan = 0, ica = 0, icol = 0, izr = 0;
     size_t istate = 0;
@@ -1220,6 +1471,8 @@ void orc_step(OrcCell* c, uint32_t nsteps) {
             }
             if (activation != 0.0) c->synAct[k] += activation;
         }
+        /* tick 1: DifShells, DifBuffers, MMPumps */
+        dif_process(c, dt);
         /* tick 4: each object -> addGkEk.  The reference's clock sends the
            HHChannel2Ds in creation order and then the SynChans in reverse
            creation order (scheduling/Clock.cpp:764-774 over the proc4 message
@@ -1262,6 +1515,7 @@ void orc_step(OrcCell* c, uint32_t nsteps) {
             orc_forward(c);
             orc_backward(c);
             advanceCalcium(c);
+            dif_send_ik(c);
             /* sendValues -> tick-4 consumers of the next step */
             for (uint32_t k = 0; k < d->n_chan2d; k++) {
                 c->c2dVm[k] = c->V[c->hinesOf[d->c2d_compt[k]]];
@@ -1503,8 +1757,22 @@ int orc_push_event(OrcCell* c, uint32_t syn, double time, double weight) {
     return 0;
 }
 
+void orc_read_dif(const OrcCell* c, double* out) {
+    for (uint32_t k = 0; k < c->dif.n; k++) {
+        int kind = c->d->dif_kind[k];
+        out[k] = kind == HS_DIF_SHELL ? c->dif.C[k] : kind == HS_DIF_BUFFER ? c->dif.bFree[k] : 0.0;
+    }
+}
+
 void orc_destroy(OrcCell* c) {
     if (!c) return;
+    {
+        DifObjs* o = &c->dif;
+        double* arrs[] = {o->C, o->prevC, o->dC, o->Cm, o->bFree, o->bBound, o->prevFree, o->Af, o->Bf,
+                          o->act, o->vol, o->outerA, o->innerA};
+        for (size_t a = 0; a < sizeof(arrs) / sizeof(arrs[0]); a++) free(arrs[a]);
+        free(o->off); free(o->dst); free(o->ikOff); free(o->ikDst);
+    }
     free(c->compartmentId); free(c->hinesOf); free(c->V); free(c->CmByDt); free(c->EmByRm);
     free(c->injPresent); free(c->injectVarying); free(c->injectBasal);
     free(c->childOff); free(c->childIdx); free(c->Ra); free(c->Rm); free(c->Cm); free(c->Em); free(c->initVm);

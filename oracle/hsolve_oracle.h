@@ -50,6 +50,9 @@ void orc_set_ca_advance(OrcCell* c, int ca_advance);
    computed in FP32 and accumulated in FP64 (the gating precision of a
    mixed-precision solver) instead of the reference's FP64 step. */
 void orc_set_f32_gate_increments(OrcCell* c, int on);
+/* Tick-1 external calcium objects: C of each DifShell, bFree of each
+   DifBuffer, 0 for an MMPump (n_dif values). */
+void orc_read_dif(const OrcCell* c, double* out);
 /* HSolve::reinit with the clock dt (also reinit of tick-1/4 objects). */
 void orc_reinit(OrcCell* c, double clock_dt);
 /* nsteps clock steps: ticks 0 (stimulus), 1, 4, 6 (HSolve), spikes. */

@@ -46,6 +46,7 @@ def lib():
         L.orc_destroy.argtypes = [vp]
         L.orc_set_ca_advance.argtypes = [vp, C.c_int]
         L.orc_set_f32_gate_increments.argtypes = [vp, C.c_int]
+        L.orc_read_dif.argtypes = [vp, pd]
         L.orc_reinit.argtypes = [vp, C.c_double]
         L.orc_step.argtypes = [vp, C.c_uint32]
         for f in ("orc_n_compt", "orc_n_pool", "orc_n_state"):
@@ -128,6 +129,13 @@ class OracleCell:
     def ca(self):
         out = np.empty(len(self.model.pool_compt))
         lib().orc_read_ca(self.h, _pd(out))
+        return out
+
+    def dif(self):
+        """C of each DifShell, bFree of each DifBuffer (0 for an MMPump)."""
+        out = np.empty(len(self.model.dif_kind))
+        if len(out):
+            lib().orc_read_dif(self.h, _pd(out))
         return out
 
     def state(self):

@@ -8,7 +8,8 @@ def load_model(z, prefix="model_"):
     sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(
         os.path.abspath(__file__)))), "moose-core_gb300"))
     from moose_gb300.abi import CellModel, _ARRAYS
-    kw = {k: z[prefix + k] for k in _ARRAYS}
+    # fixtures written before an array existed describe cells without it
+    kw = {k: z[prefix + k] for k in _ARRAYS if prefix + k in z.files}
     gates = []
     for i in range(int(z[prefix + "ngates"])):
         AB = z[prefix + "gate%d" % i]
@@ -67,3 +68,39 @@ def replay_events(z, solver, advance):
         advance(solver, stride)
         vm.append(solver.vm()[rec])
     return np.array(vm).T
+
+
+def model_from_desc(d, seed):
+    """A CellModel holding a copy of every array of the HsCellDesc `d` (a
+    ctypes structure, e.g. one the MOOSE-side binding filled), seeded at
+    `seed`."""
+    import ctypes as C
+    import sys, os
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(
+        os.path.abspath(__file__)))), "moose-core_gb300"))
+    from moose_gb300.abi import CellModel, HS_DIF_NPAR, _ARRAYS, _COUNTS
+    count_of = {first: getattr(d, cnt) for cnt, first in _COUNTS.items()}
+    kw = {}
+    for name, dt in _ARRAYS.items():
+        if name == "difpar":
+            n = HS_DIF_NPAR * d.n_dif
+        else:
+            prefix = name.split("_")[0] + "_"
+            first = next((f for f in _COUNTS.values() if f.startswith(prefix)), "parent")
+            n = count_of[first] if name not in ("Ra", "Rm", "Cm", "Em", "initVm", "Vm", "inject") else d.n_compt
+        p = getattr(d, name)
+        kw[name] = np.ctypeslib.as_array(p, shape=(n,)).astype(dt).copy() if n and p else np.zeros(0, dt)
+    gates = []
+    for i in range(d.n_gate):
+        g = d.gate[i]
+        A = np.ctypeslib.as_array(g.A, shape=(g.divs + 1,)).copy()
+        B = np.ctypeslib.as_array(g.B, shape=(g.divs + 1,)).copy()
+        gates.append((g.min, g.max, A, B))
+    gates2d = []
+    for i in range(d.n_gate2d):
+        g = d.gate2d[i]
+        shape = (g.xdivs + 1, g.ydivs + 1)
+        A = np.ctypeslib.as_array(g.A, shape=(shape[0] * shape[1],)).reshape(shape).copy()
+        B = np.ctypeslib.as_array(g.B, shape=(shape[0] * shape[1],)).reshape(shape).copy()
+        gates2d.append((g.xmin, g.xmax, g.ymin, g.ymax, A, B))
+    return CellModel(seed=int(seed), gates=gates, gates2d=gates2d, **kw)

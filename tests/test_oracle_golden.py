@@ -225,3 +225,60 @@ def test_rdesigneur_minimal_model_fields():
     got = np.array([oc.get(HS_KIND_COMPT, FIELDS[str(k)], 0) for k in z["kat_fields"]])
     assert np.array_equal(got, z["ref_values"])
     assert np.allclose(got, z["kat_values"], rtol=1e-12, atol=0.0)
+
+
+def check_ext_calcium_kat(z, sk, ca):
+    """tests/core/test_hsolve_externalCalcium.py's own assertions: min, max,
+    mean and std of the SK conductance and of the outer shell's Ca (np.allclose
+    defaults), and the counts of samples below/above its thresholds."""
+    stat = lambda v: [np.min(v), np.max(v), np.mean(v), np.std(v)]
+    assert np.allclose(stat(sk), z["kat_sk"])
+    assert np.allclose(stat(ca), z["kat_ca"])
+    assert len(np.where(sk < 1e-19)[0]) == 2001
+    assert len(np.where(ca > 50e-6)[0]) == 2000
+
+
+def run_ext_calcium(solver, z, read_shell, read_sk):
+    stride, n = int(z["stride"]), int(z["nsteps"])
+    vm, ca, sk = [solver.vm()[0]], [read_shell()], [read_sk()]
+    for _ in range(n // stride):
+        solver.step(stride) if hasattr(solver, "step") else solver.process(stride)
+        vm.append(solver.vm()[0])
+        ca.append(read_shell())
+        sk.append(read_sk())
+    return np.array(vm), np.array(ca), np.array(sk)
+
+
+def test_external_calcium_difshells_bit_exact():
+    """tests/core/test_hsolve_externalCalcium.py: a soma whose CaL12 current
+    (the solver's IkOut) flows into the outer of three DifShells and whose SK
+    gate reads that shell (concentrationOut -> HSolve::addConc), 10 s at
+    10 us (ext_calcium.npz, made by the reference itself, its model described
+    by the MOOSE-side binding): Vm, the shell's Ca and SK's Gk every 5 ms
+    equal the reference's bit for bit, and the test's own checks pass."""
+    from moose_gb300.abi import FIELDS, HS_KIND_CHAN
+    z = np.load(os.path.join(GOLDEN, "ext_calcium.npz"))
+    m = load_model(z)
+    dt = float(z["dt"])
+    oc = OracleCell(m, dt)
+    oc.reinit(dt)
+    si, ki = int(z["shell_index"]), int(z["sk_index"])
+    vm, ca, sk = run_ext_calcium(oc, z, lambda: oc.dif()[si], lambda: oc.get(HS_KIND_CHAN, FIELDS["Gk"], ki))
+    assert np.array_equal(vm, z["vm"])
+    assert np.array_equal(ca, z["shell_c"])
+    assert np.array_equal(sk, z["sk_gk"])
+    check_ext_calcium_kat(z, sk, ca)
+
+
+def test_external_calcium_drives_the_cell():
+    """The shells matter: with the IkOut influx removed the shell stays at
+    its equilibrium and the trace differs (the match above is not vacuous)."""
+    z = np.load(os.path.join(GOLDEN, "ext_calcium.npz"))
+    m = load_model(z)
+    keep = m.dmsg_kind != 6          # HS_DMSG_IK
+    m.dmsg_kind, m.dmsg_src, m.dmsg_dst = m.dmsg_kind[keep], m.dmsg_src[keep], m.dmsg_dst[keep]
+    dt = float(z["dt"])
+    oc = OracleCell(m, dt)
+    oc.reinit(dt)
+    oc.step(200000)
+    assert oc.dif()[int(z["shell_index"])] == 5e-5
