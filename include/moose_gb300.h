@@ -331,6 +331,10 @@ int hs_push_events(HsSolver* s, const uint32_t* syn, const double* time,
 int hs_read_vm(HsSolver* s, double* out, uint32_t n);
 int hs_read_ca(HsSolver* s, double* out, uint32_t n);
 
+/* Tick-1 external calcium objects in description order: C of each
+ * DifShell, bFree of each DifBuffer, 0 for an MMPump (n = n_dif). */
+int hs_read_dif(HsSolver* s, double* out, uint32_t n);
+
 /* Trace recording: every `stride` steps, Vm of the listed compartments is
  * appended to a device buffer (a Table on tick 8 reading `HSolve::getVm`). */
 int hs_record(HsSolver* s, const uint32_t* compts, uint32_t n, uint32_t stride,

@@ -752,6 +752,22 @@ int hs_read_ca(HsSolver* s, double* out, uint32_t n) {
     return HS_OK;
 }
 
+int hs_read_dif(HsSolver* s, double* out, uint32_t n) {
+    if (!s || (!out && n)) return setErr(HS_EINVAL, "null argument");
+    if (n != s->P.nDif) return setErr(HS_EINVAL, "n must equal the model's tick-1 object count");
+    if (!n) return HS_OK;
+    if (int rc = flushWrites(s)) return rc;
+    std::vector<double> st((size_t)kDifState * n);
+    cudaError_t e = cudaMemcpyAsync(st.data(), s->dc.difState, st.size() * 8, cudaMemcpyDeviceToHost, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) return cudaErr(e, "read tick-1 objects");
+    for (uint32_t k = 0; k < n; ++k) {
+        const int kind = s->P.difKind[k];
+        out[k] = kind == HS_DIF_SHELL ? st[k] : kind == HS_DIF_BUFFER ? st[4 * (size_t)n + k] : 0.0;
+    }
+    return HS_OK;
+}
+
 int hs_record(HsSolver* s, const uint32_t* compts, uint32_t n, uint32_t stride, uint32_t capacity) {
     if (!s) return setErr(HS_EINVAL, "null solver");
     if (n && (!compts || stride == 0 || capacity == 0)) return setErr(HS_EINVAL, "bad recording request");

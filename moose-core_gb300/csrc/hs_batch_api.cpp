@@ -587,6 +587,10 @@ int unionTables(HsBatch* b, bool ca, UnionTable& U) {
 
 int buildMixed(HsBatch* b) {
     const uint32_t nC = b->nCells;
+    for (const CellPlan& P : b->plans)
+        if (P.nDif)
+            return berr(HS_ENOTSUP, "mixed batch: tick-1 external calcium objects (DifShell, DifBuffer, MMPump) "
+                                    "are stepped by the FP64 solvers only");
     MixHost& H = b->mh;
     H = MixHost();
     // one V table and one Ca table for the batch: the union of the cells'

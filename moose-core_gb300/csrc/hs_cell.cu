@@ -176,6 +176,20 @@ cudaError_t layoutCell(const CellPlan& P, Arena& a, DevCell& c, uint32_t spikeCa
     c.stimCompt = u.put(P.stimCompt);
     c.stimValue = u.put(P.stimValue);
     c.injPresent = u.put(P.injPresent);
+    c.nDif = P.nDif;
+    if (P.nDif) {
+        c.difKind = u.put(P.difKind);
+        c.difPar = u.put(P.difPar);
+        c.difOff = u.put(P.difOff);
+        c.difDst = u.put(P.difDst);
+        c.ikOff = u.put(P.ikOff);
+        c.ikDst = u.put(P.ikDst);
+        // state; a DifBuffer starts from its activation field
+        std::vector<double> st((size_t)kDifState * P.nDif, 0.0);
+        for (uint32_t k = 0; k < P.nDif; ++k)
+            if (P.difKind[k] == HS_DIF_BUFFER) st[9 * (size_t)P.nDif + k] = P.difPar[(size_t)k * HS_DIF_NPAR + 11];
+        c.difState = u.put(st);
+    }
     c.nRec = 0;
     c.recStride = 1;
     c.recCap = 0;

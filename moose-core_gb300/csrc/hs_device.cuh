@@ -18,6 +18,8 @@
 
 namespace hsg {
 
+constexpr uint32_t kDifState = 13;
+
 struct DevCtl {
     unsigned long long nSteps;   // steps since reinit
     uint32_t stimPtr;
@@ -84,6 +86,14 @@ struct DevCell {
     const uint32_t *stimStep, *stimCompt;
     const double* stimValue;
     uint8_t* injPresent;
+    // tick-1 external calcium: objects, messages, state (kDifState x nDif:
+    // C, prevC, dCbyDt, Cmultiplier, bFree, bBound, prevFree, Af, Bf,
+    // activation, volume, outerArea, innerArea)
+    uint32_t nDif;
+    const int32_t* difKind;
+    const double* difPar;
+    const uint32_t *difOff, *difDst, *ikOff, *ikDst;
+    double* difState;
     // trace recording
     uint32_t nRec, recStride, recCap, recLd;
     const uint32_t* recCompt;

@@ -16,9 +16,180 @@
 // non-integer gate powers).
 #include <cuda_runtime.h>
 
+#include "../../include/moose_gb300.h"
 #include "hs_device.cuh"
+#include "hs_plan.h"
 
 namespace hsg {
+
+// ---- tick 1: external calcium (DifShell, DifBuffer, MMPump) ----------------
+// biophysics/DifShell.cpp, biophysics/DifBuffer.cpp, biophysics/MMPump.cpp.
+// The objects process in tick order and each send reaches its targets at
+// once (a target later in the same tick sees this step's value), so one
+// thread walks them in order.  State: kDifState arrays of nDif (see DevCell).
+namespace dif {
+constexpr double kF = 96485.3415;                 // DifShell::F
+constexpr double kEpsilon = 1.0e-10;              // DifShell/DifBuffer::EPSILON
+constexpr double kPi = 3.14159265358979323846;    // M_PI
+enum { C_ = 0, PREVC, DC, CM, BFREE, BBOUND, PREVFREE, AF, BF, ACT, VOL, OUTERA, INNERA };
+}  // namespace dif
+
+__device__ __forceinline__ double& difS(const DevCell& c, int field, uint32_t k) {
+    return c.difState[(size_t)field * c.nDif + k];
+}
+__device__ __forceinline__ double difP(const DevCell& c, uint32_t k, int i) {
+    return c.difPar[(size_t)k * HS_DIF_NPAR + i];
+}
+
+// DifShell::calculateVolumeArea, DifBuffer::vReinit's geometry
+__device__ void difGeometry(const DevCell& c, uint32_t k) {
+    using namespace dif;
+    const int shape = (int)difP(c, k, 4);
+    const double length = difP(c, k, 5), diameter = difP(c, k, 6), thickness = difP(c, k, 7);
+    const double rOut = diameter / 2.;
+    double rIn = rOut - thickness;
+    if (rIn < 0) rIn = 0.;
+    if (shape == 0) {
+        if (length == 0.0) {
+            difS(c, VOL, k) = 4. / 3. * kPi * (rOut * rOut * rOut - rIn * rIn * rIn);
+            difS(c, OUTERA, k) = 4 * kPi * rOut * rOut;
+            difS(c, INNERA, k) = 4 * kPi * rIn * rIn;
+        } else {
+            difS(c, VOL, k) = (kPi * length) * (rOut * rOut - rIn * rIn);
+            difS(c, OUTERA, k) = 2 * kPi * rOut * length;
+            difS(c, INNERA, k) = 2 * kPi * rIn * length;
+        }
+    } else if (shape == 1) {
+        difS(c, VOL, k) = kPi * diameter * diameter * thickness / 4.0;
+        difS(c, OUTERA, k) = kPi * diameter * diameter / 4.0;
+        difS(c, INNERA, k) = difS(c, OUTERA, k);
+    } else {
+        difS(c, VOL, k) = difP(c, k, 8);
+        difS(c, OUTERA, k) = difP(c, k, 9);
+        difS(c, INNERA, k) = difP(c, k, 10);
+    }
+}
+
+__device__ __forceinline__ double difIntegrate(double state, double dt, double A, double B) {
+    if (B > dif::kEpsilon) {
+        const double x = exp(-B * dt);
+        return state * x + (A / B) * (1 - x);
+    }
+    return state + A * dt;
+}
+
+// inner/outerDifSourceOut of object s: fluxFromIn/Out of each target
+__device__ void difSendFlux(const DevCell& c, uint32_t s, int kind, double value, double thickness) {
+    using namespace dif;
+    const uint32_t slot = s * kDifMsgKinds + kind;
+    for (uint32_t i = c.difOff[slot]; i < c.difOff[slot + 1]; ++i) {
+        const uint32_t t = c.difDst[i];
+        const bool shell = c.difKind[t] == HS_DIF_SHELL;
+        const double D = shell ? difP(c, t, 1) : difP(c, t, 3);
+        const double area = kind == HS_DMSG_OUTER ? difS(c, OUTERA, t) : difS(c, INNERA, t);
+        const double tt = difP(c, t, 7);
+        if (shell) {
+            const double diff = 2. * D / difS(c, VOL, t) * area / (thickness + tt);
+            difS(c, DC, t) += diff * value;
+            difS(c, CM, t) += diff;
+        } else {
+            const double d = 2 * D / difS(c, VOL, t) * area / (tt + thickness);
+            difS(c, AF, t) += d * value;
+            difS(c, BF, t) += d;
+        }
+    }
+}
+
+// concentrationOut of shell s: HHChannel concen (HSolve::addConc) and DifBuffer
+// concentration (its activation)
+__device__ void difSendConc(const DevCell& c, uint32_t s, double C) {
+    uint32_t slot = s * kDifMsgKinds + HS_DMSG_CONC_CHAN;
+    for (uint32_t i = c.difOff[slot]; i < c.difOff[slot + 1]; ++i) c.extCa[c.difDst[i]] = C;
+    slot = s * kDifMsgKinds + HS_DMSG_CONC_BUF;
+    for (uint32_t i = c.difOff[slot]; i < c.difOff[slot + 1]; ++i) difS(c, dif::ACT, c.difDst[i]) = C;
+}
+
+// DifShell::vReinit, DifBuffer::vReinit (MMPump::reinit does nothing)
+__device__ void difReinit(const DevCell& c) {
+    using namespace dif;
+    for (uint32_t k = 0; k < c.nDif; ++k) {
+        const int kind = c.difKind[k];
+        if (kind == HS_DIF_SHELL) {
+            difS(c, DC, k) = difP(c, k, 3);
+            difS(c, CM, k) = 0;
+            difGeometry(c, k);
+            difS(c, C_, k) = difP(c, k, 0);
+            difS(c, PREVC, k) = difP(c, k, 0);
+            difSendConc(c, k, difS(c, C_, k));
+            difSendFlux(c, k, HS_DMSG_INNER, difS(c, PREVC, k), difP(c, k, 7));
+            difSendFlux(c, k, HS_DMSG_OUTER, difS(c, PREVC, k), difP(c, k, 7));
+        } else if (kind == HS_DIF_BUFFER) {
+            difS(c, AF, k) = 0;
+            difS(c, BF, k) = 0;
+            difGeometry(c, k);
+            const double bTot = difP(c, k, 0), kf = difP(c, k, 1), kb = difP(c, k, 2);
+            difS(c, BFREE, k) = bTot / (1 + difS(c, ACT, k) * kf / kb);
+            difS(c, PREVFREE, k) = difS(c, BFREE, k);
+            difS(c, BBOUND, k) = bTot - difS(c, BFREE, k);
+            difSendFlux(c, k, HS_DMSG_INNER, difS(c, PREVFREE, k), difP(c, k, 7));
+            difSendFlux(c, k, HS_DMSG_OUTER, difS(c, PREVFREE, k), difP(c, k, 7));
+        }
+    }
+}
+
+// DifShell::vProcess, DifBuffer::vProcess, MMPump::process
+__device__ void difProcess(const DevCell& c) {
+    using namespace dif;
+    for (uint32_t k = 0; k < c.nDif; ++k) {
+        const int kind = c.difKind[k];
+        if (kind == HS_DIF_SHELL) {
+            difS(c, C_, k) = difIntegrate(difS(c, C_, k), c.dt, difS(c, DC, k), difS(c, CM, k));
+            difS(c, DC, k) = difP(c, k, 3);
+            difS(c, CM, k) = 0;
+            difS(c, PREVC, k) = difS(c, C_, k);
+            difSendFlux(c, k, HS_DMSG_INNER, difS(c, PREVC, k), difP(c, k, 7));
+            difSendFlux(c, k, HS_DMSG_OUTER, difS(c, PREVC, k), difP(c, k, 7));
+            difSendConc(c, k, difS(c, C_, k));
+        } else if (kind == HS_DIF_BUFFER) {
+            const double bTot = difP(c, k, 0), kf = difP(c, k, 1), kb = difP(c, k, 2);
+            difS(c, AF, k) += kb * difS(c, BBOUND, k);
+            difS(c, BF, k) += kf * difS(c, ACT, k);
+            difS(c, BFREE, k) = difIntegrate(difS(c, BFREE, k), c.dt, difS(c, AF, k), difS(c, BF, k));
+            difS(c, BBOUND, k) = bTot - difS(c, BFREE, k);
+            difS(c, PREVFREE, k) = difS(c, BFREE, k);
+            difSendFlux(c, k, HS_DMSG_INNER, difS(c, PREVFREE, k), difP(c, k, 7));
+            difSendFlux(c, k, HS_DMSG_OUTER, difS(c, PREVFREE, k), difP(c, k, 7));
+            const uint32_t slot = k * kDifMsgKinds + HS_DMSG_REACTION;     // reactionOut -> DifShell::vBuffer
+            for (uint32_t i = c.difOff[slot]; i < c.difOff[slot + 1]; ++i) {
+                const uint32_t t = c.difDst[i];
+                difS(c, DC, t) += kb * difS(c, BBOUND, k);
+                difS(c, CM, t) += kf * difS(c, BFREE, k);
+            }
+            difS(c, AF, k) = 0;
+            difS(c, BF, k) = 0;
+        } else {
+            const double vMax = difP(c, k, 0), Kd = difP(c, k, 1);
+            const uint32_t slot = k * kDifMsgKinds + HS_DMSG_PUMP;          // PumpOut -> DifShell::vMMPump
+            for (uint32_t i = c.difOff[slot]; i < c.difOff[slot + 1]; ++i) {
+                const uint32_t t = c.difDst[i];
+                difS(c, CM, t) += (vMax / difS(c, VOL, t)) / (difS(c, C_, t) + Kd);
+            }
+        }
+    }
+}
+
+// HSolveActive::sendValues, IkOut (hsolve/HSolveActive.cpp:367-376):
+// (Ek - Vm) Gk of each channel, channel order, to DifShell::vInflux
+__device__ void difSendIk(const DevCell& c) {
+    for (uint32_t q = 0; q < c.C; ++q) {
+        if (c.ikOff[q] == c.ikOff[q + 1]) continue;
+        const double I = (c.Ek[q] - c.V[c.chanCompt[q]]) * c.Gk[q];
+        for (uint32_t i = c.ikOff[q]; i < c.ikOff[q + 1]; ++i) {
+            const uint32_t t = c.ikDst[i];
+            difS(c, dif::DC, t) += I / (dif::kF * difP(c, t, 2) * difS(c, dif::VOL, t));
+        }
+    }
+}
 
 // ---- tick 1/4: external objects -------------------------------------------
 __device__ __forceinline__ void synchanStep(const DevCell& c, uint32_t k, double currTime) {
@@ -298,6 +469,7 @@ __device__ void stepCell(const DevCell& c, uint32_t nsteps, uint32_t tid, uint32
                 c.injBasal[h] = c.stimValue[stimPtr];
                 ++stimPtr;
             }
+            if (c.nDif) difProcess(c);     // tick 1, before the gates read extCa
         }
         for (uint32_t k = tid; k < c.S; k += nth) synchanStep(c, k, currTime);
         for (uint32_t k = tid; k < c.K2; k += nth) chan2dStep(c, k);
@@ -309,6 +481,7 @@ __device__ void stepCell(const DevCell& c, uint32_t nsteps, uint32_t tid, uint32
         groupSync<WARP>();
         for (uint32_t p = tid; p < c.P; p += nth) poolStep(c, p);
         groupSync<WARP>();
+        if (tid == 0 && c.nDif) difSendIk(c);
         // sendValues for the next step's tick-4 objects; SpikeGens; traces
         for (uint32_t k = tid; k < c.K2; k += nth) {
             c.c2dVm[k] = c.V[c.c2dCompt[k]];
@@ -455,6 +628,10 @@ __global__ void hsReinitFp64(const DevCell* __restrict__ cells, uint32_t nCells)
     }
     __syncwarp();
     // sendValues: the tick-4 objects see initVm and CaBasal
+    // tick-1 objects reinit before the solver: their concentrations reach
+    // the channels' external calcium the gates start from
+    if (lane == 0 && c.nDif) difReinit(c);
+    __syncwarp();
     for (uint32_t k = lane; k < c.K2; k += 32) {
         c.c2dX[k] = c.c2dX0[k];
         c.c2dGk[k] = 0.0;

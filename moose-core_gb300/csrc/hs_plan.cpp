@@ -757,6 +757,55 @@ bool buildPlan(const HsCellDesc& d, uint32_t seed, double dt, CellPlan& P, std::
         P.stimCompt.push_back((uint32_t)P.hinesOf[d.stim_compt[k]]);
         P.stimValue.push_back(d.stim_value[k]);
     }
+    // tick-1 external calcium objects and their messages
+    if (d.n_dif || d.n_dmsg) {
+        const uint32_t n = d.n_dif;
+        if (n && (!d.dif_kind || !d.difpar)) return fail("tick-1 objects without kinds or parameters");
+        if (d.n_dmsg && (!d.dmsg_kind || !d.dmsg_src || !d.dmsg_dst)) return fail("tick-1 messages without arrays");
+        P.nDif = n;
+        P.difKind.assign(d.dif_kind, d.dif_kind + n);
+        P.difPar.assign(d.difpar, d.difpar + (size_t)n * HS_DIF_NPAR);
+        for (int32_t k : P.difKind)
+            if (k < HS_DIF_SHELL || k > HS_DIF_PUMP) return fail("unknown tick-1 object kind");
+        std::vector<std::vector<uint32_t>> byObj((size_t)n * kDifMsgKinds), byChan(P.C);
+        for (uint32_t m = 0; m < d.n_dmsg; ++m) {
+            const int kind = d.dmsg_kind[m];
+            const uint32_t s = d.dmsg_src[m], t = d.dmsg_dst[m];
+            if (kind == HS_DMSG_IK) {
+                if (s >= d.n_chan || P.chanSolverOf[s] < 0) return fail("IkOut from a channel the solver does not hold");
+                if (t >= n || P.difKind[t] != HS_DIF_SHELL) return fail("IkOut to an object that is not a DifShell");
+                byChan[(size_t)P.chanSolverOf[s]].push_back(t);
+                continue;
+            }
+            if (kind < HS_DMSG_OUTER || kind > HS_DMSG_PUMP || s >= n) return fail("bad tick-1 message");
+            const int sk = P.difKind[s];
+            bool ok;
+            uint32_t dst = t;
+            switch (kind) {
+            case HS_DMSG_OUTER:
+            case HS_DMSG_INNER: ok = sk != HS_DIF_PUMP && t < n && P.difKind[t] != HS_DIF_PUMP; break;
+            case HS_DMSG_CONC_CHAN:
+                ok = sk == HS_DIF_SHELL && t < d.n_chan && P.chanSolverOf[t] >= 0;
+                if (ok) dst = (uint32_t)P.chanSolverOf[t];
+                break;
+            case HS_DMSG_CONC_BUF: ok = sk == HS_DIF_SHELL && t < n && P.difKind[t] == HS_DIF_BUFFER; break;
+            case HS_DMSG_REACTION: ok = sk == HS_DIF_BUFFER && t < n && P.difKind[t] == HS_DIF_SHELL; break;
+            default: ok = sk == HS_DIF_PUMP && t < n && P.difKind[t] == HS_DIF_SHELL; break;
+            }
+            if (!ok) return fail("tick-1 message between objects of the wrong kinds");
+            byObj[(size_t)s * kDifMsgKinds + kind].push_back(dst);
+        }
+        P.difOff.assign(1, 0);
+        for (const auto& v : byObj) {
+            P.difDst.insert(P.difDst.end(), v.begin(), v.end());
+            P.difOff.push_back((uint32_t)P.difDst.size());
+        }
+        P.ikOff.assign(1, 0);
+        for (const auto& v : byChan) {
+            P.ikDst.insert(P.ikDst.end(), v.begin(), v.end());
+            P.ikOff.push_back((uint32_t)P.ikDst.size());
+        }
+    }
     return true;
 }
 

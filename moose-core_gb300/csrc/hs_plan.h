@@ -113,7 +113,18 @@ struct CellPlan {
     std::vector<int32_t> sgEdge;
     std::vector<uint32_t> stimStep, stimCompt;
     std::vector<double> stimValue;
+    // tick-1 external calcium (DifShell, DifBuffer, MMPump) in process order;
+    // messages CSR by (object, kind) for kinds HS_DMSG_OUTER .. HS_DMSG_PUMP,
+    // in description order, HHChannel targets as solver channels; the
+    // solver's IkOut sends CSR by solver channel
+    uint32_t nDif = 0;
+    std::vector<int32_t> difKind;
+    std::vector<double> difPar;             // nDif x HS_DIF_NPAR
+    std::vector<uint32_t> difOff, difDst;   // nDif * kDifMsgKinds + 1
+    std::vector<uint32_t> ikOff, ikDst;     // C + 1
 };
+
+constexpr uint32_t kDifMsgKinds = 6;        // HS_DMSG_OUTER .. HS_DMSG_PUMP
 
 // Build the plan; returns false and sets err on invalid input.
 bool buildPlan(const HsCellDesc& d, uint32_t seed, double dt, CellPlan& plan, std::string& err,

@@ -203,6 +203,14 @@ class HSolve:
             _native.check(_native.load().hs_read_ca(self._h, out.ctypes.data_as(C.POINTER(C.c_double)), len(out)))
         return out
 
+    def dif(self):
+        """C of each DifShell, bFree of each DifBuffer (0 for an MMPump), in
+        the description's order."""
+        out = np.empty(len(self.model.dif_kind))
+        if len(out):
+            _native.check(_native.load().hs_read_dif(self._h, out.ctypes.data_as(C.POINTER(C.c_double)), len(out)))
+        return out
+
     def record(self, compts, stride, capacity):
         a = np.ascontiguousarray(compts, np.uint32)
         _native.check(_native.load().hs_record(self._h, a.ctypes.data_as(C.POINTER(C.c_uint32)), len(a),

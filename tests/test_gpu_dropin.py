@@ -411,3 +411,49 @@ def test_failed_record_keeps_previous_recording():
     oc.step(20)
     tr = h.trace()
     assert tr.shape == (1, 4) and tr[0, -1] == oc.vm()[3]
+
+
+def test_external_calcium_difshells_on_gpu():
+    """tests/core/test_hsolve_externalCalcium.py on the GPU drop-in: three
+    DifShells stepped on tick 1 in the reference's message order, the
+    solver's IkOut into the outer shell and its concentration into the SK
+    gate, 10 s at 10 us (1,000,000 steps).  Vm, the shell's Ca and SK's Gk
+    every 5 ms within 1e-9 relative of the reference's (the shells'
+    integration calls exp: device against glibc), and the test's own
+    checks pass.  The FP64 batch steps the same cell bit-identically."""
+    from moose_gb300.abi import FIELDS, HS_KIND_CHAN, HS_PREC_FP64
+    from moose_gb300.batch import Batch
+    from test_oracle_golden import check_ext_calcium_kat, run_ext_calcium
+    z = np.load(os.path.join(GOLDEN, "ext_calcium.npz"))
+    m = load_model(z)
+    dt = float(z["dt"])
+    h = HSolve(m, dt=dt)
+    h.target = m.seed
+    h.reinit(dt)
+    si, ki = int(z["shell_index"]), int(z["sk_index"])
+    vm, ca, sk = run_ext_calcium(h, z, lambda: h.dif()[si], lambda: h._get(HS_KIND_CHAN, FIELDS["Gk"], ki))
+    for got, ref in ((vm, z["vm"]), (ca, z["shell_c"]), (sk, z["sk_gk"])):
+        assert np.all(np.abs(got - ref) <= 1e-9 * np.maximum(np.abs(ref), 1e-30)), np.abs(got - ref).max()
+    check_ext_calcium_kat(z, sk, ca)
+    # the FP64 batch: the same arithmetic, bit-identical
+    h2 = HSolve(m, dt=dt)
+    h2.target = m.seed
+    h2.reinit(dt)
+    h2.process(20000)
+    b = Batch([m], dt, HS_PREC_FP64)
+    b.reinit(dt)
+    b.process(20000)
+    assert np.array_equal(b.vm(0), h2.vm())
+    b.close()
+    h.close()
+    h2.close()
+
+
+def test_mixed_batch_rejects_external_calcium():
+    from moose_gb300._native import HsError
+    from moose_gb300.abi import HS_ENOTSUP, HS_PREC_MIXED
+    from moose_gb300.batch import Batch
+    z = np.load(os.path.join(GOLDEN, "ext_calcium.npz"))
+    with pytest.raises(HsError) as ei:
+        Batch([load_model(z)], float(z["dt"]), HS_PREC_MIXED)
+    assert ei.value.code == HS_ENOTSUP
