@@ -339,6 +339,15 @@ int hs_read_dif(HsSolver* s, double* out, uint32_t n);
  * appended to a device buffer (a Table on tick 8 reading `HSolve::getVm`). */
 int hs_record(HsSolver* s, const uint32_t* compts, uint32_t n, uint32_t stride,
               uint32_t capacity_samples);
+/* The values the solver sends each step to objects it does not own
+ * (`HSolveActive::sendValues`, hsolve/HSolveActive.cpp:354-385), recorded
+ * on the device every `stride` steps: entry r is the Vm of compartment
+ * index[r] (kind HS_KIND_COMPT, field HS_F_VM: VmOut), the Ik = (Ek - Vm) Gk
+ * (HS_KIND_CHAN, HS_F_IK: IkOut) or Gk (HS_F_GK) of an HHChannel, or the Ca
+ * of a pool (HS_KIND_POOL, HS_F_CA: concOut).  Replaces the recording of
+ * hs_record (which records Vm only); read with hs_read_trace. */
+int hs_record_values(HsSolver* s, const int* kind, const int* field, const uint32_t* index, uint32_t n,
+                     uint32_t stride, uint32_t capacity);
 int hs_read_trace(HsSolver* s, double* out, uint32_t capacity, uint32_t* n_samples);
 
 /* Spikes from the SpikeGens: (spikegen model index, time) pairs. */

@@ -768,19 +768,13 @@ int hs_read_dif(HsSolver* s, double* out, uint32_t n) {
     return HS_OK;
 }
 
-int hs_record(HsSolver* s, const uint32_t* compts, uint32_t n, uint32_t stride, uint32_t capacity) {
-    if (!s) return setErr(HS_EINVAL, "null solver");
-    if (n && (!compts || stride == 0 || capacity == 0)) return setErr(HS_EINVAL, "bad recording request");
-    // Every target is checked before the old recording is released, so a
-    // rejected request leaves the previous recording in place.
-    std::vector<uint32_t> rows;
-    rows.reserve(n);
-    for (uint32_t r = 0; r < n; ++r) {
-        uint32_t h;
-        int rc = comptIndex(s, compts[r], &h);
-        if (rc) return rc;
-        rows.push_back(h);
-    }
+}  // extern "C"
+
+namespace {
+// Replaces the solver's recording by `rows` (device recording entries, see
+// kRecShift in hs_device.cuh), every target already checked.
+int installRecording(HsSolver* s, std::vector<uint32_t>&& rows, uint32_t stride, uint32_t capacity) {
+    const uint32_t n = (uint32_t)rows.size();
     cudaStreamSynchronize(s->st);
     // From here on the step kernel sees no recording until the new one is
     // complete, so it never writes into a released buffer.
@@ -817,6 +811,55 @@ int hs_record(HsSolver* s, const uint32_t* compts, uint32_t n, uint32_t stride, 
     s->dc.recCompt = s->recCompt;
     s->dc.recBuf = s->recBuf;
     return HS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hs_record(HsSolver* s, const uint32_t* compts, uint32_t n, uint32_t stride, uint32_t capacity) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    if (n && (!compts || stride == 0 || capacity == 0)) return setErr(HS_EINVAL, "bad recording request");
+    // Every target is checked before the old recording is released, so a
+    // rejected request leaves the previous recording in place.
+    std::vector<uint32_t> rows;
+    rows.reserve(n);
+    for (uint32_t r = 0; r < n; ++r) {
+        uint32_t h;
+        int rc = comptIndex(s, compts[r], &h);
+        if (rc) return rc;
+        rows.push_back(h | (kRecVm << kRecShift));
+    }
+    return installRecording(s, std::move(rows), stride, capacity);
+}
+
+int hs_record_values(HsSolver* s, const int* kind, const int* field, const uint32_t* index, uint32_t n,
+                     uint32_t stride, uint32_t capacity) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    if (n && (!kind || !field || !index || stride == 0 || capacity == 0))
+        return setErr(HS_EINVAL, "bad recording request");
+    std::vector<uint32_t> rows;
+    rows.reserve(n);
+    for (uint32_t r = 0; r < n; ++r) {
+        uint32_t i = 0, code;
+        int rc;
+        if (kind[r] == HS_KIND_COMPT && field[r] == HS_F_VM) {
+            rc = comptIndex(s, index[r], &i);
+            code = kRecVm;
+        } else if (kind[r] == HS_KIND_CHAN && (field[r] == HS_F_IK || field[r] == HS_F_GK)) {
+            rc = chanIndex(s, index[r], &i);
+            code = field[r] == HS_F_IK ? kRecIk : kRecGk;
+        } else if (kind[r] == HS_KIND_POOL && field[r] == HS_F_CA) {
+            rc = poolIndex(s, index[r], &i);
+            code = kRecCa;
+        } else {
+            return setErr(HS_EINVAL, "recordable values: compartment Vm, channel Ik or Gk, pool Ca");
+        }
+        if (rc) return rc;
+        if (i >> kRecShift) return setErr(HS_ECAPACITY, "recorded index beyond the recorder's range");
+        rows.push_back(i | (code << kRecShift));
+    }
+    return installRecording(s, std::move(rows), stride, capacity);
 }
 
 int hs_read_trace(HsSolver* s, double* out, uint32_t capacity, uint32_t* n_samples) {

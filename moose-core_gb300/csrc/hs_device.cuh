@@ -20,6 +20,13 @@ namespace hsg {
 
 constexpr uint32_t kDifState = 13;
 
+// A recording entry: the value's index in its array (bits 0-27) and what is
+// recorded (bits 28-31): the compartment's Vm (VmOut), the channel's Ik =
+// (Ek - Vm) Gk as HSolveActive::sendValues sends it (IkOut), the channel's
+// Gk, or the pool's Ca (concOut).
+constexpr uint32_t kRecShift = 28;
+constexpr uint32_t kRecVm = 0, kRecIk = 1, kRecGk = 2, kRecCa = 3;
+
 struct DevCtl {
     unsigned long long nSteps;   // steps since reinit
     uint32_t stimPtr;
@@ -109,6 +116,17 @@ struct FieldWrite {
     uint32_t size;
     uint32_t pad;
 };
+
+// The value a recording entry names (hsolve/HSolveActive.cpp:354-385 for Ik).
+__device__ __forceinline__ double recValue(const DevCell& c, uint32_t e) {
+    const uint32_t i = e & ((1u << kRecShift) - 1);
+    switch (e >> kRecShift) {
+    case kRecIk: return (c.Ek[i] - c.V[c.chanCompt[i]]) * c.Gk[i];
+    case kRecGk: return c.Gk[i];
+    case kRecCa: return c.ca[i];
+    default: return c.V[i];
+    }
+}
 
 // ---------------------------------------------------------------------------
 // FP64 helpers, reference order

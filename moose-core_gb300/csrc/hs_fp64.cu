@@ -511,7 +511,7 @@ __device__ void stepCell(const DevCell& c, uint32_t nsteps, uint32_t tid, uint32
         if (c.nRec && ((step + 1) % c.recStride) == 0) {
             if (nSamples < c.recCap)
                 for (uint32_t r = tid; r < c.nRec; r += nth)
-                    c.recBuf[(size_t)nSamples * c.recLd + r] = c.V[c.recCompt[r]];
+                    c.recBuf[(size_t)nSamples * c.recLd + r] = recValue(c, c.recCompt[r]);
             ++nSamples;
         }
         for (uint32_t ic = tid; ic < c.N; ic += nth) {
@@ -642,7 +642,7 @@ __global__ void hsReinitFp64(const DevCell* __restrict__ cells, uint32_t nCells)
     for (uint32_t ic = lane; ic < c.N; ic += 32) reinitGatesCompt(c, ic);
     // a Table reading Vm at reinit records sample 0
     if (c.nRec && c.recCap) {
-        for (uint32_t r = lane; r < c.nRec; r += 32) c.recBuf[r] = c.V[c.recCompt[r]];
+        for (uint32_t r = lane; r < c.nRec; r += 32) c.recBuf[r] = recValue(c, c.recCompt[r]);
         __syncwarp();
         if (lane == 0) c.ctl->nSamples = 1;
     }

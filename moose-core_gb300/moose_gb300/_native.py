@@ -65,6 +65,7 @@ def load(build_if_missing=True):
         "hs_batch_read_ca": (i32, [vp, u32, pd, u32]),
         "hs_batch_read_all": (i32, [vp, i32, pd, C.c_uint64]),
         "hs_read_dif": (i32, [vp, pd, u32]),
+        "hs_record_values": (i32, [vp, pi, pi, pu, u32, u32, u32]),
         "hs_batch_record": (i32, [vp, pu, pu, u32, u32, u32]),
         "hs_batch_read_trace": (i32, [vp, pd, u32, pu]),
         "hs_batch_read_trace_window": (i32, [vp, u32, u32, vp]),

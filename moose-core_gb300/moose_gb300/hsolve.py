@@ -217,6 +217,21 @@ class HSolve:
                                                int(stride), int(capacity)))
         self._rec = (a, int(capacity))
 
+    def record_values(self, entries, stride, capacity):
+        """Record, every `stride` steps on the device, the values the solver
+        sends to objects it does not own: entries are (kind, field, index)
+        with (HS_KIND_COMPT, Vm), (HS_KIND_CHAN, Ik or Gk), (HS_KIND_POOL,
+        Ca); fields by name or code.  Read with trace()."""
+        from .abi import FIELDS
+        kinds = np.ascontiguousarray([e[0] for e in entries], np.int32)
+        fields = np.ascontiguousarray([FIELDS[e[1]] if isinstance(e[1], str) else e[1] for e in entries], np.int32)
+        index = np.ascontiguousarray([e[2] for e in entries], np.uint32)
+        pi = C.POINTER(C.c_int)
+        _native.check(_native.load().hs_record_values(self._h, kinds.ctypes.data_as(pi), fields.ctypes.data_as(pi),
+                                                      index.ctypes.data_as(C.POINTER(C.c_uint32)), len(index),
+                                                      int(stride), int(capacity)))
+        self._rec = (index, int(capacity))
+
     def trace(self):
         a, cap = self._rec
         out = np.empty((cap, len(a)))

@@ -457,3 +457,39 @@ def test_mixed_batch_rejects_external_calcium():
     with pytest.raises(HsError) as ei:
         Batch([load_model(z)], float(z["dt"]), HS_PREC_MIXED)
     assert ei.value.code == HS_ENOTSUP
+
+
+def test_outgoing_values_recorded_on_device():
+    """The values HSolveActive::sendValues sends each step to objects the
+    solver does not own -- VmOut of compartments, IkOut = (Ek - Vm) Gk of
+    HHChannels, concOut of Ca pools -- and channel Gk, recorded on the
+    device every step, against the oracle read after each step (within
+    1e-9 relative: the cell's K(Ca) gate calls exp)."""
+    from moose_gb300.abi import HS_KIND_CHAN, HS_KIND_COMPT, HS_KIND_POOL
+    z = np.load(os.path.join(GOLDEN, "active_branched_kca.npz"))
+    m = load_model(z)
+    dt = float(z["dt"])
+    entries = ([(HS_KIND_COMPT, "Vm", i) for i in (0, 7, 31)] +
+               [(HS_KIND_CHAN, "Ik", k) for k in (0, 5, 44)] + [(HS_KIND_CHAN, "Gk", k) for k in (2, 44)] +
+               [(HS_KIND_POOL, "Ca", p) for p in (0, 9)])
+    n = 300
+    h = HSolve(m, dt=dt)
+    h.target = m.seed
+    h.record_values(entries, 1, n + 1)
+    h.reinit(dt)
+    h.process(n)
+    got = h.trace()
+    oc = OracleCell(m, dt)
+    oc.reinit(dt)
+    rows = []
+    for s in range(n):
+        oc.step(1)
+        rows.append([oc.get(k, FIELDS[f], i) if k != HS_KIND_POOL else oc.ca()[i] for k, f, i in entries])
+    want = np.array(rows).T
+    assert got.shape == (len(entries), n + 1)
+    assert np.all(np.abs(got[:, 1:] - want) <= 1e-9 * np.maximum(np.abs(want), 1e-15))
+    # Ik is what the reference sends: (Ek - Vm) Gk of the channel's compartment
+    assert np.any(np.abs(got[3:6, 1:]) > 0)
+    with pytest.raises(_native.HsError):
+        h.record_values([(HS_KIND_POOL, "Vm", 0)], 1, 4)
+    h.close()
