@@ -472,7 +472,8 @@ def run_ours(args, rank, world, cpu_pool):
     cells = [models.make_cell(CONFIG, SEED, i, t_end=t_end, kca_tables=kca, sizes=sizes)
              for i in range(args.cells)]
     ncomp = sum(m.n_compt for m in cells)
-    b = Batch(cells, DT, HS_PREC_MIXED, steps_per_launch=args.steps_per_launch)
+    b = Batch(cells, DT, HS_PREC_MIXED, steps_per_launch=args.steps_per_launch,
+              forest_nodes=args.forest_nodes, elim_warps=args.elim_warps)
     tuned = None
     if not args.no_autotune:
         from moose_gb300.autotune import autotune
@@ -688,6 +689,8 @@ def main():
     ap.add_argument("--cells", type=int, default=4096)
     ap.add_argument("--chunk", type=int, default=200, help="dt steps per bench step")
     ap.add_argument("--steps-per-launch", type=int, default=0)
+    ap.add_argument("--forest-nodes", type=int, default=0, help="mixed batch forest size (0: one cell per forest)")
+    ap.add_argument("--elim-warps", type=int, default=0, help="mixed batch eliminator warps (0: default)")
     ap.add_argument("--dropin-cells", type=int, default=128)
     ap.add_argument("--dropin-steps", type=int, default=200)
     ap.add_argument("--acc-cells", type=int, default=256)

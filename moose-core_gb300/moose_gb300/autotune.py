@@ -11,7 +11,10 @@ on the batch's stream (``Batch.kernel_time``), and keeps the fastest.
 Search: coordinate descent from the defaults -- first the packing (CTAs per
 SM x forest size, each a re-layout), then threads per CTA, eliminator warps
 and steps per launch -- so the number of timed runs grows with the sum, not
-the product, of the candidate lists.  Results are cached per workload signature in a JSON
+the product, of the candidate lists.  Packing and eliminator count interact
+(forests of a few compartments merge every cell of a CTA into one forest
+whose level sweep wants more eliminator warps), so a packing entry may carry
+its own eliminator count as a third element, tried together.  Results are cached per workload signature in a JSON
 file so that a repeated workload skips the search.
 """
 import hashlib
@@ -23,9 +26,10 @@ import numpy as np
 from .abi import HS_PREC_FP64
 
 MIXED_SPACE = {
-    "packing": [(1, 0), (1, 6000), (1, 4096), (2, 0)],       # (ctas_per_sm, forest_nodes)
+    # (ctas_per_sm, forest_nodes[, elim_warps])
+    "packing": [(1, 0), (1, 8, 8), (1, 6000), (1, 4096), (2, 0)],
     "threads_per_cta": [1024, 768, 512],
-    "elim_warps": [4, 5, 3],
+    "elim_warps": [4, 5, 3, 8],
     "steps_per_launch": [100, 50, 200],
 }
 FP64_SPACE = {
@@ -83,6 +87,8 @@ def coordinate_descent(space, measure, start):
                 continue
             cand = dict(best)
             cand[knob] = v
+            if knob == "packing" and len(v) > 2:
+                cand["elim_warps"] = v[2]
             t = measure(cand)
             trials.append((dict(cand), t))
             if t < best_t:
@@ -103,7 +109,7 @@ def autotune(batch, dt, steps=200, warmup=50, space=None, cache=None, use_cache=
     table = _load(cache) if use_cache else {}
 
     def apply(cfg):
-        cps, fn = cfg["packing"]
+        cps, fn = cfg["packing"][:2]
         batch.tune(threads_per_cta=cfg["threads_per_cta"], ctas_per_sm=cps,
                    steps_per_launch=cfg["steps_per_launch"], forest_nodes=fn,
                    elim_warps=cfg.get("elim_warps") or 0)
@@ -127,8 +133,10 @@ def autotune(batch, dt, steps=200, warmup=50, space=None, cache=None, use_cache=
         out = dict(hit)
         out["cached"] = True
         return out
-    start = {"packing": space["packing"][0], "threads_per_cta": space["threads_per_cta"][0],
-             "elim_warps": space.get("elim_warps", [0])[0], "steps_per_launch": space["steps_per_launch"][0]}
+    p0 = tuple(space["packing"][0])
+    start = {"packing": p0, "threads_per_cta": space["threads_per_cta"][0],
+             "elim_warps": p0[2] if len(p0) > 2 else space.get("elim_warps", [0])[0],
+             "steps_per_launch": space["steps_per_launch"][0]}
     best, trials = coordinate_descent(space, measure, start)
     apply(best)
     out = {"packing": list(best["packing"]), "threads_per_cta": best["threads_per_cta"],

@@ -26,6 +26,20 @@ def test_coordinate_descent_finds_the_best_along_each_knob():
     assert len(trials) == 1 + 2 + 2 + 2 == len(calls)
 
 
+def test_packing_may_carry_its_own_eliminator_count():
+    space = {"packing": [(1, 0), (1, 8, 8)], "threads_per_cta": [1024], "elim_warps": [4, 8],
+             "steps_per_launch": [100]}
+    # merged forests are slow with 4 eliminators and fast with 8: trying the
+    # packing with its own count finds the pair one knob at a time cannot
+    cost = {((1, 0), 4): 0.464, ((1, 0), 8): 0.507, ((1, 8, 8), 4): 0.635, ((1, 8, 8), 8): 0.442}
+
+    def measure(c):
+        return cost[(c["packing"], c["elim_warps"])]
+    start = {"packing": (1, 0), "threads_per_cta": 1024, "elim_warps": 4, "steps_per_launch": 100}
+    best, _ = autotune.coordinate_descent(space, measure, start)
+    assert best["packing"] == (1, 8, 8) and best["elim_warps"] == 8
+
+
 def test_signature_and_cache(tmp_path):
     class M:
         def __init__(self, n, s):
