@@ -79,9 +79,11 @@ typedef struct HsGate2DTable {
 
 typedef struct HsCellDesc {
     /* Compartments.  `parent[i]` is the morphological parent (the source of
-     * the `axial` message into i) or -1.  Several children of one parent are
-     * connected in increasing child index: that is the message order that
-     * `HSolveUtils::adjacent`/`children` see (`hsolve/HSolveUtils.cpp:27-44`). */
+     * the message into i: `axial`, or for a SymCompartment `distal`,
+     * `sphere` or `cylinder`, as `link` below says) or -1.  Several children
+     * of one parent joined by the same kind of link are connected in
+     * increasing child index: that is the message order that
+     * `HSolveUtils::adjacent`/`children` see (`hsolve/HSolveUtils.cpp:36-53`). */
     uint32_t n_compt;
     const int32_t* parent;
     const double* Ra;
@@ -202,7 +204,21 @@ typedef struct HsCellDesc {
     const int32_t* dmsg_kind;      /* HS_DMSG_* */
     const uint32_t* dmsg_src;      /* object (HHChannel for HS_DMSG_IK) */
     const uint32_t* dmsg_dst;      /* object (HHChannel for HS_DMSG_CONC_CHAN) */
+    /* How each compartment hangs on its parent (n_compt entries, HS_LINK_*;
+     * NULL: every link axial).  It places the parent and the children in
+     * the order HSolveUtils::adjacent lists them -- axial targets, raxial,
+     * distalOut, proximalOut, cylinderOut (hsolve/HSolveUtils.cpp:36-45) --
+     * and the children in HSolveUtils::children's order (axial, distalOut,
+     * cylinderOut), which set the Hines numbering and each junction's
+     * operand order. */
+    const int32_t* link;
 } HsCellDesc;
+
+#define HS_LINK_AXIAL    0   /* Compartment: parent axial -> child raxial      */
+#define HS_LINK_DISTAL   1   /* SymCompartment: parent distal -> child proximal,
+                                or parent sphere -> child proximalOnly        */
+#define HS_LINK_CYLINDER 2   /* SymCompartment: parent cylinder -> child
+                                proximalOnly (spines)                          */
 
 /* tick-1 object kinds and their parameters (difpar, HS_DIF_NPAR per object) */
 #define HS_DIF_SHELL   0   /* Ceq, D, valence, leak, shapeMode, length, diameter,
@@ -438,6 +454,21 @@ int hs_batch_set_inject(HsBatch* b, const double* values, uint32_t n);
  * persist across reinit and repacking.  Returns after the writes are done. */
 int hs_batch_set_modulation(HsBatch* b, int kind, const uint32_t* cells, const uint32_t* index,
                             const double* values, uint32_t n);
+/* Synaptic events queued at run time on batched cells: hs_push_events for
+ * many cells in one call (SimpleSynHandler::addSpike,
+ * synapse/SimpleSynHandler.cpp:86-90).  Event e reaches SynChan syn[e] (the
+ * cell's description index) of cell cell[e] at time time[e] (spike time +
+ * synapse delay) with weight weight[e]; it is delivered at the first step
+ * whose clock time is >= its time, including times already passed.  Events
+ * with equal times on one SynChan are summed in push order, after the ones
+ * already queued.  The pushes reach the device at the next
+ * hs_batch_process; hs_batch_reinit and a re-layout by hs_batch_tune drop
+ * every queued runtime event.  Both precisions; in the mixed batch the
+ * delivery step is taken at the clock dt of the last reinit.  Validates
+ * every event before queuing any (HS_EINVAL: cell or SynChan out of range,
+ * NaN time). */
+int hs_batch_push_events(HsBatch* b, const uint32_t* cell, const uint32_t* syn, const double* time,
+                         const double* weight, uint32_t n);
 /* The inject of compartment compt[k] of cell cell[k] becomes values[k], for
  * k < n, without allocating any memory: the writes go through a fixed
  * host staging array and a fixed device scratch array of 32768 entries

@@ -27,6 +27,7 @@
 
 #include "../../include/moose_gb300.h"
 #include "hs_cell.h"
+#include "hs_events.h"
 #include "hs_mixed.cuh"
 #include "hs_noalloc.h"
 #include "hs_plan.h"
@@ -169,6 +170,27 @@ struct HsBatch {
     uint32_t* dEvStep = nullptr;
     float* dEvAct = nullptr;
     float* dSynNorm = nullptr;
+    uint32_t* dEvCurDesc = nullptr;            // the description's cursors and ends
+    const uint32_t* dEvEndDesc = nullptr;
+    // run-time synaptic events (hs_batch_push_events): pushes wait on the
+    // host, by global SynChan, until the next process call; the first flush
+    // replaces the description's queues by a batch-owned queue over every
+    // SynChan (global order: FP64 cell-major, mixed forest order) holding
+    // the undelivered events, mirrored on the host
+    std::vector<uint32_t> pendSyn;
+    std::vector<double> pendTime, pendW;
+    bool evOwned = false;
+    std::vector<uint32_t> evHostPtr;           // S+1 starts of the owned queue
+    std::vector<double> evHostTime, evHostW;
+    uint32_t* dEvOwnCur = nullptr;             // cursors of the owned queue
+    DevBuf evBuf;
+    std::vector<uint32_t> synBase;             // FP64: first global SynChan of each cell
+    struct EvPtrs {
+        const uint32_t* ptr;
+        uint32_t* cur;
+        const double *time, *w;
+    };
+    std::vector<EvPtrs> evDesc;                // FP64: each cell's description queue
     // recording
     std::vector<std::pair<uint32_t, uint32_t>> rec;
     DevBuf recBuf;
@@ -333,6 +355,16 @@ int repack(HsBatch* b) {
 }
 
 // ---- FP64 batch: drop-in layout per cell, shared tables ---------------------
+// Mixed batch: the step at which an event of time t is delivered, the first
+// step whose currTime = dt (step + 1) reaches t (SimpleSynHandler delivers
+// the events with time <= currTime), as a 32-bit step count.
+uint32_t deliveryStep(double t, double dt) {
+    const double g = std::ceil(t / dt) - 3.0;
+    uint64_t s = g > 0 ? (uint64_t)std::min(g, 4294967296.0) : 0;
+    while (s < 0xffffffffull && !(t <= dt * (double)(s + 1))) ++s;
+    return (uint32_t)std::min<uint64_t>(s, 0xffffffffu);
+}
+
 int buildFp64(HsBatch* b, const HsCellDesc* cells) {
     const uint32_t nC = b->nCells;
     // shared V/Ca tables by content, 2-D tables by source identity
@@ -370,6 +402,8 @@ int buildFp64(HsBatch* b, const HsCellDesc* cells) {
             (pass ? catab : vtab)[c] = it->second;
         }
     }
+    b->synBase.assign(nC + 1, 0);
+    for (uint32_t c = 0; c < nC; ++c) b->synBase[c + 1] = b->synBase[c] + b->plans[c].S;
     // reinit arrays contiguous over cells
     size_t nInit = 0, nSyn = 0;
     b->initVmOff.resize(nC);
@@ -409,6 +443,8 @@ int buildFp64(HsBatch* b, const HsCellDesc* cells) {
     if (e != cudaSuccess) return cerr(e, "batch upload");
     b->dDcs = b->buf.alloc<DevCell>(nC);
     if (b->buf.err != cudaSuccess) return cerr(b->buf.err, "batch cells");
+    b->evDesc.resize(nC);
+    for (uint32_t c = 0; c < nC; ++c) b->evDesc[c] = {b->dcs[c].evPtr, b->dcs[c].evCur, b->dcs[c].evTime, b->dcs[c].evW};
     (void)cells;
     return HS_OK;
 }
@@ -1052,6 +1088,8 @@ int buildMixed(HsBatch* b) {
     }
     m.evCur = D.up(H.evStart, st);
     m.evEnd = D.up(H.evEnd, st);
+    b->dEvCurDesc = m.evCur;
+    b->dEvEndDesc = m.evEnd;
     b->dEvStep = D.zeros<uint32_t>(H.evTime.size(), st);
     b->dEvAct = D.zeros<float>(H.evTime.size(), st);
     b->dSynNorm = D.zeros<float>(synTypeV.size(), st);
@@ -1150,6 +1188,155 @@ int buildMixed(HsBatch* b) {
     return HS_OK;
 }
 
+// ---- run-time synaptic events ----------------------------------------------------
+// Back to the description's queues (reinit, re-layout): SimpleSynHandler's
+// vReinit empties its queue.  The owned queue is freed in stream order.
+void dropRuntimeEvents(HsBatch* b) {
+    b->pendSyn.clear();
+    b->pendTime.clear();
+    b->pendW.clear();
+    if (!b->evOwned) return;
+    if (b->precision == HS_PREC_FP64) {
+        for (uint32_t c = 0; c < b->nCells; ++c) {
+            b->dcs[c].evPtr = b->evDesc[c].ptr;
+            b->dcs[c].evCur = b->evDesc[c].cur;
+            b->dcs[c].evTime = b->evDesc[c].time;
+            b->dcs[c].evW = b->evDesc[c].w;
+        }
+    } else {
+        b->mb.evCur = b->dEvCurDesc;
+        b->mb.evEnd = b->dEvEndDesc;
+        b->mb.evStep = b->dEvStep;
+        b->mb.evAct = b->dEvAct;
+    }
+    b->evBuf.freeAll();
+    b->evBuf.err = cudaSuccess;
+    b->evHostPtr.clear();
+    b->evHostTime.clear();
+    b->evHostW.clear();
+    b->dEvOwnCur = nullptr;
+    b->evOwned = false;
+}
+
+// Hands the pushed events to the device before a process call.  The queue
+// over every SynChan of the batch is rebuilt on the host from the device
+// cursors (mergeEventQueue, hs_events.h: undelivered events merged with the
+// pushes in time order) and uploaded to a new owned buffer; the kernels walk
+// it exactly as they walk the description's events.  The old queue stays in
+// place until the new one is on the device.
+int flushRuntimeEvents(HsBatch* b) {
+    if (b->pendSyn.empty()) return HS_OK;
+    const bool fp64 = b->precision == HS_PREC_FP64;
+    MixHost& H = b->mh;
+    const uint32_t S = fp64 ? b->synBase.back() : (uint32_t)H.synGbar.size();
+    cudaError_t e = cudaStreamSynchronize(b->st);
+    if (e != cudaSuccess) return cerr(e, "push events");
+    std::vector<uint32_t> cur(S), descPtr;
+    std::vector<double> descTime, descW;
+    std::vector<uint32_t> cellEv0;            // FP64 description: first event of each cell
+    if (!b->evOwned && fp64) {
+        descPtr.resize((size_t)S + 1);
+        cellEv0.resize(b->nCells);
+        for (uint32_t c = 0; c < b->nCells; ++c) {
+            const CellPlan& P = b->plans[c];
+            const uint32_t off = (uint32_t)descTime.size();
+            cellEv0[c] = off;
+            for (uint32_t j = 0; j < P.S; ++j) descPtr[b->synBase[c] + j] = off + P.evPtr[j];
+            descTime.insert(descTime.end(), P.evTime.begin(), P.evTime.end());
+            descW.insert(descW.end(), P.evW.begin(), P.evW.end());
+            if (P.S && e == cudaSuccess)
+                e = cudaMemcpyAsync(cur.data() + b->synBase[c], b->evDesc[c].cur, P.S * sizeof(uint32_t),
+                                    cudaMemcpyDeviceToHost, b->st);
+        }
+        descPtr[S] = (uint32_t)descTime.size();
+    } else if (!b->evOwned) {
+        descPtr = H.evStart;
+        descPtr.push_back(S ? H.evEnd.back() : 0u);
+        if (S) e = cudaMemcpyAsync(cur.data(), b->mb.evCur, S * sizeof(uint32_t), cudaMemcpyDeviceToHost, b->st);
+    } else if (S) {
+        e = cudaMemcpyAsync(cur.data(), b->dEvOwnCur, S * sizeof(uint32_t), cudaMemcpyDeviceToHost, b->st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    if (e != cudaSuccess) return cerr(e, "push events");
+    if (!b->evOwned && fp64)
+        for (uint32_t c = 0; c < b->nCells; ++c)
+            for (uint32_t j = 0; j < b->plans[c].S; ++j) cur[b->synBase[c] + j] += cellEv0[c];
+    const std::vector<uint32_t>& ptr = b->evOwned ? b->evHostPtr : descPtr;
+    const std::vector<double>& tm = b->evOwned ? b->evHostTime : (fp64 ? descTime : H.evTime);
+    const std::vector<double>& wt = b->evOwned ? b->evHostW : (fp64 ? descW : H.evW);
+    std::vector<uint32_t> nptr;
+    std::vector<double> nt, nw;
+    if (!mergeEventQueue(S, ptr, tm, wt, cur, b->pendSyn, b->pendTime, b->pendW, nptr, nt, nw))
+        return berr(HS_ENOMEM, "too many queued synaptic events");
+    DevBuf nb;
+    nb.st = b->st;
+    const size_t m = nt.size();
+    if (fp64) {
+        uint32_t* idx = nb.up(nptr, b->st);
+        std::vector<double> tw(nt);
+        tw.insert(tw.end(), nw.begin(), nw.end());
+        double* ev = nb.up(tw, b->st);
+        if (nb.err == cudaSuccess) nb.err = cudaStreamSynchronize(b->st);
+        if (nb.err != cudaSuccess) {
+            cudaError_t e2 = nb.err;
+            nb.freeAll();
+            return cerr(e2, "push events");
+        }
+        std::vector<DevCell> keep(b->dcs);
+        for (uint32_t c = 0; c < b->nCells; ++c) {
+            b->dcs[c].evPtr = idx + b->synBase[c];
+            b->dcs[c].evCur = idx + S + 1 + b->synBase[c];
+            b->dcs[c].evTime = ev;
+            b->dcs[c].evW = ev + m;
+        }
+        int rc = uploadDcs(b);
+        if (rc != HS_OK) {
+            b->dcs.swap(keep);
+            nb.freeAll();
+            return rc;
+        }
+        b->dEvOwnCur = idx + S + 1;
+    } else {
+        std::vector<uint32_t> curv(nptr.begin() + S + 1, nptr.end()), end(S), step(m);
+        std::vector<float> act(m);
+        for (uint32_t k = 0; k < S; ++k) end[k] = nptr[k + 1];
+        for (size_t q = 0; q < m; ++q) {
+            step[q] = deliveryStep(nt[q], b->clockDt);
+            act[q] = (float)(nw[q] / b->clockDt);
+        }
+        uint32_t* dCur = nb.up(curv, b->st);
+        const uint32_t* dEnd = nb.up(end, b->st);
+        const uint32_t* dStep = nb.up(step, b->st);
+        const float* dAct = nb.up(act, b->st);
+        if (nb.err == cudaSuccess) nb.err = cudaStreamSynchronize(b->st);
+        if (nb.err != cudaSuccess) {
+            cudaError_t e2 = nb.err;
+            nb.freeAll();
+            return cerr(e2, "push events");
+        }
+        b->mb.evCur = dCur;
+        b->dEvOwnCur = dCur;
+        b->mb.evEnd = dEnd;
+        b->mb.evStep = dStep;
+        b->mb.evAct = dAct;
+        if (b->gexec) {             // the graph holds the kernel's parameters
+            cudaGraphExecDestroy(b->gexec);
+            b->gexec = nullptr;
+        }
+    }
+    b->evBuf.freeAll();
+    b->evBuf = nb;
+    nptr.resize((size_t)S + 1);
+    b->evHostPtr.swap(nptr);
+    b->evHostTime.swap(nt);
+    b->evHostW.swap(nw);
+    b->evOwned = true;
+    b->pendSyn.clear();
+    b->pendTime.clear();
+    b->pendW.clear();
+    return HS_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1209,7 +1396,7 @@ int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds, uint32_t n_c
             uint64_t keep = UINT64_MAX;
             cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
         }
-        b->buf.st = b->packBuf.st = b->recBuf.st = b->injBuf.st = b->st;
+        b->buf.st = b->packBuf.st = b->recBuf.st = b->injBuf.st = b->evBuf.st = b->st;
     }
     if (e != cudaSuccess) {
         delete b;
@@ -1259,6 +1446,7 @@ int hs_batch_destroy(HsBatch* b) {
     b->recBuf.freeAll();
     b->injBuf.freeAll();
     b->gatherBuf.freeAll();
+    b->evBuf.freeAll();
     if (b->arena.base) cudaFreeAsync(b->arena.base, b->st);
     if (b->st) cudaStreamDestroy(b->st);
     delete b;
@@ -1292,6 +1480,7 @@ int hs_batch_tune(HsBatch* b, const HsBatchTuning* t) {
             cudaGraphExecDestroy(b->gexec);
             b->gexec = nullptr;
         }
+        dropRuntimeEvents(b);
         b->buf.freeAll();
         b->buf.err = cudaSuccess;
         b->recBuf.freeAll();
@@ -1321,6 +1510,7 @@ int hs_batch_reinit(HsBatch* b, double clock_dt) {
     }
     b->clockDt = clock_dt;
     b->stepsDone = 0;
+    dropRuntimeEvents(b);
     cudaError_t e = cudaSuccess;
     if (b->precision == HS_PREC_FP64) {
         size_t nsc = b->synOff.back() + 5 * (size_t)b->plans.back().S;
@@ -1350,13 +1540,7 @@ int hs_batch_reinit(HsBatch* b, double clock_dt) {
         std::vector<uint32_t> evStep(H.evTime.size());
         std::vector<float> evAct(H.evTime.size());
         for (size_t e2 = 0; e2 < H.evTime.size(); ++e2) {
-            // first step whose currTime = dt * (step + 1) reaches the event
-            // time (SimpleSynHandler delivers events with time <= currTime)
-            double t = H.evTime[e2];
-            double g = std::ceil(t / clock_dt) - 3.0;
-            uint64_t s = g > 0 ? (uint64_t)g : 0;
-            while (!(t <= clock_dt * (double)(s + 1))) ++s;
-            evStep[e2] = (uint32_t)std::min<uint64_t>(s, 0xffffffffu);
+            evStep[e2] = deliveryStep(H.evTime[e2], clock_dt);
             evAct[e2] = (float)(H.evW[e2] / clock_dt);
         }
         if (!types.empty())
@@ -1387,6 +1571,7 @@ int hs_batch_process(HsBatch* b, uint32_t nsteps) {
     if (!b) return berr(HS_EINVAL, "null batch");
     if (!b->reinited) return berr(HS_ESTATE, "reinit before process");
     if (nsteps == 0) return HS_OK;
+    if (int rc = flushRuntimeEvents(b)) return rc;
     const uint32_t K = b->stepsPerLaunch;
     if (b->evUsed >= 1024) {
         // fold the timings recorded so far, so that a long-running caller
@@ -2012,6 +2197,26 @@ int hs_batch_read_spikes(HsBatch* b, uint32_t* cell, uint32_t* gen, double* time
 // keep the old one) and the external channels' own field
 // (ChanCommon::vSetModulation, biophysics/ChanCommon.cpp:46-49), as an
 // Adaptor (signeur/Adaptor.cpp) writes it from a chemical model each step.
+int hs_batch_push_events(HsBatch* b, const uint32_t* cell, const uint32_t* syn, const double* time,
+                         const double* weight, uint32_t n) {
+    if (!b) return berr(HS_EINVAL, "null batch");
+    if (n == 0) return HS_OK;
+    if (!cell || !syn || !time || !weight) return berr(HS_EINVAL, "null argument");
+    for (uint32_t i = 0; i < n; ++i) {
+        if (cell[i] >= b->nCells) return berr(HS_EINVAL, "event cell out of range");
+        if (syn[i] >= b->plans[cell[i]].S) return berr(HS_EINVAL, "event SynChan index out of range");
+        if (std::isnan(time[i])) return berr(HS_EINVAL, "event time is NaN");
+    }
+    const bool fp64 = b->precision == HS_PREC_FP64;
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t k = fp64 ? b->synBase[cell[i]] + syn[i] : (uint32_t)b->mh.synGlobal[cell[i]][syn[i]];
+        b->pendSyn.push_back(k);
+        b->pendTime.push_back(time[i]);
+        b->pendW.push_back(weight[i]);
+    }
+    return HS_OK;
+}
+
 int hs_batch_set_modulation(HsBatch* b, int kind, const uint32_t* cell, const uint32_t* index, const double* value,
                             uint32_t n) {
     if (!b || (n && (!cell || !index || !value))) return berr(HS_EINVAL, "null argument");

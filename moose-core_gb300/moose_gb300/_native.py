@@ -82,6 +82,7 @@ def load(build_if_missing=True):
         "hs_batch_idle": (i32, [vp, pi]),
         "hs_batch_poll": (i32, [vp, u32, u32, pd, C.POINTER(u64), pu]),
         "hs_batch_set_inject_at": (i32, [vp, pu, pu, pd, u32]),
+        "hs_batch_push_events": (i32, [vp, pu, pu, pd, pd, u32]),
         "hs_batch_read_spike_counts": (i32, [vp, pu, u32]),
         "hs_batch_read_cell_spikes": (i32, [vp, u32, u32, pu, pd, u32, pu]),
     }

@@ -158,6 +158,21 @@ class Batch:
         _native.check(_native.load().hs_batch_set_inject_at(self._h, c.ctypes.data_as(pu), m.ctypes.data_as(pu),
                                                             v.ctypes.data_as(C.POINTER(C.c_double)), len(v)))
 
+    def push_events(self, cells, syn, time, weight):
+        """Queue synaptic events at run time (SimpleSynHandler::addSpike):
+        event e reaches SynChan syn[e] of cell cells[e] at time[e] (spike
+        time + synapse delay) with weight[e]; delivered from the next
+        process(), dropped by reinit()."""
+        c = np.ascontiguousarray(np.atleast_1d(cells), np.uint32)
+        k = np.ascontiguousarray(np.atleast_1d(syn), np.uint32)
+        t = np.ascontiguousarray(np.atleast_1d(time), np.float64)
+        w = np.ascontiguousarray(np.atleast_1d(weight), np.float64)
+        if not (len(c) == len(k) == len(t) == len(w)):
+            raise ValueError("cells, syn, time and weight differ in length")
+        pu, pd = C.POINTER(C.c_uint32), C.POINTER(C.c_double)
+        _native.check(_native.load().hs_batch_push_events(self._h, c.ctypes.data_as(pu), k.ctypes.data_as(pu),
+                                                          t.ctypes.data_as(pd), w.ctypes.data_as(pd), len(t)))
+
     def spikes(self):
         L = _native.load()
         n = C.c_uint32()
