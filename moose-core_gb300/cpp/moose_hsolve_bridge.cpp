@@ -52,6 +52,7 @@
 #include "hsolve/HSolveActive.h"
 #include "hsolve/HSolve.h"
 #include "hsolve/HSolveUtils.h"
+#include "biophysics/SymCompartment.h"
 #include "shell/Neutral.h"
 
 #include "moose_gb300.h"
@@ -60,7 +61,7 @@ namespace moose_gb300_bridge {
 
 // Storage behind one HsCellDesc: every array the description points into.
 struct HsCellDescStore {
-    std::vector<int32_t> parent;
+    std::vector<int32_t> parent, link;
     std::vector<double> Ra, Rm, Cm, Em, initVm, Vm, inject;
     std::vector<uint32_t> leak_compt;
     std::vector<double> leak_Ek, leak_Gk;
@@ -169,6 +170,31 @@ int fillCellDesc(const HSolve& hs, HsCellDescStore& out, std::string& err) {
     out.parent.assign(N, -1);
     for (uint32_t i = 0; i < N; ++i)
         for (unsigned int c : tree[i].children) out.parent[c] = (int32_t)i;
+    // the message each compartment hangs on: HSolveUtils::children takes the
+    // parent's axial, distalOut and cylinderOut targets (in that order), and
+    // HSolveUtils::adjacent puts the parent between them by the link's kind.
+    // The compartments are zombies by now (ZombieCompartment has no
+    // distalOut/cylinderOut Finfo), but a zombie swap keeps the element's
+    // messages, so they are read with SymCompartment's own Finfos; only
+    // targets that are the node's children in tree_ count.
+    out.link.assign(N, HS_LINK_AXIAL);
+    {
+        const Cinfo* sym = SymCompartment::initCinfo();
+        const Finfo* byKind[] = {nullptr, sym->findFinfo("distalOut"), sym->findFinfo("cylinderOut")};
+        for (uint32_t i = 0; i < N; ++i) {
+            if (tree[i].children.empty()) continue;
+            vector<Id> axial;
+            HSolveUtils::targets(cid[i], "axial", axial);
+            for (int k = HS_LINK_CYLINDER; k >= HS_LINK_DISTAL; --k) {
+                vector<Id> t;
+                if (byKind[k]) cid[i].element()->getNeighbors(t, byKind[k]);
+                for (unsigned int c : tree[i].children)
+                    if (std::find(t.begin(), t.end(), cid[c]) != t.end()) out.link[c] = k;
+            }
+            for (unsigned int c : tree[i].children)
+                if (std::find(axial.begin(), axial.end(), cid[c]) != axial.end()) out.link[c] = HS_LINK_AXIAL;
+        }
+    }
     const vector<double>& V = S::V(hs);
     for (uint32_t i = 0; i < N; ++i) {
         out.Ra.push_back(tree[i].Ra);
@@ -488,6 +514,7 @@ int fillCellDesc(const HSolve& hs, HsCellDescStore& out, std::string& err) {
     HsCellDesc& d = out.desc;
     d.n_compt = N;
     d.parent = ptr(out.parent);
+    d.link = ptr(out.link);
     d.Ra = ptr(out.Ra);
     d.Rm = ptr(out.Rm);
     d.Cm = ptr(out.Cm);

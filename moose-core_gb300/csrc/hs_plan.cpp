@@ -13,8 +13,14 @@ namespace hsg {
 namespace {
 
 struct Adj {
-    std::vector<uint32_t> off, idx;   // children CSR, increasing child index
+    // children CSR in HSolveUtils::children order: by link kind (axial,
+    // distal/sphere, cylinder), increasing child index within a kind;
+    // grp[k] = the first entry of kind k+1 in each node's list
+    std::vector<uint32_t> off, idx;
+    std::vector<uint32_t> grp;     // 2 per node: ends of the axial and distal runs
 };
+
+int linkOf(const HsCellDesc& d, uint32_t i) { return d.link ? d.link[i] : HS_LINK_AXIAL; }
 
 Adj childrenOf(const HsCellDesc& d) {
     Adj a;
@@ -24,22 +30,37 @@ Adj childrenOf(const HsCellDesc& d) {
         if (d.parent[i] >= 0) a.off[d.parent[i] + 1]++;
     for (uint32_t i = 0; i < n; ++i) a.off[i + 1] += a.off[i];
     a.idx.resize(a.off[n]);
+    a.grp.assign(2 * (size_t)n, 0);
     std::vector<uint32_t> fill(n, 0);
-    for (uint32_t i = 0; i < n; ++i)
-        if (d.parent[i] >= 0) {
-            uint32_t p = (uint32_t)d.parent[i];
-            a.idx[a.off[p] + fill[p]++] = i;
-        }
+    for (int kind = HS_LINK_AXIAL; kind <= HS_LINK_CYLINDER; ++kind) {
+        for (uint32_t i = 0; i < n; ++i)
+            if (d.parent[i] >= 0 && linkOf(d, i) == kind) {
+                uint32_t p = (uint32_t)d.parent[i];
+                a.idx[a.off[p] + fill[p]++] = i;
+            }
+        if (kind < HS_LINK_CYLINDER)
+            for (uint32_t p = 0; p < n; ++p) a.grp[2 * p + kind] = a.off[p] + fill[p];
+    }
     return a;
 }
 
-// HSolveUtils::adjacent (hsolve/HSolveUtils.cpp:16-36): axial targets
-// (children, message order) then raxial targets (the parent), minus `exclude`.
+// HSolveUtils::adjacent (hsolve/HSolveUtils.cpp:36-45): axial targets (the
+// axial children, message order), raxial targets (the parent of an axial
+// link), distalOut targets (distal/sphere children), proximalOut targets
+// (the parent of a SymCompartment link), cylinderOut targets (cylinder
+// children), minus `exclude`.
 void adjacent(const HsCellDesc& d, const Adj& ch, uint32_t c, int64_t exclude,
               std::vector<int64_t>& out) {
-    for (uint32_t k = ch.off[c]; k < ch.off[c + 1]; ++k)
+    const bool hasParent = d.parent[c] >= 0 && (int64_t)d.parent[c] != exclude;
+    const bool axialUp = linkOf(d, c) == HS_LINK_AXIAL;
+    const uint32_t e0 = ch.grp[2 * c], e1 = ch.grp[2 * c + 1];
+    for (uint32_t k = ch.off[c]; k < ch.off[c + 1]; ++k) {
+        if (k == e0 && hasParent && axialUp) out.push_back(d.parent[c]);
+        if (k == e1 && hasParent && !axialUp) out.push_back(d.parent[c]);
         if ((int64_t)ch.idx[k] != exclude) out.push_back(ch.idx[k]);
-    if (d.parent[c] >= 0 && (int64_t)d.parent[c] != exclude) out.push_back(d.parent[c]);
+    }
+    const uint32_t end = ch.off[c + 1];
+    if (hasParent && ((axialUp && e0 == end) || (!axialUp && e1 == end))) out.push_back(d.parent[c]);
 }
 
 // HSolvePassive::walkTree (hsolve/HSolvePassive.cpp:45-98): from the seed,
@@ -160,6 +181,7 @@ bool buildPlan(const HsCellDesc& d, uint32_t seed, double dt, CellPlan& P, std::
     for (uint32_t i = 0; i < d.n_compt; ++i) {
         if (d.parent[i] >= (int32_t)d.n_compt || d.parent[i] == (int32_t)i || d.parent[i] < -1)
             return fail("bad parent index");
+        if (d.link && (d.link[i] < HS_LINK_AXIAL || d.link[i] > HS_LINK_CYLINDER)) return fail("bad link kind");
         if (!(d.Ra[i] != 0.0) || !(d.Rm[i] != 0.0)) return fail("Ra and Rm must be non-zero");
     }
     for (uint32_t g = 0; g < d.n_gate; ++g)

@@ -64,7 +64,11 @@ _DESC_FIELDS = [
     ("n_stim", C.c_uint32), ("stim_compt", _pu), ("stim_step", _pu), ("stim_value", _pd),
     ("n_dif", C.c_uint32), ("dif_kind", _pi), ("difpar", _pd),
     ("n_dmsg", C.c_uint32), ("dmsg_kind", _pi), ("dmsg_src", _pu), ("dmsg_dst", _pu),
+    ("link", _pi),
 ]
+
+# how a compartment hangs on its parent (include/moose_gb300.h HS_LINK_*)
+HS_LINK_AXIAL, HS_LINK_DISTAL, HS_LINK_CYLINDER = 0, 1, 2
 
 # tick-1 external calcium objects (include/moose_gb300.h HS_DIF_*, HS_DMSG_*)
 HS_DIF_SHELL, HS_DIF_BUFFER, HS_DIF_PUMP = 0, 1, 2
@@ -109,7 +113,10 @@ _ARRAYS = {
     "stim_compt": _U32, "stim_step": _U32, "stim_value": _F64,
     "dif_kind": _I32, "difpar": _F64,
     "dmsg_kind": _I32, "dmsg_src": _U32, "dmsg_dst": _U32,
+    "link": _I32,
 }
+# per-compartment arrays that may be left empty (NULL in the description)
+_OPTIONAL = {"link"}
 _COUNTS = {
     "n_compt": "parent", "n_leak": "leak_compt", "n_chan": "chan_compt",
     "n_pool": "pool_compt", "n_chan2d": "c2d_compt", "n_syn": "syn_compt",
@@ -150,7 +157,7 @@ class CellModel:
         return len(self.parent)
 
     def validate(self):
-        groups = {"parent": ("Ra", "Rm", "Cm", "Em", "initVm", "Vm", "inject")}
+        groups = {"parent": ("Ra", "Rm", "Cm", "Em", "initVm", "Vm", "inject", "link")}
         for first in _COUNTS.values():
             if first != "parent":
                 prefix = first.split("_")[0] + "_"
@@ -158,6 +165,8 @@ class CellModel:
         for first, members in groups.items():
             n = len(getattr(self, first))
             for name in members:
+                if name in _OPTIONAL and len(getattr(self, name)) == 0:
+                    continue
                 if len(getattr(self, name)) != n:
                     raise ValueError("array %s has length %d, expected %d"
                                      % (name, len(getattr(self, name)), n))
@@ -166,7 +175,18 @@ class CellModel:
                                                                     HS_DIF_NPAR * len(self.dif_kind)))
 
     def desc(self):
-        """Build an ``HsCellDesc`` pointing into this model's arrays."""
+        """Build an ``HsCellDesc`` pointing into this model's arrays.
+
+        A model whose SymCompartments are joined by sibling messages (a
+        GENESIS ``*symmetric`` cell with a branch point, ``meta["sibling_links"]``)
+        is refused: the reference HSolve's tree walk follows the sibling
+        messages' ``distalOut`` (``hsolve/HSolveUtils.cpp:36-45``) and never
+        ends, so there is no reference setup to reproduce."""
+        links = self.meta.get("sibling_links")
+        if links is not None and len(links):
+            raise ValueError("SymCompartments joined by sibling messages (%d links, e.g. compartments %d and %d): "
+                             "the reference HSolve cannot set this cell up (its tree walk follows them)"
+                             % (len(links), links[0][0], links[0][1]))
         self.validate()
         d = HsCellDesc()
         keep = []

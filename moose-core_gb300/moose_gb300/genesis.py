@@ -18,7 +18,7 @@ values and coordinates come out bit for bit:
     starts with ``*`` is read as a command, as in the reference), ``*``
     commands, data lines;
   * ``readScript`` (``:220-306``): ``*cartesian``/``*polar``,
-    ``*relative``/``*absolute``, ``*asymmetric``, ``*set_global`` /
+    ``*relative``/``*absolute``, ``*symmetric``/``*asymmetric``, ``*set_global`` /
     ``*set_compt_param`` RM RA CM EREST_ACT ELEAK, ``*start_cell``,
     ``*double_endpoint``/``*double_endpoint_off``, ``*makeproto``;
   * ``readData`` (``:308-375``): coordinates in um (polar: r, theta and phi
@@ -41,9 +41,25 @@ from the CaConc's thick, length and diameter (``CaConcBase::zombify``,
 ``updateDimensions``, ``CaConcBase.cpp:259-269, 347-391``), i.e. the
 prototype's geometry, not the compartment's.
 
-Not supported (ValueError): ``*symmetric`` (SymCompartment),
-``*compt`` (compartment prototypes), grafted cells (``*start_cell path``),
-``addmsg`` wiring other than IkOut->current and concOut->concen/concen2.
+Symmetric cells (``*symmetric``): the compartments are SymCompartments,
+joined to their parent by a ``distal`` -> ``proximal`` message and, as
+``ReadCell.cpp:501-510`` does, to every object the parent's ``distalOut``
+already reaches (its earlier children and its own siblings) by ``sibling``
+messages.  HSolve reads a SymCompartment exactly as a Compartment (same
+fields, same matrix: ``HSolve.cpp:505-513``, ``HSolvePassive.cpp:100-165``),
+so an unbranched symmetric cell solves to the same numbers as the
+asymmetric one.  A ``sibling`` message carries ``distalOut``, which
+``HSolveUtils::adjacent`` (``HSolveUtils.cpp:36-45``) follows, so the
+reference's tree walk (``HSolvePassive::walkTree``) never ends on a cell
+with sibling messages; such a model is loaded with its sibling links in
+``meta["sibling_links"]`` and ``CellModel.desc()`` refuses it (ValueError)
+instead of describing a tree the reference cannot set up.  A symmetric
+compartment on a non-symmetric parent is rejected (ValueError): ReadCell's
+``distal`` message needs a SymCompartment at both ends.
+
+Not supported (ValueError): ``*compt`` (compartment prototypes), grafted
+cells (``*start_cell path``), ``addmsg`` wiring other than IkOut->current
+and concOut->concen/concen2.
 """
 import math
 import re
@@ -129,7 +145,7 @@ def _tokens(line):
 
 class _Compt:
     __slots__ = ("name", "parent", "x0", "y0", "z0", "x", "y", "z", "d", "length", "Rm", "Ra", "Cm",
-                 "initVm", "Em", "objs")
+                 "initVm", "Em", "objs", "sym", "distal", "sibs")
 
 
 class ReadCell:
@@ -140,7 +156,7 @@ class ReadCell:
         self.RM, self.CM, self.RA = 10.0, 0.01, 1.0
         self.EREST_ACT, self.ELEAK = -0.065, -0.065
         self.erest_flag = self.eleak_flag = 0
-        self.polar = self.relative = self.double_endpoint = 0
+        self.polar = self.relative = self.double_endpoint = self.symmetric = 0
         self.compts = []
         self.by_name = {}
         self.last = None
@@ -196,9 +212,9 @@ class ReadCell:
         elif c == "*absolute":
             self.relative = 0
         elif c == "*symmetric":
-            raise ValueError("*symmetric (SymCompartment) cells are not supported")
+            self.symmetric = 1
         elif c == "*asymmetric":
-            pass
+            self.symmetric = 0
         elif c in ("*set_global", "*set_compt_param"):
             if len(argv) != 3:
                 self._warn("bad line")
@@ -282,6 +298,11 @@ class ReadCell:
             raise ValueError("line %d: a second compartment named %s" % (self.line_num, name))
         c = _Compt()
         c.name, c.parent, c.objs = name, pa, []
+        c.sym, c.distal, c.sibs = bool(self.symmetric), [], []
+        if pa is not None and c.sym and not self.compts[pa].sym:
+            raise ValueError("line %d: symmetric compartment %s on the non-symmetric parent %s (ReadCell's "
+                             "distal -> proximal message needs a SymCompartment at both ends)"
+                             % (self.line_num, name, self.compts[pa].name))
         idx = len(self.compts)
         self.compts.append(c)
         self.by_name[name] = idx
@@ -301,6 +322,16 @@ class ReadCell:
                     z0 += pz
             dx, dy, dz = x - x0, y - y0, z - z0
             length = math.sqrt(dx * dx + dy * dy + dz * dz)
+            if c.sym:
+                # ReadCell: the parent's distalOut targets before this child
+                # (its children and its siblings) become siblings, then the
+                # distal -> proximal message, then the sibling messages
+                # (both ends send distalOut)
+                c.sibs = list(p.distal)
+                p.distal.append(idx)
+                for q in c.sibs:
+                    c.distal.append(q)
+                    self.compts[q].distal.append(idx)
         else:
             length = math.sqrt(x * x + y * y + z * z)
         surf = calc_surf(length, d)
@@ -543,5 +574,7 @@ def load_p(path, library, seed=0):
               "coords": f64([(c.x0, c.y0, c.z0, c.x, c.y, c.z) for c in cs]).reshape(-1, 6),
               "chan_name": [o[0] for c in cs for o in c.objs if isinstance(o[1], HHChannelProto)],
               "pool_diameter": f64(pool["d"]), "pool_length": f64(pool["L"]), "pool_thick": f64(pool["thick"]),
+              "classes": ["SymCompartment" if c.sym else "Compartment" for c in cs],
+              "sibling_links": [(i, q) for i, c in enumerate(cs) for q in c.sibs],
               "warnings": rc.warnings})
     return m

@@ -219,8 +219,15 @@ static double ca_process(CaConcStruct* s, double activation) {
 }
 
 /* ------------------------------------------------------------------ */
-/* adjacency: children (axial, increasing child index) then parent (raxial) */
-typedef struct { uint32_t* off; uint32_t* idx; } Adj;
+/* Adjacency (HSolveUtils::adjacent, hsolve/HSolveUtils.cpp:36-45): axial
+ * targets (axial children), raxial (the parent of an axial link), distalOut
+ * (distal/sphere children), proximalOut (the parent of a SymCompartment
+ * link), cylinderOut (cylinder children).  Children are kept in
+ * HSolveUtils::children order (hsolve/HSolveUtils.cpp:47-53): by link kind,
+ * increasing child index within a kind; e0/e1 end the axial and distal runs. */
+typedef struct { uint32_t* off; uint32_t* idx; uint32_t* grp; } Adj;
+
+static int link_of(const HsCellDesc* d, uint32_t i) { return d->link ? d->link[i] : HS_LINK_AXIAL; }
 
 static Adj build_children(const HsCellDesc* d) {
     Adj a;
@@ -228,20 +235,31 @@ static Adj build_children(const HsCellDesc* d) {
     a.off = (uint32_t*)xcalloc(n + 1, sizeof(uint32_t));
     for (uint32_t i = 0; i < n; i++) if (d->parent[i] >= 0) a.off[d->parent[i] + 1]++;
     for (uint32_t i = 0; i < n; i++) a.off[i + 1] += a.off[i];
-    a.idx = (uint32_t*)xcalloc(a.off[n], sizeof(uint32_t));
-    uint32_t* fill = (uint32_t*)xcalloc(n, sizeof(uint32_t));
-    for (uint32_t i = 0; i < n; i++) if (d->parent[i] >= 0) {
-        uint32_t p = (uint32_t)d->parent[i];
-        a.idx[a.off[p] + fill[p]++] = i;
+    a.idx = (uint32_t*)xcalloc(a.off[n] + 1, sizeof(uint32_t));
+    a.grp = (uint32_t*)xcalloc(2 * (size_t)n + 1, sizeof(uint32_t));
+    uint32_t* fill = (uint32_t*)xcalloc(n + 1, sizeof(uint32_t));
+    for (int kind = HS_LINK_AXIAL; kind <= HS_LINK_CYLINDER; kind++) {
+        for (uint32_t i = 0; i < n; i++) if (d->parent[i] >= 0 && link_of(d, i) == kind) {
+            uint32_t p = (uint32_t)d->parent[i];
+            a.idx[a.off[p] + fill[p]++] = i;
+        }
+        if (kind < HS_LINK_CYLINDER)
+            for (uint32_t p = 0; p < n; p++) a.grp[2 * p + kind] = a.off[p] + fill[p];
     }
     free(fill);
     return a;
 }
 
 static void adjacent(const HsCellDesc* d, const Adj* ch, uint32_t c, int64_t exclude, ivec* ret) {
-    for (uint32_t k = ch->off[c]; k < ch->off[c + 1]; k++)
+    int has_parent = d->parent[c] >= 0 && (int64_t)d->parent[c] != exclude;
+    int axial_up = link_of(d, c) == HS_LINK_AXIAL;
+    uint32_t e0 = ch->grp[2 * c], e1 = ch->grp[2 * c + 1], end = ch->off[c + 1];
+    for (uint32_t k = ch->off[c]; k < end; k++) {
+        if (k == e0 && has_parent && axial_up) ipush(ret, d->parent[c]);
+        if (k == e1 && has_parent && !axial_up) ipush(ret, d->parent[c]);
         if ((int64_t)ch->idx[k] != exclude) ipush(ret, ch->idx[k]);
-    if (d->parent[c] >= 0 && (int64_t)d->parent[c] != exclude) ipush(ret, d->parent[c]);
+    }
+    if (has_parent && ((axial_up && e0 == end) || (!axial_up && e1 == end))) ipush(ret, d->parent[c]);
 }
 
 /* HSolvePassive::walkTree (hsolve/HSolvePassive.cpp:45-98) */
@@ -903,10 +921,12 @@ OrcCell* orc_create(const HsCellDesc* d, uint32_t seed, double dt, char* err, ui
     if (!d || d->n_compt == 0) FAIL("empty cell");
     if (seed >= d->n_compt) FAIL("seed out of range");
     if (!(dt > 0)) FAIL("dt must be positive");
-    for (uint32_t i = 0; i < d->n_compt; i++)
+    for (uint32_t i = 0; i < d->n_compt; i++) {
         if (d->parent[i] >= (int32_t)d->n_compt || d->parent[i] == (int32_t)i) FAIL("bad parent index");
+        if (d->link && (d->link[i] < HS_LINK_AXIAL || d->link[i] > HS_LINK_CYLINDER)) FAIL("bad link kind");
+    }
     Adj ch = build_children(d);
-    if (walkTree(c, &ch, seed) != 0) { free(ch.off); free(ch.idx); FAIL("compartment graph is not a tree"); }
+    if (walkTree(c, &ch, seed) != 0) { free(ch.off); free(ch.idx); free(ch.grp); FAIL("compartment graph is not a tree"); }
     uint32_t n = c->nCompt;
     c->hinesOf = (uint32_t*)xcalloc(d->n_compt, sizeof(uint32_t));
     for (uint32_t i = 0; i < d->n_compt; i++) c->hinesOf[i] = UINT32_MAX;
@@ -946,7 +966,7 @@ OrcCell* orc_create(const HsCellDesc* d, uint32_t seed, double dt, char* err, ui
         c->Ra[ic] = d->Ra[m]; c->Rm[ic] = d->Rm[m]; c->Cm[ic] = d->Cm[m];
         c->Em[ic] = d->Em[m]; c->initVm[ic] = d->initVm[m];
     }
-    free(ch.off); free(ch.idx);
+    free(ch.off); free(ch.idx); free(ch.grp);
     hines_setup(c);
 
     /* readHHChannels (hsolve/HSolveActiveSetup.cpp:162-235) */

@@ -14,7 +14,8 @@
    spherical soma (length 0), ``*double_endpoint`` lines, ``*set_global`` /
    ``*set_compt_param`` changes part way, EREST_ACT / ELEAK flags, the ``.``
    parent, RA/RM/CM and Ra/Rm/Cm overrides, absolute (negative) densities,
-   ``//`` and ``/* */`` comments, blank lines and tabs.
+   ``//`` and ``/* */`` comments, blank lines and tabs; and an unbranched
+   ``*symmetric`` cable (SymCompartments, each compartment's class saved).
 3. Each file loaded by the reference ``moose.loadModel`` (``ReadCell``):
    every compartment (creation order: name, parent, Ra, Rm, Cm, Em, initVm,
    diameter, length, coordinates), every channel (compartment, name, Gbar,
@@ -188,6 +189,18 @@ def synth_p(seed, n, header, chans, polar=False, relative=True, double_every=0, 
     return "\n".join(out) + "\n"
 
 
+def chain_p(seed, n, header, chans):
+    """A .p file: a soma and an unbranched dendrite of n - 1 compartments."""
+    rng = np.random.default_rng(seed)
+    out = ["// synthetic GENESIS cable, seed %d" % seed] + header + ["*start_cell"]
+    out.append("soma none 18 0 0 18  " + chans(0, rng))
+    for i in range(1, n):
+        v = rng.uniform(3.0, 12.0) * np.array([1.0, rng.uniform(-0.3, 0.3), rng.uniform(-0.3, 0.3)])
+        par = "." if i > 1 and rng.random() < 0.5 else ("soma" if i == 1 else "d%d" % (i - 1))
+        out.append("d%d %s %.5g %.5g %.5g %.4g  %s" % (i, par, v[0], v[1], v[2], rng.uniform(0.8, 2.5), chans(i, rng)))
+    return "\n".join(out) + "\n"
+
+
 def _chans_hh(i, rng):
     return "Na 1200 K 360"
 
@@ -217,6 +230,10 @@ def fixtures():
         "spherical_soma": synth_p(23, 40, ["*relative", "*cartesian", "*set_global EREST_ACT -0.07",
                                            "*set_global ELEAK -0.06"], _chans_hh, spherical_soma=True,
                                   double_every=11),
+        # SymCompartments (distal -> proximal messages; unbranched, so no
+        # sibling messages, which the reference's tree walk cannot take)
+        "symmetric_cable": chain_p(24, 45, ["*relative", "*cartesian", "*symmetric", "*set_global RM 1.5",
+                                            "*set_global RA 1.2"], _chans_full),
     }
 
 
@@ -238,8 +255,10 @@ def make():
         names = [c.name for c in cs]
         idx = {c: i for i, c in enumerate(names)}
         out[name + "/names"] = np.array(names)
-        out[name + "/parent"] = np.array([idx[c.neighbors["raxial"][0].name] if len(c.neighbors["raxial"]) else -1
-                                          for c in cs], np.int32)
+        # the parent: the raxial source (Compartment) or the proximal end (SymCompartment)
+        up = [c.neighbors["proximalOut"] if c.className == "SymCompartment" else c.neighbors["raxial"] for c in cs]
+        out[name + "/parent"] = np.array([idx[u[0].name] if len(u) else -1 for u in up], np.int32)
+        out[name + "/classes"] = np.array([c.className for c in cs])
         for f in ("Ra", "Rm", "Cm", "Em", "initVm", "diameter", "length", "x0", "y0", "z0", "x", "y", "z"):
             out[name + "/" + f] = np.array([getattr(c, f) for c in cs], np.float64)
         chans = []

@@ -34,6 +34,7 @@ def path(name):
 def test_compartments_bit_exact(name):
     m = genesis.load_p(path(name), LIB)
     assert m.meta["names"] == list(Z[name + "/names"])
+    assert m.meta["classes"] == list(Z[name + "/classes"])
     assert np.array_equal(m.parent, Z[name + "/parent"])
     for f in ("Ra", "Rm", "Cm", "Em", "initVm"):
         assert np.array_equal(getattr(m, f), Z[name + "/" + f]), f
@@ -79,13 +80,47 @@ def test_oracle_on_loaded_cell_matches_reference_hsolve(name):
 
 
 def test_unsupported_forms_are_rejected(tmp_path):
-    for body in ("*symmetric\n*start_cell\nsoma none 10 0 0 10\n",
-                 "*compt /library/proto\nsoma none 10 0 0 10\n",
-                 "*start_cell /other/cell\nsoma none 10 0 0 10\n"):
+    for body in ("*compt /library/proto\nsoma none 10 0 0 10\n",
+                 "*start_cell /other/cell\nsoma none 10 0 0 10\n",
+                 # a SymCompartment on a Compartment: no distal -> proximal message
+                 "soma none 10 0 0 10\n*symmetric\nd1 soma 10 0 0 2\n"):
         p = tmp_path / "x.p"
         p.write_text(body)
         with pytest.raises(ValueError):
             genesis.load_p(str(p), LIB)
+
+
+def test_symmetric_cable_solves_as_the_asymmetric_one():
+    """HSolve reads a SymCompartment as a Compartment: the unbranched
+    symmetric cable is the asymmetric cable's model, array for array."""
+    text = open(path("symmetric_cable")).read()
+    sym = genesis.ReadCell(LIB).read(text)
+    asym = genesis.ReadCell(LIB).read(text.replace("*symmetric", "*asymmetric"))
+    assert all(c.sym for c in sym.compts) and not any(c.sym for c in asym.compts)
+    a = genesis.load_p(path("symmetric_cable"), LIB)
+    import tempfile
+    with tempfile.NamedTemporaryFile("w", suffix=".p", delete=False) as f:
+        f.write(text.replace("*symmetric", "*asymmetric"))
+    b = genesis.load_p(f.name, LIB)
+    os.unlink(f.name)
+    for k in ("parent", "Ra", "Rm", "Cm", "Em", "initVm", "chan_compt", "chan_Gbar", "pool_B"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+
+
+def test_symmetric_branch_has_the_sibling_messages_of_readcell(tmp_path):
+    """ReadCell joins a symmetric child to everything its parent's
+    distalOut reaches -- earlier children and the parent's own siblings --
+    by sibling messages, which the reference's tree walk follows without
+    end; the model keeps the links and refuses to be described."""
+    p = tmp_path / "b.p"
+    p.write_text("*symmetric\nsoma none 20 0 0 20\nd1 soma 10 0 0 2\nd2 d1 10 0 0 2\n"
+                 "b1 d1 0 10 0 1.5\nb2 b1 0 10 0 1.5\nd3 d2 10 0 0 2\n")
+    m = genesis.load_p(str(p), LIB)
+    # b1 joins its brother d2; b2 joins its uncle d2; d3 joins what d2's
+    # distalOut reaches by then: its brother b1 and b1's child b2
+    assert sorted(m.meta["sibling_links"]) == [(3, 2), (4, 2), (5, 3), (5, 4)]
+    with pytest.raises(ValueError, match="sibling"):
+        m.desc()
 
 
 def test_comment_block_line_starting_with_star_is_a_command(tmp_path):
