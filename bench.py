@@ -165,14 +165,17 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def _traffic_from_profiles():
-    """DRAM bytes per stepping launch per compartment-step from the committed
-    ncu summary, if there is one."""
+def _traffic_from_profiles(layout):
+    """DRAM bytes per compartment-step of the stepping kernel from the
+    committed ncu summary, for the forest layout the batch runs with:
+    "shared" (forests eliminated in shared memory) or "global" (merged small
+    forests eliminated in global memory).  None if there is no figure."""
     path = os.path.join(ROOT, "profiles", "hsForestStepMixed_4096cells.md")
     if not os.path.exists(path):
         return None
+    key = "dram_bytes_per_compartment_step_%s:" % layout
     for line in open(path):
-        if line.startswith("dram_bytes_per_compartment_step:"):
+        if line.startswith(key):
             try:
                 return float(line.split(":", 1)[1])
             except ValueError:
@@ -539,10 +542,13 @@ def run_ours(args, rank, world, cpu_pool):
         peak, peak_kind = _peaks()
         bytes_step, bpc = algorithmic_bytes(cells, HS_PREC_MIXED)
         achieved = bytes_step * spl / (k_ms / 1e3) / 1e9 if k_ms > 0 else None
-        tpc = _traffic_from_profiles()
+        info = b.info()
+        layout = "global" if info["n_shared_forests"] == 0 else "shared"
+        tpc = _traffic_from_profiles(layout)
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if achieved else None,
                 "traffic": tpc * ncomp * spl if tpc else None,
+                "traffic_layout": layout,
                 "kernel": "hsForestStepMixed", "algorithmic_bytes_per_compartment_step": round(bpc, 1),
                 "launch_ms": k_ms, "launches_timed": k_n, "peak_source": peak_kind}
         # plain FP64 drop-in on a sample of the same cells: one HSolve per cell

@@ -514,6 +514,10 @@ int hs_batch_stream(HsBatch* b, void** stream);
 /* Statistics of the packing: compartments, cells, CTAs, launches/step. */
 int hs_batch_info(HsBatch* b, uint64_t* n_compt, uint32_t* n_ctas,
                   uint32_t* threads_per_cta, uint32_t* steps_per_launch);
+/* Mixed batch: how many elimination forests the packing made and how many
+ * of them are eliminated in shared memory (the others in global memory);
+ * 0 and 0 for an FP64 batch. */
+int hs_batch_forests(HsBatch* b, uint32_t* n_forests, uint32_t* n_shared);
 /* Average duration (ms) of the stepping kernel launches timed with CUDA
  * events on the batch's stream since the last call, and their count. */
 int hs_batch_kernel_time(HsBatch* b, double* avg_ms, uint32_t* launches);

@@ -1697,6 +1697,14 @@ int hs_batch_info(HsBatch* b, uint64_t* n_compt, uint32_t* n_ctas, uint32_t* thr
     return HS_OK;
 }
 
+int hs_batch_forests(HsBatch* b, uint32_t* n_forests, uint32_t* n_shared) {
+    if (!b) return berr(HS_EINVAL, "null batch");
+    const bool mixed = b->precision == HS_PREC_MIXED;
+    if (n_forests) *n_forests = mixed ? b->mh.nForests : 0;
+    if (n_shared) *n_shared = mixed ? b->mh.nShared : 0;
+    return HS_OK;
+}
+
 int hs_batch_set_stop_steps(HsBatch* b, const uint64_t* stop, uint32_t n) {
     if (!b || !stop) return berr(HS_EINVAL, "null argument");
     if (b->precision != HS_PREC_MIXED) return berr(HS_ENOTSUP, "stop steps are a mixed-batch feature");

@@ -74,6 +74,7 @@ def load(build_if_missing=True):
         "hs_batch_set_modulation": (i32, [vp, i32, pu, pu, pd, u32]),
         "hs_batch_read_spikes": (i32, [vp, pu, pu, pd, u32, pu]),
         "hs_batch_info": (i32, [vp, C.POINTER(u64), pu, pu, pu]),
+        "hs_batch_forests": (i32, [vp, pu, pu]),
         "hs_batch_stream": (i32, [vp, C.POINTER(vp)]),
         "hs_batch_kernel_time": (i32, [vp, pd, pu]),
         "hs_batch_set_stop_steps": (i32, [vp, C.POINTER(u64), u32]),

@@ -245,7 +245,10 @@ class Batch:
         nc = C.c_uint64()
         ctas, tpc, spl = C.c_uint32(), C.c_uint32(), C.c_uint32()
         _native.check(_native.load().hs_batch_info(self._h, C.byref(nc), C.byref(ctas), C.byref(tpc), C.byref(spl)))
-        return dict(n_compt=nc.value, n_ctas=ctas.value, threads_per_cta=tpc.value, steps_per_launch=spl.value)
+        nf, ns = C.c_uint32(), C.c_uint32()
+        _native.check(_native.load().hs_batch_forests(self._h, C.byref(nf), C.byref(ns)))
+        return dict(n_compt=nc.value, n_ctas=ctas.value, threads_per_cta=tpc.value, steps_per_launch=spl.value,
+                    n_forests=nf.value, n_shared_forests=ns.value)
 
     def kernel_time(self):
         """(average ms per stepping launch, launches) since the last call."""
