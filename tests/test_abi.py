@@ -59,3 +59,12 @@ def test_valid_model_without_gpu_reports_device_error():
         pytest.skip("a GPU is present")
     rc, msg = _create(models.config1_cell(n_cable=5))
     assert rc == HS_EDEVICE
+
+
+def test_empty_batch_is_refused_before_any_device_call():
+    """hs_batch_create with no cells returns HS_EINVAL (checked before the
+    device is touched, so this holds on a machine without a GPU)."""
+    from moose_gb300 import _native
+    from moose_gb300.batch import Batch
+    with pytest.raises(_native.HsError):
+        Batch([], 25e-6)
