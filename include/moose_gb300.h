@@ -405,6 +405,15 @@ typedef struct HsBatchTuning {
                                    hs_batch_sync returns HS_ETIMEOUT until the
                                    next reinit (default 2^24, about 2 s; 0 keeps
                                    the current value) */
+    uint32_t cluster_ctas;      /* mixed: CTAs (SMs) that step each group of
+                                   forests together, as one thread-block
+                                   cluster (0 or 1: one CTA per group, the
+                                   throughput layout; 2..8: a large cell
+                                   assembled by several SMs, for latency).
+                                   With 2 or more every forest is eliminated
+                                   in global memory and may have at most 255
+                                   levels (else HS_ENOTSUP); changing it
+                                   re-lays the batch out. */
 } HsBatchTuning;
 
 int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds,

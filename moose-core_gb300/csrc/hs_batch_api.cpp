@@ -37,6 +37,10 @@ int setLastError(int code, const std::string& msg);
 cudaError_t launchForestStepMixed(const MixBatch& b, const uint32_t* ctaPtr, const uint32_t* ctaForests,
                                   uint32_t nCtas, uint32_t threadsPerCta, uint32_t smemBytes, uint32_t cap,
                                   uint32_t elimWarps, uint32_t nsteps, cudaStream_t st);
+cudaError_t launchForestStepMixedCluster(const MixBatch& b, const uint32_t* ctaPtr, const uint32_t* ctaForests,
+                                         uint32_t nClusters, uint32_t kC, uint32_t threadsPerCta,
+                                         uint32_t smemBytes, uint32_t cap, uint32_t stageCap, uint32_t elimWarps,
+                                         uint32_t nsteps, cudaStream_t st);
 cudaError_t launchBatchReinitMixed(const MixBatch& b, uint32_t nNodes, const double* initVm, const float* c2dX0,
                                    const uint32_t* evStart, cudaStream_t st);
 cudaError_t launchScatterInject(double* const* addr, uint8_t* const* flag, const double* val, uint32_t n,
@@ -138,6 +142,8 @@ struct HsBatch {
     uint32_t threadsPerCta = 128, ctasPerSm = 4, stepsPerLaunch = 100;
     uint32_t forestNodes = 0;    // mixed: forest size limit (0: shared-memory capacity)
     uint32_t maxCtas = 0;        // mixed: CTA limit of the packing (0: one wave)
+    uint32_t clusterCtas = 1;    // mixed: CTAs per forest group (2..8: a thread-block cluster)
+    uint32_t mixStageCap = 0;    // mixed, clusters: largest forest whose OFF/TOPO/PAR rank 0 stages
     uint32_t elimWarps = 4;      // mixed: eliminator warps of the split step (0: no split)
     uint32_t waitRounds = 1u << 24;   // mixed: sleep rounds of one bounded wait (~128 ns each)
     bool useGraph = true;
@@ -231,6 +237,14 @@ cudaError_t launchStep(HsBatch* b, uint32_t k) {
                                    b->threadsPerCta, b->st);
     const uint32_t ew = b->elimWarps && b->threadsPerCta > 32 * b->elimWarps ? b->elimWarps : 0;
     b->mb.waitRounds = b->waitRounds;
+    if (b->clusterCtas > 1) {
+        // every forest is in global memory: twice the eliminator warps, as
+        // the one-CTA serving kernel gives its global forests
+        const uint32_t ce = std::min<uint32_t>(2 * (ew ? ew : 4), std::min<uint32_t>(16, b->threadsPerCta / 64));
+        return launchForestStepMixedCluster(b->mb, b->dCtaPtr, b->dCtaForests, b->nCtas, b->clusterCtas,
+                                            b->threadsPerCta, b->mixSmem, b->mixCap, b->mixStageCap, ce, k,
+                                            b->st);
+    }
     return launchForestStepMixed(b->mb, b->dCtaPtr, b->dCtaForests, b->nCtas, b->threadsPerCta, b->mixSmem,
                                  b->mixCap, ew, k, b->st);
 }
@@ -644,10 +658,20 @@ int buildMixed(HsBatch* b) {
     const uint32_t reserve = (kSmemLevels + kWsLevels) * 4;
     if (perCta < reserve + 8 * kForestNodeBytes) return berr(HS_EINVAL, "too many CTAs per SM");
     uint32_t cap = std::min<uint32_t>(kMaxForestNodes, (perCta - reserve) / kForestNodeBytes) / 8 * 8;
+    // a cluster keeps only D and R (16 B a node) of its forest in rank 0's
+    // shared memory, after the level offsets, counters and barrier word
+    const uint32_t reserveCl = (kSmemLevels + kWsLevels + 4) * 4;
+    if (b->clusterCtas > 1) cap = std::min<uint32_t>(kMaxForestNodes, (perCta - reserveCl) / 16) / 8 * 8;
     if (b->forestNodes) cap = std::min(cap, b->forestNodes / 8 * 8);
     if (cap < 8) return berr(HS_EINVAL, "forest_nodes too small");
     b->mixCap = cap;
     b->mixSmem = (reserve + cap * kForestNodeBytes + 15) / 16 * 16;
+    if (b->clusterCtas > 1) {
+        b->mixSmem = reserveCl + 16 * cap;
+        b->mixStageCap = (b->mixSmem - reserveCl) / kForestNodeBytes / 8 * 8;
+        if (b->threadsPerCta <= 32 * (b->elimWarps ? b->elimWarps : 4))
+            return berr(HS_EINVAL, "cluster_ctas: threads_per_cta must exceed the eliminator warps");
+    }
 
     // 1. star trees
     std::vector<StarTree> trees(nC);
@@ -662,6 +686,10 @@ int buildMixed(HsBatch* b) {
     // larger cells into global forests of up to 65535 nodes
     uint32_t nCtas = std::max<uint32_t>(1, b->nSm * b->ctasPerSm);
     if (b->maxCtas) nCtas = std::min(nCtas, b->maxCtas);
+    // with clusters, a "CTA" of the packing below is a group of clusterCtas
+    // CTAs, and every forest goes to global memory
+    const bool clustered = b->clusterCtas > 1;
+    if (clustered) nCtas = std::max<uint32_t>(1, nCtas / b->clusterCtas);
     std::vector<uint32_t> order(nC);
     for (uint32_t c = 0; c < nC; ++c) order[c] = c;
     std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return trees[x].T > trees[y].T; });
@@ -687,6 +715,8 @@ int buildMixed(HsBatch* b) {
         for (uint32_t c : ctaCells[k]) {      // decreasing size
             const uint32_t T = trees[c].T;
             const bool sh = T <= cap;
+            if (clustered && !sh)
+                return berr(HS_ENOTSUP, "mixed batch: a cell too large for a cluster's shared-memory forest");
             const uint32_t lim = sh ? cap : kMaxForestNodes;
             size_t f = 0;
             while (f < fs.size() && (fs[f].shared != sh || fs[f].nodes + T > lim)) ++f;
@@ -756,6 +786,8 @@ int buildMixed(HsBatch* b) {
         }
         F.nLevels = (uint32_t)(levelPtr.size() - F.level0 - 1);
         if (nodeCT.size() - F.node0 != F.nNodes) return berr(HS_EINVAL, "mixed batch: forest layout failed");
+        if (clustered && F.nLevels > kWsLevels - 1)
+            return berr(HS_ENOTSUP, "mixed batch: a forest stepped by a cluster has more than 255 tree levels");
     }
     const uint32_t nN = (uint32_t)nodeCT.size();
     // 4. per-cell lists: inject entries, stimulus, SpikeGens; model maps
@@ -1414,7 +1446,12 @@ int hs_batch_create(const HsCellDesc* cells, const uint32_t* seeds, uint32_t n_c
         b->maxCtas = tuning->max_ctas;
         if (tuning->elim_warps) b->elimWarps = tuning->elim_warps == 0xFFFFFFFFu ? 0 : tuning->elim_warps;
         if (tuning->wait_rounds) b->waitRounds = tuning->wait_rounds;
+        if (tuning->cluster_ctas) b->clusterCtas = tuning->cluster_ctas;
         b->useGraph = tuning->use_graph != 0;
+    }
+    if (b->clusterCtas > 8 || (b->clusterCtas > 1 && precision != HS_PREC_MIXED)) {
+        hs_batch_destroy(b);
+        return berr(HS_EINVAL, "cluster_ctas: 1..8, mixed precision only");
     }
     const uint32_t maxTpc = precision == HS_PREC_FP64 ? 256 : 1024;
     if (b->threadsPerCta % 32 || b->threadsPerCta == 0 || b->threadsPerCta > maxTpc) {
@@ -1464,8 +1501,13 @@ int hs_batch_tune(HsBatch* b, const HsBatchTuning* t) {
     cudaError_t e = cudaStreamSynchronize(b->st);
     if (e != cudaSuccess) return cerr(e, "batch tune");
     const uint32_t cps = t->ctas_per_sm ? t->ctas_per_sm : b->ctasPerSm;
+    const uint32_t ccl = t->cluster_ctas ? t->cluster_ctas : b->clusterCtas;
+    if (ccl > 8 || (ccl > 1 && b->precision != HS_PREC_MIXED))
+        return berr(HS_EINVAL, "cluster_ctas: 1..8, mixed precision only");
     const bool relayout = b->precision == HS_PREC_MIXED &&
-                          (cps != b->ctasPerSm || t->forest_nodes != b->forestNodes || t->max_ctas != b->maxCtas);
+                          (cps != b->ctasPerSm || t->forest_nodes != b->forestNodes || t->max_ctas != b->maxCtas ||
+                           ccl != b->clusterCtas);
+    b->clusterCtas = ccl;
     b->ctasPerSm = cps;
     b->forestNodes = t->forest_nodes;
     b->maxCtas = t->max_ctas;
@@ -1691,7 +1733,7 @@ int hs_batch_info(HsBatch* b, uint64_t* n_compt, uint32_t* n_ctas, uint32_t* thr
                   uint32_t* steps_per_launch) {
     if (!b) return berr(HS_EINVAL, "null batch");
     if (n_compt) *n_compt = b->nCompt;
-    if (n_ctas) *n_ctas = b->nCtas;
+    if (n_ctas) *n_ctas = b->nCtas * (b->precision == HS_PREC_MIXED ? b->clusterCtas : 1);
     if (threads_per_cta) *threads_per_cta = b->threadsPerCta;
     if (steps_per_launch) *steps_per_launch = b->stepsPerLaunch;
     return HS_OK;

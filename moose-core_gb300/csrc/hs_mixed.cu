@@ -18,6 +18,7 @@
 // 246-401 (the same elimination, tree form), biophysics/HHChannel2D.cpp:327-369,
 // biophysics/SynChan.cpp:200-224, synapse/SimpleSynHandler.cpp:98-113,
 // biophysics/SpikeGen.cpp:202-216.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "hs_mixed.cuh"
@@ -795,6 +796,250 @@ cudaError_t launchScatterInject(double* const* addr, uint8_t* const* flag, const
     if (!n) return cudaSuccess;
     hsScatterInject<<<(n + 255) / 256, 256, 0, st>>>(addr, flag, val, n);
     return cudaGetLastError();
+}
+
+// ---- several SMs per forest: a thread-block cluster -------------------------------
+// For latency: the forests of one cluster of kC CTAs are stepped by all of
+// them together.  A forest's pivots/couplings D and right-hand sides R live
+// in rank 0's shared memory (16 B a node; OFF, TOPO and PAR stay in global
+// memory); every CTA assembles (rank 0's first `elimWarps` warps excepted),
+// writing each node's row into rank 0's D and R through distributed shared
+// memory and adding the per-level completion counts there.  Rank 0's
+// eliminator warps walk the levels as in stepForestWS, then rank 0 alone
+// substitutes back.  The CTAs of the cluster meet at bounded barriers
+// (clusterMeet) twice per step: after assembly and elimination, and after the
+// back substitution (by when rank 0 has also reset the level counters and
+// applied the next step's stimulus).  The arithmetic of every node is
+// that of the one-CTA step, so results are bit-identical.
+
+// This CTA's writes (global and shared) made visible at cluster scope.
+__device__ __forceinline__ void fenceCluster() { asm volatile("fence.acq_rel.cluster;" ::: "memory"); }
+
+// A bounded barrier of the kC CTAs of a cluster on a counter in rank 0's
+// shared memory (`bar`, a distributed shared memory address): each CTA adds
+// 1 and waits for the count of this meeting, `gen` x kC.  Every wait is
+// bounded by b.waitRounds sleeps; after a timeout, or once the batch's error
+// flag is set, a CTA waits no more in this launch (the launch then ends with
+// its results marked invalid, as with waitLevel).
+__device__ __forceinline__ void clusterMeet(const MixBatch& b, uint32_t* bar, uint32_t& gen, uint32_t kC,
+                                            bool& gaveUp) {
+    __syncthreads();
+    ++gen;
+    if (threadIdx.x == 0) {
+        fenceCluster();
+        atomicAdd(bar, 1u);
+        uint32_t rounds = 0;
+        while (!gaveUp && *(volatile const uint32_t*)bar < gen * kC) {
+            ++rounds;
+            if (rounds > b.waitRounds || ((rounds & 1023u) == 0 && *(volatile const uint32_t*)b.err)) {
+                atomicExch(b.err, 1u);
+                gaveUp = true;
+                break;
+            }
+            __nanosleep(64);
+        }
+        fenceCluster();
+    }
+    __syncthreads();
+}
+
+// `nsteps` steps of forest F by the cluster.  E.D and E.R point into rank
+// 0's shared memory (its own, or through distributed shared memory).
+__device__ void stepForestCluster(const MixBatch& b, const MixForest& F, uint32_t f, const Elim& E,
+                                  const uint32_t* lp, uint32_t* done, uint32_t* doneR0, uint32_t* barR0,
+                                  uint32_t& gen, uint32_t rank, uint32_t kC, uint32_t elimWarps, uint32_t nsteps,
+                                  bool& gaveUp) {
+    const uint32_t tid = threadIdx.x, nth = blockDim.x;
+    const uint32_t nE = rank == 0 ? 32 * elimWarps : 0;
+    const bool elim = tid < nE;
+    const uint32_t nAL = nth - 32 * elimWarps;              // assemblers of rank 0
+    const uint32_t ga = rank == 0 ? tid - nE : nAL + (rank - 1) * nth + tid;
+    const uint32_t T = nAL + (kC - 1) * nth;                // assemblers of the cluster
+    const uint32_t gt = rank * nth + tid, GT = kC * nth;     // every thread of the cluster
+    unsigned long long step = b.forestStep[f];
+    const uint32_t k0 = __ldg(b.syn0 + F.node0), k1 = __ldg(b.syn0 + F.node0 + F.nNodes);
+    for (uint32_t k = k0 + gt; k < k1; k += GT) synapseStep(b, k, step);
+    bool waitGaveUp = false;
+    // each step's level counters and stimulus are set before the meeting
+    // that ends the step before it (here, for the first step)
+    if (rank == 0) {
+        for (uint32_t L = tid; L < F.nLevels; L += nth) done[L] = 0;
+        forestStimulus(b, F, step);
+    }
+    clusterMeet(b, barR0, gen, kC, gaveUp);
+    for (uint32_t s = 0; s < nsteps; ++s, ++step) {
+        if (elim) {
+            for (int L = (int)F.nLevels - 1; L >= 0; --L) {
+                const uint32_t b0 = lp[L], e = lp[L + 1];
+                waitLevel(b, &done[L], e - b0, waitGaveUp);
+                fenceCluster();
+                if (2 * (e - b0) <= nE) {
+                    const uint32_t i = b0 + (tid >> 1);
+                    const bool rl = tid & 1u;
+                    const bool on = i < e;
+                    const uint32_t t = on ? E.TOPO[i] : 0u;
+                    const uint32_t c0 = t & 0xFFFF, c1 = c0 + ((t >> 16) & 0xFF);
+                    double* const A = rl ? E.R : E.D;
+                    double x = on ? A[i] : 1.0;
+                    for (uint32_t c = c0; c < c1; ++c) x = fma(-E.OFF[c], A[c], x);
+                    const double ivd = rcpPivot(x);
+                    const double iv = __shfl_sync(0xFFFFFFFFu, ivd, (tid & 31u) & ~1u);
+                    const double y = (rl ? x : (on ? E.OFF[i] : 0.0)) * iv;
+                    if (on) A[i] = y;
+                } else {
+                    for (uint32_t i = b0 + tid; i < e; i += nE) {
+                        const uint32_t t = E.TOPO[i];
+                        const uint32_t c0 = t & 0xFFFF, c1 = c0 + ((t >> 16) & 0xFF);
+                        double d = E.D[i], r = E.R[i];
+                        for (uint32_t c = c0; c < c1; ++c) {
+                            const double oc = E.OFF[c];
+                            d = fma(-oc, E.D[c], d);
+                            r = fma(-oc, E.R[c], r);
+                        }
+                        const double iv = rcpPivot(d);
+                        E.R[i] = r * iv;
+                        E.D[i] = E.OFF[i] * iv;
+                    }
+                }
+                groupSync(1, nE);
+            }
+        } else {
+            for (uint32_t j = ga; j < F.nNodes; j += T) {
+                const uint32_t i = F.nNodes - 1 - j;
+                if (ga < b.nPf && j + T - ga < F.nNodes) {
+                    const uint32_t hi = F.nNodes - (j + T - ga);
+                    prefetchNodes(b, ga, F.node0 + (hi > T ? hi - T : 0), hi > T ? T : hi);
+                }
+                const uint32_t n = F.node0 + i;
+                const uint32_t info = __ldg(b.nodeInfo + n);
+                const unsigned long long stop = b.anyStop ? b.stopStep[__ldg(b.cellOf + n)] : ~0ull;
+                const bool live = step < stop;
+                const bool pending = s > 0 && step - 1 < stop;
+                double d = 1.0, r = 0.0;
+                if (info & kNodeCenter) {
+                    if (live) d = __ldg(b.HS2 + n);
+                } else if (live) {
+                    assembleNode(b, n, info, pending, pending ? E.R[i] : 0.0, step, d, r);
+                } else if (pending) {
+                    updateNode(b, n, info, E.R[i]);
+                }
+                E.D[i] = d;
+                E.R[i] = r;
+                fenceCluster();
+                atomicAdd(doneR0 + (E.TOPO[i] >> 24), 1u);
+            }
+        }
+        clusterMeet(b, barR0, gen, kC, gaveUp);
+        // the previous step's outputs (the update ran in this assembly), the
+        // next step's SynChans, then rank 0 substitutes back
+        if (rank == 0 && s > 0) forestOutputs(b, F, step - 1, tid, nth);
+        if (s + 1 < nsteps)
+            for (uint32_t k = k0 + gt; k < k1; k += GT) synapseStep(b, k, step + 1);
+        if (rank == 0) {
+            __syncthreads();
+            for (uint32_t L = 0; L < F.nLevels; ++L) {
+                const uint32_t e = lp[L + 1];
+                for (uint32_t i = lp[L] + tid; i < e; i += nth) {
+                    const uint32_t p = E.PAR[i];
+                    double vm = E.R[i];
+                    if (p != kNoParent) vm = fma(-E.D[i], E.R[p], vm);
+                    E.R[i] = vm;
+                }
+                __syncthreads();
+            }
+            if (s + 1 < nsteps) {
+                for (uint32_t L = tid; L < F.nLevels; L += nth) done[L] = 0;
+                forestStimulus(b, F, step + 1);
+            }
+        }
+        clusterMeet(b, barR0, gen, kC, gaveUp);
+    }
+    if (rank == 0) finishForest(b, F, f, E, step);
+    clusterMeet(b, barR0, gen, kC, gaveUp);
+}
+
+// Forests of cluster blockIdx.x / kC (ctaPtr/ctaForests per cluster), each
+// of at most `cap` nodes and kWsLevels - 1 levels (the host packs them so).
+// Dynamic shared memory: kSmemLevels level offsets, kWsLevels counters, a
+// barrier counter (4 words), then the forest's D and R (used in rank 0): a
+// forest of at most `stageCap` nodes also gets OFF, TOPO and PAR there
+// (30 B a node, like a one-CTA shared forest), a larger one keeps them in
+// global memory (D and R only, 16 B a node, up to `cap` nodes).
+__global__ void __launch_bounds__(1024, 1) hsForestStepMixedCluster(MixBatch b, const uint32_t* __restrict__ ctaPtr,
+                                                                    const uint32_t* __restrict__ ctaForests,
+                                                                    uint32_t kC, uint32_t cap, uint32_t stageCap,
+                                                                    uint32_t elimWarps, uint32_t nsteps) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t* sLp = reinterpret_cast<uint32_t*>(smem);
+    uint32_t* sDone = sLp + kSmemLevels;
+    uint32_t* sBar = sDone + kWsLevels;
+    double* sArea = reinterpret_cast<double*>(sBar + 4);
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const uint32_t rank = cluster.block_rank();
+    if (threadIdx.x == 0) *sBar = 0;
+    for (uint32_t L = threadIdx.x; L < kWsLevels; L += blockDim.x) sDone[L] = 0;
+    cluster.sync();                                   // rank 0's counters are set before anyone adds
+    uint32_t* doneR0 = cluster.map_shared_rank(sDone, 0);
+    uint32_t* barR0 = cluster.map_shared_rank(sBar, 0);
+    uint32_t gen = 0;
+    bool gaveUp = false;
+    const uint32_t c = blockIdx.x / kC;
+    for (uint32_t k = ctaPtr[c]; k < ctaPtr[c + 1]; ++k) {
+        const MixForest F = b.forests[ctaForests[k]];
+        const uint32_t* lp = b.levelPtr + F.level0;
+        for (uint32_t i = threadIdx.x; i <= F.nLevels; i += blockDim.x) sLp[i] = lp[i];
+        const bool stage = F.nNodes <= stageCap;
+        double* sD = sArea;
+        double* sR = sD + (stage ? stageCap : cap);
+        double* sOff = sR + stageCap;
+        uint32_t* sTopo = reinterpret_cast<uint32_t*>(sOff + stageCap);
+        uint16_t* sPar = reinterpret_cast<uint16_t*>(sTopo + stageCap);
+        Elim E;
+        E.D = cluster.map_shared_rank(sD, 0);
+        E.R = cluster.map_shared_rank(sR, 0);
+        E.OFF = b.off + F.node0;
+        E.TOPO = b.topo + F.node0;
+        E.PAR = b.par + F.node0;
+        if (stage && rank == 0) {
+            for (uint32_t i = threadIdx.x; i < F.nNodes; i += blockDim.x) {
+                sOff[i] = b.off[F.node0 + i];
+                sTopo[i] = b.topo[F.node0 + i];
+                sPar[i] = b.par[F.node0 + i];
+            }
+            E.OFF = sOff;
+            E.TOPO = sTopo;
+            E.PAR = sPar;
+        }
+        __syncthreads();
+        stepForestCluster(b, F, ctaForests[k], E, sLp, sDone, doneR0, barR0, gen, rank, kC, elimWarps, nsteps,
+                          gaveUp);
+    }
+    cluster.sync();                                   // rank 0's shared memory outlives every remote access
+}
+
+// One launch of the cluster kernel: nClusters clusters of kC CTAs.
+cudaError_t launchForestStepMixedCluster(const MixBatch& b, const uint32_t* ctaPtr, const uint32_t* ctaForests,
+                                         uint32_t nClusters, uint32_t kC, uint32_t threadsPerCta,
+                                         uint32_t smemBytes, uint32_t cap, uint32_t stageCap, uint32_t elimWarps,
+                                         uint32_t nsteps, cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(hsForestStepMixedCluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smemBytes);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nClusters * kC);
+    cfg.blockDim = dim3(threadsPerCta);
+    cfg.dynamicSmemBytes = smemBytes;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kC;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, hsForestStepMixedCluster, b, ctaPtr, ctaForests, kC, cap, stageCap, elimWarps,
+                              nsteps);
 }
 
 cudaError_t launchForestStepMixed(const MixBatch& b, const uint32_t* ctaPtr, const uint32_t* ctaForests,

@@ -85,7 +85,7 @@ class HsBatchTuning(C.Structure):
     _fields_ = [("threads_per_cta", C.c_uint32), ("ctas_per_sm", C.c_uint32),
                 ("steps_per_launch", C.c_uint32), ("use_graph", C.c_uint32),
                 ("forest_nodes", C.c_uint32), ("max_ctas", C.c_uint32), ("elim_warps", C.c_uint32),
-                ("wait_rounds", C.c_uint32)]
+                ("wait_rounds", C.c_uint32), ("cluster_ctas", C.c_uint32)]
 
 
 # numpy dtype per array field

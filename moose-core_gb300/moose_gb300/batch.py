@@ -16,7 +16,7 @@ from .abi import HS_PREC_FP64, HsBatchTuning, HsCellDesc
 class Batch:
     def __init__(self, cells, dt, precision=HS_PREC_FP64, seeds=None, threads_per_cta=0,
                  ctas_per_sm=0, steps_per_launch=0, use_graph=True, forest_nodes=0, max_ctas=0, elim_warps=0,
-                 wait_rounds=0):
+                 wait_rounds=0, cluster_ctas=0):
         self.cells = list(cells)
         self.n = len(self.cells)
         descs = (HsCellDesc * self.n)()
@@ -26,7 +26,7 @@ class Batch:
         seeds = np.ascontiguousarray([m.seed for m in self.cells] if seeds is None else seeds, np.uint32)
         self._seeds = seeds
         tun = HsBatchTuning(threads_per_cta, ctas_per_sm, steps_per_launch, 1 if use_graph else 0, forest_nodes,
-                            max_ctas, elim_warps, wait_rounds)
+                            max_ctas, elim_warps, wait_rounds, cluster_ctas)
         h = C.c_void_p()
         _native.check(_native.load().hs_batch_create(descs, seeds.ctypes.data_as(C.POINTER(C.c_uint32)), self.n,
                                                      float(dt), int(precision), C.byref(tun), C.byref(h)))
@@ -46,12 +46,12 @@ class Batch:
             pass
 
     def tune(self, threads_per_cta=0, ctas_per_sm=0, steps_per_launch=0, use_graph=True, forest_nodes=0,
-             max_ctas=0, elim_warps=0, wait_rounds=0):
+             max_ctas=0, elim_warps=0, wait_rounds=0, cluster_ctas=0):
         """New launch shape.  On a mixed batch a new ctas_per_sm or
         forest_nodes rebuilds the layout: reinit (and re-register recording
         and inject targets) before the next process()."""
         t = HsBatchTuning(threads_per_cta, ctas_per_sm, steps_per_launch, 1 if use_graph else 0, forest_nodes,
-                          max_ctas, elim_warps, wait_rounds)
+                          max_ctas, elim_warps, wait_rounds, cluster_ctas)
         _native.check(_native.load().hs_batch_tune(self._h, C.byref(t)))
 
     def reinit(self, dt):
