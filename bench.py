@@ -720,6 +720,9 @@ def main():
     ap.add_argument("--fp64-batch-steps", type=int, default=100)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--serving-only", action="store_true", help="print only the serving measurement")
+    ap.add_argument("--serve-capacity", type=float, default=0.0,
+                    help="with --serving-only: the batch throughput (compartment-steps/s) that sets the "
+                         "sustained rate (0: no sustained run)")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s")
     ap.add_argument("--serve-window", type=float, default=0.5, help="s of arrivals at the offered rate")
     ap.add_argument("--serve-rate-low", type=float, default=10.0, help="a second, low arrival rate")
@@ -744,7 +747,7 @@ def main():
     if args.serving_only:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        print(json.dumps({"serving": run_serving(args)}))
+        print(json.dumps({"serving": run_serving(args, args.serve_capacity or None)}))
         return 0
     # the CPU pool is spawned before the first GPU call
     cpu_pool = None

@@ -157,10 +157,17 @@ class Server:
     need.  At most
     ``max_cohorts`` cohorts run at once (the hardware work queues of the
     context); requests that arrive meanwhile wait and start together as the
-    next cohort.  An admission round makes one cohort per duration class
-    (``duration_classes``: dt-step boundaries): the requests that share a
-    cohort, and so its forests, then end at about the same time, and the
-    kernel skips a forest whose cells have all stopped, which frees its SM.
+    next cohort.  An admission round makes one cohort per class of request
+    present: a duration class (``duration_classes``: dt-step boundaries)
+    crossed with a size class (``size_classes``: compartment-count
+    boundaries).  The requests that share a cohort, and so its forests, then
+    end at about the same time, and the kernel skips a forest whose cells
+    have all stopped, which frees its SM.  And a launch of a cohort lasts as
+    long as its slowest CTA, so a small request is not held to the step time
+    of a large cell admitted beside it.  A cohort of the largest size class
+    gets ``cluster_ctas`` SMs per request (a thread-block cluster assembles
+    each cell, ~20 % less step latency for 5,000-10,000 compartments) while
+    the GPU has that many SMs free.
 
     Cohorts overlap on the GPU only as far as the context's hardware work
     queues allow: call ``configure_work_queues(max_cohorts)`` before CUDA
@@ -168,7 +175,8 @@ class Server:
 
     def __init__(self, dt, budget_bytes=150 * 10**9, chunk=4000, record_stride=40, max_cohort=4096,
                  admit_interval=0.05, dense=True, forest_nodes=7000, max_cohorts=32, sms=152, tuning=None,
-                 clock=time.perf_counter, cohort_factory=None, duration_classes=(16000, 40000)):
+                 clock=time.perf_counter, cohort_factory=None, duration_classes=(16000, 40000),
+                 size_classes=(1000, 4000), cluster_ctas=4):
         self.dt = dt
         self.budget = budget_bytes
         self.chunk = chunk
@@ -183,6 +191,8 @@ class Server:
         self.clock = clock
         self.cohort_factory = cohort_factory or _Cohort
         self.duration_classes = tuple(sorted(duration_classes or ()))
+        self.size_classes = tuple(sorted(size_classes or ()))
+        self.cluster_ctas = int(cluster_ctas or 1)
         self.cohorts = []
         self.waiting = []
         self.results = []
@@ -193,7 +203,9 @@ class Server:
         return sum(c.bytes for c in self.cohorts)
 
     def _class(self, r):
-        return sum(r.n_steps >= b for b in self.duration_classes)
+        """(duration class, size class) of a request."""
+        return (sum(r.n_steps >= b for b in self.duration_classes),
+                sum(r.cell.n_compt >= b for b in self.size_classes))
 
     def _admit(self, now):
         """A cohort of waiting requests of the first waiting request's
@@ -221,7 +233,13 @@ class Server:
         tuning = dict(self.tuning)
         if "max_ctas" not in tuning:
             busy = sum(getattr(c, "ctas", 0) for c in self.cohorts)
-            if busy + len(take) <= self.sms or not self.dense:
+            big = self.size_classes and cls[1] == len(self.size_classes)
+            if big and self.cluster_ctas > 1 and busy + len(take) * self.cluster_ctas <= self.sms:
+                # the largest cells, SMs to spare: a cluster of SMs per
+                # request for the step latency
+                tuning["max_ctas"] = len(take) * self.cluster_ctas
+                tuning["cluster_ctas"] = self.cluster_ctas
+            elif busy + len(take) <= self.sms or not self.dense:
                 # room on the GPU: one CTA (one SM) per request, each runs
                 # as fast as alone
                 tuning["max_ctas"] = len(take)
@@ -246,8 +264,8 @@ class Server:
             progressed = False
             if self.waiting and now - last_admit >= self.admit_interval and len(self.cohorts) < self.max_cohorts:
                 last_admit = now
-                # one cohort per duration class present
-                for _ in range(len(self.duration_classes) + 1):
+                # one cohort per class present
+                for _ in range((len(self.duration_classes) + 1) * (len(self.size_classes) + 1)):
                     if not self.waiting or len(self.cohorts) >= self.max_cohorts:
                         break
                     fresh = self._admit(now)

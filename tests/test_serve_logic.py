@@ -21,6 +21,7 @@ class FakeCohort:
 
     def __init__(self, reqs, dt, stride, chunk, now, tuning):
         self.reqs = reqs
+        self.tuning = dict(tuning)
         self.admitted = now
         self.bytes = serve.cohort_overhead(reqs[0].cell) + sum(
             serve.estimate_bytes(r.cell, r.n_steps, stride) for r in reqs)
@@ -109,3 +110,29 @@ def test_a_round_makes_one_cohort_per_duration_class():
     assert len(FakeCohort.created) == 3
     # all three were admitted in the first round
     assert len({c.admitted for c in FakeCohort.created}) == 1
+
+
+def test_a_round_separates_small_and_large_cells():
+    """Requests of one duration but of cells on both sides of a size
+    boundary go to different cohorts, so a small cell is not held to the
+    step time of a large one."""
+    FakeCohort.created = []
+    sizes = [150, 6000, 300, 8000, 2500]
+    reqs = [serve.Request(i, _Cell(n), 4000, arrival=0.0) for i, n in enumerate(sizes)]
+    srv = make_server(chunk=4000, record_stride=40, duration_classes=(16000,), size_classes=(1000, 4000))
+    res = srv.run(reqs, real_time=False)
+    assert sorted(r.rid for r in res) == list(range(len(sizes)))
+    groups = sorted(sorted(r.cell.n_compt for r in c.reqs) for c in FakeCohort.created)
+    assert groups == [[150, 300], [2500], [6000, 8000]]
+
+
+def test_largest_cells_get_clusters_while_sms_are_free():
+    FakeCohort.created = []
+    sizes = [6000, 7000, 200]
+    reqs = [serve.Request(i, _Cell(n), 4000, arrival=0.0) for i, n in enumerate(sizes)]
+    srv = make_server(chunk=4000, record_stride=40, duration_classes=(16000,), size_classes=(1000, 4000),
+                      cluster_ctas=4)
+    srv.run(reqs, real_time=False)
+    tun = {tuple(sorted(r.cell.n_compt for r in c.reqs)): c.tuning for c in FakeCohort.created}
+    assert tun[(6000, 7000)].get("cluster_ctas") == 4 and tun[(6000, 7000)]["max_ctas"] == 8
+    assert "cluster_ctas" not in tun[(200,)]
