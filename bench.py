@@ -418,7 +418,7 @@ def run_config2(args, cpu_pool):
     --config2-steps dt steps, wall-clocked; beside the CPU HSolve restatement
     on the same cells on the host cores."""
     from moose_gb300 import models
-    from moose_gb300.hsolve import HSolve
+    from moose_gb300.hsolve import HSolve, process_group
     n_cells = 256
     sizes, _, _ = models.population_sizes(2, SEED, n_cells)
     kca = models.kca_2d_tables()
@@ -440,19 +440,33 @@ def run_config2(args, cpu_pool):
     for h in hs:
         h.sync()
     wall = time.perf_counter() - t0
+    # the same solvers stepped together, one hs_process_group call (one
+    # launch per cluster size, a CTA or cluster per solver) in place of 256
+    # hs_process calls
+    process_group(hs, 20)
+    for h in hs:
+        h.sync()
+    t0 = time.perf_counter()
+    process_group(hs, args.config2_steps)
+    for h in hs:
+        h.sync()
+    wall_g = time.perf_counter() - t0
     for h in hs:
         h.close()
     ncomp = int(sum(m.n_compt for m in cells))
     out = {"workload": "256 cells, binary branching, 100..1,000 compartments, HH + Ca(HVA) + K(Ca) HHChannel2D + "
                        "CaConc, each its own FP64 drop-in HSolve", "cells": n_cells, "compartments": ncomp,
            "dt_steps": args.config2_steps, "wall_s": wall, "value": ncomp * args.config2_steps / wall,
-           "unit": "compartment-steps/s"}
+           "unit": "compartment-steps/s",
+           "group": {"call": "hs_process_group over the 256 solvers", "wall_s": wall_g,
+                     "value": ncomp * args.config2_steps / wall_g}}
     if cpu_pool is not None:
         tcpu = cpu_pool.step(args.config2_cpu_steps)
         cv = cpu_pool.ncomp * args.config2_cpu_steps / tcpu
         out["cpu_baseline"] = {"value": cv, "unit": "compartment-steps/s", "cores": cpu_pool.workers,
                                "kind": "port", "sample": "all 256 cells x %d dt steps" % args.config2_cpu_steps}
         out["gpu_over_cpu"] = out["value"] / cv
+        out["group"]["gpu_over_cpu"] = out["group"]["value"] / cv
     return out
 
 
@@ -462,7 +476,7 @@ def run_ours(args, rank, world, cpu_pool):
     from moose_gb300 import models
     from moose_gb300.abi import HS_PREC_FP64, HS_PREC_MIXED
     from moose_gb300.batch import Batch
-    from moose_gb300.hsolve import HSolve
+    from moose_gb300.hsolve import HSolve, process_group
     from moose_gb300.perf import algorithmic_bytes
     from moose_gb300.replicas import barrier, job_throughput, max_over_ranks
 
@@ -571,12 +585,22 @@ def run_ours(args, rank, world, cpu_pool):
             for h in hs:
                 h.sync()
             wall = time.perf_counter() - t0
+            process_group(hs, 20)
+            for h in hs:
+                h.sync()
+            t0 = time.perf_counter()
+            process_group(hs, args.dropin_steps)
+            for h in hs:
+                h.sync()
+            wall_g = time.perf_counter() - t0
             nc = sum(cells[i].n_compt for i in ids)
             dv = nc * args.dropin_steps / wall
             dropin = {"value": dv, "unit": "compartment-steps/s",
                       "sample": "%d of %d cells as separate FP64 HSolve instances (one stream each), %d dt steps"
                                 % (len(ids), args.cells, args.dropin_steps),
-                      "mixed_batch_over_fp64_dropin": value / world / dv}
+                      "mixed_batch_over_fp64_dropin": value / world / dv,
+                      "group": {"call": "hs_process_group over the same instances",
+                                "value": nc * args.dropin_steps / wall_g}}
             for h in hs:
                 h.close()
         # the FP64 batch (warp per cell, the drop-in's arithmetic) on the same workload

@@ -264,6 +264,24 @@ int hs_destroy(HsSolver* s);
 int hs_reinit(HsSolver* s, double clock_dt);
 /* nsteps calls of HSolve::process, with tick-1/4 external objects. */
 int hs_process(HsSolver* s, uint32_t nsteps);
+/* CTAs that step the solver's cell: 1 = one CTA; 2..8 = a thread-block
+ * cluster whose CTAs share the channel and matrix-row work while one of them
+ * eliminates (same arithmetic, bit-identical results); 0 (the default) =
+ * by the cell's size (one CTA below 1,024 compartments, then one CTA per
+ * 512 compartments, at most 8).  hs_get_cluster_ctas gives the number in
+ * use.  No reference counterpart: a launch-shape choice. */
+int hs_set_cluster_ctas(HsSolver* s, uint32_t ctas);
+int hs_get_cluster_ctas(HsSolver* s, uint32_t* ctas);
+/* hs_process(solvers[k], nsteps) for every k < n, in one launch per
+ * cluster size: each solver is stepped by its own CTA (or cluster) with the
+ * arithmetic hs_process uses, so the results are bit-identical.  For a Clock
+ * tick that processes many HSolve objects (`scheduling/Clock.cpp:872-921`
+ * calls each one's process in turn): one launch instead of one per solver,
+ * all running at once.  The solvers keep their own streams; the launch is
+ * ordered after the work already queued on each of them, and work queued on
+ * any of them afterwards runs after it.  All solvers must be reinited
+ * (HS_ESTATE) and distinct (HS_EINVAL); otherwise nothing is launched. */
+int hs_process_group(HsSolver* const* solvers, uint32_t n, uint32_t nsteps);
 /* Wait for queued device work of this solver. */
 int hs_sync(HsSolver* s);
 

@@ -50,6 +50,7 @@ struct HsSolver {
     double clockDt = 0;
     bool reinited = false;
     int precision = HS_PREC_FP64;
+    uint32_t clusterCtas = 0;    // CTAs stepping the cell (0: by its size)
     std::vector<double> initVm, injBasal;
     std::vector<uint8_t> injPresent;
     uint32_t* recCompt = nullptr;
@@ -354,6 +355,33 @@ int hs_reinit(HsSolver* s, double clock_dt) {
     return HS_OK;
 }
 
+// CTAs that step a solver's cell: the size rule unless set.  A cell's step
+// on one CTA is bound by one SM's FP64 issue of its channel and matrix-row
+// work (~1 us per step per 2 compartments on GB300); from kClusterRows
+// compartments on, a cluster of up to 8 CTAs shares that work (the
+// elimination, a few dozen levels, stays on one CTA).
+constexpr uint32_t kClusterRows = 1024;
+
+uint32_t stepCtas(const HsSolver* s) {
+    if (s->clusterCtas) return s->clusterCtas;
+    const uint32_t n = s->P.N;
+    if (n < kClusterRows) return 1;
+    return std::min<uint32_t>(8, n / (kClusterRows / 2));
+}
+
+int hs_set_cluster_ctas(HsSolver* s, uint32_t ctas) {
+    if (!s) return setErr(HS_EINVAL, "null solver");
+    if (ctas > 8) return setErr(HS_EINVAL, "cluster_ctas: 0 (by cell size) or 1..8");
+    s->clusterCtas = ctas;
+    return HS_OK;
+}
+
+int hs_get_cluster_ctas(HsSolver* s, uint32_t* out) {
+    if (!s || !out) return setErr(HS_EINVAL, "null argument");
+    *out = stepCtas(s);
+    return HS_OK;
+}
+
 int hs_process(HsSolver* s, uint32_t nsteps) {
     if (!s) return setErr(HS_EINVAL, "null solver");
     if (!s->reinited) return setErr(HS_ESTATE, "reinit before process");
@@ -362,8 +390,70 @@ int hs_process(HsSolver* s, uint32_t nsteps) {
     if (!rc) rc = flushWrites(s);
     if (rc) return rc;
     arenaMoved(s);
-    cudaError_t e = launchStepFp64(s->dc, nsteps, s->st);
+    const uint32_t ctas = stepCtas(s);
+    cudaError_t e = ctas > 1 ? launchStepFp64Cluster(s->dc, ctas, nsteps, s->st)
+                             : launchStepFp64(s->dc, nsteps, s->st);
     if (e != cudaSuccess) return cudaErr(e, "process");
+    return HS_OK;
+}
+
+int hs_process_group(HsSolver* const* solvers, uint32_t n, uint32_t nsteps) {
+    if (n == 0) return HS_OK;
+    if (!solvers) return setErr(HS_EINVAL, "null argument");
+    for (uint32_t k = 0; k < n; ++k) {
+        if (!solvers[k]) return setErr(HS_EINVAL, "null solver");
+        if (!solvers[k]->reinited) return setErr(HS_ESTATE, "reinit before process");
+        for (uint32_t j = 0; j < k; ++j)
+            if (solvers[j] == solvers[k]) return setErr(HS_EINVAL, "a solver appears twice in the group");
+    }
+    if (nsteps == 0) return HS_OK;
+    // members by the CTAs that step them: one launch per class, on the
+    // stream of the class's first member, after the work queued on every
+    // member's stream; every other member's stream then waits for it
+    std::vector<std::vector<uint32_t>> cls(9);
+    for (uint32_t k = 0; k < n; ++k) {
+        HsSolver* s = solvers[k];
+        int rc = flushEvents(s);
+        if (!rc) rc = flushWrites(s);
+        if (rc) return rc;
+        arenaMoved(s);
+        cls[stepCtas(s)].push_back(k);
+    }
+    std::vector<cudaEvent_t> evs;
+    cudaError_t e = cudaSuccess;
+    auto newEvent = [&](cudaEvent_t* ev) {
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) evs.push_back(*ev);
+    };
+    // (the clusters first: they need whole free SM groups)
+    for (uint32_t ctas = 8; ctas >= 1 && e == cudaSuccess; --ctas) {
+        const std::vector<uint32_t>& m = cls[ctas];
+        if (m.empty()) continue;
+        cudaStream_t gst = solvers[m[0]]->st;
+        std::vector<DevCell> cells(m.size());
+        for (size_t k = 0; k < m.size(); ++k) cells[k] = solvers[m[k]]->dc;
+        for (size_t k = 1; k < m.size() && e == cudaSuccess; ++k) {
+            cudaEvent_t ev;
+            newEvent(&ev);
+            if (e == cudaSuccess) e = cudaEventRecord(ev, solvers[m[k]]->st);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(gst, ev, 0);
+        }
+        DevCell* dCells = nullptr;
+        if (e == cudaSuccess) e = cudaMallocAsync(&dCells, m.size() * sizeof(DevCell), gst);
+        // (a copy from pageable memory has read `cells` when it returns)
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dCells, cells.data(), m.size() * sizeof(DevCell), cudaMemcpyHostToDevice, gst);
+        if (e == cudaSuccess) e = launchGroupStepFp64(dCells, (uint32_t)m.size(), ctas, nsteps, gst);
+        if (dCells) cudaFreeAsync(dCells, gst);
+        cudaEvent_t done;
+        newEvent(&done);
+        if (e == cudaSuccess) e = cudaEventRecord(done, gst);
+        for (size_t k = 1; k < m.size() && e == cudaSuccess; ++k)
+            e = cudaStreamWaitEvent(solvers[m[k]]->st, done, 0);
+    }
+    // an event destroyed while still pending is released once it completes
+    for (cudaEvent_t ev : evs) cudaEventDestroy(ev);
+    if (e != cudaSuccess) return cudaErr(e, "process group");
     return HS_OK;
 }
 

@@ -73,6 +73,9 @@ cudaError_t layoutCell(const CellPlan& P, Arena& a, DevCell& c, uint32_t spikeCa
     c.fRunRow = u.put(P.fRunRow);
     c.bRun = u.put(P.bRun);
     c.bRunRow = u.put(P.bRunRow);
+    c.fWaves = P.fWavePtr.empty() ? 0 : (uint32_t)P.fWavePtr.size() - 1;
+    c.fWavePtr = u.put(P.fWavePtr);
+    c.fWaveOps = reinterpret_cast<const int4*>(u.put(P.fWaveOps));
     c.Gbar = u.put(P.Gbar);
     c.Ek = u.put(P.Ek);
     c.Xpow = u.put(P.Xpow);

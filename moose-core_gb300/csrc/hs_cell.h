@@ -45,6 +45,9 @@ cudaError_t layoutCell(const CellPlan& P, Arena& a, DevCell& dc, uint32_t spikeC
 void synConsts(const CellPlan& P, double dt, double* out);
 
 cudaError_t launchStepFp64(const DevCell& c, uint32_t nsteps, cudaStream_t st);
+cudaError_t launchStepFp64Cluster(const DevCell& c, uint32_t ctas, uint32_t nsteps, cudaStream_t st);
+cudaError_t launchGroupStepFp64(const DevCell* cells, uint32_t n, uint32_t ctas, uint32_t nsteps,
+                                cudaStream_t st);
 // The queued field writes of a drop-in solver, one thread each (distinct
 // addresses).
 cudaError_t launchScatterFields(const FieldWrite* w, uint32_t n, cudaStream_t st);

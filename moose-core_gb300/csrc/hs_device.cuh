@@ -38,6 +38,7 @@ struct DevCtl {
 struct DevCell {
     uint32_t N, H, C, G, P, K2, S, SG, nStim;
     uint32_t fLevels, bLevels;
+    uint32_t fWaves;             // forward sweep as waves (0: level programs)
     int caAdvance;
     double dt;                   // clock dt
     // compartments
@@ -51,6 +52,8 @@ struct DevCell {
     const uint32_t *bLevelPtr, *bRows, *bTermPtr;
     const int2* bTerms;
     const uint32_t *fRun, *fRunRow, *bRun, *bRunRow;   // cable runs per level
+    const uint32_t* fWavePtr;
+    const int4* fWaveOps;        // per fused update: {t1, a1, t2, a2}, {l, p, -, -}
     // channels
     double *Gbar, *Ek, *Xpow, *Ypow, *Zpow, *mod, *Gk, *state, *extCa;
     int32_t* instant;

@@ -14,6 +14,7 @@
 // operation in the reference's order, so Vm/Ca are bit-identical to the CPU
 // HSolve wherever no libm call is involved (exp/log only in HHChannel2D and
 // non-integer gate powers).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "../../include/moose_gb300.h"
@@ -372,7 +373,19 @@ __device__ __forceinline__ void levelSync() {
 template <bool WARP>
 __device__ __forceinline__ void eliminate(const DevCell& c, uint32_t tid, uint32_t nth) {
     double* M = c.M;
-    for (uint32_t l = 0; l < c.fLevels; ++l) {
+    // Waves (CellPlan::fWavePtr): the level programs' updates, each wave's
+    // on disjoint entries, so the group shares a wave update by update
+    // instead of walking a row's chain per thread.
+    for (uint32_t w = 0; w < c.fWaves; ++w) {
+        for (uint32_t k = c.fWavePtr[w] + tid; k < c.fWavePtr[w + 1]; k += nth) {
+            const int4 x = c.fWaveOps[2 * k], y = c.fWaveOps[2 * k + 1];
+            const double q = M[y.x] / M[y.y];
+            M[x.x] -= q * M[x.y];
+            if (x.z >= 0) M[x.z] -= q * M[x.w];
+        }
+        levelSync<WARP>();
+    }
+    for (uint32_t l = 0; l < (c.fWaves ? 0u : c.fLevels); ++l) {
         if (const uint32_t run = c.fRun[l]) {
             if (tid == 0) forwardCableRun(c, c.fRunRow[l], run);
             levelSync<WARP>();
@@ -531,6 +544,107 @@ __device__ void stepCell(const DevCell& c, uint32_t nsteps, uint32_t tid, uint32
 
 __global__ void __launch_bounds__(256, 1) hsStepFp64(DevCell c, uint32_t nsteps) {
     stepCell<false>(c, nsteps, threadIdx.x, blockDim.x);
+}
+
+// One cell stepped by a thread-block cluster.  On one SM a large cell's step
+// is bound by the FP64 work of its channels and matrix rows (one SM's FP64
+// pipe; the elimination is a few dozen levels); the cluster's CTAs share
+// that work -- object k goes to thread k of the cluster -- and rank 0 alone
+// eliminates and substitutes back with its CTA, as the one-CTA step does.
+// Every object's arithmetic is unchanged and the phases keep their order,
+// so the results are bit-identical to stepCell.  The hardware cluster
+// barrier (release/acquire at cluster scope) orders the phases; all data
+// stays in the cell's global arena.
+__device__ void stepCellCluster(const DevCell& c, uint32_t nsteps) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const uint32_t rank = cl.block_rank();
+    const uint32_t tid = threadIdx.x, nth = blockDim.x;
+    const uint32_t g = rank * nth + tid, G = cl.num_blocks() * nth;
+    unsigned long long step = c.ctl->nSteps;
+    uint32_t stimPtr = c.ctl->stimPtr, nSpikes = c.ctl->nSpikes, nSamples = c.ctl->nSamples;
+    cl.sync();
+    for (uint32_t s = 0; s < nsteps; ++s, ++step) {
+        const double currTime = c.dt * (double)(step + 1);
+        if (g == 0) {
+            while (stimPtr < c.nStim && c.stimStep[stimPtr] <= step) {
+                uint32_t h = c.stimCompt[stimPtr];
+                c.injPresent[h] = 1;
+                c.injBasal[h] = c.stimValue[stimPtr];
+                ++stimPtr;
+            }
+            if (c.nDif) difProcess(c);
+        }
+        for (uint32_t k = g; k < c.S; k += G) synchanStep(c, k, currTime);
+        for (uint32_t k = g; k < c.K2; k += G) chan2dStep(c, k);
+        cl.sync();
+        for (uint32_t h = g; h < c.H; h += G) c.M[2 * c.N + h] = c.HJ0[h];
+        for (uint32_t ic = g; ic < c.N; ic += G) comptStep(c, ic);
+        cl.sync();
+        if (rank == 0) eliminate<false>(c, tid, nth);
+        cl.sync();
+        for (uint32_t p = g; p < c.P; p += G) poolStep(c, p);
+        cl.sync();
+        if (g == 0 && c.nDif) difSendIk(c);
+        for (uint32_t k = g; k < c.K2; k += G) {
+            c.c2dVm[k] = c.V[c.c2dCompt[k]];
+            if (c.c2dConc1[k] >= 0) c.c2dC1[k] = c.ca[c.c2dConc1[k]];
+            if (c.c2dConc2[k] >= 0) c.c2dC2[k] = c.ca[c.c2dConc2[k]];
+        }
+        if (g == 0) {
+            for (uint32_t k = 0; k < c.SG; ++k) {
+                double V = c.V[c.sgCompt[k]];
+                if (V > c.sgThreshold[k]) {
+                    if ((currTime + c.dt / 2.0) >= (c.sgLast[k] + c.sgRefract[k])) {
+                        if (!(c.sgEdge[k] && c.sgFired[k])) {
+                            if (nSpikes < c.spikeCap) {
+                                c.spikeGen[nSpikes] = k;
+                                c.spikeTime[nSpikes] = currTime;
+                            }
+                            ++nSpikes;
+                            c.sgLast[k] = currTime;
+                            c.sgFired[k] = 1;
+                        }
+                    }
+                } else {
+                    c.sgFired[k] = 0;
+                }
+            }
+        }
+        if (c.nRec && ((step + 1) % c.recStride) == 0) {
+            if (nSamples < c.recCap)
+                for (uint32_t r = g; r < c.nRec; r += G)
+                    c.recBuf[(size_t)nSamples * c.recLd + r] = recValue(c, c.recCompt[r]);
+            ++nSamples;
+        }
+        for (uint32_t ic = g; ic < c.N; ic += G) {
+            c.injVarying[ic] = 0.0;
+            c.ext[2 * ic] = 0.0;
+            c.ext[2 * ic + 1] = 0.0;
+        }
+        cl.sync();
+    }
+    if (g == 0) {
+        c.ctl->nSteps = step;
+        c.ctl->stimPtr = stimPtr;
+        c.ctl->nSpikes = nSpikes;
+        c.ctl->nSamples = nSamples;
+    }
+}
+
+__global__ void __launch_bounds__(256, 1) hsStepFp64Cluster(DevCell c, uint32_t nsteps) {
+    stepCellCluster(c, nsteps);
+}
+
+// Separate drop-in solvers stepped in one launch (hs_process_group): CTA k
+// steps solver k exactly as hsStepFp64 steps it alone; in the cluster form
+// cluster k steps solver k exactly as hsStepFp64Cluster does.
+__global__ void __launch_bounds__(256) hsGroupStepFp64(const DevCell* __restrict__ cells, uint32_t nsteps) {
+    stepCell<false>(cells[blockIdx.x], nsteps, threadIdx.x, blockDim.x);
+}
+
+__global__ void __launch_bounds__(256) hsGroupStepFp64Cluster(const DevCell* __restrict__ cells, uint32_t nsteps) {
+    stepCellCluster(cells[blockIdx.x / cooperative_groups::this_cluster().num_blocks()], nsteps);
 }
 
 // Batched FP64.  A CTA either steps its cells one after the other with all
@@ -732,6 +846,43 @@ cudaError_t launchScatterFields(const FieldWrite* w, uint32_t n, cudaStream_t st
 cudaError_t launchStepFp64(const DevCell& c, uint32_t nsteps, cudaStream_t st) {
     hsStepFp64<<<1, 256, 0, st>>>(c, nsteps);
     return cudaGetLastError();
+}
+
+cudaError_t launchStepFp64Cluster(const DevCell& c, uint32_t ctas, uint32_t nsteps, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = ctas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(ctas);
+    cfg.blockDim = dim3(256);
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, hsStepFp64Cluster, c, nsteps);
+}
+
+// `ctas` CTAs per solver: 1 = one CTA each (no cluster), 2..8 = a cluster each
+cudaError_t launchGroupStepFp64(const DevCell* cells, uint32_t n, uint32_t ctas, uint32_t nsteps,
+                                cudaStream_t st) {
+    if (!n) return cudaSuccess;
+    if (ctas <= 1) {
+        hsGroupStepFp64<<<n, 256, 0, st>>>(cells, nsteps);
+        return cudaGetLastError();
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = ctas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(n * ctas);
+    cfg.blockDim = dim3(256);
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, hsGroupStepFp64Cluster, cells, nsteps);
 }
 
 cudaError_t launchBatchStepFp64(const DevCell* cells, const uint32_t* warpCellPtr,

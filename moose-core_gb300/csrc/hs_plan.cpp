@@ -481,6 +481,73 @@ bool buildPlan(const HsCellDesc& d, uint32_t seed, double dt, CellPlan& P, std::
             P.bRunRow[l] = i0;
             l += len;
         }
+        // Waves of the forward sweep.  A level costs the group stepping the
+        // cell one update chain of its longest row (a quotient and two FP64
+        // operations per update, on a pipe that issues an FP64 warp
+        // instruction every 64 cycles per SM sub-partition); a wave costs
+        // one fused update.  Waves are kept where they are fewer than the
+        // level programs' chained updates (runs of cable rows count one
+        // update per row: their pivot stays in registers).
+        std::vector<FwdPair> fused;
+        std::vector<uint32_t> longestOf(LF, 0);
+        for (uint32_t l = 0; l < LF; ++l) {
+            uint32_t longest = 0;
+            for (uint32_t k = P.fLevelPtr[l]; k < P.fLevelPtr[l + 1]; ++k) {
+                uint32_t chain = 0;
+                for (uint32_t o = P.fOpPtr[k]; o < P.fOpPtr[k + 1]; ++o) {
+                    const FwdOp& a = P.fOps[o];
+                    FwdPair f{a.t, a.a, -1, -1, a.l, a.p, 0, 0};
+                    if (o + 1 < P.fOpPtr[k + 1] && a.t != a.l && a.t != a.p) {
+                        const FwdOp& b = P.fOps[o + 1];
+                        if (b.l == a.l && b.p == a.p) {
+                            f.t2 = b.t;
+                            f.a2 = b.a;
+                            ++o;
+                        }
+                    }
+                    fused.push_back(f);
+                    ++chain;
+                }
+                longest = std::max(longest, chain);
+            }
+            longestOf[l] = longest;
+        }
+        double levelCost = 0;
+        for (uint32_t l = 0; l < LF; ++l) {
+            if (P.fRun[l]) {
+                levelCost += P.fRun[l];
+                l += P.fRun[l] - 1;
+            } else {
+                levelCost += longestOf[l];
+            }
+        }
+        const size_t nEnt = 3 * (size_t)N + H;
+        std::vector<int64_t> lastW(nEnt, -1), lastR(nEnt, -1);
+        std::vector<uint32_t> wave(fused.size());
+        uint32_t nWaves = 0;
+        for (size_t k = 0; k < fused.size(); ++k) {
+            const FwdPair& f = fused[k];
+            const int32_t rd[6] = {f.l, f.p, f.a1, f.t1, f.a2, f.t2};
+            int64_t w = 0;
+            for (int32_t e : rd)
+                if (e >= 0) w = std::max(w, lastW[e] + 1);
+            for (int32_t e : {f.t1, f.t2})
+                if (e >= 0) w = std::max(w, lastR[e] + 1);
+            wave[k] = (uint32_t)w;
+            for (int32_t e : rd)
+                if (e >= 0) lastR[e] = std::max(lastR[e], w);
+            for (int32_t e : {f.t1, f.t2})
+                if (e >= 0) lastW[e] = w;
+            nWaves = std::max(nWaves, (uint32_t)w + 1);
+        }
+        if (nWaves < levelCost) {
+            P.fWavePtr.assign(nWaves + 1, 0);
+            for (uint32_t w : wave) P.fWavePtr[w + 1]++;
+            for (uint32_t w = 0; w < nWaves; ++w) P.fWavePtr[w + 1] += P.fWavePtr[w];
+            P.fWaveOps.resize(fused.size());
+            std::vector<uint32_t> fill(P.fWavePtr.begin(), P.fWavePtr.end() - 1);
+            for (size_t k = 0; k < fused.size(); ++k) P.fWaveOps[fill[wave[k]]++] = fused[k];
+        }
     }
 
     // readHHChannels (hsolve/HSolveActiveSetup.cpp:162-235)

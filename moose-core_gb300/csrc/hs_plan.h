@@ -30,6 +30,11 @@ namespace hsg {
 struct FwdOp {
     int32_t t, l, a, p;
 };
+// Two forward updates that share one quotient: M[t1] -= q * M[a1], then
+// M[t2] -= q * M[a2] (t2 < 0: none), q = M[l] / M[p].
+struct FwdPair {
+    int32_t t1, a1, t2, a2, l, p, pad0, pad1;
+};
 // One back-substitution term `v -= coef * VMid[src]`.
 struct BwdTerm {
     int32_t coef, src;
@@ -75,6 +80,16 @@ struct CellPlan {
     // row; 0 elsewhere.  Per level.
     std::vector<uint32_t> fRun, fRunRow, bRun, bRunRow;
     uint32_t maxLevelWidthF = 0, maxLevelWidthB = 0;
+    // The forward sweep as waves (empty: the level programs are used).  The
+    // updates of the level programs, in their order, with each pair that
+    // shares a quotient fused, are placed in the earliest wave after every
+    // update they depend on: after the last write of each entry they read
+    // or write, and after the last read of each entry they write.  The
+    // updates of a wave touch disjoint entries, so a wave runs in any order
+    // or all at once, and each entry sees the updates of the level programs
+    // in their order: the same operations on the same values.
+    std::vector<uint32_t> fWavePtr;
+    std::vector<FwdPair> fWaveOps;
     // channels (solver order)
     uint32_t C = 0, G = 0;
     std::vector<uint32_t> chanPtr;      // N+1

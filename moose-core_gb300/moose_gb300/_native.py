@@ -36,6 +36,9 @@ def load(build_if_missing=True):
         "hs_destroy": (i32, [vp]),
         "hs_reinit": (i32, [vp, d]),
         "hs_process": (i32, [vp, u32]),
+        "hs_process_group": (i32, [C.POINTER(vp), u32, u32]),
+        "hs_set_cluster_ctas": (i32, [vp, u32]),
+        "hs_get_cluster_ctas": (i32, [vp, C.POINTER(u32)]),
         "hs_sync": (i32, [vp]),
         "hs_set_ca_advance": (i32, [vp, i32]),
         "hs_get_ca_advance": (i32, [vp, pi]),

@@ -154,6 +154,18 @@ class HSolve:
     def process(self, nsteps=1):
         _native.check(_native.load().hs_process(self._h, int(nsteps)))
 
+    @property
+    def cluster_ctas(self):
+        """CTAs stepping the cell (hs_get_cluster_ctas); set 0 for the size
+        rule, 1 for one CTA, 2..8 for a thread-block cluster."""
+        out = C.c_uint32()
+        _native.check(_native.load().hs_get_cluster_ctas(self._h, C.byref(out)))
+        return out.value
+
+    @cluster_ctas.setter
+    def cluster_ctas(self, v):
+        _native.check(_native.load().hs_set_cluster_ctas(self._h, int(v)))
+
     def sync(self):
         _native.check(_native.load().hs_sync(self._h))
 
@@ -278,3 +290,13 @@ class HSolve:
             self._h, syn.ctypes.data_as(C.POINTER(C.c_uint32)),
             time.ctypes.data_as(C.POINTER(C.c_double)),
             weight.ctypes.data_as(C.POINTER(C.c_double)), len(syn)))
+
+
+def process_group(solvers, nsteps):
+    """hs_process(s, nsteps) for every HSolve in `solvers`, in one launch
+    (hs_process_group): bit-identical to stepping each alone."""
+    hs = [s._h for s in solvers]
+    if any(h is None for h in hs):
+        raise ValueError("every HSolve needs its target set")
+    arr = (C.c_void_p * len(hs))(*[h.value if hasattr(h, "value") else h for h in hs])
+    _native.check(_native.load().hs_process_group(arr, len(hs), int(nsteps)))

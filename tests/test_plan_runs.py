@@ -74,3 +74,40 @@ def test_unbranched_tails_on_a_branched_cell(lib):
         rc, (nn, fr, br, fl, bl) = check(lib, m, seed)
         assert rc == 0 and nn == n
         assert fr > 0 and br > 0 and fr < n - 1
+
+
+def waves(L, m, seed):
+    d = m.desc()
+    st = (C.c_uint32 * 4)()
+    L.plan_waves_check.argtypes = [C.POINTER(HsCellDesc), C.c_uint32, C.POINTER(C.c_uint32)]
+    rc = L.plan_waves_check(C.byref(d), seed, st)
+    return rc, list(st)
+
+
+def test_forward_waves_bit_identical(lib):
+    """The forward sweep as waves of fused updates, each wave run last to
+    first, gives M, VMid and V bit-identical to the level programs: random
+    trees (junctions of rank 1 to 6, seeds anywhere), workload-like cells up
+    to 10,000 compartments and a rank-41 star.  Branched cells take waves,
+    the cable keeps its runs."""
+    rng = np.random.default_rng(8)
+    taken = 0
+    for _ in range(40):
+        n = int(rng.integers(2, 900))
+        parent, d, L = models.branched_morphology(rng, n, float(rng.uniform(0.02, 0.9)), int(rng.integers(2, 7)))
+        m = models.active_cell(parent, d, L, gkca=0.0)
+        rc, st = waves(lib, m, int(rng.integers(0, n)))
+        assert rc == 0
+        taken += st[1] > 0
+    assert taken > 20
+    for n in (2000, 10000):
+        parent, d, L = models.branched_morphology(np.random.default_rng(n), n, 0.5, 4)
+        m = models.active_cell(parent, d, L, gkca=0.0)
+        rc, (nn, nw, nf, nl) = waves(lib, m, m.seed)
+        assert rc == 0 and nw > 0 and nw < 2 * nl
+    star = [-1] + [0] * 40 + list(range(1, 41))
+    m = models.active_cell(np.array(star, np.int32), np.full(81, 2e-6), np.full(81, 10e-6), gkca=0.0)
+    rc, st = waves(lib, m, 0)
+    assert rc == 0 and st[1] > 0
+    rc, st = waves(lib, models.config1_cell(), 0)
+    assert rc == 0 and st[1] == 0
