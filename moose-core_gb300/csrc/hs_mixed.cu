@@ -595,7 +595,10 @@ __device__ void stepForestWS(const MixBatch& b, const MixForest& F, uint32_t f, 
                 groupSync(1, nE);
             }
         } else {
-            // assembly, deepest level first (the highest node indices)
+            // assembly, deepest level first (the highest node indices); each
+            // node's info word is loaded one node ahead, which takes the
+            // first of the node's dependent memory round trips off its chain
+            uint32_t infoNext = atid < F.nNodes ? __ldg(b.nodeInfo + F.node0 + F.nNodes - 1 - atid) : 0u;
             for (uint32_t j = atid; j < F.nNodes; j += nA) {
                 const uint32_t i = F.nNodes - 1 - j;
                 if (atid < b.nPf && j + nA - atid < F.nNodes) {
@@ -603,7 +606,8 @@ __device__ void stepForestWS(const MixBatch& b, const MixForest& F, uint32_t f, 
                     prefetchNodes(b, atid, F.node0 + (hi > nA ? hi - nA : 0), hi > nA ? nA : hi);
                 }
                 const uint32_t n = F.node0 + i;
-                const uint32_t info = __ldg(b.nodeInfo + n);
+                const uint32_t info = infoNext;
+                if (j + nA < F.nNodes) infoNext = __ldg(b.nodeInfo + F.node0 + F.nNodes - 1 - (j + nA));
                 const unsigned long long stop = b.anyStop ? b.stopStep[__ldg(b.cellOf + n)] : ~0ull;
                 const bool live = step < stop;
                 const bool pending = s > 0 && step - 1 < stop;
@@ -627,15 +631,50 @@ __device__ void stepForestWS(const MixBatch& b, const MixForest& F, uint32_t f, 
         }
         __syncthreads();
         // back substitution by the whole CTA
-        for (uint32_t L = 0; L < F.nLevels; ++L) {
-            const uint32_t e = lp[L + 1];
-            for (uint32_t i = lp[L] + tid; i < e; i += nth) {
-                const uint32_t p = E.PAR[i];
-                double vm = E.R[i];
-                if (p != kNoParent) vm = fma(-E.D[i], E.R[p], vm);
-                E.R[i] = vm;
+        if (F.shared) {
+            for (uint32_t L = 0; L < F.nLevels; ++L) {
+                const uint32_t e = lp[L + 1];
+                for (uint32_t i = lp[L] + tid; i < e; i += nth) {
+                    const uint32_t p = E.PAR[i];
+                    double vm = E.R[i];
+                    if (p != kNoParent) vm = fma(-E.D[i], E.R[p], vm);
+                    E.R[i] = vm;
+                }
+                __syncthreads();
             }
-            __syncthreads();
+        } else {
+            // in global memory: a thread's first node of the next level has
+            // its parent index, coupling and right-hand side (none of which
+            // this level changes) loaded before the barrier, leaving one
+            // dependent load (the parent's value) per level
+            uint32_t nb = lp[0] + tid, ne = lp[1], pn = 0;
+            double dn = 0.0, rn = 0.0;
+            if (nb < ne) {
+                pn = E.PAR[nb];
+                dn = E.D[nb];
+                rn = E.R[nb];
+            }
+            for (uint32_t L = 0; L < F.nLevels; ++L) {
+                const uint32_t i0 = nb, e = ne, p0 = pn;
+                const double d0 = dn, r0 = rn;
+                if (L + 1 < F.nLevels) {
+                    nb = lp[L + 1] + tid;
+                    ne = lp[L + 2];
+                    if (nb < ne) {
+                        pn = E.PAR[nb];
+                        dn = E.D[nb];
+                        rn = E.R[nb];
+                    }
+                }
+                if (i0 < e) E.R[i0] = p0 != kNoParent ? fma(-d0, E.R[p0], r0) : r0;
+                for (uint32_t i = i0 + nth; i < e; i += nth) {
+                    const uint32_t p = E.PAR[i];
+                    double vm = E.R[i];
+                    if (p != kNoParent) vm = fma(-E.D[i], E.R[p], vm);
+                    E.R[i] = vm;
+                }
+                __syncthreads();
+            }
         }
     }
     finishForest(b, F, f, E, step);
