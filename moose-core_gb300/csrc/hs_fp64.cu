@@ -375,15 +375,50 @@ __device__ __forceinline__ void eliminate(const DevCell& c, uint32_t tid, uint32
     double* M = c.M;
     // Waves (CellPlan::fWavePtr): the level programs' updates, each wave's
     // on disjoint entries, so the group shares a wave update by update
-    // instead of walking a row's chain per thread.
-    for (uint32_t w = 0; w < c.fWaves; ++w) {
-        for (uint32_t k = c.fWavePtr[w] + tid; k < c.fWavePtr[w + 1]; k += nth) {
-            const int4 x = c.fWaveOps[2 * k], y = c.fWaveOps[2 * k + 1];
-            const double q = M[y.x] / M[y.y];
-            M[x.x] -= q * M[x.y];
-            if (x.z >= 0) M[x.z] -= q * M[x.w];
+    // instead of walking a row's chain per thread.  With a whole CTA, a
+    // thread's first update of the next wave (read-only descriptors) is
+    // loaded before the barrier.
+    if (WARP) {
+        for (uint32_t w = 0; w < c.fWaves; ++w) {
+            for (uint32_t k = c.fWavePtr[w] + tid; k < c.fWavePtr[w + 1]; k += nth) {
+                const int4 x = c.fWaveOps[2 * k], y = c.fWaveOps[2 * k + 1];
+                const double q = M[y.x] / M[y.y];
+                M[x.x] -= q * M[x.y];
+                if (x.z >= 0) M[x.z] -= q * M[x.w];
+            }
+            levelSync<WARP>();
         }
-        levelSync<WARP>();
+    } else if (c.fWaves) {
+        uint32_t kb = c.fWavePtr[0] + tid, ke = c.fWavePtr[1];
+        int4 xn = make_int4(0, 0, -1, 0), yn = make_int4(0, 0, 0, 0);
+        if (kb < ke) {
+            xn = c.fWaveOps[2 * kb];
+            yn = c.fWaveOps[2 * kb + 1];
+        }
+        for (uint32_t w = 0; w < c.fWaves; ++w) {
+            const uint32_t k0 = kb, e = ke;
+            const int4 x0 = xn, y0 = yn;
+            if (w + 1 < c.fWaves) {
+                kb = c.fWavePtr[w + 1] + tid;
+                ke = c.fWavePtr[w + 2];
+                if (kb < ke) {
+                    xn = c.fWaveOps[2 * kb];
+                    yn = c.fWaveOps[2 * kb + 1];
+                }
+            }
+            if (k0 < e) {
+                const double q = M[y0.x] / M[y0.y];
+                M[x0.x] -= q * M[x0.y];
+                if (x0.z >= 0) M[x0.z] -= q * M[x0.w];
+            }
+            for (uint32_t k = k0 + nth; k < e; k += nth) {
+                const int4 x = c.fWaveOps[2 * k], y = c.fWaveOps[2 * k + 1];
+                const double q = M[y.x] / M[y.y];
+                M[x.x] -= q * M[x.y];
+                if (x.z >= 0) M[x.z] -= q * M[x.w];
+            }
+            levelSync<WARP>();
+        }
     }
     for (uint32_t l = 0; l < (c.fWaves ? 0u : c.fLevels); ++l) {
         if (const uint32_t run = c.fRun[l]) {
@@ -413,15 +448,73 @@ __device__ __forceinline__ void eliminate(const DevCell& c, uint32_t tid, uint32
         }
         levelSync<WARP>();
     }
+    // Back substitution.  With a whole CTA, a thread's first row of the next
+    // level has its index, right-hand side, diagonal, old V and term range
+    // (none of which this level writes) loaded before the barrier; the level
+    // then waits only on the VMid values its terms read.
     const uint32_t N = c.N;
+    if (WARP) {
+        for (uint32_t l = 0; l < c.bLevels; ++l) {
+            if (const uint32_t run = c.bRun[l]) {
+                if (tid == 0) backwardCableRun(c, c.bRunRow[l], run);
+                levelSync<WARP>();
+                l += run - 1;
+                continue;
+            }
+            for (uint32_t k = c.bLevelPtr[l] + tid; k < c.bLevelPtr[l + 1]; k += nth) {
+                uint32_t i = c.bRows[k];
+                double v = M[N + i];
+                for (uint32_t t = c.bTermPtr[k]; t < c.bTermPtr[k + 1]; ++t) {
+                    int2 term = c.bTerms[t];
+                    v -= M[term.x] * c.VMid[term.y];
+                }
+                v /= M[i];
+                c.VMid[i] = v;
+                c.V[i] = 2 * v - c.V[i];
+            }
+            levelSync<WARP>();
+        }
+        return;
+    }
+    uint32_t nk = 0, ne = 0, ni = 0, nt0 = 0, nt1 = 0;
+    double nr = 0.0, nd = 1.0, nv = 0.0;
+    auto preload = [&](uint32_t l) {
+        nk = c.bLevelPtr[l] + tid;
+        ne = c.bLevelPtr[l + 1];
+        if (nk < ne) {
+            ni = c.bRows[nk];
+            nr = M[N + ni];
+            nd = M[ni];
+            nv = c.V[ni];
+            nt0 = c.bTermPtr[nk];
+            nt1 = c.bTermPtr[nk + 1];
+        }
+    };
+    bool ahead = false;
     for (uint32_t l = 0; l < c.bLevels; ++l) {
         if (const uint32_t run = c.bRun[l]) {
             if (tid == 0) backwardCableRun(c, c.bRunRow[l], run);
             levelSync<WARP>();
             l += run - 1;
+            ahead = false;
             continue;
         }
-        for (uint32_t k = c.bLevelPtr[l] + tid; k < c.bLevelPtr[l + 1]; k += nth) {
+        if (!ahead) preload(l);
+        const uint32_t k0 = nk, e = ne, i0 = ni, t0 = nt0, t1 = nt1;
+        const double r0 = nr, d0 = nd, v0 = nv;
+        ahead = l + 1 < c.bLevels && !c.bRun[l + 1];
+        if (ahead) preload(l + 1);
+        if (k0 < e) {
+            double v = r0;
+            for (uint32_t t = t0; t < t1; ++t) {
+                int2 term = c.bTerms[t];
+                v -= M[term.x] * c.VMid[term.y];
+            }
+            v /= d0;
+            c.VMid[i0] = v;
+            c.V[i0] = 2 * v - v0;
+        }
+        for (uint32_t k = k0 + nth; k < e; k += nth) {
             uint32_t i = c.bRows[k];
             double v = M[N + i];
             for (uint32_t t = c.bTermPtr[k]; t < c.bTermPtr[k + 1]; ++t) {
