@@ -280,7 +280,8 @@ int hs_get_cluster_ctas(HsSolver* s, uint32_t* ctas);
  * all running at once.  The solvers keep their own streams; the launch is
  * ordered after the work already queued on each of them, and work queued on
  * any of them afterwards runs after it.  All solvers must be reinited
- * (HS_ESTATE) and distinct (HS_EINVAL); otherwise nothing is launched. */
+ * (HS_ESTATE), distinct and created on one device (HS_EINVAL); otherwise
+ * nothing is launched. */
 int hs_process_group(HsSolver* const* solvers, uint32_t n, uint32_t nsteps);
 /* Wait for queued device work of this solver. */
 int hs_sync(HsSolver* s);

@@ -403,6 +403,8 @@ int hs_process_group(HsSolver* const* solvers, uint32_t n, uint32_t nsteps) {
     for (uint32_t k = 0; k < n; ++k) {
         if (!solvers[k]) return setErr(HS_EINVAL, "null solver");
         if (!solvers[k]->reinited) return setErr(HS_ESTATE, "reinit before process");
+        if (solvers[k]->device != solvers[0]->device)
+            return setErr(HS_EINVAL, "the solvers of a group must be on one device");
         for (uint32_t j = 0; j < k; ++j)
             if (solvers[j] == solvers[k]) return setErr(HS_EINVAL, "a solver appears twice in the group");
     }
