@@ -641,13 +641,102 @@ __global__ void __launch_bounds__(256, 1) hsStepFp64(DevCell c, uint32_t nsteps)
 
 // One cell stepped by a thread-block cluster.  On one SM a large cell's step
 // is bound by the FP64 work of its channels and matrix rows (one SM's FP64
-// pipe; the elimination is a few dozen levels); the cluster's CTAs share
-// that work -- object k goes to thread k of the cluster -- and rank 0 alone
-// eliminates and substitutes back with its CTA, as the one-CTA step does.
+// pipe); the cluster's CTAs share that work -- object k goes to thread k of
+// the cluster -- and the wide waves and levels of the elimination
+// (eliminateCluster), while rank 0's CTA walks the narrow ones.
 // Every object's arithmetic is unchanged and the phases keep their order,
 // so the results are bit-identical to stepCell.  The hardware cluster
 // barrier (release/acquire at cluster scope) orders the phases; all data
 // stays in the cell's global arena.
+// One fused forward update and one back-substitution row, as eliminate does
+// them.
+__device__ __forceinline__ void waveUpdate(const DevCell& c, double* M, uint32_t k) {
+    const int4 x = c.fWaveOps[2 * k], y = c.fWaveOps[2 * k + 1];
+    const double q = M[y.x] / M[y.y];
+    M[x.x] -= q * M[x.y];
+    if (x.z >= 0) M[x.z] -= q * M[x.w];
+}
+
+__device__ __forceinline__ void backRow(const DevCell& c, const double* M, uint32_t N, uint32_t k) {
+    uint32_t i = c.bRows[k];
+    double v = M[N + i];
+    for (uint32_t t = c.bTermPtr[k]; t < c.bTermPtr[k + 1]; ++t) {
+        int2 term = c.bTerms[t];
+        v -= M[term.x] * c.VMid[term.y];
+    }
+    v /= M[i];
+    c.VMid[i] = v;
+    c.V[i] = 2 * v - c.V[i];
+}
+
+// The elimination of a cell stepped by a cluster.  A forward wave or a
+// back-substitution level of at least kClusterWide updates or rows is
+// shared by all the cluster's CTAs, a cluster barrier after it (and before
+// it, when rank 0 wrote alone since the last one); narrower ones are
+// walked by rank 0's CTA with a CTA barrier, as eliminate walks them.  The
+// updates of a wave, and the rows of a level, are independent, so which
+// thread of which CTA does one changes nothing: bit-identical to
+// eliminate.  Every CTA takes the same branches (they depend on the sizes
+// alone), so all meet at every cluster barrier.  Cells without waves (the
+// cable runs' level programs) and cells below kClusterElimRows compartments
+// are eliminated by rank 0 alone, as eliminate does it: sharing pays from
+// ~4,000 compartments on (one GB300, 8 CTAs: 5,000 compartments 407 -> 378
+// us per step, 10,000: 631 -> 498), and costs below (1,000: 171 -> 190,
+// 2,000: 231 -> 244; the shared waves' cluster barriers and the L2 reads
+// after them outweigh the work they split).
+constexpr uint32_t kClusterWide = 1024;
+constexpr uint32_t kClusterElimRows = 4096;
+
+__device__ void eliminateCluster(const DevCell& c, cooperative_groups::cluster_group& cl, uint32_t rank,
+                                 uint32_t tid, uint32_t nth, uint32_t g, uint32_t G) {
+    if (!c.fWaves || c.N < kClusterElimRows) {
+        if (rank == 0) eliminate<false>(c, tid, nth);
+        return;
+    }
+    double* M = c.M;
+    bool alone = false;      // rank 0 wrote since the last cluster barrier
+    for (uint32_t w = 0; w < c.fWaves; ++w) {
+        const uint32_t b0 = c.fWavePtr[w], e = c.fWavePtr[w + 1];
+        if (e - b0 >= kClusterWide) {
+            if (alone) cl.sync();
+            alone = false;
+            for (uint32_t k = b0 + g; k < e; k += G) waveUpdate(c, M, k);
+            cl.sync();
+        } else {
+            if (rank == 0) {
+                for (uint32_t k = b0 + tid; k < e; k += nth) waveUpdate(c, M, k);
+                __syncthreads();
+            }
+            alone = true;
+        }
+    }
+    const uint32_t N = c.N;
+    for (uint32_t l = 0; l < c.bLevels; ++l) {
+        if (const uint32_t run = c.bRun[l]) {
+            if (rank == 0) {
+                if (tid == 0) backwardCableRun(c, c.bRunRow[l], run);
+                __syncthreads();
+            }
+            alone = true;
+            l += run - 1;
+            continue;
+        }
+        const uint32_t b0 = c.bLevelPtr[l], e = c.bLevelPtr[l + 1];
+        if (e - b0 >= kClusterWide) {
+            if (alone) cl.sync();
+            alone = false;
+            for (uint32_t k = b0 + g; k < e; k += G) backRow(c, M, N, k);
+            cl.sync();
+        } else {
+            if (rank == 0) {
+                for (uint32_t k = b0 + tid; k < e; k += nth) backRow(c, M, N, k);
+                __syncthreads();
+            }
+            alone = true;
+        }
+    }
+}
+
 __device__ void stepCellCluster(const DevCell& c, uint32_t nsteps) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
@@ -674,7 +763,7 @@ __device__ void stepCellCluster(const DevCell& c, uint32_t nsteps) {
         for (uint32_t h = g; h < c.H; h += G) c.M[2 * c.N + h] = c.HJ0[h];
         for (uint32_t ic = g; ic < c.N; ic += G) comptStep(c, ic);
         cl.sync();
-        if (rank == 0) eliminate<false>(c, tid, nth);
+        eliminateCluster(c, cl, rank, tid, nth, g, G);
         cl.sync();
         for (uint32_t p = g; p < c.P; p += G) poolStep(c, p);
         cl.sync();

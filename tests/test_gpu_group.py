@@ -8,7 +8,10 @@ Events pushed and fields written between calls, recording and spikes are
 each solver's own, so a group is bit-identical to the same solvers stepped
 one by one.  A cell stepped by a thread-block cluster (its channel and row
 work shared by the CTAs, the elimination on one) is bit-identical to the
-one-CTA step, and so to the oracle where no libm call is on the path.
+one-CTA step, and so to the oracle where no libm call is on the path;
+from 4,096 compartments on, the cluster also shares the elimination's wide
+waves and levels (5,000- and 4,500-compartment cells below, and the
+20,000-compartment edge case).
 """
 import numpy as np
 import pytest
@@ -146,7 +149,7 @@ def test_cluster_sizes_by_rule():
 @pytest.mark.parametrize("ctas", [2, 3, 5, 8])
 def test_cluster_step_bit_identical_to_one_cta(ctas):
     rng = np.random.default_rng([17, ctas])
-    parent, d, L = models.branched_morphology(rng, 3000, 0.5, 4)
+    parent, d, L = models.branched_morphology(rng, 5000, 0.5, 4)     # wide waves shared by the cluster
     m = models.active_cell(parent, d, L, inject=0.6e-9, n_syn=40, rng=rng, t_end=0.05,
                            kca_tables=models.kca_2d_tables(vdivs=300, cadivs=300), syn_rate=30.0)
     one = _drive([m], False, ctas=1)[0]
@@ -161,7 +164,7 @@ def test_cluster_step_bit_exact_with_oracle():
     """No HHChannel2D (its exp is libm's on the host): the cluster step
     equals the oracle bit for bit, Vm and Ca, every 100 steps."""
     rng = np.random.default_rng(29)
-    parent, d, L = models.branched_morphology(rng, 4000, 0.5, 4)
+    parent, d, L = models.branched_morphology(rng, 4500, 0.5, 4)
     m = models.active_cell(parent, d, L, inject=1.0e-9, gca=10.0, gkca=0.0, n_syn=20, rng=rng,
                            t_end=0.05, syn_rate=40.0)
     for k in list(vars(m)):
