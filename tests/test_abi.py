@@ -68,3 +68,20 @@ def test_empty_batch_is_refused_before_any_device_call():
     from moose_gb300.batch import Batch
     with pytest.raises(_native.HsError):
         Batch([], 25e-6)
+
+
+def test_group_and_cluster_calls_check_their_arguments():
+    """hs_process_group and hs_set/get_cluster_ctas validate on the host
+    (no device call), as every other entry point does."""
+    L = _native.load()
+    assert L.hs_process_group(None, 0, 10) == 0                 # an empty group is a no-op
+    assert L.hs_process_group(None, 2, 10) == HS_EINVAL
+    two = (C.c_void_p * 2)(None, None)
+    assert L.hs_process_group(two, 2, 10) == HS_EINVAL          # null members
+    assert L.hs_set_cluster_ctas(None, 2) == HS_EINVAL
+    out = C.c_uint32()
+    assert L.hs_get_cluster_ctas(None, C.byref(out)) == HS_EINVAL
+    from moose_gb300.hsolve import HSolve, process_group
+    h = HSolve(models.config1_cell(n_cable=5))
+    with pytest.raises(ValueError):
+        process_group([h], 10)                                   # no target set
