@@ -5,7 +5,8 @@ cell files, built the way MOOSE's ``ReadCell`` builds them
 
 The channel library -- MOOSE's ``/library`` of prototype objects that a .p
 file names -- is a dict of the prototype classes below (HHChannelProto,
-HHChannel2DProto, CaConcProto, SpikeGenProto).  A prototype's ``addmsg``
+HHChannel2DProto, CaConcProto, SpikeGenProto, and CompartmentProto for
+``*compt``).  A prototype's ``addmsg``
 strings are GENESIS ``addmsg`` fields (``"src srcField dest destField"``,
 ``.`` the object itself, ``../NAME`` a sibling in the same compartment),
 resolved after each line's channels are made, as
@@ -57,9 +58,24 @@ instead of describing a tree the reference cannot set up.  A symmetric
 compartment on a non-symmetric parent is rejected (ValueError): ReadCell's
 ``distal`` message needs a SymCompartment at both ends.
 
-Not supported (ValueError): ``*compt`` (compartment prototypes), grafted
-cells (``*start_cell path``), ``addmsg`` wiring other than IkOut->current
-and concOut->concen/concen2.
+Compartment prototypes (``*compt <path>``, ``ReadCell.cpp:274-291,
+447-470``): from that line on, each compartment is a copy of the
+prototype (``Shell::doCopy``): its child objects with their own field
+values (a channel's Gbar as set in the prototype, not scaled), the
+messages among them, and its inject; then the line's geometry, passive
+values and channels apply as for a plain compartment, the line's channels
+after the prototype's.  A prototype is a ``CompartmentProto`` in the
+library; ``*compt`` takes it only when the path equals the prototype's
+``Id::path()`` -- ``/library[0]/NAME`` for the library entry ``NAME``
+(``Neutral::path`` puts ``[0]`` on every element but the last, and
+``Id::path`` trims only the last) -- and otherwise warns and keeps the
+previous prototype, as the reference's path check does.
+
+Not supported (ValueError): grafted cells (``*start_cell path``), a
+compartment prototype whose class (Compartment or SymCompartment) differs
+from ``*symmetric``/``*asymmetric`` (ReadCell's messages would not join
+it to its parent), ``addmsg`` wiring other than IkOut->current and
+concOut->concen/concen2.
 """
 import math
 import re
@@ -123,6 +139,29 @@ class SpikeGenProto:
         self.addmsg = list(addmsg)
 
 
+class CompartmentProto:
+    """A compartment prototype for ``*compt``: the copied compartment's
+    children as (name, prototype, fields) in the order of the compartment's
+    messages to them (a channel's ``Gbar``, absolute; a SpikeGen's
+    ``threshold``; a CaConc needs none), the messages among them as
+    (src, srcField, dst, dstField) with IkOut -> current and concOut ->
+    concen/concen2, the compartment's inject, and its class."""
+
+    def __init__(self, children=(), msgs=(), inject=0.0, symmetric=False):
+        self.children = [(n, p, dict(f)) for n, p, f in children]
+        self.msgs = [tuple(m) for m in msgs]
+        self.inject = inject
+        self.symmetric = bool(symmetric)
+
+
+def proto_path(name):
+    """``Id::path()`` of a library entry: every element but the last with
+    its ``[0]`` (``/library[0]/NAME``); a name given as an absolute path is
+    taken as the element's path."""
+    parts = name.strip("/").split("/") if name.startswith("/") else ["library", name]
+    return "/" + "".join(p + "[0]/" for p in parts[:-1]) + parts[-1]
+
+
 def calc_surf(length, dia):
     """calcSurf (ReadCell.cpp:617-626): a sphere when length is 0."""
     return dia * dia * M_PI if length == 0.0 else length * dia * M_PI
@@ -145,7 +184,7 @@ def _tokens(line):
 
 class _Compt:
     __slots__ = ("name", "parent", "x0", "y0", "z0", "x", "y", "z", "d", "length", "Rm", "Ra", "Cm",
-                 "initVm", "Em", "objs", "sym", "distal", "sibs")
+                 "initVm", "Em", "objs", "sym", "distal", "sibs", "inject")
 
 
 class ReadCell:
@@ -157,6 +196,7 @@ class ReadCell:
         self.EREST_ACT, self.ELEAK = -0.065, -0.065
         self.erest_flag = self.eleak_flag = 0
         self.polar = self.relative = self.double_endpoint = self.symmetric = 0
+        self.proto = None
         self.compts = []
         self.by_name = {}
         self.last = None
@@ -234,7 +274,15 @@ class ReadCell:
             if len(argv) != 1:
                 raise ValueError("grafted cells (*start_cell <path>) are not supported")
         elif c == "*compt":
-            raise ValueError("compartment prototypes (*compt) are not supported")
+            if len(argv) != 2:
+                self._warn("bad line")
+                return
+            for key, p in self.lib.items():
+                if isinstance(p, CompartmentProto) and proto_path(key) == argv[1]:
+                    self.proto = p
+                    break
+            else:
+                self._warn("bad path: %s" % argv[1])
         elif c == "*double_endpoint":
             self.double_endpoint = 1
         elif c == "*double_endpoint_off":
@@ -297,8 +345,18 @@ class ReadCell:
         if name in self.by_name:
             raise ValueError("line %d: a second compartment named %s" % (self.line_num, name))
         c = _Compt()
-        c.name, c.parent, c.objs = name, pa, []
+        c.name, c.parent, c.objs, c.inject = name, pa, [], 0.0
         c.sym, c.distal, c.sibs = bool(self.symmetric), [], []
+        if self.proto is not None:
+            if self.proto.symmetric != c.sym:
+                raise ValueError("line %d: a %s prototype under %s" % (
+                    self.line_num, "SymCompartment" if self.proto.symmetric else "Compartment",
+                    "*symmetric" if c.sym else "*asymmetric"))
+            # Shell::doCopy: the children with their values, their messages
+            c.objs = [[n, p, dict(f)] for n, p, f in self.proto.children]
+            for src, sf, dst, df in self.proto.msgs:
+                self._link(c, src, sf, dst, df, "%s %s %s %s" % (src, sf, dst, df))
+            c.inject = self.proto.inject
         if pa is not None and c.sym and not self.compts[pa].sym:
             raise ValueError("line %d: symmetric compartment %s on the non-symmetric parent %s (ReadCell's "
                              "distal -> proximal message needs a SymCompartment at both ends)"
@@ -449,19 +507,26 @@ class ReadCell:
             t = _tokens(s)
             if len(t) != 4:
                 raise ValueError("addmsg '%s': four fields expected" % s)
-            src, sf, dst, df = find(t[0]), t[1], find(t[2]), t[3]
+            src, dst = find(t[0]), find(t[2])
             if src is None or dst is None:
                 continue             # as the reference: a missing end skips the message
-            if sf == "IkOut" and df == "current" and isinstance(src[1], HHChannelProto) \
-                    and isinstance(dst[1], CaConcProto):
-                src[2]["ca_target"] = dst[0]
-            elif sf == "concOut" and df in ("concen", "concen2") and isinstance(src[1], CaConcProto) \
-                    and isinstance(dst[1], (HHChannelProto, HHChannel2DProto)):
-                key = "ca_depend" if isinstance(dst[1], HHChannelProto) else \
-                    ("conc1" if df == "concen" else "conc2")
-                dst[2][key] = src[0]
-            else:
-                raise ValueError("addmsg '%s' is not supported" % s)
+            self._link(c, src[0], t[1], dst[0], t[3], s)
+
+    def _link(self, c, src_name, sf, dst_name, df, text):
+        """A message between two objects of compartment `c`."""
+        here = {x[0]: x for x in c.objs}
+        src, dst = here.get(src_name), here.get(dst_name)
+        if src is None or dst is None:
+            raise ValueError("message '%s': no object %s" % (text, src_name if src is None else dst_name))
+        if sf == "IkOut" and df == "current" and isinstance(src[1], HHChannelProto) \
+                and isinstance(dst[1], CaConcProto):
+            src[2]["ca_target"] = dst[0]
+        elif sf == "concOut" and df in ("concen", "concen2") and isinstance(src[1], CaConcProto) \
+                and isinstance(dst[1], (HHChannelProto, HHChannel2DProto)):
+            key = "ca_depend" if isinstance(dst[1], HHChannelProto) else ("conc1" if df == "concen" else "conc2")
+            dst[2][key] = src[0]
+        else:
+            raise ValueError("addmsg '%s' is not supported" % text)
 
 
 def read_cell(path, library):
@@ -553,7 +618,7 @@ def load_p(path, library, seed=0):
         parent=i32([-1 if c.parent is None else c.parent for c in cs]),
         Ra=f64([c.Ra for c in cs]), Rm=f64([c.Rm for c in cs]), Cm=f64([c.Cm for c in cs]),
         Em=f64([c.Em for c in cs]), initVm=f64([c.initVm for c in cs]), Vm=f64([c.initVm for c in cs]),
-        inject=np.zeros(n),
+        inject=f64([c.inject for c in cs]),
         chan_compt=u32(ch["compt"]), chan_Gbar=f64(ch["Gbar"]), chan_Ek=f64(ch["Ek"]),
         chan_Xpower=f64(ch["Xp"]), chan_Ypower=f64(ch["Yp"]), chan_Zpower=f64(ch["Zp"]),
         chan_xgate=i32(ch["xg"]), chan_ygate=i32(ch["yg"]), chan_zgate=i32(ch["zg"]),

@@ -14,8 +14,12 @@
    spherical soma (length 0), ``*double_endpoint`` lines, ``*set_global`` /
    ``*set_compt_param`` changes part way, EREST_ACT / ELEAK flags, the ``.``
    parent, RA/RM/CM and Ra/Rm/Cm overrides, absolute (negative) densities,
-   ``//`` and ``/* */`` comments, blank lines and tabs; and an unbranched
-   ``*symmetric`` cable (SymCompartments, each compartment's class saved).
+   ``//`` and ``/* */`` comments, blank lines and tabs; an unbranched
+   ``*symmetric`` cable (SymCompartments, each compartment's class saved);
+   and a cell of compartment prototypes (``*compt``: two prototype
+   compartments in ``/library`` with copied channels, a CaConc, their
+   messages and an inject; a ``*compt`` whose path is not the prototype's
+   Id path, which the reference ignores).
 3. Each file loaded by the reference ``moose.loadModel`` (``ReadCell``):
    every compartment (creation order: name, parent, Ra, Rm, Cm, Em, initVm,
    diameter, length, coordinates), every channel (compartment, name, Gbar,
@@ -65,7 +69,13 @@ def _tables(z=None):
 
 def library(z=None):
     """The channel library as moose_gb300.genesis prototypes (tables from
-    the golden file `z` when given)."""
+    the golden file `z` when given), with the compartment prototypes."""
+    lib = _channel_library(z)
+    lib.update(compartment_protos(lib))
+    return lib
+
+
+def _channel_library(z=None):
     V = (models.VMIN, models.VMAX)
     t = _tables(z)
     mA, mB, hA, hB, nA, nB = t["mA"], t["mB"], t["hA"], t["hB"], t["nA"], t["nB"]
@@ -83,6 +93,23 @@ def library(z=None):
                                         addmsg=["../Ca_conc concOut . concen"]),
         "Ca_conc": genesis.CaConcProto(tau=0.02, CaBasal=5e-5, thick=0.1e-6, diameter=2e-6, length=10e-6),
         "spike": genesis.SpikeGenProto(refractT=2e-3, edgeTriggered=1),
+    }
+
+
+def compartment_protos(lib):
+    """Compartment prototypes for ``*compt`` (built in the reference's
+    /library by build_reference_library): children copied from the
+    library with absolute conductances, their messages and an inject."""
+    return {
+        "protoSoma": genesis.CompartmentProto(
+            children=[("K", lib["K"], {"Gbar": 3.1e-7}), ("Na", lib["Na"], {"Gbar": 1.25e-6}),
+                      ("CaHVA", lib["CaHVA"], {"Gbar": 4.5e-9}), ("Ca_conc", lib["Ca_conc"], {}),
+                      ("SK", lib["SK"], {"Gbar": 2.2e-9})],
+            msgs=[("CaHVA", "IkOut", "Ca_conc", "current"), ("Ca_conc", "concOut", "SK", "concen")]),
+        "protoDend": genesis.CompartmentProto(
+            children=[("CaHVA", lib["CaHVA"], {"Gbar": 1.3e-9}), ("Ca_conc", lib["Ca_conc"], {}),
+                      ("K", lib["K"], {"Gbar": 6.5e-8})],
+            msgs=[("CaHVA", "IkOut", "Ca_conc", "current")], inject=4e-12),
     }
 
 
@@ -122,13 +149,31 @@ def build_reference_library(lib):
         elif isinstance(p, genesis.SpikeGenProto):
             ch = moose.SpikeGen(path)
             ch.refractT, ch.edgeTriggered = p.refractT, p.edgeTriggered
+        elif isinstance(p, genesis.CompartmentProto):
+            # children copied from the library entries, in message order
+            pc = moose.SymCompartment(path) if p.symmetric else moose.Compartment(path)
+            pc.inject = p.inject
+            kids = {}
+            for cname, cp, f in p.children:
+                src = next(k for k, v in lib.items() if v is cp)
+                e = moose.element(moose.copy("/library/" + src, pc, cname))
+                for k, v in f.items():
+                    setattr(e, k, v)
+                if isinstance(cp, (genesis.HHChannelProto, genesis.HHChannel2DProto)):
+                    moose.connect(pc, "channel", e, "channel")
+                elif isinstance(cp, genesis.SpikeGenProto):
+                    moose.connect(pc, "VmOut", e, "Vm")
+                kids[cname] = e
+            for s, sf, d, df in p.msgs:
+                moose.connect(kids[s], sf, kids[d], df)
+            continue
         for k, v in enumerate(getattr(p, "addmsg", ())):
             ms = moose.Mstring(path + "/addmsg%d" % (k + 1))
             ms.value = v
 
 
 def synth_p(seed, n, header, chans, polar=False, relative=True, double_every=0, spherical_soma=False,
-            midfile=None, overrides=False):
+            midfile=None, overrides=False, after_soma=()):
     """A .p file: a seeded tree of n compartments below a soma."""
     rng = np.random.default_rng(seed)
     out = ["// synthetic GENESIS cell, seed %d" % seed, "/* header comment", "   spans lines */"]
@@ -136,6 +181,7 @@ def synth_p(seed, n, header, chans, polar=False, relative=True, double_every=0, 
     out.append("*start_cell")
     soma = "soma none 0 0 0 18" if spherical_soma else "soma none 18 0 0 18"
     out.append(soma + "  " + chans(0, rng))
+    out += list(after_soma)
     names, pos = ["soma"], [np.array([0.0, 0.0, 0.0]) if spherical_soma else np.array([18.0, 0.0, 0.0])]
     tips = [0, 0, 0]
     last = 0
@@ -215,6 +261,14 @@ def _chans_full(i, rng):
     return s
 
 
+def _chans_proto(i, rng):
+    """Line channels on top of the prototypes' children (no name twice)."""
+    if i == 0:
+        return "KCa 40 spike 0.0"
+    s = "Na -2e-09" if i % 5 == 2 else "Na %g" % (900 * rng.uniform(0.8, 1.2))
+    return s + (" KCa 30" if i % 3 == 0 else "")
+
+
 def _chans_abs(i, rng):
     return "Na %g K -%g" % (1000.0, 3e-9 * rng.uniform(0.5, 1.5)) + (" spike -0.01" if i == 0 else "")
 
@@ -234,6 +288,13 @@ def fixtures():
         # sibling messages, which the reference's tree walk cannot take)
         "symmetric_cable": chain_p(24, 45, ["*relative", "*cartesian", "*symmetric", "*set_global RM 1.5",
                                             "*set_global RA 1.2"], _chans_full),
+        # compartment prototypes: the soma a copy of protoSoma, the rest of
+        # protoDend; the *compt half way names the prototype by a path that
+        # is not its Id::path, so the reference warns and keeps protoDend
+        "compt_proto": synth_p(25, 36, ["*relative", "*cartesian", "*set_global RM 2.5",
+                                        "*compt /library[0]/protoSoma"], _chans_proto,
+                               after_soma=["*compt /library[0]/protoDend"],
+                               midfile=["*compt /library/protoSoma", "*set_global CM 0.015"]),
     }
 
 

@@ -80,8 +80,11 @@ def test_oracle_on_loaded_cell_matches_reference_hsolve(name):
 
 
 def test_unsupported_forms_are_rejected(tmp_path):
-    for body in ("*compt /library/proto\nsoma none 10 0 0 10\n",
-                 "*start_cell /other/cell\nsoma none 10 0 0 10\n",
+    for body in ("*start_cell /other/cell\nsoma none 10 0 0 10\n",
+                 # a Compartment prototype under *symmetric
+                 "*symmetric\n*compt /library[0]/protoDend\nsoma none 10 0 0 10\n",
+                 # a line channel of the same name as a prototype child
+                 "*compt /library[0]/protoDend\nsoma none 10 0 0 10 K 300\n",
                  # a SymCompartment on a Compartment: no distal -> proximal message
                  "soma none 10 0 0 10\n*symmetric\nd1 soma 10 0 0 2\n"):
         p = tmp_path / "x.p"
@@ -131,3 +134,28 @@ def test_comment_block_line_starting_with_star_is_a_command(tmp_path):
     rc = genesis.read_cell(str(p), LIB)
     assert rc.polar == 1
     assert abs(rc.compts[0].y - 10e-6) < 1e-12
+
+
+def test_compartment_prototype_path_and_copies(tmp_path):
+    """``*compt`` takes a prototype only by its Id::path (``/library[0]/NAME``);
+    any other spelling warns and keeps the previous prototype.  A copy
+    carries the prototype's children (absolute Gbar), their messages and
+    its inject; the line's channels follow them and wire to them."""
+    assert genesis.proto_path("protoDend") == "/library[0]/protoDend"
+    assert genesis.proto_path("/a/b/c") == "/a[0]/b[0]/c"
+    p = tmp_path / "c.p"
+    p.write_text("*compt /library/protoSoma\nsoma none 10 0 0 10\n"
+                 "*compt /library[0]/protoDend\nd1 soma 10 0 0 2 KCa 20\n"
+                 "*compt protoSoma\nd2 d1 10 0 0 2\n")
+    rc = genesis.read_cell(str(p), LIB)
+    assert sum("bad path" in w for w in rc.warnings) == 2
+    soma, d1, d2 = rc.compts
+    assert soma.objs == [] and soma.inject == 0.0
+    assert [o[0] for o in d1.objs] == ["CaHVA", "Ca_conc", "K", "KCa"]
+    assert [o[0] for o in d2.objs] == ["CaHVA", "Ca_conc", "K"]
+    assert d1.inject == d2.inject == LIB["protoDend"].inject
+    assert d1.objs[0][2]["Gbar"] == LIB["protoDend"].children[0][2]["Gbar"]
+    assert d1.objs[0][2]["ca_target"] == "Ca_conc" and d1.objs[3][2]["conc1"] == "Ca_conc"
+    # the copies' dictionaries are their own
+    d1.objs[2][2]["Gbar"] = 0.0
+    assert d2.objs[2][2]["Gbar"] == LIB["protoDend"].children[2][2]["Gbar"]
