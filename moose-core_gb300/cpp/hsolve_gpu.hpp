@@ -122,6 +122,22 @@ public:
     }
     void process(uint32_t nsteps = 1) { check(hs_process(handle(), nsteps)); }
     void sync() { check(hs_sync(handle())); }
+    // The process of every HSolve of a clock tick in one launch
+    // (hs_process_group; the Clock calls them in turn,
+    // scheduling/Clock.cpp:872-921), bit-identical to each process().
+    static void processGroup(const std::vector<HSolve*>& tick, uint32_t nsteps = 1) {
+        std::vector<HsSolver*> s;
+        s.reserve(tick.size());
+        for (HSolve* h : tick) s.push_back(h->handle());
+        check(hs_process_group(s.data(), (uint32_t)s.size(), nsteps));
+    }
+    // CTAs stepping this cell: 0 = by its size, 1 = one, 2..8 = a cluster.
+    void setClusterCtas(uint32_t n) { check(hs_set_cluster_ctas(handle(), n)); }
+    uint32_t getClusterCtas() const {
+        uint32_t n = 0;
+        check(hs_get_cluster_ctas(handle(), &n));
+        return n;
+    }
     uint64_t steps() const {
         uint64_t n = 0;
         check(hs_get_nsteps(handle(), &n));

@@ -1,7 +1,8 @@
 // C entry points over the C++ HSolve mirror (moose-core_gb300/cpp/hsolve_gpu.hpp)
 // for tests/test_cpp_mirror.py: the test hands a cell description to
 // hsolve_cpp_run, which drives it through moose_gb300::HSolve -- field
-// writes, message destinations, process -- and returns Vm and Ca;
+// writes, message destinations, process and the group call -- and returns
+// Vm and Ca;
 // hsolve_cpp_errors checks the error behaviour, which needs no GPU.
 #include <cstring>
 
@@ -34,7 +35,8 @@ extern "C" int hsolve_cpp_run(const HsCellDesc* d, uint32_t seed, double dt, uin
         h.setHHmodulation(1, 0.0);            // ignored: a value <= 0 keeps the old one
         h.setEm(nCompt > 1 ? 1 : 0, -0.07);
         if (nPool) h.iCa(0, 1e-12);
-        h.process(nsteps - nsteps / 2);
+        // the rest through the tick's group call (a group of one here)
+        moose_gb300::HSolve::processGroup({&h}, nsteps - nsteps / 2);
         const std::vector<double> v = h.vm(nCompt);
         const std::vector<double> c = h.ca(nPool);
         for (uint32_t i = 0; i < nCompt; ++i) vmOut[i] = v[i];
