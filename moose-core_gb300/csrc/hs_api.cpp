@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <new>
 #include <string>
 #include <unordered_map>
@@ -39,9 +40,26 @@ namespace hsg {
 int setLastError(int code, const std::string& msg) { return setErr(code, msg); }
 }  // namespace hsg
 
+// The completion of one group launch (hs_process_group), shared by the
+// solvers it stepped until each has ordered its own stream after it.
+struct HsGroupDone {
+    cudaEvent_t ev = nullptr;
+    cudaStream_t st = nullptr;          // the stream the launch ran on
+    ~HsGroupDone() {
+        if (ev) cudaEventDestroy(ev);   // released once it has completed
+    }
+};
+
 struct HsSolver {
     int device = 0;
-    cudaStream_t st = nullptr;
+    cudaStream_t st = nullptr;          // new work goes through stOf()
+    // hs_process_group: the last group launch that stepped this solver on
+    // another stream (work queued here next must wait for it); whether work
+    // was queued on this stream since then (a group launch elsewhere must
+    // wait for it, through evQueued)
+    std::shared_ptr<HsGroupDone> group;
+    bool queued = true;
+    cudaEvent_t evQueued = nullptr;
     CellPlan P;
     Arena arena;
     DevCell dc;
@@ -85,6 +103,18 @@ struct HsSolver {
 
 namespace {
 
+// The solver's stream for new work: it first waits for the group launch
+// that last stepped the solver on another stream, and what it receives
+// must come before the solver's next group launch.
+cudaStream_t stOf(HsSolver* s) {
+    if (s->group) {
+        cudaStreamWaitEvent(s->st, s->group->ev, 0);
+        s->group.reset();
+    }
+    s->queued = true;
+    return s->st;
+}
+
 // ---- field access between process calls ------------------------------------
 // The zombie get/set calls (hsolve/HSolveInterface.cpp) arrive one field at a
 // time, typically many between two steps (a script reading every
@@ -108,7 +138,7 @@ int flushWrites(HsSolver* s) {
     if (n > s->dWritesCap) {
         // no scatter may still read the old list when it is freed
         if (s->dWrites) {
-            cudaError_t e = cudaStreamSynchronize(s->st);
+            cudaError_t e = cudaStreamSynchronize(stOf(s));
             if (e != cudaSuccess) return cudaErr(e, "field write");
             cudaFree(s->dWrites);
         }
@@ -124,8 +154,8 @@ int flushWrites(HsSolver* s) {
     }
     // the pageable source is staged by the copy call itself
     cudaError_t e = cudaMemcpyAsync(s->dWrites, s->writeList.data(), n * sizeof(FieldWrite),
-                                    cudaMemcpyHostToDevice, s->st);
-    if (e == cudaSuccess) e = launchScatterFields(s->dWrites, (uint32_t)n, s->st);
+                                    cudaMemcpyHostToDevice, stOf(s));
+    if (e == cudaSuccess) e = launchScatterFields(s->dWrites, (uint32_t)n, stOf(s));
     if (e != cudaSuccess) return cudaErr(e, "field write");
     s->writes.clear();
     return HS_OK;
@@ -153,8 +183,8 @@ int mirrorPage(HsSolver* s, size_t idx, uint8_t** out) {
         if (rc) return rc;
         const size_t off = idx * kPage, n = std::min(kPage, s->arena.size - off);
         pg.second.resize(n);
-        cudaError_t e = cudaMemcpyAsync(pg.second.data(), s->arena.base + off, n, cudaMemcpyDeviceToHost, s->st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        cudaError_t e = cudaMemcpyAsync(pg.second.data(), s->arena.base + off, n, cudaMemcpyDeviceToHost, stOf(s));
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stOf(s));
         if (e != cudaSuccess) {
             pg.first = 0;
             return cudaErr(e, "field read");
@@ -173,7 +203,7 @@ int flushEvents(HsSolver* s) {
     if (s->pendSyn.empty()) return HS_OK;
     const uint32_t S = s->P.S;
     std::vector<uint32_t> cur(S);
-    cudaError_t e = cudaStreamSynchronize(s->st);
+    cudaError_t e = cudaStreamSynchronize(stOf(s));
     if (e == cudaSuccess)
         e = cudaMemcpy(cur.data(), s->dc.evCur, S * sizeof(uint32_t), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cudaErr(e, "push events");
@@ -201,12 +231,12 @@ int flushEvents(HsSolver* s) {
         if (e != cudaSuccess) return cudaErr(e, "push events");
     }
     e = cudaMemcpyAsync(s->ownIdx, nptr.data(), nptr.size() * sizeof(uint32_t),
-                        cudaMemcpyHostToDevice, s->st);
+                        cudaMemcpyHostToDevice, stOf(s));
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(ev, nt.data(), m * sizeof(double), cudaMemcpyHostToDevice, s->st);
+        e = cudaMemcpyAsync(ev, nt.data(), m * sizeof(double), cudaMemcpyHostToDevice, stOf(s));
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(ev + cap, nw.data(), m * sizeof(double), cudaMemcpyHostToDevice, s->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        e = cudaMemcpyAsync(ev + cap, nw.data(), m * sizeof(double), cudaMemcpyHostToDevice, stOf(s));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stOf(s));
     if (e != cudaSuccess) {
         if (ev != s->ownEv) cudaFree(ev);
         return cudaErr(e, "push events");
@@ -279,18 +309,18 @@ int hs_create(const HsCellDesc* cell, uint32_t seed, double dt, int precision, H
     }
     const uint32_t spikeCap = 1u << 16;
     Arena dry;
-    layoutCell(s->P, dry, s->dc, spikeCap, s->st);
+    layoutCell(s->P, dry, s->dc, spikeCap, stOf(s));
     dry.take<DevCell>(1);
     s->arena.size = dry.used + 256;
     e = cudaMalloc(&s->arena.base, s->arena.size);
-    if (e == cudaSuccess) e = cudaMemsetAsync(s->arena.base, 0, s->arena.size, s->st);
-    if (e == cudaSuccess) e = layoutCell(s->P, s->arena, s->dc, spikeCap, s->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->arena.base, 0, s->arena.size, stOf(s));
+    if (e == cudaSuccess) e = layoutCell(s->P, s->arena, s->dc, spikeCap, stOf(s));
     s->dcDev = s->arena.take<DevCell>(1);
     s->descPtr = s->dc.evPtr;
     s->descCur = s->dc.evCur;
     s->descTime = s->dc.evTime;
     s->descW = s->dc.evW;
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stOf(s));
     if (e != cudaSuccess) {
         int rc = cudaErr(e, "device setup");
         hs_destroy(s);
@@ -308,13 +338,14 @@ int hs_create(const HsCellDesc* cell, uint32_t seed, double dt, int precision, H
 
 int hs_destroy(HsSolver* s) {
     if (!s) return HS_OK;
-    if (s->st) cudaStreamSynchronize(s->st);
+    if (s->st) cudaStreamSynchronize(stOf(s));
     if (s->arena.base) cudaFree(s->arena.base);
     if (s->recCompt) cudaFree(s->recCompt);
     if (s->recBuf) cudaFree(s->recBuf);
     if (s->ownIdx) cudaFree(s->ownIdx);
     if (s->ownEv) cudaFree(s->ownEv);
     if (s->dWrites) cudaFree(s->dWrites);
+    if (s->evQueued) cudaEventDestroy(s->evQueued);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
     return HS_OK;
@@ -344,12 +375,12 @@ int hs_reinit(HsSolver* s, double clock_dt) {
     if (rc) return rc;
     arenaMoved(s);
     cudaError_t e = cudaMemcpyAsync((void*)s->dc.synConst, sc.data(), 5 * (size_t)s->P.S * 8,
-                                    cudaMemcpyHostToDevice, s->st);
+                                    cudaMemcpyHostToDevice, stOf(s));
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(s->dc.initVm, s->initVm.data(), s->P.N * 8, cudaMemcpyHostToDevice, s->st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(s->dcDev, &s->dc, sizeof(DevCell), cudaMemcpyHostToDevice, s->st);
-    if (e == cudaSuccess) e = launchReinitFp64(s->dcDev, 1, s->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        e = cudaMemcpyAsync(s->dc.initVm, s->initVm.data(), s->P.N * 8, cudaMemcpyHostToDevice, stOf(s));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->dcDev, &s->dc, sizeof(DevCell), cudaMemcpyHostToDevice, stOf(s));
+    if (e == cudaSuccess) e = launchReinitFp64(s->dcDev, 1, stOf(s));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stOf(s));
     if (e != cudaSuccess) return cudaErr(e, "reinit");
     s->reinited = true;
     return HS_OK;
@@ -391,8 +422,8 @@ int hs_process(HsSolver* s, uint32_t nsteps) {
     if (rc) return rc;
     arenaMoved(s);
     const uint32_t ctas = stepCtas(s);
-    cudaError_t e = ctas > 1 ? launchStepFp64Cluster(s->dc, ctas, nsteps, s->st)
-                             : launchStepFp64(s->dc, nsteps, s->st);
+    cudaError_t e = ctas > 1 ? launchStepFp64Cluster(s->dc, ctas, nsteps, stOf(s))
+                             : launchStepFp64(s->dc, nsteps, stOf(s));
     if (e != cudaSuccess) return cudaErr(e, "process");
     return HS_OK;
 }
@@ -410,8 +441,8 @@ int hs_process_group(HsSolver* const* solvers, uint32_t n, uint32_t nsteps) {
     }
     if (nsteps == 0) return HS_OK;
     // members by the CTAs that step them: one launch per class, on the
-    // stream of the class's first member, after the work queued on every
-    // member's stream; every other member's stream then waits for it
+    // stream of the class's first member (the clusters first: they need
+    // whole free SM groups)
     std::vector<std::vector<uint32_t>> cls(9);
     for (uint32_t k = 0; k < n; ++k) {
         HsSolver* s = solvers[k];
@@ -421,24 +452,26 @@ int hs_process_group(HsSolver* const* solvers, uint32_t n, uint32_t nsteps) {
         arenaMoved(s);
         cls[stepCtas(s)].push_back(k);
     }
-    std::vector<cudaEvent_t> evs;
     cudaError_t e = cudaSuccess;
-    auto newEvent = [&](cudaEvent_t* ev) {
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
-        if (e == cudaSuccess) evs.push_back(*ev);
-    };
-    // (the clusters first: they need whole free SM groups)
     for (uint32_t ctas = 8; ctas >= 1 && e == cudaSuccess; --ctas) {
         const std::vector<uint32_t>& m = cls[ctas];
         if (m.empty()) continue;
         cudaStream_t gst = solvers[m[0]]->st;
+        // The launch follows each member's work: what was queued on its own
+        // stream since its last group launch (an event there) and the
+        // group launch that last stepped it on another stream.  A group
+        // that repeats on the same streams, with nothing queued between
+        // its calls, needs neither: stream order covers it.
         std::vector<DevCell> cells(m.size());
-        for (size_t k = 0; k < m.size(); ++k) cells[k] = solvers[m[k]]->dc;
-        for (size_t k = 1; k < m.size() && e == cudaSuccess; ++k) {
-            cudaEvent_t ev;
-            newEvent(&ev);
-            if (e == cudaSuccess) e = cudaEventRecord(ev, solvers[m[k]]->st);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(gst, ev, 0);
+        for (size_t k = 0; k < m.size() && e == cudaSuccess; ++k) {
+            HsSolver* s = solvers[m[k]];
+            cells[k] = s->dc;
+            if (s->st != gst && s->queued) {
+                if (!s->evQueued) e = cudaEventCreateWithFlags(&s->evQueued, cudaEventDisableTiming);
+                if (e == cudaSuccess) e = cudaEventRecord(s->evQueued, s->st);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(gst, s->evQueued, 0);
+            }
+            if (e == cudaSuccess && s->group && s->group->st != gst) e = cudaStreamWaitEvent(gst, s->group->ev, 0);
         }
         DevCell* dCells = nullptr;
         if (e == cudaSuccess) e = cudaMallocAsync(&dCells, m.size() * sizeof(DevCell), gst);
@@ -447,14 +480,24 @@ int hs_process_group(HsSolver* const* solvers, uint32_t n, uint32_t nsteps) {
             e = cudaMemcpyAsync(dCells, cells.data(), m.size() * sizeof(DevCell), cudaMemcpyHostToDevice, gst);
         if (e == cudaSuccess) e = launchGroupStepFp64(dCells, (uint32_t)m.size(), ctas, nsteps, gst);
         if (dCells) cudaFreeAsync(dCells, gst);
-        cudaEvent_t done;
-        newEvent(&done);
-        if (e == cudaSuccess) e = cudaEventRecord(done, gst);
-        for (size_t k = 1; k < m.size() && e == cudaSuccess; ++k)
-            e = cudaStreamWaitEvent(solvers[m[k]]->st, done, 0);
+        auto done = std::make_shared<HsGroupDone>();
+        done->st = gst;
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done->ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(done->ev, gst);
+        if (e != cudaSuccess) break;
+        // the members' next work waits for the launch (stOf); the first
+        // member's stream holds it already
+        for (size_t k = 0; k < m.size(); ++k) {
+            HsSolver* s = solvers[m[k]];
+            if (s->st == gst) {
+                s->group.reset();
+                s->queued = true;
+            } else {
+                s->group = done;
+                s->queued = false;
+            }
+        }
     }
-    // an event destroyed while still pending is released once it completes
-    for (cudaEvent_t ev : evs) cudaEventDestroy(ev);
     if (e != cudaSuccess) return cudaErr(e, "process group");
     return HS_OK;
 }
@@ -462,7 +505,7 @@ int hs_process_group(HsSolver* const* solvers, uint32_t n, uint32_t nsteps) {
 int hs_sync(HsSolver* s) {
     if (!s) return setErr(HS_EINVAL, "null solver");
     if (int rc = flushWrites(s)) return rc;
-    cudaError_t e = cudaStreamSynchronize(s->st);
+    cudaError_t e = cudaStreamSynchronize(stOf(s));
     if (e != cudaSuccess) return cudaErr(e, "sync");
     return HS_OK;
 }
@@ -496,8 +539,8 @@ int hs_get_nsteps(HsSolver* s, uint64_t* out) {
     if (!s || !out) return setErr(HS_EINVAL, "null argument");
     if (int rc = flushWrites(s)) return rc;
     DevCtl ctl;
-    cudaError_t e = cudaMemcpyAsync(&ctl, s->dc.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, s->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    cudaError_t e = cudaMemcpyAsync(&ctl, s->dc.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, stOf(s));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stOf(s));
     if (e != cudaSuccess) return cudaErr(e, "get nsteps");
     *out = ctl.nSteps;
     return HS_OK;
@@ -514,8 +557,8 @@ int readDev(HsSolver* s, const T* p, T* out) {
     if (idx < 0) {
         int rc = flushWrites(s);
         if (rc) return rc;
-        cudaError_t e = cudaMemcpyAsync(out, p, sizeof(T), cudaMemcpyDeviceToHost, s->st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        cudaError_t e = cudaMemcpyAsync(out, p, sizeof(T), cudaMemcpyDeviceToHost, stOf(s));
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stOf(s));
         return e == cudaSuccess ? HS_OK : cudaErr(e, "field read");
     }
     uint8_t* pg;
@@ -531,8 +574,8 @@ int writeDev(HsSolver* s, T* p, T v) {
     if (idx < 0 || ((uintptr_t)p % sizeof(T)) != 0) {
         int rc = flushWrites(s);
         if (rc) return rc;
-        cudaError_t e = cudaMemcpyAsync(p, &v, sizeof(T), cudaMemcpyHostToDevice, s->st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        cudaError_t e = cudaMemcpyAsync(p, &v, sizeof(T), cudaMemcpyHostToDevice, stOf(s));
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stOf(s));
         arenaMoved(s);
         return e == cudaSuccess ? HS_OK : cudaErr(e, "field write");
     }
@@ -825,8 +868,8 @@ int hs_read_vm(HsSolver* s, double* out, uint32_t n) {
     if (n != s->P.hinesOf.size()) return setErr(HS_EINVAL, "n must equal the model's compartment count");
     if (int rc = flushWrites(s)) return rc;
     std::vector<double> v(s->P.N);
-    cudaError_t e = cudaMemcpyAsync(v.data(), s->dc.V, v.size() * 8, cudaMemcpyDeviceToHost, s->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    cudaError_t e = cudaMemcpyAsync(v.data(), s->dc.V, v.size() * 8, cudaMemcpyDeviceToHost, stOf(s));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stOf(s));
     if (e != cudaSuccess) return cudaErr(e, "read vm");
     for (uint32_t m = 0; m < n; ++m) out[m] = s->P.hinesOf[m] < 0 ? NAN : v[s->P.hinesOf[m]];
     return HS_OK;
@@ -837,8 +880,8 @@ int hs_read_ca(HsSolver* s, double* out, uint32_t n) {
     if (n != s->P.poolSolverOf.size()) return setErr(HS_EINVAL, "n must equal the model's pool count");
     if (int rc = flushWrites(s)) return rc;
     std::vector<double> v(s->P.P + 1);
-    cudaError_t e = cudaMemcpyAsync(v.data(), s->dc.ca, s->P.P * 8, cudaMemcpyDeviceToHost, s->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    cudaError_t e = cudaMemcpyAsync(v.data(), s->dc.ca, s->P.P * 8, cudaMemcpyDeviceToHost, stOf(s));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stOf(s));
     if (e != cudaSuccess) return cudaErr(e, "read ca");
     for (uint32_t m = 0; m < n; ++m) out[m] = s->P.poolSolverOf[m] < 0 ? NAN : v[s->P.poolSolverOf[m]];
     return HS_OK;
@@ -850,8 +893,8 @@ int hs_read_dif(HsSolver* s, double* out, uint32_t n) {
     if (!n) return HS_OK;
     if (int rc = flushWrites(s)) return rc;
     std::vector<double> st((size_t)kDifState * n);
-    cudaError_t e = cudaMemcpyAsync(st.data(), s->dc.difState, st.size() * 8, cudaMemcpyDeviceToHost, s->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    cudaError_t e = cudaMemcpyAsync(st.data(), s->dc.difState, st.size() * 8, cudaMemcpyDeviceToHost, stOf(s));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stOf(s));
     if (e != cudaSuccess) return cudaErr(e, "read tick-1 objects");
     for (uint32_t k = 0; k < n; ++k) {
         const int kind = s->P.difKind[k];
@@ -867,7 +910,7 @@ namespace {
 // kRecShift in hs_device.cuh), every target already checked.
 int installRecording(HsSolver* s, std::vector<uint32_t>&& rows, uint32_t stride, uint32_t capacity) {
     const uint32_t n = (uint32_t)rows.size();
-    cudaStreamSynchronize(s->st);
+    cudaStreamSynchronize(stOf(s));
     // From here on the step kernel sees no recording until the new one is
     // complete, so it never writes into a released buffer.
     s->dc.nRec = 0;
@@ -879,15 +922,15 @@ int installRecording(HsSolver* s, std::vector<uint32_t>&& rows, uint32_t stride,
     s->recBuf = nullptr;
     s->recHost = std::move(rows);
     // The sample count restarts with the new buffer (reinit sets it again).
-    cudaError_t e = cudaMemsetAsync(&s->dc.ctl->nSamples, 0, sizeof(uint32_t), s->st);
+    cudaError_t e = cudaMemsetAsync(&s->dc.ctl->nSamples, 0, sizeof(uint32_t), stOf(s));
     if (e != cudaSuccess) return cudaErr(e, "record");
     if (!n) return HS_OK;
     e = cudaMalloc(&s->recCompt, n * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc(&s->recBuf, (size_t)n * capacity * sizeof(double));
-    if (e == cudaSuccess) e = cudaMemsetAsync(s->recBuf, 0, (size_t)n * capacity * sizeof(double), s->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->recBuf, 0, (size_t)n * capacity * sizeof(double), stOf(s));
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(s->recCompt, s->recHost.data(), n * 4, cudaMemcpyHostToDevice, s->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        e = cudaMemcpyAsync(s->recCompt, s->recHost.data(), n * 4, cudaMemcpyHostToDevice, stOf(s));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stOf(s));
     if (e != cudaSuccess) {
         if (s->recCompt) cudaFree(s->recCompt);
         if (s->recBuf) cudaFree(s->recBuf);
@@ -958,8 +1001,8 @@ int hs_read_trace(HsSolver* s, double* out, uint32_t capacity, uint32_t* n_sampl
     if (!s || !n_samples) return setErr(HS_EINVAL, "null argument");
     if (int rc = flushWrites(s)) return rc;
     DevCtl ctl;
-    cudaError_t e = cudaMemcpyAsync(&ctl, s->dc.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, s->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    cudaError_t e = cudaMemcpyAsync(&ctl, s->dc.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, stOf(s));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stOf(s));
     if (e != cudaSuccess) return cudaErr(e, "read trace");
     uint32_t stored = ctl.nSamples < s->dc.recCap ? ctl.nSamples : s->dc.recCap;
     *n_samples = ctl.nSamples;
@@ -975,8 +1018,8 @@ int hs_read_spikes(HsSolver* s, uint32_t* gen, double* time, uint32_t capacity, 
     if (!s || !n) return setErr(HS_EINVAL, "null argument");
     if (int rc = flushWrites(s)) return rc;
     DevCtl ctl;
-    cudaError_t e = cudaMemcpyAsync(&ctl, s->dc.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, s->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    cudaError_t e = cudaMemcpyAsync(&ctl, s->dc.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, stOf(s));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stOf(s));
     if (e != cudaSuccess) return cudaErr(e, "read spikes");
     *n = ctl.nSpikes;
     uint32_t stored = ctl.nSpikes < s->dc.spikeCap ? ctl.nSpikes : s->dc.spikeCap;

@@ -183,3 +183,46 @@ def test_cluster_step_bit_exact_with_oracle():
         assert np.array_equal(h.vm(), oc.vm())
         assert np.array_equal(h.ca(), oc.ca())
     h.close()
+
+
+def _clock(ms, use_group, pattern):
+    """A clock loop of one-step calls: each step either the whole tick as
+    one group or every solver's own process, with field reads and writes
+    between steps; `pattern` also alternates two overlapping groups whose
+    first members differ (launches on different streams)."""
+    hs = []
+    for m in ms:
+        h = HSolve(m, dt=DT)
+        h.target = m.seed
+        h.reinit(DT)
+        hs.append(h)
+    seen = []
+    for step in range(60):
+        if use_group:
+            if pattern and step % 2:
+                process_group([hs[2], hs[0]], 1)
+                process_group([hs[1], hs[3]], 1)
+            else:
+                process_group(hs, 1)
+        else:
+            for h in hs:
+                h.process(1)
+        if step % 7 == 3:
+            hs[1].compartment(0).inject = 1e-9 * (step % 3)
+            seen.append(hs[0].compartment(hs[0].model.n_compt - 1).Vm)
+        if step % 11 == 5:
+            seen.append(float(hs[2].vm().sum()))
+    out = [h.vm() for h in hs]
+    for h in hs:
+        h.close()
+    return out, seen
+
+
+@pytest.mark.parametrize("pattern", [False, True])
+def test_one_step_group_calls_with_field_access_between(pattern):
+    ms = _models()[2:6]
+    a, sa = _clock(ms, False, pattern)
+    b, sb = _clock(ms, True, pattern)
+    assert sa == sb
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
