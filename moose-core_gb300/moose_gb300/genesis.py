@@ -5,8 +5,8 @@ cell files, built the way MOOSE's ``ReadCell`` builds them
 
 The channel library -- MOOSE's ``/library`` of prototype objects that a .p
 file names -- is a dict of the prototype classes below (HHChannelProto,
-HHChannel2DProto, CaConcProto, SpikeGenProto, and CompartmentProto for
-``*compt``).  A prototype's ``addmsg``
+HHChannel2DProto, SynChanProto, CaConcProto, SpikeGenProto, and
+CompartmentProto for ``*compt``).  A prototype's ``addmsg``
 strings are GENESIS ``addmsg`` fields (``"src srcField dest destField"``,
 ``.`` the object itself, ``../NAME`` a sibling in the same compartment),
 resolved after each line's channels are made, as
@@ -110,6 +110,19 @@ class HHChannel2DProto:
 
     def __init__(self, Ek, Xpower, table, Xindex="VOLT_C1_INDEX", addmsg=()):
         self.Ek, self.Xpower, self.table, self.Xindex = Ek, Xpower, table, Xindex
+        self.addmsg = list(addmsg)
+
+
+class SynChanProto:
+    """A SynChan prototype (Ek, tau1, tau2) with its SimpleSynHandler of one
+    synapse of the given weight, as ``rdesigneurProtos.make_glu`` builds
+    one.  ReadCell adds it as it adds an HHChannel (``addCanonicalChannel``,
+    ``ReadCell.cpp:773-800``: the ``channel`` message and Gbar).  The
+    loader queues no events: they are the model's ``ev_*`` arrays, or
+    arrive at run time (``hs_push_events``)."""
+
+    def __init__(self, Ek, tau1, tau2, weight=1.0, addmsg=()):
+        self.Ek, self.tau1, self.tau2, self.weight = Ek, tau1, tau2, weight
         self.addmsg = list(addmsg)
 
 
@@ -467,7 +480,7 @@ class ReadCell:
             self._wire(c, o)
 
     def _add(self, c, name, proto, value):
-        if isinstance(proto, (HHChannelProto, HHChannel2DProto)):
+        if isinstance(proto, (HHChannelProto, HHChannel2DProto, SynChanProto)):
             g = value * calc_surf(c.length, c.d) if value > 0 else -value
             o = [name, proto, {"Gbar": g}]
         elif isinstance(proto, SpikeGenProto):
@@ -557,6 +570,7 @@ def load_p(path, library, seed=0):
     c2 = {k: [] for k in ("compt", "Gbar", "Ek", "Xp", "xg", "xi", "c1", "c2")}
     pool = {k: [] for k in ("compt", "Ca", "basal", "tau", "B", "ceil", "floor", "d", "L", "thick")}
     sg = {k: [] for k in ("compt", "th", "ref", "edge")}
+    sy = {k: [] for k in ("compt", "Gbar", "Ek", "tau1", "tau2", "name")}
     pool_of = []              # per compartment: CaConc name -> pool index
     for i, c in enumerate(cs):
         names = {}
@@ -609,6 +623,13 @@ def load_p(path, library, seed=0):
                 sg["th"].append(f["threshold"])
                 sg["ref"].append(proto.refractT)
                 sg["edge"].append(proto.edgeTriggered)
+            elif isinstance(proto, SynChanProto):
+                sy["compt"].append(i)
+                sy["Gbar"].append(f["Gbar"])
+                sy["Ek"].append(proto.Ek)
+                sy["tau1"].append(proto.tau1)
+                sy["tau2"].append(proto.tau2)
+                sy["name"].append(name)
     nc, n2 = len(ch["compt"]), len(c2["compt"])
     f64 = lambda v: np.asarray(v, np.float64)
     i32 = lambda v: np.asarray(v, np.int32)
@@ -634,10 +655,15 @@ def load_p(path, library, seed=0):
         c2d_X=np.zeros(n2),
         sg_compt=u32(sg["compt"]), sg_threshold=f64(sg["th"]), sg_refractT=f64(sg["ref"]),
         sg_edge=i32(sg["edge"]),
+        syn_compt=u32(sy["compt"]), syn_Gbar=f64(sy["Gbar"]), syn_Ek=f64(sy["Ek"]), syn_tau1=f64(sy["tau1"]),
+        syn_tau2=f64(sy["tau2"]), syn_modulation=np.ones(len(sy["compt"])),
+        ev_syn=np.zeros(0, np.uint32), ev_time=np.zeros(0), ev_weight=np.zeros(0),
         meta={"names": [c.name for c in cs], "diameter": f64([c.d for c in cs]),
               "length": f64([c.length for c in cs]),
               "coords": f64([(c.x0, c.y0, c.z0, c.x, c.y, c.z) for c in cs]).reshape(-1, 6),
               "chan_name": [o[0] for c in cs for o in c.objs if isinstance(o[1], HHChannelProto)],
+              "syn_name": sy["name"],
+              "syn_weight": f64([o[1].weight for c in cs for o in c.objs if isinstance(o[1], SynChanProto)]),
               "pool_diameter": f64(pool["d"]), "pool_length": f64(pool["L"]), "pool_thick": f64(pool["thick"]),
               "classes": ["SymCompartment" if c.sym else "Compartment" for c in cs],
               "sibling_links": [(i, q) for i, c in enumerate(cs) for q in c.sibs],

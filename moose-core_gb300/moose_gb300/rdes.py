@@ -42,8 +42,11 @@ arguments:
 The channel library (rdesigneur's ``chanProto``, made by
 ``rdesigneurProtos`` functions in the reference) is a dict of the
 ``genesis`` prototype classes (``HHChannelProto``, ``HHChannel2DProto``,
-``CaConcProto``), each with a ``Gbar`` attribute for the prototype's own
-Gbar (kept where a distribution does not set it).  The HSolve target is the
+``SynChanProto`` -- ``make_glu`` and the like; ``assignParam`` treats a
+SynChan as every ChanBase: Gbar per area, Ek -- and ``CaConcProto``),
+each with a ``Gbar`` attribute for the prototype's own Gbar (kept where a
+distribution does not set it).  SynChans get no events from the loader
+(the model's ``ev_*`` arrays, or ``hs_push_events`` at run time).  The HSolve target is the
 largest-diameter compartment whose name contains ``oma``, as rdesigneur
 picks its soma.  Not built: spines, chemistry, adaptors, plots, other
 stimulus kinds.
@@ -501,13 +504,15 @@ def _to_model(cell, seed, inject0, sched):
                 names[name] = len(pools)
                 pools.append((i, f))
         pool_of.append(names)
-    ch, c2 = [], []
+    ch, c2, sy = [], [], []
     for i, c in enumerate(cell):
         for name, proto, f in c.objs:
             if isinstance(proto, genesis.HHChannelProto):
                 ch.append((i, name, proto, f))
             elif isinstance(proto, genesis.HHChannel2DProto):
                 c2.append((i, name, proto, f))
+            elif isinstance(proto, genesis.SynChanProto):
+                sy.append((i, name, proto, f))
     f64 = lambda v: np.asarray(v, np.float64)
     i32 = lambda v: np.asarray(v, np.int32)
     u32 = lambda v: np.asarray(v, np.uint32)
@@ -549,9 +554,13 @@ def _to_model(cell, seed, inject0, sched):
         c2d_conc1_pool=i32([pool_of[r[0]][r[3]["ca_depend"]] if "ca_depend" in r[3] else -1 for r in c2]),
         c2d_conc2_pool=i32([pool_of[r[0]][r[3]["conc2"]] if "conc2" in r[3] else -1 for r in c2]),
         c2d_instant=np.zeros(n2, np.int32), c2d_modulation=np.ones(n2), c2d_X=np.zeros(n2),
+        syn_compt=u32([r[0] for r in sy]), syn_Gbar=f64([r[3]["Gbar"] for r in sy]),
+        syn_Ek=f64([r[3]["Ek"] for r in sy]), syn_tau1=f64([r[2].tau1 for r in sy]),
+        syn_tau2=f64([r[2].tau2 for r in sy]), syn_modulation=np.ones(len(sy)),
+        ev_syn=np.zeros(0, np.uint32), ev_time=np.zeros(0), ev_weight=np.zeros(0),
         stim_compt=u32([s[1] for s in stim]), stim_step=u32([s[0] for s in stim]),
         stim_value=f64([s[2] for s in stim]),
         meta={"names": [c.name for c in cell], "diameter": f64([c.dia for c in cell]),
               "length": f64([c.length for c in cell]),
               "coords": f64([(c.x0, c.y0, c.z0, c.x, c.y, c.z) for c in cell]).reshape(-1, 6),
-              "chan_name": [r[1] for r in ch]})
+              "chan_name": [r[1] for r in ch], "syn_name": [r[1] for r in sy]})

@@ -5,7 +5,8 @@
    (n^4), Ca(HVA) (m^2 h) whose ``addmsg1`` sends IkOut to the sibling
    ``Ca_conc``, an SK-type channel on concentration and a K(Ca)
    HHChannel2D on (Vm, Ca), both fed by ``Ca_conc`` through ``addmsg1``,
-   a CaConc and a SpikeGen.  The same library is written as
+   a CaConc, a SpikeGen and a glu SynChan with its one-synapse handler (as
+   ``rdesigneurProtos.make_glu``).  The same library is written as
    ``moose_gb300.genesis`` prototypes by ``library()`` below, which the
    tests import; its gate tables are saved with the results (``lib_*``)
    so that the tests step the very tables the reference stepped.
@@ -16,6 +17,8 @@
    parent, RA/RM/CM and Ra/Rm/Cm overrides, absolute (negative) densities,
    ``//`` and ``/* */`` comments, blank lines and tabs; an unbranched
    ``*symmetric`` cable (SymCompartments, each compartment's class saved);
+   a cell with glu SynChans (density and absolute) and events queued on
+   them after reinit (saved as ``ev_*``);
    and a cell of compartment prototypes (``*compt``: two prototype
    compartments in ``/library`` with copied channels, a CaConc, their
    messages and an inject; a ``*compt`` whose path is not the prototype's
@@ -23,7 +26,8 @@
 3. Each file loaded by the reference ``moose.loadModel`` (``ReadCell``):
    every compartment (creation order: name, parent, Ra, Rm, Cm, Em, initVm,
    diameter, length, coordinates), every channel (compartment, name, Gbar,
-   Ek), CaConc B after zombification, SpikeGen threshold; then a soma inject
+   Ek), every SynChan (compartment, Gbar, Ek, tau1, tau2), CaConc B after
+   zombification, SpikeGen threshold; then a soma inject
    of 0.3 nA and 4,000 steps of 25 us under an HSolve with target = the
    first compartment: Vm and Ca traces (every 20th step), spikes, final Vm.
 
@@ -93,6 +97,7 @@ def _channel_library(z=None):
                                         addmsg=["../Ca_conc concOut . concen"]),
         "Ca_conc": genesis.CaConcProto(tau=0.02, CaBasal=5e-5, thick=0.1e-6, diameter=2e-6, length=10e-6),
         "spike": genesis.SpikeGenProto(refractT=2e-3, edgeTriggered=1),
+        "glu": genesis.SynChanProto(Ek=0.0, tau1=2e-3, tau2=9e-3, weight=1.0),
     }
 
 
@@ -149,6 +154,14 @@ def build_reference_library(lib):
         elif isinstance(p, genesis.SpikeGenProto):
             ch = moose.SpikeGen(path)
             ch.refractT, ch.edgeTriggered = p.refractT, p.edgeTriggered
+        elif isinstance(p, genesis.SynChanProto):
+            # as rdesigneurProtos.make_glu: the SynChan and a one-synapse handler
+            ch = moose.SynChan(path)
+            ch.Ek, ch.tau1, ch.tau2 = p.Ek, p.tau1, p.tau2
+            sh = moose.SimpleSynHandler(path + "/sh")
+            moose.connect(sh, "activationOut", ch, "activation")
+            sh.numSynapses = 1
+            moose.element(sh.path + "/synapse[0]").weight = p.weight
         elif isinstance(p, genesis.CompartmentProto):
             # children copied from the library entries, in message order
             pc = moose.SymCompartment(path) if p.symmetric else moose.Compartment(path)
@@ -269,6 +282,17 @@ def _chans_proto(i, rng):
     return s + (" KCa 30" if i % 3 == 0 else "")
 
 
+def _chans_syn(i, rng):
+    """HH channels and, on most compartments, a glu SynChan (density, or
+    absolute on a few)."""
+    s = "Na 1200 K 360"
+    if i % 4 == 1:
+        s += " glu -2e-10"
+    elif i % 4 != 3:
+        s += " glu %g" % (8.0 * rng.uniform(0.5, 1.5))
+    return s + (" spike 0.0" if i == 0 else "")
+
+
 def _chans_abs(i, rng):
     return "Na %g K -%g" % (1000.0, 3e-9 * rng.uniform(0.5, 1.5)) + (" spike -0.01" if i == 0 else "")
 
@@ -291,6 +315,8 @@ def fixtures():
         # compartment prototypes: the soma a copy of protoSoma, the rest of
         # protoDend; the *compt half way names the prototype by a path that
         # is not its Id::path, so the reference warns and keeps protoDend
+        # glu SynChans (ReadCell's canonical channels) with queued events
+        "synapses": synth_p(26, 40, ["*relative", "*cartesian", "*set_global RM 1.8"], _chans_syn),
         "compt_proto": synth_p(25, 36, ["*relative", "*cartesian", "*set_global RM 2.5",
                                         "*compt /library[0]/protoSoma"], _chans_proto,
                                after_soma=["*compt /library[0]/protoDend"],
@@ -334,6 +360,12 @@ def make():
         out[name + "/chan_Ek"] = np.array([x[3] for x in chans])
         sgs = moose.wildcardFind(where + "/##[ISA=SpikeGen]")
         out[name + "/sg_threshold"] = np.array([s.threshold for s in sgs])
+        syns = moose.wildcardFind(where + "/##[ISA=SynChan]")
+        syns.sort(key=lambda c: int(re.search(r"id=(\d+)", str(c.id)).group(1)))
+        out[name + "/syn_compt"] = np.array([idx[moose.element(s.neighbors["channel"][0]).name] for s in syns],
+                                            np.int32)
+        for f in ("Gbar", "Ek", "tau1", "tau2"):
+            out[name + "/syn_" + f] = np.array([getattr(s, f) for s in syns], np.float64)
         for t in range(8):
             moose.setClock(t, DT)
         moose.setClock(8, DT * STRIDE)
@@ -361,6 +393,16 @@ def make():
         h.dt = DT
         h.target = soma.path
         moose.reinit()
+        # synaptic events, queued after reinit (SimpleSynHandler::vReinit
+        # drops earlier ones): SynChan k gets six, 11 ms apart
+        ev = [(k, 0.004 + 0.0031 * k + 0.011 * j) for k in range(len(syns)) for j in range(6)]
+        for k, t in ev:
+            moose.element(syns[k].path + "/sh/synapse[0]").addSpike(t)
+        if syns:
+            out[name + "/ev_syn"] = np.array([k for k, _ in ev], np.uint32)
+            out[name + "/ev_time"] = np.array([t for _, t in ev])
+            out[name + "/ev_weight"] = np.array([moose.element(syns[k].path + "/sh/synapse[0]").weight
+                                                 for k, _ in ev])
         moose.start(NSTEPS * DT)
         out[name + "/pool_B"] = np.array([p.B for p in pools])
         out[name + "/vm"] = np.array([t.vector for t in vt])

@@ -19,7 +19,10 @@ Cases:
 * ``branched_distrib``: a branchedCell with a passive distribution and
   channel distributions that use p, g, L, dia, maxP, exp, H, ?: and ^,
   HH Na/K, a Ca channel feeding a CaConc (IkOut) and a K_AHP reading it
-  (concen), a current pulse.
+  (concen), a current pulse;
+* ``glu_distrib``: a branchedCell with HH Na/K and ``make_glu()`` SynChans
+  distributed over the dendrites (Gbar growing with p, Ek set), a step
+  current.
 
 Saved per case (``rdes_model_<case>.npz``): the rdesigneur arguments
 (JSON), the /library prototypes the model used (fields and gate tables),
@@ -81,6 +84,14 @@ CASES = {
                      ["K_AHP", "#", "Gbar", "8 + 2 * (p/maxP)^2"]],
         stimList=[["soma", "1", ".", "inject", "(t>0.005 && t<0.045) * 3e-10"]],
         plotList=[["soma", "1", ".", "Vm", "soma Vm"]]),
+    "glu_distrib": lambda: dict(
+        t_end=0.04,
+        cellProto=[["branchedCell", "cell", 15e-6, 15e-6, 3e-6, 120e-6, 4, 1.5e-6, 100e-6, 4]],
+        chanProto=[["make_HH_Na()", "Na"], ["make_HH_K()", "K"], ["make_glu()", "glu"]],
+        chanDistrib=[["Na", "soma", "Gbar", "1200"], ["K", "#", "Gbar", "360"],
+                     ["glu", "dend#,branch#", "Gbar", "5 + 2e4 * p", "Ek", "-0.005"]],
+        stimList=[["soma", "1", ".", "inject", "(t>0.004) * 2e-10"]],
+        plotList=[["soma", "1", ".", "Vm", "soma Vm"]]),
 }
 
 
@@ -100,6 +111,9 @@ def library(moose):
         elif cls in ("CaConc", "ZombieCaConc"):
             d.update(tau=e.tau, CaBasal=e.CaBasal, thick=e.thick, diameter=e.diameter, length=e.length,
                      ceiling=e.ceiling, floor=e.floor, B=e.B)
+        elif cls == "SynChan":
+            d.update(Ek=e.Ek, Gbar=e.Gbar, tau1=e.tau1, tau2=e.tau2,
+                     weight=moose.element(e.path + "/sh/synapse[0]").weight)
         else:
             continue
         d["addmsg"] = [moose.element(m).value for m in moose.wildcardFind(e.path + "/addmsg#")]

@@ -3,8 +3,9 @@ ReadCell builds.
 
 tests/golden/genesis/*.p are seeded synthetic cell files; genesis_golden.npz
 holds, for each, every compartment the reference loadModel made (creation
-order), every channel's Gbar and Ek, CaConc B after zombification, SpikeGen
-thresholds and an HSolve run with a soma inject (written by
+order), every channel's Gbar and Ek, every SynChan's Gbar, Ek and time
+constants, CaConc B after zombification, SpikeGen thresholds and an HSolve
+run with a soma inject and queued synaptic events (written by
 tests/golden/make_golden_genesis.py, which also defines the channel library
 used here).  The bar is bit-for-bit equality.
 """
@@ -28,6 +29,13 @@ LIB = library(Z)
 
 def path(name):
     return os.path.join(GOLDEN, "genesis", name + ".p")
+
+
+def with_events(m, name):
+    """The synaptic events the reference run queued (after reinit)."""
+    if name + "/ev_syn" in Z.files:
+        m.ev_syn, m.ev_time, m.ev_weight = Z[name + "/ev_syn"], Z[name + "/ev_time"], Z[name + "/ev_weight"]
+    return m
 
 
 @pytest.mark.parametrize("name", FILES)
@@ -56,11 +64,14 @@ def test_channels_pools_spikegens(name):
     m = genesis.load_p(path(name), LIB)
     assert np.array_equal(m.pool_B, Z[name + "/pool_B"])
     assert np.array_equal(m.sg_threshold, Z[name + "/sg_threshold"])
+    assert np.array_equal(m.syn_compt, Z[name + "/syn_compt"])
+    for f in ("Gbar", "Ek", "tau1", "tau2"):
+        assert np.array_equal(getattr(m, "syn_" + f), Z[name + "/syn_" + f]), f
 
 
 @pytest.mark.parametrize("name", FILES)
 def test_oracle_on_loaded_cell_matches_reference_hsolve(name):
-    m = genesis.load_p(path(name), LIB)
+    m = with_events(genesis.load_p(path(name), LIB), name)
     m.inject[0] = float(Z["inject"])
     dt, stride, n = float(Z["dt"]), int(Z["stride"]), int(Z["nsteps"])
     rec = Z[name + "/rec"]

@@ -36,8 +36,11 @@ def test_dropin_matches_reference_hsolve(name):
     """Against the oracle on the same loaded model: bit-exact unless the cell
     has a K(Ca) gate (exp).  Against the reference's traces: bit-exact when
     neither the cell (K(Ca)) nor the loader (polar coordinates: sin/cos of
-    this machine's libm) calls libm, else within 1e-9."""
+    this machine's libm) calls libm, else within 1e-9.  The synaptic events
+    the reference queued are the model's queued events."""
     m = genesis.load_p(path(name), LIB)
+    if name + "/ev_syn" in Z.files:
+        m.ev_syn, m.ev_time, m.ev_weight = Z[name + "/ev_syn"], Z[name + "/ev_time"], Z[name + "/ev_weight"]
     m.inject[0] = float(Z["inject"])
     dt, stride, n = float(Z["dt"]), int(Z["stride"]), int(Z["nsteps"])
     rec = Z[name + "/rec"]

@@ -2,7 +2,8 @@
 own rdesigneur built (tests/golden/make_golden_rdes_model.py): the test_41
 ball and stick, the test_20 passive soma under a pulse, and a branchedCell
 with passive and channel distributions over p, g, L, dia, maxP (exp, H,
-?:, ^), a Ca channel feeding a CaConc and a K_AHP reading it.
+?:, ^), a Ca channel feeding a CaConc and a K_AHP reading it, and one
+with make_glu SynChans distributed over the dendrites.
 
 From the same rdesigneur arguments and the reference's /library prototypes,
 the loader's model equals the reference HSolve's description (from the
@@ -23,7 +24,7 @@ from moose_gb300 import genesis
 from moose_gb300.rdes import Rdesigneur
 from oracle import OracleCell
 
-CASES = ["ball_and_stick", "soma_pulse", "branched_distrib"]
+CASES = ["ball_and_stick", "soma_pulse", "branched_distrib", "glu_distrib"]
 
 
 def _z(name):
@@ -39,6 +40,9 @@ def library_from(z):
             p = genesis.CaConcProto(tau=d["tau"], CaBasal=d["CaBasal"], thick=d["thick"],
                                     diameter=d["diameter"], length=d["length"], ceiling=d["ceiling"],
                                     floor=d["floor"], addmsg=d["addmsg"])
+        elif d["class"] == "SynChan":
+            p = genesis.SynChanProto(Ek=d["Ek"], tau1=d["tau1"], tau2=d["tau2"], weight=d["weight"],
+                                     addmsg=d["addmsg"])
         else:
             gate = {}
             for g in ("X", "Y", "Z"):
@@ -91,6 +95,13 @@ def test_loader_model_equals_reference_description(name):
             a, b = getattr(m, f)[got], getattr(ref, f)[exp]
             assert np.array_equal(a >= 0, b >= 0), (names[i], f)
             assert np.array_equal(m.pool_compt[a[a >= 0]], where[ref.pool_compt[b[b >= 0]]]), (names[i], f)
+    # SynChans of each compartment, in order
+    assert len(m.syn_compt) == len(ref.syn_compt)
+    for r_i, i in enumerate(where):
+        got = np.nonzero(m.syn_compt == i)[0]
+        exp = np.nonzero(ref.syn_compt == r_i)[0]
+        for f in ("syn_Gbar", "syn_Ek", "syn_tau1", "syn_tau2"):
+            assert np.array_equal(getattr(m, f)[got], getattr(ref, f)[exp]), (names[i], f)
     # pools
     assert len(m.pool_compt) == len(ref.pool_compt)
     for r_k in range(len(ref.pool_compt)):
