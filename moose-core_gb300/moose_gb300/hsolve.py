@@ -292,11 +292,37 @@ class HSolve:
             weight.ctypes.data_as(C.POINTER(C.c_double)), len(syn)))
 
 
-def process_group(solvers, nsteps):
-    """hs_process(s, nsteps) for every HSolve in `solvers`, in one launch
-    (hs_process_group): bit-identical to stepping each alone."""
+def _handles(solvers):
     hs = [s._h for s in solvers]
     if any(h is None for h in hs):
         raise ValueError("every HSolve needs its target set")
-    arr = (C.c_void_p * len(hs))(*[h.value if hasattr(h, "value") else h for h in hs])
+    return hs
+
+
+def process_group(solvers, nsteps):
+    """hs_process(s, nsteps) for every HSolve in `solvers`, in one launch
+    per cluster size (hs_process_group): bit-identical to stepping each
+    alone."""
+    hs = _handles(solvers)
+    arr = (C.c_void_p * len(hs))(*[h.value for h in hs])
     _native.check(_native.load().hs_process_group(arr, len(hs), int(nsteps)))
+
+
+class Tick:
+    """The HSolves of one clock tick (the Clock processes a tick's objects
+    in turn, scheduling/Clock.cpp:872-921), stepped together by
+    hs_process_group.  For a loop of short calls: the handle array is built
+    once and again only when a member's solver changed (a new target)."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        self._hs = None
+        self._arr = None
+
+    def process(self, nsteps=1):
+        hs = [s._h for s in self.solvers]
+        if self._hs is None or any(a is not b for a, b in zip(hs, self._hs)):
+            hs = _handles(self.solvers)
+            self._arr = (C.c_void_p * len(hs))(*[h.value for h in hs])
+            self._hs = hs
+        _native.check(_native.load().hs_process_group(self._arr, len(hs), int(nsteps)))

@@ -85,3 +85,35 @@ def test_group_and_cluster_calls_check_their_arguments():
     h = HSolve(models.config1_cell(n_cable=5))
     with pytest.raises(ValueError):
         process_group([h], 10)                                   # no target set
+
+
+def test_tick_builds_its_handle_array_once(monkeypatch):
+    """moose_gb300.hsolve.Tick passes hs_process_group the members' handles
+    in order, builds the array once, and again when a member's solver was
+    replaced (a fake library records the calls: no GPU)."""
+    from moose_gb300 import hsolve
+
+    class S:
+        def __init__(self, v):
+            self._h = C.c_void_p(v)
+
+    calls = []
+
+    class Fake:
+        def hs_process_group(self, arr, n, k):
+            calls.append((id(arr), [arr[i] for i in range(n)], n, k))
+            return 0
+
+    monkeypatch.setattr(hsolve._native, "load", lambda: Fake())
+    ss = [S(0x1000 + 16 * i) for i in range(5)]
+    t = hsolve.Tick(ss)
+    t.process()
+    t.process(3)
+    assert calls[0][1] == [0x1000 + 16 * i for i in range(5)] and calls[0][2:] == (5, 1)
+    assert calls[1][0] == calls[0][0] and calls[1][3] == 3          # the same array
+    ss[2]._h = C.c_void_p(0x9000)                                    # a new target
+    t.process()
+    assert calls[2][1][2] == 0x9000
+    ss[4]._h = None
+    with pytest.raises(ValueError):
+        t.process()
