@@ -1,5 +1,6 @@
-"""Synaptic input from MOOSE ``TimeTable`` objects, as queued events of the
-solver.
+"""Inputs that MOOSE scripts drive a solved cell with, as the solver's own
+inputs: synaptic input from ``TimeTable`` objects as queued events, and
+``PulseGen`` output into ``injectMsg`` as the inject schedule.
 
 A script drives a SynChan's synapse with a ``TimeTable``
 (``builtins/TimeTable.cpp:181-205``) on tick 8: each time the tick fires,
@@ -15,6 +16,8 @@ than the step after the send, else that step's clock time exactly (the
 same ``dt x step`` product the solver compares with).  The activation it
 adds (weight / dt) does not depend on the time.
 """
+import math
+
 import numpy as np
 
 
@@ -49,4 +52,85 @@ def add_timetables(model, tables, dt, nsteps, stride=1):
     model.ev_syn = np.concatenate(syn).astype(np.uint32)
     model.ev_time = np.concatenate(tim)
     model.ev_weight = np.concatenate(wts)
+    return model
+
+
+class PulseGen:
+    """``device/PulseGen.cpp`` in free-run mode (trigMode 0): pulses of
+    ``level[i]`` for ``width[i]`` after ``delay[i]``, ``baseLevel``
+    otherwise, repeating with the reference's period; the output is kept
+    from the previous call where no pulse or gap claims the phase, as
+    ``PulseGen::process`` keeps ``output_``."""
+
+    def __init__(self, level, width, delay, baseLevel=0.0):
+        self.level = [float(x) for x in level]
+        self.width = [float(x) for x in width]
+        self.delay = [float(x) for x in delay]
+        if not (len(self.level) == len(self.width) == len(self.delay)) or not self.level:
+            raise ValueError("PulseGen: level, width and delay need one entry per pulse")
+        self.baseLevel = float(baseLevel)
+        self.output = self.baseLevel
+
+    def reinit(self):
+        self.output = self.baseLevel
+        return self.output
+
+    def process(self, t):
+        w, d = self.width, self.delay
+        period = w[0] + d[0]
+        for i in range(1, len(w)):
+            if not (w[i] > 0.0 or d[i] > 0.0):
+                break
+            incr = d[i] + w[i] - w[i - 1]
+            if incr > 0:
+                period += incr
+        phase = math.fmod(t, period)
+        if phase >= period:
+            self.output = self.baseLevel
+            return self.output
+        for i in range(len(w)):
+            if phase < d[i]:
+                self.output = self.baseLevel
+                break
+            elif phase < d[i] + w[i]:
+                self.output = self.level[i]
+                break
+            phase -= d[i]
+        return self.output
+
+
+def add_pulsegen(model, compt, pulse, dt, nsteps, stride=1):
+    """A PulseGen's ``output`` into compartment `compt`'s ``injectMsg``, as
+    the model's inject schedule.  The PulseGen runs on a tick of `stride`
+    steps (tick 0 by default, before the solver's tick 6) and its output
+    reaches the step's right-hand side through ``HSolve::addInject``
+    (``injectVarying``, used and cleared by that step's matrix update,
+    ``hsolve/HSolveActive.cpp:118-126``); the value it sends at reinit stays
+    in ``injectVarying`` until the first step uses it.  The schedule sets
+    the compartment's basal inject each step to what the reference adds:
+    (the step's messages) + (the compartment's inject), in that order.
+    The model must have no other schedule entries for `compt`."""
+    base = float(model.inject[compt])
+    if np.any(model.stim_compt == compt):
+        raise ValueError("add_pulsegen: compartment %d already has scheduled injects" % compt)
+    pending = pulse.reinit()              # sent at reinit, kept until step 0
+    steps, vals = [], []
+    prev = base
+    for s in range(nsteps):
+        E = s + 1
+        varying = pending
+        pending = 0.0
+        if E % stride == 0:
+            varying = varying + pulse.process(dt * E)   # Clock: currTime = dt x endStep
+        v = varying + base if varying != 0.0 else base
+        if v != prev or s == 0:
+            steps.append(s)
+            vals.append(v)
+            prev = v
+    model.stim_step = np.concatenate([model.stim_step, np.array(steps, np.uint32)])
+    model.stim_compt = np.concatenate([model.stim_compt, np.full(len(steps), compt, np.uint32)])
+    model.stim_value = np.concatenate([model.stim_value, np.array(vals, np.float64)])
+    order = np.lexsort((model.stim_compt, model.stim_step))
+    model.stim_step, model.stim_compt, model.stim_value = (model.stim_step[order], model.stim_compt[order],
+                                                           model.stim_value[order])
     return model

@@ -47,3 +47,41 @@ def test_one_entry_per_tick_and_delivery_step():
     assert ev[0] == 1e-3 + 1e-3
     # an entry the run never reaches is not sent
     assert len(inputs.timetable_events([1.0], dt, 200)) == 0
+
+
+P = np.load(os.path.join(GOLDEN, "pulsegen_golden.npz"))
+
+
+def test_pulsegens_reproduce_the_reference_run():
+    """Two free-running PulseGens into injectMsg (one with a base level
+    that its reinit also sends, one on a tick of three steps into a
+    compartment with its own inject field): the oracle with the derived
+    inject schedule equals the reference's traces (every 4 steps) and
+    final Vm bit for bit."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    from make_golden_pulsegen import PULSES
+    m = load_model(P)
+    dt, n = float(P["dt"]), int(P["nsteps"])
+    for c, (level, width, delay, base, tick, k) in PULSES.items():
+        inputs.add_pulsegen(m, c, inputs.PulseGen(level, width, delay, base), dt, n, stride=k)
+    oc = OracleCell(m, dt)
+    oc.reinit(dt)
+    rec = P["rec"]
+    vm = [oc.vm()[rec]]
+    for _ in range(n // 4):
+        oc.step(4)
+        vm.append(oc.vm()[rec])
+    assert np.array_equal(np.array(vm).T, P["vm"])
+    assert np.array_equal(oc.vm(), P["final_vm"])
+
+
+def test_pulsegen_output_keeps_the_reference_rules():
+    pg = inputs.PulseGen([1.0, 2.0], [0.01, 0.02], [0.005, 0.01], baseLevel=0.5)
+    assert pg.reinit() == 0.5
+    # period: w0 + d0, plus d1 + w1 - w0 = 0.035; the second pulse's delay
+    # counts from the first pulse's start
+    assert pg.process(0.001) == 0.5          # before the first pulse
+    assert pg.process(0.006) == 1.0          # first pulse
+    assert pg.process(0.016) == 2.0          # second pulse
+    assert pg.process(0.036) == 0.5          # the next period
