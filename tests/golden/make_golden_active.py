@@ -53,12 +53,14 @@ def synapse(sh, j):
     return moose.element("%s/synapse[%d]" % (sh.path, j))
 
 
-def build_moose(m, dt, cell="/cell"):
+def build_moose(m, dt, cell="/cell", library="/library"):
+    """`library`: where the channel prototypes go (copied channels share
+    their prototype's gates, so cells built side by side need their own)."""
     import moose
-    for p in ("/cell", "/library"):
+    for p in (cell, library):
         if moose.exists(p):
             moose.delete(p)
-    moose.Neutral("/library")
+    moose.Neutral(library)
     root = moose.Neutral(cell)
     n = m.n_compt
     comp = []
@@ -82,7 +84,7 @@ def build_moose(m, dt, cell="/cell"):
                m.chan_ygate[k], m.chan_zgate[k], m.chan_use_conc[k])
         if sig in protos:
             return protos[sig]
-        p = moose.HHChannel("/library/proto%d" % len(protos))
+        p = moose.HHChannel("%s/proto%d" % (library, len(protos)))
         p.Xpower, p.Ypower, p.Zpower = m.chan_Xpower[k], m.chan_Ypower[k], m.chan_Zpower[k]
         p.useConcentration = int(m.chan_use_conc[k])
         for name, pw, g in (("gateX", m.chan_Xpower[k], m.chan_xgate[k]),
@@ -136,7 +138,7 @@ def build_moose(m, dt, cell="/cell"):
     for k in range(len(m.c2d_compt)):
         g = int(m.c2d_xgate[k])
         if g not in protos2d:
-            p = moose.HHChannel2D("/library/proto2d%d" % g)
+            p = moose.HHChannel2D("%s/proto2d%d" % (library, g))
             p.Xindex = DEP_NAME[int(m.c2d_xindex[k])]
             p.Xpower = m.c2d_Xpower[k]
             xmn, xmx, ymn, ymx, A, B = m.gates2d[g]
