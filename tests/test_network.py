@@ -98,3 +98,42 @@ def test_network_of_dropin_solvers_on_gpu():
         assert np.array_equal(c.h.trace()[0], Z["vm%d" % i]), i
         assert np.array_equal(c.h.spikes()[1], Z["spikes%d" % i]), i
         c.h.close()
+
+
+class OracleBatch:
+    """Oracle cells behind the batch's interface (spikes of all cells in
+    one list, events addressed by cell)."""
+
+    def __init__(self, ms, dt):
+        self.cells = [Stepper(m, dt) for m in ms]
+
+    def process(self, n):
+        for c in self.cells:
+            c.process(n)
+
+    def spikes(self):
+        cs, gs, ts = [], [], []
+        for i, c in enumerate(self.cells):
+            g, t = c.spikes()
+            cs += [i] * len(t)
+            gs += list(g)
+            ts += list(t)
+        return np.array(cs, np.uint32), np.array(gs, np.uint32), np.array(ts)
+
+    def push_events(self, cells, syn, time, weight):
+        for c, k, t, w in zip(cells, syn, time, weight):
+            self.cells[int(c)].push_events([k], [t], [w])
+
+
+def test_batch_network_reproduces_the_reference_run():
+    """BatchNetwork over the batch interface: the spikes are read after each
+    chunk (the batch lists every cell's spikes, not in time order across
+    cells) and pushed in one call."""
+    from moose_gb300.network import BatchNetwork
+    dt, n = float(Z["dt"]), int(Z["nsteps"])
+    b = OracleBatch([load_model(Z, prefix="m%d_" % i) for i in range(3)], dt)
+    conns = [(int(a), int(b_), int(c), int(d), float(e), float(f)) for a, b_, c, d, e, f in Z["connections"]]
+    net = BatchNetwork(b, conns, dt)
+    net.run(n)
+    for i, c in enumerate(b.cells):
+        assert np.array_equal(np.array(c.vm), Z["vm%d" % i]), i
