@@ -1,6 +1,7 @@
 """Inputs that MOOSE scripts drive a solved cell with, as the solver's own
 inputs: synaptic input from ``TimeTable`` objects as queued events, and
-``PulseGen`` output into ``injectMsg`` as the inject schedule.
+``PulseGen`` or ``StimulusTable`` output into ``injectMsg`` as the inject
+schedule.
 
 A script drives a SynChan's synapse with a ``TimeTable``
 (``builtins/TimeTable.cpp:181-205``) on tick 8: each time the tick fires,
@@ -99,6 +100,56 @@ class PulseGen:
         return self.output
 
 
+class StimulusTable:
+    """``builtins/StimulusTable.cpp``: the table ``vector`` spread over
+    [startTime, stopTime] and read by ``TableBase::interpolate``
+    (``builtins/TableBase.cpp:470-495``) at a position that advances by
+    ``stepSize`` per call (accumulated), or is the clock time when
+    ``stepSize`` is 0; with ``doLoop`` the position wraps every
+    ``loopTime`` after ``startTime``."""
+
+    def __init__(self, vector, startTime, stopTime, stepSize=0.0, doLoop=False, loopTime=0.0):
+        self.vec = [float(v) for v in vector]
+        self.start, self.stop = float(startTime), float(stopTime)
+        self.stepSize, self.doLoop, self.loopTime = float(stepSize), bool(doLoop), float(loopTime)
+        self.pos = 0.0
+
+    def _interpolate(self, x):
+        v, xmin, xmax = self.vec, self.start, self.stop
+        if not v:
+            return 0.0
+        if len(v) == 1 or x < xmin or xmin >= xmax:
+            return v[0]
+        if x > xmax:
+            return v[-1]
+        xdivs = len(v) - 1
+        fraction = (x - xmin) / (xmax - xmin)
+        if fraction < 0:
+            return v[0]
+        j = int(xdivs * fraction)
+        if j >= len(v) - 1:
+            return v[-1]
+        dx = (xmax - xmin) / xdivs
+        lower = xmin + j * dx
+        sub = (x - lower) / dx
+        return v[j] + (v[j + 1] - v[j]) * sub
+
+    def reinit(self):
+        self.pos = 0.0
+        return self._interpolate(self.pos)
+
+    def process(self, t):
+        if self.stepSize > 0:
+            self.pos += self.stepSize
+        else:
+            self.pos = t
+        x = self.pos
+        if self.doLoop and self.pos > self.start + self.loopTime:
+            i = math.floor((self.pos - self.start) / self.loopTime)
+            x = self.pos - self.loopTime * i
+        return self._interpolate(x)
+
+
 def add_pulsegen(model, compt, pulse, dt, nsteps, stride=1):
     """A PulseGen's ``output`` into compartment `compt`'s ``injectMsg``, as
     the model's inject schedule.  The PulseGen runs on a tick of `stride`
@@ -134,3 +185,7 @@ def add_pulsegen(model, compt, pulse, dt, nsteps, stride=1):
     model.stim_step, model.stim_compt, model.stim_value = (model.stim_step[order], model.stim_compt[order],
                                                            model.stim_value[order])
     return model
+
+
+# any source with reinit() and process(t) (PulseGen, StimulusTable) into injectMsg
+add_injector = add_pulsegen

@@ -8,8 +8,10 @@ inject field.  Two free-running PulseGens send ``output`` to
 ``injectMsg``: one into the soma on tick 0 (two pulses, a non-zero base
 level, which PulseGen::reinit also sends), one into the compartment with
 the inject field on tick 2 at three steps per tick (its output reaches
-only the steps its tick fires on).  Tables record both compartments' Vm
-every step; 0.06 s at 25 us.
+only the steps its tick fires on).  Two StimulusTables on tick 0 send
+``output`` to ``injectMsg`` of two more compartments: one read at the
+clock time and looping, one advancing by its own step size.  Tables
+record the PulseGens' compartments' Vm; 0.06 s at 25 us.
 
 Output: ``tests/golden/pulsegen_golden.npz``.  Prerequisite: the reference
 build (``python oracle/build_ref.py``).
@@ -35,6 +37,11 @@ PULSES = {
     3: ([3e-10], [0.003], [0.002], 0.0, 2, 3),
 }
 FIELD_INJECT = {3: 2e-11}
+STIMTABLES = {
+    # compartment: (vector, startTime, stopTime, stepSize, doLoop, loopTime)
+    7: ([0.0, 3e-10, -1e-10, 2e-10, 0.0], 0.004, 0.024, 0.0, True, 0.03),
+    12: ([1e-10, 4e-10, 0.0], 0.01, 0.04, 1.3 * 25e-6, False, 0.0),
+}
 
 
 def pulse_model():
@@ -64,6 +71,12 @@ def main():
         if tick != 0:
             moose.setClock(tick, DT * k)
             moose.useClock(tick, pg.path, "process")
+    for c, (vec, start, stop, step, loop, loop_t) in STIMTABLES.items():
+        st = moose.StimulusTable("/cell/st%d" % c)
+        st.vector = vec
+        st.startTime, st.stopTime, st.stepSize = start, stop, step
+        st.doLoop, st.loopTime = loop, loop_t
+        moose.connect(st, "output", comp[c], "injectMsg")
     tabs = []
     for c in PULSES:
         t = moose.Table("/cell/vm%d" % c)

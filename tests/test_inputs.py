@@ -55,16 +55,19 @@ P = np.load(os.path.join(GOLDEN, "pulsegen_golden.npz"))
 def test_pulsegens_reproduce_the_reference_run():
     """Two free-running PulseGens into injectMsg (one with a base level
     that its reinit also sends, one on a tick of three steps into a
-    compartment with its own inject field): the oracle with the derived
-    inject schedule equals the reference's traces (every 4 steps) and
-    final Vm bit for bit."""
+    compartment with its own inject field) and two StimulusTables (one
+    looping at the clock time, one advancing by its own step): the oracle
+    with the derived inject schedule equals the reference's traces (every
+    4 steps) and final Vm bit for bit."""
     import sys
     sys.path.insert(0, GOLDEN)
-    from make_golden_pulsegen import PULSES
+    from make_golden_pulsegen import PULSES, STIMTABLES
     m = load_model(P)
     dt, n = float(P["dt"]), int(P["nsteps"])
     for c, (level, width, delay, base, tick, k) in PULSES.items():
         inputs.add_pulsegen(m, c, inputs.PulseGen(level, width, delay, base), dt, n, stride=k)
+    for c, (vec, start, stop, step, loop, loop_t) in STIMTABLES.items():
+        inputs.add_injector(m, c, inputs.StimulusTable(vec, start, stop, step, loop, loop_t), dt, n)
     oc = OracleCell(m, dt)
     oc.reinit(dt)
     rec = P["rec"]
