@@ -150,14 +150,15 @@ class StimulusTable:
         return self._interpolate(x)
 
 
-def add_pulsegen(model, compt, pulse, dt, nsteps, stride=1):
+def add_pulsegen(model, compt, pulse, dt, nsteps, stride=1, after_solver=False):
     """A PulseGen's ``output`` into compartment `compt`'s ``injectMsg``, as
     the model's inject schedule.  The PulseGen runs on a tick of `stride`
-    steps (tick 0 by default, before the solver's tick 6) and its output
-    reaches the step's right-hand side through ``HSolve::addInject``
-    (``injectVarying``, used and cleared by that step's matrix update,
-    ``hsolve/HSolveActive.cpp:118-126``); the value it sends at reinit stays
-    in ``injectVarying`` until the first step uses it.  The schedule sets
+    steps and its output reaches a step's right-hand side through
+    ``HSolve::addInject`` (``injectVarying``, used and cleared by the next
+    matrix update, ``hsolve/HSolveActive.cpp:118-126``): on a tick before
+    the solver's tick 6 (tick 0, the default) the same step's, on a later
+    tick (`after_solver`) the next step's.  The value it sends at reinit
+    stays in ``injectVarying`` until the first step uses it.  The schedule sets
     the compartment's basal inject each step to what the reference adds:
     (the step's messages) + (the compartment's inject), in that order.
     The model must have no other schedule entries for `compt`."""
@@ -168,10 +169,10 @@ def add_pulsegen(model, compt, pulse, dt, nsteps, stride=1):
     steps, vals = [], []
     prev = base
     for s in range(nsteps):
-        E = s + 1
+        E = s if after_solver else s + 1      # the end step whose tick sent this step's value
         varying = pending
         pending = 0.0
-        if E % stride == 0:
+        if E >= 1 and E % stride == 0:
             varying = varying + pulse.process(dt * E)   # Clock: currTime = dt x endStep
         v = varying + base if varying != 0.0 else base
         if v != prev or s == 0:

@@ -8,7 +8,8 @@ inject field.  Two free-running PulseGens send ``output`` to
 ``injectMsg``: one into the soma on tick 0 (two pulses, a non-zero base
 level, which PulseGen::reinit also sends), one into the compartment with
 the inject field on tick 2 at three steps per tick (its output reaches
-only the steps its tick fires on).  Two StimulusTables on tick 0 send
+only the steps its tick fires on); a third, on tick 9 after the solver,
+reaches each step after the one its tick fires on.  Two StimulusTables on tick 0 send
 ``output`` to ``injectMsg`` of two more compartments: one read at the
 clock time and looping, one advancing by its own step size.  Tables
 record the PulseGens' compartments' Vm; 0.06 s at 25 us.
@@ -35,6 +36,8 @@ PULSES = {
     # compartment: (level, width, delay, baseLevel, tick, steps per tick)
     0: ([4e-10, 7e-10], [0.01, 0.005], [0.005, 0.02], 5e-11, 0, 1),
     3: ([3e-10], [0.003], [0.002], 0.0, 2, 3),
+    # on tick 9, after the solver: its output reaches the next step
+    20: ([5e-10, 2e-10], [0.004, 0.006], [0.008, 0.01], 2e-11, 9, 2),
 }
 FIELD_INJECT = {3: 2e-11}
 STIMTABLES = {

@@ -53,9 +53,10 @@ P = np.load(os.path.join(GOLDEN, "pulsegen_golden.npz"))
 
 
 def test_pulsegens_reproduce_the_reference_run():
-    """Two free-running PulseGens into injectMsg (one with a base level
+    """Three free-running PulseGens into injectMsg (one with a base level
     that its reinit also sends, one on a tick of three steps into a
-    compartment with its own inject field) and two StimulusTables (one
+    compartment with its own inject field, one on a tick after the
+    solver's) and two StimulusTables (one
     looping at the clock time, one advancing by its own step): the oracle
     with the derived inject schedule equals the reference's traces (every
     4 steps) and final Vm bit for bit."""
@@ -65,7 +66,8 @@ def test_pulsegens_reproduce_the_reference_run():
     m = load_model(P)
     dt, n = float(P["dt"]), int(P["nsteps"])
     for c, (level, width, delay, base, tick, k) in PULSES.items():
-        inputs.add_pulsegen(m, c, inputs.PulseGen(level, width, delay, base), dt, n, stride=k)
+        inputs.add_pulsegen(m, c, inputs.PulseGen(level, width, delay, base), dt, n, stride=k,
+                            after_solver=tick > 6)
     for c, (vec, start, stop, step, loop, loop_t) in STIMTABLES.items():
         inputs.add_injector(m, c, inputs.StimulusTable(vec, start, stop, step, loop, loop_t), dt, n)
     oc = OracleCell(m, dt)
