@@ -22,11 +22,13 @@ import math
 import numpy as np
 
 
-def timetable_events(times, dt, nsteps, stride=1, delay=0.0):
+def timetable_events(times, dt, nsteps, stride=1, delay=0.0, before_handler=False):
     """Queued event times for the entries `times` of one TimeTable on a tick
     of `stride` base steps of `dt`, over `nsteps` steps, into a synapse of
-    the given `delay`.  Entries the table has not sent by the end of the
-    run are left out."""
+    the given `delay`.  On its default tick 8 the table sends after the
+    handler's tick 1, so an entry reaches the synapse from the next step
+    on; on tick 0 (`before_handler`) from the step it is sent in.  Entries
+    the table has not sent by the end of the run are left out."""
     vec = [float(t) for t in np.asarray(times, np.float64).ravel()]
     out = []
     cur = 0
@@ -34,19 +36,20 @@ def timetable_events(times, dt, nsteps, stride=1, delay=0.0):
         now = dt * E                          # Clock: currTime = dt x endStep
         if cur < len(vec) and now >= vec[cur]:
             t = vec[cur] + delay
-            first = dt * (E + 1)              # the next step's clock time
+            first = dt * (E if before_handler else E + 1)   # the first step that may deliver it
             out.append(t if t > first else first)
             cur += 1
     return np.array(out, np.float64)
 
 
-def add_timetables(model, tables, dt, nsteps, stride=1):
+def add_timetables(model, tables, dt, nsteps, stride=1, before_handler=()):
     """Queue the events of TimeTables on a model's SynChans: `tables` maps a
-    SynChan index to (times, delay, weight).  The model's existing events
-    are kept."""
+    SynChan index to (times, delay, weight); `before_handler` lists the
+    SynChans whose table runs on tick 0.  The model's existing events are
+    kept."""
     syn, tim, wts = [model.ev_syn], [model.ev_time], [model.ev_weight]
     for k, (times, delay, weight) in sorted(tables.items()):
-        ev = timetable_events(times, dt, nsteps, stride, delay)
+        ev = timetable_events(times, dt, nsteps, stride, delay, before_handler=k in before_handler)
         syn.append(np.full(len(ev), k, np.uint32))
         tim.append(ev)
         wts.append(np.full(len(ev), float(weight)))

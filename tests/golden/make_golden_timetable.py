@@ -8,7 +8,9 @@ the reference pymoose by make_golden_active.build_moose; each SynChan's
 synapse is driven by a ``TimeTable`` on tick 8 (every 4 steps of 25 us):
 tables with entries closer together than a tick (sent one per tick, so
 they lag), entries between steps, synapse delays of 0 to 2.5 ms and
-different weights.  A Table on tick 8 records the soma Vm; 0.1 s.
+different weights; one table on tick 0 instead (it runs every step there,
+before the handler, so its entries can reach the synapse in the step
+they are sent in).  A Table on tick 8 records the soma Vm; 0.1 s.
 
 Output: ``tests/golden/timetable_golden.npz`` (the model, each table's
 entries, delay and weight, the trace).  Prerequisite: the reference build
@@ -29,6 +31,7 @@ from make_golden_active import build_moose, save_model, synapse  # noqa: E402
 from moose_gb300 import models  # noqa: E402
 
 DT, NSTEPS, STRIDE = 25e-6, 4000, 4
+EARLY = (3,)      # these SynChans' tables run on tick 0, before the handler
 
 
 def timetable_model():
@@ -71,6 +74,8 @@ def main():
         t = moose.TimeTable("/cell/tt%d" % k)
         t.vector = times
         moose.connect(t, "eventOut", s, "addSpike")
+        if k in EARLY:
+            moose.useClock(0, t.path, "process")
     vt = moose.Table("/cell/vm")
     moose.connect(vt, "requestOut", comp[0], "getVm")
     h = moose.HSolve("/cell/hsolve")

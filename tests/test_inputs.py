@@ -2,8 +2,10 @@
 HSolve with real TimeTables (tests/golden/make_golden_timetable.py): the
 oracle, given the queued events the helper derives, reproduces the
 reference's soma trace and final Vm bit for bit -- including entries sent
-one per tick (bursts closer than a tick), entries between steps and
-synapse delays."""
+one per tick (bursts closer than a tick), entries between steps, synapse
+delays and a table on tick 0 (before the handler: an entry can reach the
+synapse in the step it is sent in).  PulseGens and StimulusTables into
+injectMsg likewise (tests/golden/make_golden_pulsegen.py)."""
 import os
 
 import numpy as np
@@ -21,7 +23,12 @@ def _model():
     dt, n, stride = float(Z["dt"]), int(Z["nsteps"]), int(Z["stride"])
     tables = {k: (Z["tt%d_times" % k], float(Z["tt%d_delay" % k]), float(Z["tt%d_weight" % k]))
               for k in range(len(m.syn_compt))}
-    return inputs.add_timetables(m, tables, dt, n, stride), dt, n, stride
+    import sys
+    sys.path.insert(0, GOLDEN)
+    from make_golden_timetable import EARLY
+    m = inputs.add_timetables(m, {k: v for k, v in tables.items() if k not in EARLY}, dt, n, stride)
+    m = inputs.add_timetables(m, {k: v for k, v in tables.items() if k in EARLY}, dt, n, 1, before_handler=EARLY)
+    return m, dt, n, stride
 
 
 def test_timetable_events_reproduce_the_reference_run():
